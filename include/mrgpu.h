@@ -1,0 +1,220 @@
+/*
+ * mrgpu.h -- C ABI of the GB300 coupled-region LDU solver library (libmrgpu).
+ *
+ * This is the boundary a foam-extend 4.1 build of multiRegionFoam calls
+ * through: the lduMatrix::solver adapters (gpuPCG, gpuPBiCG, gpuMixedPCG,
+ * gpuMixedPBiCG) and the GGI transfer adapter hand plain host or device
+ * pointers and sizes to these functions.  No C++ or torch types cross it.
+ *
+ * Conventions
+ *   - Every function returns an int status (MRG_OK or an MRG_E_* code); the
+ *     text of the last error on the calling thread is mrg_last_error().
+ *   - Arrays follow foam's lduAddressing/lduMatrix layout: lowerAddr (owner)
+ *     and upperAddr (neighbour) per internal face, lower < upper, faces in
+ *     upper-triangular order; diag[n], upper[F], lower[F] (NULL when the
+ *     matrix is symmetric); int32 labels and double scalars (-DWM_LABEL_SIZE=32
+ *     -DWM_DP in the reference's compile_commands.json).
+ *   - Caller owns every host array; the library reads it during the call and
+ *     keeps no reference.  The library owns its device copies.
+ *   - x_inout is foam's psi: the initial guess on entry, the solution on exit.
+ *   - One context per host thread, or external synchronisation.  Each context
+ *     owns one CUDA stream; calls are synchronous with respect to the host
+ *     unless stated otherwise.
+ */
+#ifndef MRGPU_H
+#define MRGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+enum {
+    MRG_OK = 0,
+    MRG_E_INVALID = 1,   /* bad argument, size or addressing               */
+    MRG_E_OOM = 2,       /* device allocation failed or HBM budget exceeded */
+    MRG_E_BREAKDOWN = 3, /* non-finite coefficients / factor breakdown      */
+    MRG_E_TIMEOUT = 4,   /* a device-side wait gave up (watchdog)           */
+    MRG_E_CUDA = 5,      /* CUDA runtime error                              */
+    MRG_E_BUSY = 6       /* server queue full                               */
+};
+
+/* ---- solver selection (the fvSolution "solver" / "preconditioner" words) */
+enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1 };
+enum {
+    MRG_PRECOND_NONE = 0,     /* "none"     */
+    MRG_PRECOND_DIAGONAL = 1, /* "diagonal" */
+    MRG_PRECOND_DIC = 2,      /* "DIC"      */
+    MRG_PRECOND_DILU = 3      /* "DILU"     */
+};
+enum {
+    MRG_PRECISION_FP64 = 0,  /* plain method: FP64 throughout, foam order   */
+    MRG_PRECISION_MIXED = 1  /* FP32 Krylov inner loop inside FP64 iterative
+                                refinement (FP64 residual, solution, dots and
+                                convergence test)                           */
+};
+enum {
+    MRG_ORDER_EXACT = 0,   /* preconditioner sweeps in foam's face order
+                              (level-scheduled; identical to the sequential
+                              sweep)                                        */
+    MRG_ORDER_COLOUR = 1   /* multi-colour renumbering for the
+                              preconditioner (fewer sweep levels, different
+                              incomplete factorisation)                      */
+};
+
+typedef struct mrg_ctx mrg_ctx;
+typedef struct mrg_mesh mrg_mesh;
+typedef struct mrg_ggi mrg_ggi;
+typedef struct mrg_batch mrg_batch;
+typedef struct mrg_server mrg_server;
+
+/* The lduMatrix::solver controls dictionary (tolerance, relTol, minIter,
+ * maxIter, preconditioner) plus the GPU-specific choices.  Zero-initialise
+ * and call mrg_controls_default() to get foam's defaults. */
+typedef struct {
+    double tolerance;      /* foam default 1e-6                             */
+    double rel_tol;        /* foam default 0                                */
+    int min_iter;          /* foam default 0                                */
+    int max_iter;          /* foam default 1000                             */
+    int solver;            /* MRG_SOLVER_*                                  */
+    int preconditioner;    /* MRG_PRECOND_*                                 */
+    int precision;         /* MRG_PRECISION_*                               */
+    int ordering;          /* MRG_ORDER_*                                   */
+    double inner_rel_tol;  /* mixed: inner FP32 residual reduction per outer
+                              step (default 1e-4)                           */
+    int inner_max_iter;    /* mixed: inner iterations per outer step (default
+                              = max_iter)                                    */
+    int max_outer;         /* mixed: refinement steps (default 50)          */
+    int iters_per_launch;  /* iterations per CUDA-graph launch (default 16) */
+} mrg_controls;
+
+/* lduSolverPerformance (initialResidual, finalResidual, nIterations,
+ * converged) + GPU extras. */
+typedef struct {
+    double initial_residual;
+    double final_residual;
+    int n_iter;            /* Krylov iterations (mixed: total inner)        */
+    int converged;
+    int singular;
+    int status;            /* MRG_OK or MRG_E_*                              */
+    int n_outer;           /* mixed: refinement steps                       */
+    int reserved;
+    double solve_ms;       /* device time of the solve (CUDA events)        */
+} mrg_perf;
+
+/* One coupled interface patch seen from one side: faceCells plus the GGI
+ * weights that give each face's neighbour value from the shadow side's
+ * cells (monolithicCouplingFvPatchField::initInterfaceMatrixUpdate,
+ * monolithicCouplingFvPatchField.C:381-417).  src_ptr == NULL means one
+ * source per face with weight 1 (conformal / directMap). */
+typedef struct {
+    int n_faces;
+    const int32_t* face_cells;  /* [n_faces] cells receiving the update     */
+    const int32_t* src_ptr;     /* [n_faces+1] CSR into src_cell/src_weight */
+    const int32_t* src_cell;    /* shadow cells feeding each weight         */
+    const double* src_weight;   /* GGI weights (NULL: all 1)                */
+} mrg_iface_desc;
+
+/* ---- library / context ---------------------------------------------- */
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* mrg_last_error(void);
+
+/* Library version string. */
+const char* mrg_version(void);
+
+/* Fill c with foam's defaults (tolerance 1e-6, relTol 0, minIter 0,
+ * maxIter 1000, PCG, DIC, FP64, exact order). */
+void mrg_controls_default(mrg_controls* c);
+
+/* Create a context on CUDA device `device` with an HBM budget in bytes for
+ * all meshes, coefficients and workspaces it allocates (0 = no limit).
+ * Replaces the per-process set-up foam does in lduMatrix::solver::New. */
+int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out);
+int mrg_ctx_destroy(mrg_ctx* ctx);
+/* Bytes currently allocated against the budget. */
+int mrg_ctx_mem_used(mrg_ctx* ctx, size_t* bytes);
+
+/* Pinned host memory (for callers that want asynchronous copies). */
+int mrg_host_alloc(size_t bytes, void** out);
+int mrg_host_free(void* p);
+
+/* ---- mesh addressing (resident) -------------------------------------
+ * Replaces foam's lduAddressing (lowerAddr/upperAddr, ownerStartAddr,
+ * losortAddr) consumed by lduMatrix::Amul and the DIC/DILU
+ * preconditioners, plus the interface patches of
+ * monolithicCouplingFvPatchField (monolithicCouplingFvPatchField.C:381-464).
+ * The addressing stays on the device until mrg_mesh_destroy. */
+int mrg_mesh_upload(mrg_ctx* ctx, int n_cells, int n_faces,
+                    const int32_t* lower_addr, const int32_t* upper_addr,
+                    int n_iface, const mrg_iface_desc* ifaces,
+                    mrg_mesh** out);
+int mrg_mesh_destroy(mrg_mesh* mesh);
+/* Number of preconditioner sweep levels of the chosen ordering (critical
+ * path length of the DIC/DILU triangular solves). */
+int mrg_mesh_levels(mrg_mesh* mesh, int ordering, int* n_levels);
+
+/* ---- coefficients (per time step) -----------------------------------
+ * lduMatrix::diag()/upper()/lower() plus the interfaces' coupleBouCoeffs
+ * (Amul, sumA) and coupleIntCoeffs (Tmul; NULL = same as bou), each in
+ * interface order (patches in mrg_mesh_upload order, faces within).
+ * Host pointers; the _device variant takes device pointers. */
+int mrg_coeffs_upload(mrg_mesh* mesh, const double* diag, const double* upper,
+                      const double* lower_or_null, const double* iface_bou,
+                      const double* iface_int_or_null);
+int mrg_coeffs_upload_device(mrg_mesh* mesh, const double* diag,
+                             const double* upper, const double* lower_or_null,
+                             const double* iface_bou,
+                             const double* iface_int_or_null);
+
+/* ---- solve ------------------------------------------------------------
+ * lduMatrix::solver::solve(psi, source, cmpt) of foam's PCG / PBiCG with the
+ * DIC / DILU / diagonal / none preconditioners
+ * (called from multiRegionSystem.C:150-153 via coupledFvMatrix::solve and
+ * :293 via fvMatrix::solve).  b and x_inout are host arrays of n_cells in
+ * the caller's numbering; perf may be NULL. */
+int mrg_solve(mrg_mesh* mesh, const double* b, double* x_inout,
+              const mrg_controls* controls, mrg_perf* perf);
+/* Same with device-resident b and x (no host copies). */
+int mrg_solve_device(mrg_mesh* mesh, const double* d_b, double* d_x_inout,
+                     const mrg_controls* controls, mrg_perf* perf);
+
+/* ---- building blocks (each one of the hot-path kernels) ---------------
+ * y = A x (lduMatrix::Amul with interface update) or y = A^T x (Tmul),
+ * host arrays in the caller's numbering. */
+int mrg_amul(mrg_mesh* mesh, const double* x, double* y, int transpose);
+/* foam-normalised residual sum|b - A x| / normFactor of x for b
+ * (lduMatrix::solver::normFactor + gSumMag). */
+int mrg_residual(mrg_mesh* mesh, const double* b, const double* x,
+                 double* residual, double* norm_factor);
+/* w = M^-1 r (transpose != 0: M^-T r, DILU's preconditionT) for
+ * preconditioner `precond` in ordering `ordering`. */
+int mrg_precondition(mrg_mesh* mesh, int precond, int ordering,
+                     const double* r, double* w, int transpose);
+/* Reciprocal factor diagonal rD of DIC / DILU, caller's numbering. */
+int mrg_factor_diag(mrg_mesh* mesh, int precond, int ordering, double* rD);
+
+/* ---- GGI interpolation ----------------------------------------------
+ * GGIInterpolation::masterToSlave / slaveToMaster as called from
+ * ggiInterfaceToInterfaceMapping::transferFacesZoneToZone
+ * (ggiInterfaceToInterfaceMappingTemplates.C:37-77) and
+ * regionInterfaceType::interpolateFacesFrom{A,B}
+ * (regionInterfaceTypeTemplates.C:35-133): dst[i] = sum_k w_ik src[addr_ik]
+ * for n_dst faces, ncomp interleaved components (1 scalar, 3 vector,
+ * 4 VectorN<scalar,4>).  Faces with no weights (uncovered) get 0. */
+int mrg_ggi_create(mrg_ctx* ctx, int n_dst, int n_src, const int32_t* row_ptr,
+                   const int32_t* src_addr, const double* weights,
+                   mrg_ggi** out);
+int mrg_ggi_destroy(mrg_ggi* ggi);
+int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp);
+int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst,
+                         int ncomp);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRGPU_H */

@@ -1,0 +1,489 @@
+// api.cu -- the extern "C" boundary declared in include/mrgpu.h.
+// Every entry point converts C++ exceptions into status codes; nothing
+// throws across the ABI.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
+#include "../../include/mrgpu.h"
+#include "engine.h"
+#include "kernels.h"
+
+using namespace mrg;
+
+struct mrg_ctx {
+    Ctx c;
+};
+struct mrg_mesh {
+    Mesh m;
+};
+struct mrg_ggi {
+    Ggi g;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+template <typename F>
+int guard(F&& f)
+{
+    try {
+        g_last_error.clear();
+        return f();
+    } catch (const Error& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(MRG_E_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(MRG_E_INVALID, e.what());
+    }
+}
+
+Controls to_controls(const mrg_controls* c)
+{
+    Controls k;
+    if (!c) return k;
+    k.tol = c->tolerance;
+    k.rel_tol = c->rel_tol;
+    k.min_iter = c->min_iter;
+    k.max_iter = c->max_iter;
+    k.solver = c->solver;
+    k.pc = c->preconditioner;
+    k.precision = c->precision;
+    k.ordering = c->ordering;
+    k.inner_rel_tol = c->inner_rel_tol > 0 ? c->inner_rel_tol : 1e-4;
+    k.inner_max_iter = c->inner_max_iter;
+    k.max_outer = c->max_outer > 0 ? c->max_outer : 50;
+    k.k_launch = c->iters_per_launch > 0 ? c->iters_per_launch : 16;
+    if (k.solver < 0 || k.solver > 1) throw Error(MRG_E_INVALID, "unknown solver");
+    if (k.pc < 0 || k.pc > 3) throw Error(MRG_E_INVALID, "unknown preconditioner");
+    if (k.precision < 0 || k.precision > 1) throw Error(MRG_E_INVALID, "unknown precision");
+    if (k.ordering < 0 || k.ordering > 1) throw Error(MRG_E_INVALID, "unknown ordering");
+    if (k.max_iter < 0 || k.min_iter < 0) throw Error(MRG_E_INVALID, "negative iteration bounds");
+    return k;
+}
+
+void fill_perf(mrg_perf* p, const Perf& r)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->initial_residual = r.res0;
+    p->final_residual = r.res;
+    p->n_iter = r.iters;
+    p->converged = r.converged;
+    p->singular = r.singular;
+    p->status = r.status;
+    p->n_outer = r.outer;
+    p->solve_ms = r.ms;
+}
+
+// Scratch device buffers of a context for host-pointer entry points.
+struct HostStage {
+    double* d[3] = {nullptr, nullptr, nullptr};
+    size_t cap = 0;
+};
+thread_local std::map<Ctx*, HostStage> g_stage;
+
+double* stage(Ctx* c, int k, size_t n)
+{
+    HostStage& s = g_stage[c];
+    if (s.cap < n) {
+        for (auto& p : s.d) {
+            c->release(p);
+            p = nullptr;
+        }
+        s.cap = n;
+    }
+    if (!s.d[k]) s.d[k] = (double*)c->alloc(8 * s.cap);
+    return s.d[k];
+}
+
+void h2d(Ctx* c, double* d, const double* h, size_t n)
+{
+    MRG_CUDA(cudaMemcpyAsync(d, h, 8 * n, cudaMemcpyHostToDevice, c->st));
+}
+void d2h(Ctx* c, double* h, const double* d, size_t n)
+{
+    MRG_CUDA(cudaMemcpyAsync(h, d, 8 * n, cudaMemcpyDeviceToHost, c->st));
+    MRG_CUDA(cudaStreamSynchronize(c->st));
+}
+
+void upload_coeffs(Mesh& m, const double* diag, const double* upper, const double* lower, const double* ibou,
+                   const double* iint, cudaMemcpyKind kind)
+{
+    if (!diag || (m.nf > 0 && !upper)) throw Error(MRG_E_INVALID, "diag/upper must not be NULL");
+    if (m.ni > 0 && !ibou) throw Error(MRG_E_INVALID, "interface coefficients must not be NULL");
+    Ctx* c = m.ctx;
+    if (!m.raw_diag) m.raw_diag = (double*)c->alloc(8 * (size_t)m.n);
+    if (!m.raw_upper) m.raw_upper = (double*)c->alloc(8 * (size_t)std::max(m.nf, 1));
+    if (lower && !m.raw_lower) m.raw_lower = (double*)c->alloc(8 * (size_t)std::max(m.nf, 1));
+    if (m.ni && !m.raw_ibou) m.raw_ibou = (double*)c->alloc(8 * (size_t)m.ni);
+    if (iint && !m.raw_iint) m.raw_iint = (double*)c->alloc(8 * (size_t)m.ni);
+    MRG_CUDA(cudaMemcpyAsync(m.raw_diag, diag, 8 * (size_t)m.n, kind, c->st));
+    if (m.nf) MRG_CUDA(cudaMemcpyAsync(m.raw_upper, upper, 8 * (size_t)m.nf, kind, c->st));
+    if (lower && m.nf) MRG_CUDA(cudaMemcpyAsync(m.raw_lower, lower, 8 * (size_t)m.nf, kind, c->st));
+    if (m.ni) MRG_CUDA(cudaMemcpyAsync(m.raw_ibou, ibou, 8 * (size_t)m.ni, kind, c->st));
+    if (iint && m.ni) MRG_CUDA(cudaMemcpyAsync(m.raw_iint, iint, 8 * (size_t)m.ni, kind, c->st));
+    const bool new_sym = lower == nullptr, new_int = iint != nullptr;
+    if (m.have_coeffs && (new_sym != m.sym || new_int != m.has_int)) {
+        // symmetry changed: the transposed views must be rebuilt
+        for (auto& p : m.plans)
+            if (p) p->scattered = 0;
+    }
+    m.sym = new_sym;
+    m.has_int = new_int;
+    m.have_coeffs = true;
+    ++m.version;
+    if (kind == cudaMemcpyHostToDevice) MRG_CUDA(cudaStreamSynchronize(c->st));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mrg_last_error(void) { return g_last_error.c_str(); }
+
+const char* mrg_version(void) { return "mrgpu 0.1 (sm_103a)"; }
+
+void mrg_controls_default(mrg_controls* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof *c);
+    c->tolerance = 1e-6;
+    c->rel_tol = 0.0;
+    c->min_iter = 0;
+    c->max_iter = 1000;
+    c->solver = MRG_SOLVER_PCG;
+    c->preconditioner = MRG_PRECOND_DIC;
+    c->precision = MRG_PRECISION_FP64;
+    c->ordering = MRG_ORDER_EXACT;
+    c->inner_rel_tol = 1e-4;
+    c->inner_max_iter = 0;
+    c->max_outer = 50;
+    c->iters_per_launch = 16;
+}
+
+int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out)
+{
+    return guard([&] {
+        if (!out) return fail(MRG_E_INVALID, "out is NULL");
+        *out = nullptr;
+        int ndev = 0;
+        MRG_CUDA(cudaGetDeviceCount(&ndev));
+        if (device < 0 || device >= ndev) return fail(MRG_E_INVALID, "no such CUDA device");
+        MRG_CUDA(cudaSetDevice(device));
+        auto* c = new mrg_ctx();
+        try {
+            c->c.device = device;
+            c->c.budget = hbm_budget_bytes;
+            MRG_CUDA(cudaDeviceGetAttribute(&c->c.nsm, cudaDevAttrMultiProcessorCount, device));
+            MRG_CUDA(cudaStreamCreateWithFlags(&c->c.st, cudaStreamNonBlocking));
+            c->c.d_ctl = (Ctl*)c->c.alloc(sizeof(Ctl));
+            MRG_CUDA(cudaStreamSynchronize(c->c.st));
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *out = c;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ctx_destroy(mrg_ctx* ctx)
+{
+    return guard([&] {
+        if (!ctx) return (int)MRG_OK;
+        g_stage.erase(&ctx->c);
+        delete ctx;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ctx_mem_used(mrg_ctx* ctx, size_t* bytes)
+{
+    if (!ctx || !bytes) return fail(MRG_E_INVALID, "NULL argument");
+    *bytes = ctx->c.used;
+    return MRG_OK;
+}
+
+int mrg_host_alloc(size_t bytes, void** out)
+{
+    return guard([&] {
+        if (!out) return fail(MRG_E_INVALID, "out is NULL");
+        MRG_CUDA(cudaMallocHost(out, bytes ? bytes : 16));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_host_free(void* p)
+{
+    return guard([&] {
+        if (p) MRG_CUDA(cudaFreeHost(p));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mesh_upload(mrg_ctx* ctx, int n_cells, int n_faces, const int32_t* lower_addr, const int32_t* upper_addr,
+                    int n_iface, const mrg_iface_desc* ifaces, mrg_mesh** out)
+{
+    return guard([&] {
+        if (!ctx || !out) return fail(MRG_E_INVALID, "NULL argument");
+        *out = nullptr;
+        if (n_iface < 0 || (n_iface > 0 && !ifaces)) return fail(MRG_E_INVALID, "bad interface list");
+        MRG_CUDA(cudaSetDevice(ctx->c.device));
+        IfaceHost ifc;
+        ifc.ptr.push_back(0);
+        for (int p = 0; p < n_iface; ++p) {
+            const mrg_iface_desc& d = ifaces[p];
+            if (d.n_faces < 0 || (d.n_faces > 0 && (!d.face_cells || !d.src_cell)))
+                return fail(MRG_E_INVALID, "interface " + std::to_string(p) + ": NULL arrays");
+            for (int i = 0; i < d.n_faces; ++i) {
+                ifc.cells.push_back(d.face_cells[i]);
+                const int k0 = d.src_ptr ? d.src_ptr[i] : i, k1 = d.src_ptr ? d.src_ptr[i + 1] : i + 1;
+                if (k1 < k0) return fail(MRG_E_INVALID, "interface CSR pointer decreases");
+                for (int k = k0; k < k1; ++k) {
+                    ifc.src.push_back(d.src_cell[k]);
+                    ifc.w.push_back(d.src_weight ? d.src_weight[k] : 1.0);
+                }
+                ifc.ptr.push_back((int32_t)ifc.src.size());
+            }
+        }
+        std::string msg = validate_addressing(n_cells, n_faces, lower_addr, upper_addr, ifc);
+        if (!msg.empty()) return fail(MRG_E_INVALID, msg);
+        if ((long long)n_cells + 1024 > (1LL << 30)) return fail(MRG_E_INVALID, "mesh too large for int32 layout");
+        auto* m = new mrg_mesh();
+        m->m.ctx = &ctx->c;
+        m->m.n = n_cells;
+        m->m.nf = n_faces;
+        m->m.ni = ifc.size();
+        m->m.lower.assign(lower_addr, lower_addr + n_faces);
+        m->m.upper.assign(upper_addr, upper_addr + n_faces);
+        m->m.ifc = std::move(ifc);
+        *out = m;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mesh_destroy(mrg_mesh* mesh)
+{
+    return guard([&] {
+        delete mesh;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mesh_levels(mrg_mesh* mesh, int ordering, int* n_levels)
+{
+    return guard([&] {
+        if (!mesh || !n_levels) return fail(MRG_E_INVALID, "NULL argument");
+        *n_levels = mesh->m.plan(ordering).sys.nlevels;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_coeffs_upload(mrg_mesh* mesh, const double* diag, const double* upper, const double* lower_or_null,
+                      const double* iface_bou, const double* iface_int_or_null)
+{
+    return guard([&] {
+        if (!mesh) return fail(MRG_E_INVALID, "mesh is NULL");
+        upload_coeffs(mesh->m, diag, upper, lower_or_null, iface_bou, iface_int_or_null, cudaMemcpyHostToDevice);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_coeffs_upload_device(mrg_mesh* mesh, const double* diag, const double* upper, const double* lower_or_null,
+                             const double* iface_bou, const double* iface_int_or_null)
+{
+    return guard([&] {
+        if (!mesh) return fail(MRG_E_INVALID, "mesh is NULL");
+        upload_coeffs(mesh->m, diag, upper, lower_or_null, iface_bou, iface_int_or_null, cudaMemcpyDeviceToDevice);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_solve(mrg_mesh* mesh, const double* b, double* x_inout, const mrg_controls* controls, mrg_perf* perf)
+{
+    return guard([&] {
+        if (!mesh || !b || !x_inout) return fail(MRG_E_INVALID, "NULL argument");
+        Controls k = to_controls(controls);
+        Mesh& m = mesh->m;
+        Ctx* c = m.ctx;
+        double* db = stage(c, 0, m.n);
+        double* dx = stage(c, 1, m.n);
+        h2d(c, db, b, m.n);
+        h2d(c, dx, x_inout, m.n);
+        Perf r = solve_device(m, db, dx, k);
+        d2h(c, x_inout, dx, m.n);
+        fill_perf(perf, r);
+        if (r.status != MRG_OK) return fail(r.status, "non-finite residual (breakdown)");
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_solve_device(mrg_mesh* mesh, const double* d_b, double* d_x_inout, const mrg_controls* controls,
+                     mrg_perf* perf)
+{
+    return guard([&] {
+        if (!mesh || !d_b || !d_x_inout) return fail(MRG_E_INVALID, "NULL argument");
+        Controls k = to_controls(controls);
+        Perf r = solve_device(mesh->m, d_b, d_x_inout, k);
+        fill_perf(perf, r);
+        if (r.status != MRG_OK) return fail(r.status, "non-finite residual (breakdown)");
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_amul(mrg_mesh* mesh, const double* x, double* y, int transpose)
+{
+    return guard([&] {
+        if (!mesh || !x || !y) return fail(MRG_E_INVALID, "NULL argument");
+        Mesh& m = mesh->m;
+        Ctx* c = m.ctx;
+        double* dx = stage(c, 0, m.n);
+        double* dy = stage(c, 1, m.n);
+        h2d(c, dx, x, m.n);
+        amul_device(m, dx, dy, transpose);
+        d2h(c, y, dy, m.n);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_residual(mrg_mesh* mesh, const double* b, const double* x, double* residual, double* norm_factor)
+{
+    return guard([&] {
+        if (!mesh || !b || !x) return fail(MRG_E_INVALID, "NULL argument");
+        Mesh& m = mesh->m;
+        Ctx* c = m.ctx;
+        double* db = stage(c, 0, m.n);
+        double* dx = stage(c, 1, m.n);
+        h2d(c, db, b, m.n);
+        h2d(c, dx, x, m.n);
+        residual_device(m, db, dx, residual, norm_factor);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_precondition(mrg_mesh* mesh, int precond, int ordering, const double* r, double* w, int transpose)
+{
+    return guard([&] {
+        if (!mesh || !r || !w) return fail(MRG_E_INVALID, "NULL argument");
+        if (precond < 0 || precond > 3) return fail(MRG_E_INVALID, "unknown preconditioner");
+        Mesh& m = mesh->m;
+        Ctx* c = m.ctx;
+        double* dr = stage(c, 0, m.n);
+        double* dw = stage(c, 1, m.n);
+        h2d(c, dr, r, m.n);
+        precondition_device(m, precond, ordering, dr, dw, transpose);
+        d2h(c, w, dw, m.n);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_factor_diag(mrg_mesh* mesh, int precond, int ordering, double* rD)
+{
+    return guard([&] {
+        if (!mesh || !rD) return fail(MRG_E_INVALID, "NULL argument");
+        if (precond < 1 || precond > 3) return fail(MRG_E_INVALID, "preconditioner has no factor");
+        Mesh& m = mesh->m;
+        double* d = stage(m.ctx, 2, m.n);
+        factor_diag_device(m, precond, ordering, d);
+        d2h(m.ctx, rD, d, m.n);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_create(mrg_ctx* ctx, int n_dst, int n_src, const int32_t* row_ptr, const int32_t* src_addr,
+                   const double* weights, mrg_ggi** out)
+{
+    return guard([&] {
+        if (!ctx || !out || !row_ptr || n_dst < 0 || n_src < 0) return fail(MRG_E_INVALID, "bad argument");
+        *out = nullptr;
+        if (row_ptr[0] != 0) return fail(MRG_E_INVALID, "row_ptr must start at 0");
+        for (int i = 0; i < n_dst; ++i)
+            if (row_ptr[i + 1] < row_ptr[i]) return fail(MRG_E_INVALID, "row_ptr decreases");
+        const int nnz = row_ptr[n_dst];
+        if (nnz > 0 && (!src_addr || !weights)) return fail(MRG_E_INVALID, "NULL weights");
+        for (int k = 0; k < nnz; ++k)
+            if (src_addr[k] < 0 || src_addr[k] >= n_src) return fail(MRG_E_INVALID, "source face out of range");
+        Ctx* c = &ctx->c;
+        auto* g = new mrg_ggi();
+        try {
+            g->g.ctx = c;
+            g->g.n_dst = n_dst;
+            g->g.n_src = n_src;
+            g->g.ptr = (int32_t*)c->alloc(4 * (size_t)(n_dst + 1));
+            g->g.addr = (int32_t*)c->alloc(4 * (size_t)std::max(nnz, 1));
+            g->g.w = (double*)c->alloc(8 * (size_t)std::max(nnz, 1));
+            MRG_CUDA(cudaMemcpyAsync(g->g.ptr, row_ptr, 4 * (size_t)(n_dst + 1), cudaMemcpyHostToDevice, c->st));
+            if (nnz) {
+                MRG_CUDA(cudaMemcpyAsync(g->g.addr, src_addr, 4 * (size_t)nnz, cudaMemcpyHostToDevice, c->st));
+                MRG_CUDA(cudaMemcpyAsync(g->g.w, weights, 8 * (size_t)nnz, cudaMemcpyHostToDevice, c->st));
+            }
+            MRG_CUDA(cudaStreamSynchronize(c->st));
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_destroy(mrg_ggi* ggi)
+{
+    return guard([&] {
+        delete ggi;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst, int ncomp)
+{
+    return guard([&] {
+        if (!ggi || !d_src || !d_dst || ncomp < 1 || ncomp > 16) return fail(MRG_E_INVALID, "bad argument");
+        Ggi& g = ggi->g;
+        launch_ggi(g.n_dst, g.ptr, g.addr, g.w, d_src, d_dst, ncomp, g.ctx->st);
+        MRG_CUDA(cudaGetLastError());
+        MRG_CUDA(cudaStreamSynchronize(g.ctx->st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp)
+{
+    return guard([&] {
+        if (!ggi || !src || !dst || ncomp < 1 || ncomp > 16) return fail(MRG_E_INVALID, "bad argument");
+        Ggi& g = ggi->g;
+        Ctx* c = g.ctx;
+        if (g.cap_comp < ncomp) {
+            c->release(g.d_src);
+            c->release(g.d_dst);
+            g.d_src = (double*)c->alloc(8 * (size_t)std::max(g.n_src, 1) * ncomp);
+            g.d_dst = (double*)c->alloc(8 * (size_t)std::max(g.n_dst, 1) * ncomp);
+            g.cap_comp = ncomp;
+        }
+        MRG_CUDA(cudaMemcpyAsync(g.d_src, src, 8 * (size_t)g.n_src * ncomp, cudaMemcpyHostToDevice, c->st));
+        launch_ggi(g.n_dst, g.ptr, g.addr, g.w, g.d_src, g.d_dst, ncomp, c->st);
+        MRG_CUDA(cudaGetLastError());
+        MRG_CUDA(cudaMemcpyAsync(dst, g.d_dst, 8 * (size_t)g.n_dst * ncomp, cudaMemcpyDeviceToHost, c->st));
+        MRG_CUDA(cudaStreamSynchronize(c->st));
+        return (int)MRG_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace mrg {
+Ggi::~Ggi()
+{
+    if (!ctx) return;
+    for (void* p : {(void*)ptr, (void*)addr, (void*)w, (void*)d_src, (void*)d_dst}) ctx->release(p);
+}
+}  // namespace mrg

@@ -1,0 +1,111 @@
+// engine.h -- host-side objects behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "dev.h"
+#include "plan.h"
+
+namespace mrg {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+#define MRG_CUDA(x) ::mrg::cuda_check((x), #x)
+
+struct Ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t st = nullptr;
+    size_t budget = 0, used = 0;
+    std::map<void*, size_t> allocs;
+    Ctl* d_ctl = nullptr;
+    void* alloc(size_t bytes);
+    void release(void* p);
+    ~Ctx();
+};
+
+// Device copy of one plan + coefficient views + workspaces for one ordering.
+struct PlanState {
+    Ctx* ctx = nullptr;
+    PlanHost host;  // large host arrays are released after upload
+    int32_t *perm = nullptr, *a_sptr = nullptr, *a_col = nullptr, *a_src = nullptr;
+    int32_t *chunk_start = nullptr, *lvl_chunk = nullptr;
+    int32_t *f_sptr = nullptr, *f_col = nullptr, *f_src = nullptr;
+    int32_t *b_sptr = nullptr, *b_col = nullptr, *b_src = nullptr;
+    int32_t *g_ptr = nullptr, *g_src = nullptr;
+    double* g_w = nullptr;
+    float* g_w32 = nullptr;
+    SysDev sys{};           // host mirror
+    SysDev* d_sys = nullptr;
+    int2* d_tiles = nullptr;
+    int ntiles = 0;
+    bool have32 = false, haveT = false;
+    uint64_t scattered = 0;   // coefficient version scattered into the views
+    uint64_t factored = 0;    // coefficient version factored
+    int factored_pc = -1;
+    bool factored32 = false;
+    std::map<std::string, cudaGraphExec_t> graphs;
+    ~PlanState();
+    void sync_sys();  // copy host mirror to device
+};
+
+struct Mesh {
+    Ctx* ctx = nullptr;
+    int n = 0, nf = 0, ni = 0;
+    std::vector<int32_t> lower, upper;
+    IfaceHost ifc;
+    double *raw_diag = nullptr, *raw_upper = nullptr, *raw_lower = nullptr;
+    double *raw_ibou = nullptr, *raw_iint = nullptr;
+    bool sym = true, has_int = false, have_coeffs = false;
+    uint64_t version = 0;
+    size_t nnz_cache[2][3] = {};  // per ordering: Amul, forward, backward entries
+    std::unique_ptr<PlanState> plans[2];
+    PlanState& plan(int ordering);
+    ~Mesh();
+};
+
+struct Ggi {
+    Ctx* ctx = nullptr;
+    int n_dst = 0, n_src = 0;
+    int32_t *ptr = nullptr, *addr = nullptr;
+    double* w = nullptr;
+    double *d_src = nullptr, *d_dst = nullptr;
+    int cap_comp = 0;
+    ~Ggi();
+};
+
+struct Controls {
+    double tol = 1e-6, rel_tol = 0.0;
+    int min_iter = 0, max_iter = 1000;
+    int solver = 0, pc = 2, precision = 0, ordering = 0;
+    double inner_rel_tol = 1e-4;
+    int inner_max_iter = 0, max_outer = 50, k_launch = 16;
+};
+
+struct Perf {
+    double res0 = 0, res = 0;
+    int iters = 0, converged = 0, singular = 0, status = 0, outer = 0;
+    double ms = 0;
+};
+
+// Prepare views (+FP32 copies) and factor for a solve; returns the plan.
+PlanState& prepare(Mesh& m, const Controls& c);
+// Solve with device-resident b and x (caller numbering).
+Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& c);
+
+void amul_device(Mesh& m, const double* d_x, double* d_y, int transpose);
+void residual_device(Mesh& m, const double* d_b, const double* d_x, double* res, double* nfac);
+void precondition_device(Mesh& m, int pc, int ordering, const double* d_r, double* d_w, int transpose);
+void factor_diag_device(Mesh& m, int pc, int ordering, double* d_rD);
+
+}  // namespace mrg

@@ -1,0 +1,762 @@
+// kernels.cu -- sm_103a kernels of the coupled-region LDU solve path.
+//
+// Arithmetic contract.  Every FP64 operation is an explicit IEEE intrinsic
+// (__dmul_rn, __fma_rn, __dadd_rn, __ddiv_rn), so the per-cell results of
+// Amul, sumA, the DIC/DILU factor, the sweeps and the GGI gather are
+// bit-identical to the oracle's "fused" mode (same operations, same order).
+// The order is foam's: each cell accumulates its face terms in ascending face
+// index, interface terms after all face terms (lduMatrix::Amul then
+// updateMatrixInterfaces), forward sweep terms in ascending and backward
+// terms in descending face order.
+//
+// GB300 notes.  FP64 issue rate is ~1/64 of FP32 on this part, so FP64 kernels
+// are written to minimise FP64 instructions: one FMA per matrix entry, sweep
+// coefficients rD[row]*a pre-multiplied once per factorisation, no FP64 work
+// on padding.  Everything else is HBM- or latency-bound: no tensor cores.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.h"
+#include "plan.h"
+
+namespace mrg {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr long long kSentBits64 = 0x7FF4DEADBEEF0001LL;  // signalling-NaN payload
+constexpr unsigned kSentBits32 = 0x7FA5A5A5u;
+// A sync-free wait gives up after this many SM cycles (~2 s) and flags
+// ERR_TIMEOUT, so no kernel can spin forever.
+constexpr long long kWaitCycles = 4000000000LL;
+
+template <typename V> __device__ __forceinline__ V sent();
+template <> __device__ __forceinline__ double sent<double>() { return __longlong_as_double(kSentBits64); }
+template <> __device__ __forceinline__ float sent<float>() { return __uint_as_float(kSentBits32); }
+__device__ __forceinline__ bool is_sent(double v) { return __double_as_longlong(v) == kSentBits64; }
+__device__ __forceinline__ bool is_sent(float v) { return __float_as_uint(v) == kSentBits32; }
+
+__device__ __forceinline__ double vmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double vfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+__device__ __forceinline__ double ld_relaxed(const double* p)
+{
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ float ld_relaxed(const float* p)
+{
+    float v;
+    asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(double* p, double v)
+{
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(float* p, float v)
+{
+    asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+
+// Wait until a value produced in the same launch is published (not the
+// sentinel).  Bounded: on timeout, or when another wait already timed out,
+// it returns whatever it read and the error bit stays set for the host.
+template <typename V>
+__device__ __forceinline__ V wait_ready(const V* p, Ctl* ctl)
+{
+    V v = ld_relaxed(p);
+    if (!is_sent(v)) return v;
+    long long t0 = clock64();
+    for (int it = 1;; ++it) {
+        if (it > 32) __nanosleep(64);
+        v = ld_relaxed(p);
+        if (!is_sent(v)) return v;
+        if ((it & 255) == 0) {
+            if (*(volatile unsigned*)&ctl->err) return v;
+            if (clock64() - t0 > kWaitCycles) {
+                atomicOr(&ctl->err, ERR_TIMEOUT);
+                return v;
+            }
+        }
+    }
+}
+
+// Coefficient value for a plan source code (see plan.h).
+__device__ __forceinline__ double src_val(const SysDev& S, int s, bool trans)
+{
+    const int F = S.nf;
+    if (s < 2 * F) {
+        if (trans) s = (s < F) ? s + F : s - F;
+        if (s < F) return S.raw_upper[s];
+        return S.sym ? S.raw_upper[s - F] : S.raw_lower[s - F];
+    }
+    const int j = s - 2 * F;
+    const double c = (trans && S.raw_iint) ? S.raw_iint[j] : S.raw_ibou[j];
+    return -c;
+}
+__device__ __forceinline__ int swap_src(int s, int F) { return s < F ? s + F : (s < 2 * F ? s - F : s); }
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    return v;
+}
+
+// Deterministic block sum of NR values (fixed tree).  Result valid in tid 0.
+template <int NR>
+__device__ __forceinline__ void block_sum(double (&a)[NR], double* sh)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) a[k] = warp_sum(a[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NR; ++k) sh[wid * NR + k] = a[k];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            double v = lane < (kBlock / 32) ? sh[lane * NR + k] : 0.0;
+            a[k] = warp_sum(v);
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- vector picks
+template <typename V> struct VP;
+template <> struct VP<double> {
+    static __device__ __forceinline__ const Vecs<double>& v(const SysDev& S) { return S.v64; }
+    static __device__ __forceinline__ const double* aval(const SysDev& S, bool t) { return t ? S.aT_val : S.a_val; }
+    static __device__ __forceinline__ const double* diag(const SysDev& S) { return S.diag; }
+    static __device__ __forceinline__ const double* rD(const SysDev& S) { return S.rD; }
+    static __device__ __forceinline__ const double* fc(const SysDev& S, bool t) { return t ? S.f_cT : S.f_c; }
+    static __device__ __forceinline__ const double* bc(const SysDev& S, bool t) { return t ? S.b_cT : S.b_c; }
+    static __device__ __forceinline__ const double* gw(const SysDev& S) { return S.g_w; }
+};
+template <> struct VP<float> {
+    static __device__ __forceinline__ const Vecs<float>& v(const SysDev& S) { return S.v32; }
+    static __device__ __forceinline__ const float* aval(const SysDev& S, bool t) { return t ? S.aT_val32 : S.a_val32; }
+    static __device__ __forceinline__ const float* diag(const SysDev& S) { return S.diag32; }
+    static __device__ __forceinline__ const float* rD(const SysDev& S) { return S.rD32; }
+    static __device__ __forceinline__ const float* fc(const SysDev& S, bool t) { return t ? S.f_cT32 : S.f_c32; }
+    static __device__ __forceinline__ const float* bc(const SysDev& S, bool t) { return t ? S.b_cT32 : S.b_c32; }
+    static __device__ __forceinline__ const float* gw(const SysDev& S) { return S.g_w32; }
+};
+
+// Sliced-ELL row product y_i = diag_i x_i + sum_k a_k x[col_k] (foam order).
+template <typename V>
+__device__ __forceinline__ V ell_row(const SysDev& S, const V* __restrict__ val, const V* __restrict__ dg,
+                                     const V* __restrict__ x, int i)
+{
+    const int sl = i >> 5, lane = i & 31;
+    const int e0 = S.a_sptr[sl], W = (S.a_sptr[sl + 1] - e0) >> 5;
+    V y = vmul(dg[i], x[i]);
+    const int* __restrict__ col = S.a_col + e0 + lane;
+    const V* __restrict__ v = val + e0 + lane;
+    for (int k = 0; k < W; ++k) {
+        const int c = __ldg(col + k * 32);
+        if (c < 0) break;
+        y = vfma(__ldg(v + k * 32), x[c], y);
+    }
+    return y;
+}
+
+// Per-system finalisation, executed by thread 0 of the last tile.
+__device__ void finalize(const SysDev& S, RowOp op, const double* sums)
+{
+    Scal* sc = S.sc;
+    sc->red[0] = sums[0];
+    sc->red[1] = sums[1];
+    switch (op) {
+    case OP_SUMX:
+        sc->xsum = sums[0];
+        break;
+    case OP_INIT_RES: {
+        sc->nfac = sums[0] + 1.0e-20;
+        sc->res0 = sums[1] / sc->nfac;
+        sc->res = sc->res0;
+        sc->iter = 0;
+        sc->singular = 0;
+        sc->rho = 1.0e20;
+        const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
+        sc->converged = conv;
+        sc->active = (sc->min_iter > 0 || !conv) ? 1 : 0;
+        break;
+    }
+    case OP_RHO:
+        sc->rho_old = sc->rho;
+        sc->rho = sums[0];
+        sc->beta = sc->iter > 0 ? sc->rho / sc->rho_old : 0.0;
+        break;
+    case OP_SPMV_QP:
+        if (fabs(sums[0]) / sc->nfac < 1.0e-300) {
+            sc->singular = 1;
+            sc->active = 0;
+            sc->alpha = 0.0;
+        } else {
+            sc->alpha = sc->rho / sums[0];
+        }
+        break;
+    case OP_UPDATE: {
+        sc->res = sums[0] / sc->nfac;
+        sc->iter += 1;
+        const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
+        sc->converged = conv;
+        const bool more = (sc->iter < sc->max_iter && !conv) || sc->iter < sc->min_iter;
+        if (!more) sc->active = 0;
+        break;
+    }
+    case OP_RESID64:
+        sc->osum = sums[0];
+        break;
+    case OP_TO32:
+        // inner solve state: residual measured relative to the start
+        sc->inv_scale = sc->osum > 0.0 ? sc->osum / (double)S.n : 1.0;
+        sc->nfac = sums[0] > 0.0 ? sums[0] : 1.0;
+        sc->res0 = sums[0] / sc->nfac;
+        sc->res = sc->res0;
+        sc->iter = 0;
+        sc->singular = 0;
+        sc->rho = 1.0e20;
+        sc->converged = 0;
+        sc->active = sums[0] > 0.0 ? 1 : 0;
+        break;
+    default:
+        break;
+    }
+}
+
+// ---------------------------------------------------------------- row kernel
+template <typename V, RowOp OP, bool PB>
+__global__ void __launch_bounds__(kBlock) k_rows(const SysDev* __restrict__ Ss, const int2* __restrict__ tiles,
+                                                 int ntiles)
+{
+    constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
+                           OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32);
+    constexpr bool kNeedActive = !(OP == OP_SCATTER || OP == OP_SUMX || OP == OP_INIT_RES ||
+                                   OP == OP_AMUL || OP == OP_TMUL || OP == OP_DIAG_RD ||
+                                   OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
+    __shared__ double sh[(kBlock / 32) * kMaxRed];
+    __shared__ int s_last;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const SysDev& S = Ss[tl.x];
+        if (kNeedActive && !S.sc->active) continue;
+        const int row0 = tl.y * kTileRows;
+        double acc[kMaxRed] = {0.0, 0.0};
+        const Vecs<V>& v = VP<V>::v(S);
+
+        if constexpr (OP == OP_SCATTER) {
+            // FP64 views (+ FP32 copies when allocated); one warp per slice.
+            const bool asym = S.aT_val != S.a_val;
+            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
+                const int e0 = S.a_sptr[sl], e1 = S.a_sptr[sl + 1];
+                const int i = sl * 32 + lane;
+                double d = i < S.n ? S.raw_diag[S.perm[i]] : 0.0;
+                S.diag[i] = d;
+                if (S.diag32) S.diag32[i] = (float)d;
+                double s = d;
+                for (int e = e0 + lane; e < e1; e += 32) {
+                    const int sc = S.a_src[e];
+                    const double a = sc < 0 ? 0.0 : src_val(S, sc, false);
+                    S.a_val[e] = a;
+                    if (S.a_val32) S.a_val32[e] = (float)a;
+                    if (asym) {
+                        const double at = sc < 0 ? 0.0 : src_val(S, sc, true);
+                        S.aT_val[e] = at;
+                        if (S.aT_val32) S.aT_val32[e] = (float)at;
+                    }
+                    if (sc >= 0) s = __dadd_rn(s, a);
+                }
+                S.sumA[i] = s;
+            }
+        } else if constexpr (OP == OP_SUMX) {
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) acc[0] += (double)v.x[i];
+        } else if constexpr (OP == OP_INIT_RES) {
+            const double xbar = S.sc->xsum / (double)S.n;
+            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
+                const int i = sl * 32 + lane;
+                const double ax = ell_row<double>(S, S.a_val, S.diag, S.v64.x, i);
+                const double b = S.v64.b[i];
+                const double tr = __dmul_rn(S.sumA[i], xbar);
+                acc[0] += fabs(ax - tr) + fabs(b - tr);
+                const double r = b - ax;
+                S.v64.r[i] = r;
+                acc[1] += fabs(r);
+                if (PB) {
+                    const double at = ell_row<double>(S, S.aT_val, S.diag, S.v64.x, i);
+                    S.v64.rT[i] = b - at;
+                }
+            }
+        } else if constexpr (OP == OP_RHO) {
+            const V* rr = PB ? v.rT : v.r;
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
+                acc[0] = __fma_rn((double)v.w[i], (double)rr[i], acc[0]);
+        } else if constexpr (OP == OP_PUPDATE) {
+            const int it = S.sc->iter;
+            const V beta = (V)S.sc->beta;
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+                v.p[i] = it == 0 ? v.w[i] : vfma(beta, v.p[i], v.w[i]);
+                if (PB) v.pT[i] = it == 0 ? v.wT[i] : vfma(beta, v.pT[i], v.wT[i]);
+            }
+        } else if constexpr (OP == OP_SPMV_QP) {
+            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
+                const int i = sl * 32 + lane;
+                const V q = ell_row<V>(S, VP<V>::aval(S, false), VP<V>::diag(S), v.p, i);
+                v.q[i] = q;
+                if (PB) {
+                    const V qt = ell_row<V>(S, VP<V>::aval(S, true), VP<V>::diag(S), v.pT, i);
+                    v.qT[i] = qt;
+                    acc[0] = __fma_rn((double)q, (double)v.pT[i], acc[0]);
+                } else {
+                    acc[0] = __fma_rn((double)q, (double)v.p[i], acc[0]);
+                }
+            }
+        } else if constexpr (OP == OP_UPDATE) {
+            const V alpha = (V)S.sc->alpha;
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+                v.x[i] = vfma(alpha, v.p[i], v.x[i]);
+                const V r = vfma(-alpha, v.q[i], v.r[i]);
+                v.r[i] = r;
+                if (PB) v.rT[i] = vfma(-alpha, v.qT[i], v.rT[i]);
+                acc[0] += fabs((double)r);
+            }
+        } else if constexpr (OP == OP_PRECOND_DIAG) {
+            const V* rD = VP<V>::rD(S);
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+                v.w[i] = vmul(rD[i], v.r[i]);
+                if (PB) v.wT[i] = vmul(rD[i], v.rT[i]);
+            }
+        } else if constexpr (OP == OP_PRECOND_NONE) {
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+                v.w[i] = v.r[i];
+                if (PB) v.wT[i] = v.rT[i];
+            }
+        } else if constexpr (OP == OP_DIAG_RD) {
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+                const double r = i < S.n ? __ddiv_rn(1.0, S.diag[i]) : 0.0;
+                S.rD[i] = r;
+                if (S.rD32) S.rD32[i] = (float)r;
+            }
+        } else if constexpr (OP == OP_RESID64) {
+            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
+                const int i = sl * 32 + lane;
+                const double ax = ell_row<double>(S, S.a_val, S.diag, S.v64.x, i);
+                const double r = S.v64.b[i] - ax;
+                S.v64.r[i] = r;
+                acc[0] += fabs(r);
+            }
+        } else if constexpr (OP == OP_TO32) {
+            // s scales the FP64 residual to O(1) per cell before rounding to FP32.
+            const double s = S.sc->osum > 0.0 ? (double)S.n / S.sc->osum : 1.0;
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+                const float r = (float)(S.v64.r[i] * s);
+                S.v32.r[i] = r;
+                S.v32.x[i] = 0.0f;
+                acc[0] += fabs((double)r);
+            }
+        } else if constexpr (OP == OP_CORRECT) {
+            const double s = S.sc->inv_scale;
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
+                S.v64.x[i] = __fma_rn((double)S.v32.x[i], s, S.v64.x[i]);
+        } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
+            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
+                const int i = sl * 32 + lane;
+                S.v64.q[i] = ell_row<double>(S, OP == OP_TMUL ? S.aT_val : S.a_val, S.diag, S.v64.p, i);
+            }
+        }
+
+        if constexpr (kRed) {
+            block_sum<kMaxRed>(acc, sh);
+            if (tid == 0) {
+                S.partials[tl.y * kMaxRed + 0] = acc[0];
+                S.partials[tl.y * kMaxRed + 1] = acc[1];
+                __threadfence();
+                const unsigned prev = atomicAdd(S.counter, 1u);
+                s_last = (prev == (unsigned)S.ntiles - 1u);
+            }
+            __syncthreads();
+            if (s_last) {
+                double tot[kMaxRed] = {0.0, 0.0};
+                for (int k = tid; k < S.ntiles; k += kBlock) {
+                    tot[0] += __ldcg(S.partials + k * kMaxRed + 0);
+                    tot[1] += __ldcg(S.partials + k * kMaxRed + 1);
+                }
+                block_sum<kMaxRed>(tot, sh);
+                if (tid == 0) {
+                    finalize(S, OP, tot);
+                    *S.counter = 0u;
+                    __threadfence();
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <typename V, RowOp OP>
+void launch_one(const SysDev* d, const int2* tiles, int ntiles, int grid, int pb, cudaStream_t st)
+{
+    if (pb)
+        k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(d, tiles, ntiles);
+    else
+        k_rows<V, OP, false><<<grid, kBlock, 0, st>>>(d, tiles, ntiles);
+}
+
+// ---------------------------------------------------------------- factor
+// D_row = diag_row - sum_deps (A[row][dep]*A[dep][row]) / D_dep  (DIC: upper^2,
+// DILU: upper*lower), then rD = 1/D and the sweep coefficients
+// rD_row*A[row][dep] (forward, backward) and rD_row*A[dep][row] (transpose).
+__device__ __forceinline__ void factor_row(const SysDev& S, int c, int lane, Ctl* ctl, int with32)
+{
+    const int r0 = S.chunk_start[c], r1 = S.chunk_start[c + 1];
+    const int i = r0 + lane;
+    if (i >= r1) return;
+    const int F = S.nf;
+    double D = S.diag[i];
+    const int fe0 = S.f_sptr[c], fW = (S.f_sptr[c + 1] - fe0) >> 5;
+    for (int k = 0; k < fW; ++k) {
+        const int e = fe0 + k * 32 + lane;
+        const int col = S.f_col[e];
+        if (col < 0) break;
+        const int sc = S.f_src[e];
+        const double a = src_val(S, sc, false), at = src_val(S, swap_src(sc, F), false);
+        const double Dd = wait_ready(S.D + col, ctl);
+        D = __dsub_rn(D, __ddiv_rn(__dmul_rn(a, at), Dd));
+    }
+    st_relaxed(S.D + i, D);
+    const double rd = __ddiv_rn(1.0, D);
+    S.rD[i] = rd;
+    if (with32) S.rD32[i] = (float)rd;
+    for (int k = 0; k < fW; ++k) {
+        const int e = fe0 + k * 32 + lane;
+        const int sc = S.f_src[e];
+        if (sc < 0) break;
+        const double a = src_val(S, sc, false), at = src_val(S, swap_src(sc, F), false);
+        const double cf = __dmul_rn(rd, a), cfT = __dmul_rn(rd, at);
+        S.f_c[e] = cf;
+        S.f_cT[e] = cfT;
+        if (with32) {
+            S.f_c32[e] = (float)cf;
+            S.f_cT32[e] = (float)cfT;
+        }
+    }
+    const int be0 = S.b_sptr[c], bW = (S.b_sptr[c + 1] - be0) >> 5;
+    for (int k = 0; k < bW; ++k) {
+        const int e = be0 + k * 32 + lane;
+        const int sc = S.b_src[e];
+        if (sc < 0) break;
+        const double a = src_val(S, sc, false), at = src_val(S, swap_src(sc, F), false);
+        const double cb = __dmul_rn(rd, a), cbT = __dmul_rn(rd, at);
+        S.b_c[e] = cb;
+        S.b_cT[e] = cbT;
+        if (with32) {
+            S.b_c32[e] = (float)cb;
+            S.b_cT32[e] = (float)cbT;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_factor(const SysDev* __restrict__ Ss, int nsys, int maxchunks,
+                                                   Ctl* ctl, int with32)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned total = (unsigned)nsys * (unsigned)maxchunks;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->ticket[0], 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
+        const SysDev& S = Ss[s];
+        if (c >= S.nchunks || S.pc < PC_DIC) continue;  // warp-uniform
+        factor_row(S, c, lane, ctl, with32);
+    }
+    // Last warp out resets the work counter for the next launch.
+    if (lane == 0) {
+        const unsigned nw = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[1], 1u) == nw - 1u) {
+            ctl->ticket[0] = 0u;
+            ctl->ticket[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- sweeps
+// Forward:  y_i = rD_i r_i - sum_{deps ascending} (rD_i A[i][d]) y_d
+// Backward: w_i = y_i     - sum_{deps descending} (rD_i A[i][d]) w_d
+// Sync-free variant: one launch covers every level; a warp claims chunks in
+// topological order from a counter and waits (bounded) for each dependency
+// to leave the sentinel state.  The forward sweep re-arms w with sentinels
+// for the backward sweep and vice versa.
+template <typename V, bool FWD>
+__device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, bool syncfree, Ctl* ctl)
+{
+    const int lane = threadIdx.x & 31;
+    const int r0 = S.chunk_start[c], r1 = S.chunk_start[c + 1];
+    const int i = r0 + lane;
+    if (i >= r1) return;
+    const Vecs<V>& v = VP<V>::v(S);
+    V* y = trans ? v.yT : v.y;
+    V* w = trans ? v.wT : v.w;
+    const V* r = trans ? v.rT : v.r;
+    const int* sptr = FWD ? S.f_sptr : S.b_sptr;
+    const int* colp = FWD ? S.f_col : S.b_col;
+    const V* coef = FWD ? VP<V>::fc(S, trans) : VP<V>::bc(S, trans);
+    V* dep = FWD ? y : w;
+    const int e0 = sptr[c], W = (sptr[c + 1] - e0) >> 5;
+    V acc = FWD ? vmul(VP<V>::rD(S)[i], r[i]) : y[i];
+    for (int k = 0; k < W; ++k) {
+        const int e = e0 + k * 32 + lane;
+        const int col = __ldg(colp + e);
+        if (col < 0) break;
+        const V cf = __ldg(coef + e);
+        const V d = syncfree ? wait_ready(dep + col, ctl) : dep[col];
+        acc = vfma(-cf, d, acc);
+    }
+    if (FWD) {
+        if (syncfree) {
+            st_relaxed(y + i, acc);
+            w[i] = sent<V>();
+        } else {
+            y[i] = acc;
+        }
+    } else {
+        if (syncfree) {
+            st_relaxed(w + i, acc);
+            y[i] = sent<V>();
+        } else {
+            w[i] = acc;
+        }
+    }
+}
+
+template <typename V, bool FWD>
+__global__ void __launch_bounds__(kBlock) k_sweep_sf(const SysDev* __restrict__ Ss, int nsys, int maxchunks,
+                                                     Ctl* ctl, int trans)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned total = (unsigned)nsys * (unsigned)maxchunks;
+    const int slot = FWD ? 2 : 4;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->ticket[slot], 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
+        const SysDev& S = Ss[s];
+        if (c >= S.nchunks || !S.sc->active) continue;
+        sweep_chunk<V, FWD>(S, FWD ? c : S.nchunks - 1 - c, trans != 0, true, ctl);
+    }
+    if (lane == 0) {
+        const unsigned nw = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[slot + 1], 1u) == nw - 1u) {
+            ctl->ticket[slot] = 0u;
+            ctl->ticket[slot + 1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+template <typename V, bool FWD>
+__global__ void __launch_bounds__(kBlock) k_sweep_lvl(const SysDev* __restrict__ Ss, int nsys, int level, int trans)
+{
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int s = 0; s < nsys; ++s) {
+        const SysDev& S = Ss[s];
+        if (!S.sc->active || level >= S.nlevels) continue;
+        const int L = FWD ? level : S.nlevels - 1 - level;
+        for (int c = S.lvl_chunk[L] + gw; c < S.lvl_chunk[L + 1]; c += nw)
+            sweep_chunk<V, FWD>(S, c, trans != 0, false, nullptr);
+    }
+}
+
+// ---------------------------------------------------------------- misc
+template <typename V>
+__global__ void k_fill_sent(V* p, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = sent<V>();
+}
+
+template <typename V>
+__global__ void k_iface_gather(const SysDev* __restrict__ Ss, int nsys, int which)
+{
+    for (int s = 0; s < nsys; ++s) {
+        const SysDev& S = Ss[s];
+        if (S.ngen == 0) continue;
+        if ((which == 0 || which == 2) && !S.sc->active) continue;
+        const Vecs<V>& v = VP<V>::v(S);
+        V* x = (which == 0 || which == 3) ? v.p : (which == 1 ? v.x : v.pT);
+        const V* w = VP<V>::gw(S);
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < S.ngen; j += gridDim.x * blockDim.x) {
+            V acc = V(0);
+            for (int k = S.g_ptr[j]; k < S.g_ptr[j + 1]; ++k) acc = vfma(w[k], x[S.g_src[k]], acc);
+            x[S.npad + j] = acc;
+        }
+    }
+}
+
+__global__ void k_permute(const SysDev* __restrict__ Ss, int s, int to_internal, const double* __restrict__ src,
+                          double* __restrict__ dst, int n)
+{
+    const SysDev& S = Ss[s];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int c = S.perm[i];
+        if (to_internal)
+            dst[i] = src[c];
+        else
+            dst[c] = src[i];
+    }
+}
+
+// GGI weighted gather, one thread per (face, component):
+// dst[i*nc + c] = sum_k w_k src[addr_k*nc + c], accumulated from 0 in weight order.
+__global__ void k_ggi(int n_dst, const int32_t* __restrict__ ptr, const int32_t* __restrict__ addr,
+                      const double* __restrict__ w, const double* __restrict__ src, double* __restrict__ dst,
+                      int nc)
+{
+    const long long tot = (long long)n_dst * nc;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / nc), c = (int)(t % nc);
+        double acc = 0.0;
+        for (int k = __ldg(ptr + i); k < __ldg(ptr + i + 1); ++k)
+            acc = __fma_rn(__ldg(w + k), __ldg(src + (size_t)__ldg(addr + k) * nc + c), acc);
+        dst[t] = acc;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+void launch_rows(RowOp op, int precision, const SysDev* d, const int2* tiles, int ntiles, int grid, int pb,
+                 cudaStream_t st)
+{
+    if (ntiles <= 0) return;
+    if (grid > ntiles) grid = ntiles;
+#define MRG_CASE64(OPX) \
+    case OPX: launch_one<double, OPX>(d, tiles, ntiles, grid, pb, st); break;
+#define MRG_CASE32(OPX) \
+    case OPX: launch_one<float, OPX>(d, tiles, ntiles, grid, pb, st); break;
+    if (precision == 0) {
+        switch (op) {
+            MRG_CASE64(OP_SCATTER)
+            MRG_CASE64(OP_SUMX)
+            MRG_CASE64(OP_INIT_RES)
+            MRG_CASE64(OP_RHO)
+            MRG_CASE64(OP_PUPDATE)
+            MRG_CASE64(OP_SPMV_QP)
+            MRG_CASE64(OP_UPDATE)
+            MRG_CASE64(OP_PRECOND_DIAG)
+            MRG_CASE64(OP_PRECOND_NONE)
+            MRG_CASE64(OP_RESID64)
+            MRG_CASE64(OP_TO32)
+            MRG_CASE64(OP_CORRECT)
+            MRG_CASE64(OP_AMUL)
+            MRG_CASE64(OP_TMUL)
+            MRG_CASE64(OP_DIAG_RD)
+        default: break;
+        }
+    } else {
+        switch (op) {
+            MRG_CASE32(OP_RHO)
+            MRG_CASE32(OP_PUPDATE)
+            MRG_CASE32(OP_SPMV_QP)
+            MRG_CASE32(OP_UPDATE)
+            MRG_CASE32(OP_PRECOND_DIAG)
+            MRG_CASE32(OP_PRECOND_NONE)
+        default: break;
+        }
+    }
+#undef MRG_CASE64
+#undef MRG_CASE32
+}
+
+void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st)
+{
+    if (n <= 0) return;
+    int grid = (int)((n + 255) / 256);
+    if (grid > 4096) grid = 4096;
+    if (precision == 0)
+        k_fill_sent<double><<<grid, 256, 0, st>>>((double*)p, n);
+    else
+        k_fill_sent<float><<<grid, 256, 0, st>>>((float*)p, n);
+}
+
+void launch_factor(const SysDev* d, int nsys, int maxchunks, Ctl* ctl, int grid, int with32, cudaStream_t st)
+{
+    k_factor<<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, with32);
+}
+
+void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const SysDev* d, int nsys,
+                  int maxchunks, Ctl* ctl, int grid, cudaStream_t st)
+{
+    if (syncfree) {
+        if (precision == 0) {
+            if (fwd)
+                k_sweep_sf<double, true><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+            else
+                k_sweep_sf<double, false><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+        } else {
+            if (fwd)
+                k_sweep_sf<float, true><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+            else
+                k_sweep_sf<float, false><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+        }
+    } else {
+        if (precision == 0) {
+            if (fwd)
+                k_sweep_lvl<double, true><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+            else
+                k_sweep_lvl<double, false><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+        } else {
+            if (fwd)
+                k_sweep_lvl<float, true><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+            else
+                k_sweep_lvl<float, false><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+        }
+    }
+}
+
+void launch_iface_gather(int precision, int which, const SysDev* d, int nsys, int grid, cudaStream_t st)
+{
+    if (precision == 0)
+        k_iface_gather<double><<<grid, 256, 0, st>>>(d, nsys, which);
+    else
+        k_iface_gather<float><<<grid, 256, 0, st>>>(d, nsys, which);
+}
+
+void launch_permute(int to_internal, const SysDev* d, int s, const double* src, double* dst, int n, cudaStream_t st)
+{
+    int grid = (n + 255) / 256;
+    if (grid > 2048) grid = 2048;
+    if (grid < 1) grid = 1;
+    k_permute<<<grid, 256, 0, st>>>(d, s, to_internal, src, dst, n);
+}
+
+void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double* w, const double* src, double* dst,
+                int ncomp, cudaStream_t st)
+{
+    long long tot = (long long)n_dst * ncomp;
+    if (tot <= 0) return;
+    int grid = (int)((tot + 255) / 256);
+    if (grid > 4096) grid = 4096;
+    k_ggi<<<grid, 256, 0, st>>>(n_dst, ptr, addr, w, src, dst, ncomp);
+}
+
+}  // namespace mrg

@@ -1,0 +1,66 @@
+// kernels.h -- launchers for the sm_103a kernels in kernels.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dev.h"
+
+namespace mrg {
+
+// Row-kernel operations (one tile of 1024 rows per CTA iteration).
+enum RowOp {
+    OP_SCATTER = 0,     // raw coefficients -> internal views (+ sumA)
+    OP_SUMX,            // xsum = sum(x)
+    OP_INIT_RES,        // r = b - A x (rT = b - A^T x), normFactor, initial residual
+    OP_RHO,             // rho = (w, r)  [PBiCG: (w, rT)], beta
+    OP_PUPDATE,         // p = w + beta p  [+ pT]
+    OP_SPMV_QP,         // q = A p [+ qT = A^T pT], (q, p) [PBiCG: (q, pT)], alpha
+    OP_UPDATE,          // x += alpha p, r -= alpha q [+ rT], final residual, convergence
+    OP_PRECOND_DIAG,    // w = rD r  [+ wT]
+    OP_PRECOND_NONE,    // w = r     [+ wT]
+    OP_RESID64,         // mixed: r64 = b - A x (FP64), sum|r64| -> res
+    OP_TO32,            // mixed: r32 = float(s * r64), inner state reset
+    OP_CORRECT,         // mixed: x64 += d32 / s
+    OP_AMUL,            // y = A x (test hook; x in v64.p, y in v64.q)
+    OP_TMUL,            // y = A^T x (test hook)
+    OP_DIAG_RD,         // rD = 1/diag (diagonal preconditioner)
+    OP_COUNT
+};
+
+struct LaunchCfg {
+    int grid_rows;     // CTAs for row kernels
+    int grid_sweep;    // CTAs for sync-free sweeps
+};
+
+// precision: 0 = FP64 vectors/coefficients, 1 = FP32 (mixed inner loop)
+void launch_rows(RowOp op, int precision, const SysDev* d_sys, const int2* d_tiles,
+                 int ntiles, int grid, int pbicg, cudaStream_t st);
+
+// Sentinel fill of a vector (sync-free readiness marker).
+void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st);
+
+// Level-scheduled DIC/DILU factor, sync-free over chunks (forward order).
+// with32: also write FP32 copies of rD and sweep coefficients.
+void launch_factor(const SysDev* d_sys, int nsys, int maxchunks, Ctl* ctl, int grid,
+                   int with32, cudaStream_t st);
+
+// One triangular sweep.  fwd: y = forward(r); else w = backward(y).
+// trans selects DILU's preconditionT coefficients and the T vectors.
+// syncfree=1: all levels in one launch (exact ordering); else one level.
+void launch_sweep(int precision, int fwd, int trans, int syncfree, int level,
+                  const SysDev* d_sys, int nsys, int maxchunks, Ctl* ctl, int grid,
+                  cudaStream_t st);
+
+// GGI gather of the general interface faces: x[npad + j] = sum w x[src]
+// (which: 0 = p, 1 = x, 2 = pT; 0 and 2 skip inactive systems, 3 = p always).
+void launch_iface_gather(int precision, int which, const SysDev* d_sys, int nsys,
+                         int grid, cudaStream_t st);
+
+// Internal <-> caller numbering (FP64).
+void launch_permute(int to_internal, const SysDev* d_sys, int sysidx, const double* src,
+                    double* dst, int n, cudaStream_t st);
+
+// Stand-alone GGI weighted gather (mrg_ggi_apply).
+void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double* w,
+                const double* src, double* dst, int ncomp, cudaStream_t st);
+
+}  // namespace mrg

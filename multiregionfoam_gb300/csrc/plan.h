@@ -1,0 +1,69 @@
+// plan.h -- host-side layout planning for one LDU mesh (addressing only).
+//
+// A plan fixes, for one cell ordering, everything the kernels need that does
+// not depend on the coefficient values:
+//   * the internal row order (perm: internal row -> caller's cell),
+//   * the Amul/Tmul rows as a sliced ELL (32-row slices, column-major inside
+//     a slice) with the entries of every row in ascending foam face order,
+//     followed by the row's interface entries in interface order -- the
+//     accumulation order of lduMatrix::Amul + updateMatrixInterfaces,
+//   * the preconditioner sweep structure: chunks of <= 32 rows that share a
+//     sweep level, and per chunk a sliced ELL of forward dependencies
+//     (ascending face order) and backward dependencies (descending face
+//     order) -- the per-cell order of foam's face-ordered DIC/DILU sweeps,
+//   * the general (non-conformal) interface faces as a GGI gather CSR.
+//
+// Coefficient "source" codes used by the scatter kernels:
+//   s in [0,F)        -> upper[s]            (A[lowerAddr][upperAddr])
+//   s in [F,2F)       -> lower[s-F]          (A[upperAddr][lowerAddr])
+//   s in [2F,2F+NI)   -> -iface_coeff[s-2F]  (bou for Amul, int for Tmul)
+//   s = -1            -> padding
+// The transpose of a face source swaps the two halves.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mrg {
+
+constexpr int kSlice = 32;     // rows per ELL slice (one warp)
+constexpr int kTileRows = 1024; // rows per reduction tile
+
+struct IfaceHost {
+    // Flattened over patches.
+    std::vector<int32_t> cells;  // faceCells
+    std::vector<int32_t> ptr;    // CSR into src/w
+    std::vector<int32_t> src;    // shadow cells
+    std::vector<double> w;       // GGI weights
+    int size() const { return (int)cells.size(); }
+};
+
+struct PlanHost {
+    int n = 0, npad = 0, nf = 0, ni = 0;
+    int ordering = 0;
+    int nlevels = 0, nchunks = 0;
+    int ngen = 0;  // general interface faces (gathered into x[npad + j])
+    std::vector<int32_t> perm, iperm, level_of_row;
+    // Amul sliced ELL: npad/32 slices
+    std::vector<int32_t> a_sptr, a_col, a_src;
+    // sweep chunks
+    std::vector<int32_t> chunk_start;  // [nchunks+1]
+    std::vector<int32_t> lvl_chunk;    // [nlevels+1]
+    std::vector<int32_t> f_sptr, f_col, f_src;  // forward deps, per chunk
+    std::vector<int32_t> b_sptr, b_col, b_src;  // backward deps, per chunk
+    // general interface gather
+    std::vector<int32_t> g_ptr, g_src;
+    std::vector<double> g_w;
+    int max_row_len = 0;
+};
+
+// Validates the addressing; returns "" on success, else a message.
+std::string validate_addressing(int n, int nf, const int32_t* lower,
+                                const int32_t* upper, const IfaceHost& ifc);
+
+// ordering: 0 = exact (level order of foam's face-ordered sweeps),
+//           1 = greedy multi-colour.
+PlanHost build_plan(int n, int nf, const int32_t* lower, const int32_t* upper,
+                    const IfaceHost& ifc, int ordering);
+
+}  // namespace mrg

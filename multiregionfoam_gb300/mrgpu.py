@@ -1,0 +1,262 @@
+"""ctypes binding of libmrgpu (the C ABI in include/mrgpu.h).
+
+This module is the Python-side host mirror of the foam-extend plug-in
+boundary.  It loads the in-tree ``_lib/libmrgpu.so`` and fails loudly when the
+library is missing or no CUDA device is present: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmrgpu.so")
+
+MRG_OK, MRG_E_INVALID, MRG_E_OOM, MRG_E_BREAKDOWN, MRG_E_TIMEOUT, MRG_E_CUDA, MRG_E_BUSY = range(7)
+SOLVERS = {"PCG": 0, "PBiCG": 1}
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+ORDERINGS = {"exact": 0, "colour": 1}
+
+EXPORTED = [
+    "mrg_last_error", "mrg_version", "mrg_controls_default", "mrg_ctx_create", "mrg_ctx_destroy",
+    "mrg_ctx_mem_used", "mrg_host_alloc", "mrg_host_free", "mrg_mesh_upload", "mrg_mesh_destroy",
+    "mrg_mesh_levels", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
+    "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
+    "mrg_ggi_apply", "mrg_ggi_apply_device",
+]
+
+
+class MrgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"mrgpu error {code}: {msg}")
+        self.code = code
+
+
+class Controls(C.Structure):
+    _fields_ = [("tolerance", C.c_double), ("rel_tol", C.c_double), ("min_iter", C.c_int),
+                ("max_iter", C.c_int), ("solver", C.c_int), ("preconditioner", C.c_int),
+                ("precision", C.c_int), ("ordering", C.c_int), ("inner_rel_tol", C.c_double),
+                ("inner_max_iter", C.c_int), ("max_outer", C.c_int), ("iters_per_launch", C.c_int)]
+
+
+class Perf(C.Structure):
+    _fields_ = [("initial_residual", C.c_double), ("final_residual", C.c_double), ("n_iter", C.c_int),
+                ("converged", C.c_int), ("singular", C.c_int), ("status", C.c_int), ("n_outer", C.c_int),
+                ("reserved", C.c_int), ("solve_ms", C.c_double)]
+
+    def as_dict(self):
+        return {"initial_residual": self.initial_residual, "final_residual": self.final_residual,
+                "n_iter": self.n_iter, "converged": bool(self.converged), "singular": bool(self.singular),
+                "status": self.status, "n_outer": self.n_outer, "solve_ms": self.solve_ms}
+
+
+class IfaceDesc(C.Structure):
+    _fields_ = [("n_faces", C.c_int), ("face_cells", C.POINTER(C.c_int32)), ("src_ptr", C.POINTER(C.c_int32)),
+                ("src_cell", C.POINTER(C.c_int32)), ("src_weight", C.POINTER(C.c_double))]
+
+
+_LIB = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libmrgpu; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmrgpu not built ({path}); run __graft_entry__.build()")
+    L = C.CDLL(path)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    L.mrg_last_error.restype = C.c_char_p
+    L.mrg_version.restype = C.c_char_p
+    L.mrg_controls_default.argtypes = [C.POINTER(Controls)]
+    L.mrg_ctx_create.argtypes = [C.c_int, C.c_size_t, C.POINTER(vp)]
+    L.mrg_ctx_destroy.argtypes = [vp]
+    L.mrg_ctx_mem_used.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.mrg_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+    L.mrg_host_free.argtypes = [vp]
+    L.mrg_mesh_upload.argtypes = [vp, C.c_int, C.c_int, ip, ip, C.c_int, C.POINTER(IfaceDesc), C.POINTER(vp)]
+    L.mrg_mesh_destroy.argtypes = [vp]
+    L.mrg_mesh_levels.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.mrg_coeffs_upload.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.mrg_coeffs_upload_device.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.mrg_solve.argtypes = [vp, dp, dp, C.POINTER(Controls), C.POINTER(Perf)]
+    L.mrg_solve_device.argtypes = [vp, vp, vp, C.POINTER(Controls), C.POINTER(Perf)]
+    L.mrg_amul.argtypes = [vp, dp, dp, C.c_int]
+    L.mrg_residual.argtypes = [vp, dp, dp, dp, dp]
+    L.mrg_precondition.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.c_int]
+    L.mrg_factor_diag.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.mrg_ggi_create.argtypes = [vp, C.c_int, C.c_int, ip, ip, dp, C.POINTER(vp)]
+    L.mrg_ggi_destroy.argtypes = [vp]
+    L.mrg_ggi_apply.argtypes = [vp, dp, dp, C.c_int]
+    L.mrg_ggi_apply_device.argtypes = [vp, vp, vp, C.c_int]
+    _LIB = L
+    return L
+
+
+def _check(rc):
+    if rc != MRG_OK:
+        raise MrgError(rc, load().mrg_last_error().decode())
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", precond="DIC",
+             precision="fp64", ordering="exact", inner_rel_tol=1e-4, inner_max_iter=0, max_outer=50,
+             iters_per_launch=16) -> Controls:
+    c = Controls()
+    load().mrg_controls_default(C.byref(c))
+    c.tolerance, c.rel_tol, c.min_iter, c.max_iter = tol, rel_tol, min_iter, max_iter
+    c.solver, c.preconditioner = SOLVERS[solver], PRECONDITIONERS[precond]
+    c.precision, c.ordering = PRECISIONS[precision], ORDERINGS[ordering]
+    c.inner_rel_tol, c.inner_max_iter, c.max_outer = inner_rel_tol, inner_max_iter, max_outer
+    c.iters_per_launch = iters_per_launch
+    return c
+
+
+class Context:
+    """A device context (one CUDA stream, an HBM budget)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        L = load()
+        h = C.c_void_p()
+        _check(L.mrg_ctx_create(device, hbm_budget, C.byref(h)))
+        self.h = h
+        self._meshes = []
+
+    def mem_used(self) -> int:
+        v = C.c_size_t()
+        _check(load().mrg_ctx_mem_used(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        for m in self._meshes:
+            m.close()
+        self._meshes = []
+        if self.h:
+            _check(load().mrg_ctx_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mesh:
+    """Resident LDU addressing (+ interface patches) on the device."""
+
+    def __init__(self, ctx: Context, n, lower, upper, iface=None):
+        L = load()
+        self.ctx = ctx
+        self.n = int(n)
+        self._lower = np.ascontiguousarray(lower, dtype=np.int32)
+        self._upper = np.ascontiguousarray(upper, dtype=np.int32)
+        self.nf = len(self._lower)
+        descs = None
+        nif = 0
+        self.ni = 0
+        if iface is not None and len(iface["cells"]) > 0:
+            self._if = {k: np.ascontiguousarray(iface[k], dtype=np.int32) for k in ("cells", "ptr", "src")}
+            self._if["w"] = np.ascontiguousarray(iface["w"], dtype=np.float64)
+            d = IfaceDesc()
+            d.n_faces = len(self._if["cells"])
+            d.face_cells, d.src_ptr, d.src_cell = _i(self._if["cells"]), _i(self._if["ptr"]), _i(self._if["src"])
+            d.src_weight = _d(self._if["w"])
+            descs = (IfaceDesc * 1)(d)
+            nif = 1
+            self.ni = d.n_faces
+        h = C.c_void_p()
+        _check(L.mrg_mesh_upload(ctx.h, self.n, self.nf, _i(self._lower), _i(self._upper), nif, descs,
+                                 C.byref(h)))
+        self.h = h
+        ctx._meshes.append(self)
+
+    def close(self):
+        if self.h:
+            _check(load().mrg_mesh_destroy(self.h))
+            self.h = None
+
+    def levels(self, ordering="exact") -> int:
+        v = C.c_int()
+        _check(load().mrg_mesh_levels(self.h, ORDERINGS[ordering], C.byref(v)))
+        return v.value
+
+    def upload(self, diag, upper, lower=None, iface_bou=None, iface_int=None):
+        self._c = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None
+                   for a in (diag, upper, lower, iface_bou, iface_int)]
+        _check(load().mrg_coeffs_upload(self.h, *[_d(a) for a in self._c]))
+
+    def solve(self, b, x0, ctl: Controls | None = None, **kw):
+        ctl = ctl if ctl is not None else controls(**kw)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.array(x0, dtype=np.float64, copy=True)
+        p = Perf()
+        _check(load().mrg_solve(self.h, _d(b), _d(x), C.byref(ctl), C.byref(p)))
+        return x, p.as_dict()
+
+    def solve_device(self, d_b: int, d_x: int, ctl: Controls):
+        p = Perf()
+        _check(load().mrg_solve_device(self.h, C.c_void_p(d_b), C.c_void_p(d_x), C.byref(ctl), C.byref(p)))
+        return p.as_dict()
+
+    def amul(self, x, transpose=False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n)
+        _check(load().mrg_amul(self.h, _d(x), _d(y), int(transpose)))
+        return y
+
+    def residual(self, b, x):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        r, nf = C.c_double(), C.c_double()
+        _check(load().mrg_residual(self.h, _d(b), _d(x), C.byref(r), C.byref(nf)))
+        return r.value, nf.value
+
+    def precondition(self, precond, r, transpose=False, ordering="exact"):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        w = np.empty(self.n)
+        _check(load().mrg_precondition(self.h, PRECONDITIONERS[precond], ORDERINGS[ordering], _d(r), _d(w),
+                                       int(transpose)))
+        return w
+
+    def factor_diag(self, precond, ordering="exact"):
+        out = np.empty(self.n)
+        _check(load().mrg_factor_diag(self.h, PRECONDITIONERS[precond], ORDERINGS[ordering], _d(out)))
+        return out
+
+
+class Ggi:
+    """Resident GGI weights: dst[i] = sum_k w_ik src[addr_ik]."""
+
+    def __init__(self, ctx: Context, ptr, addr, w, n_src):
+        self._ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+        self._addr = np.ascontiguousarray(addr, dtype=np.int32)
+        self._w = np.ascontiguousarray(w, dtype=np.float64)
+        self.n_dst = len(self._ptr) - 1
+        self.n_src = int(n_src)
+        h = C.c_void_p()
+        _check(load().mrg_ggi_create(ctx.h, self.n_dst, self.n_src, _i(self._ptr), _i(self._addr), _d(self._w),
+                                     C.byref(h)))
+        self.h = h
+
+    def apply(self, src, ncomp=1):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = np.empty(self.n_dst * ncomp)
+        _check(load().mrg_ggi_apply(self.h, _d(src), _d(dst), int(ncomp)))
+        return dst if ncomp == 1 else dst.reshape(self.n_dst, ncomp)
+
+    def close(self):
+        if self.h:
+            _check(load().mrg_ggi_destroy(self.h))
+            self.h = None

@@ -213,6 +213,30 @@ int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp);
 int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst,
                          int ncomp);
 
+/* ---- device buffers, timing and diagnostics --------------------------
+ * No counterpart in the reference (foam-extend times solves with
+ * cpuTimeIncrement, multiRegionSystem.C:546-650).  They let a caller keep
+ * inputs resident in HBM and time work on the context's own stream. */
+int mrg_dev_alloc(mrg_ctx* ctx, size_t bytes, void** out);
+int mrg_dev_free(mrg_ctx* ctx, void* p);
+/* kind: 0 host->device, 1 device->host, 2 device->device (ctx stream, then
+ * synchronised). */
+int mrg_dev_copy(mrg_ctx* ctx, void* dst, const void* src, size_t bytes, int kind);
+/* Record CUDA event `slot` (0..63) on the context's stream; elapsed time in
+ * ms between two recorded slots (synchronises on the later one). */
+int mrg_event_record(mrg_ctx* ctx, int slot);
+int mrg_event_elapsed(mrg_ctx* ctx, int slot_a, int slot_b, float* ms);
+/* Total kernels this library has launched in this process (graph nodes
+ * counted per graph launch). */
+int mrg_kernel_launches(uint64_t* count);
+/* Time `reps` back-to-back launches of one hot-path kernel on the mesh's
+ * current state (after a solve with the same controls): kernel 0 = Amul +
+ * (q,p) reduction of the Krylov loop in `precision`, 1 = one preconditioner
+ * application (forward + backward sweep).  Returns the mean ms per launch
+ * measured with CUDA events on the context's stream. */
+int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel,
+                    int reps, float* ms_per_launch);
+
 #ifdef __cplusplus
 }
 #endif

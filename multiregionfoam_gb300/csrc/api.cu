@@ -478,6 +478,78 @@ int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp)
     });
 }
 
+int mrg_dev_alloc(mrg_ctx* ctx, size_t bytes, void** out)
+{
+    return guard([&] {
+        if (!ctx || !out) return fail(MRG_E_INVALID, "NULL argument");
+        *out = ctx->c.alloc(bytes);
+        MRG_CUDA(cudaStreamSynchronize(ctx->c.st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dev_free(mrg_ctx* ctx, void* p)
+{
+    return guard([&] {
+        if (!ctx) return fail(MRG_E_INVALID, "NULL context");
+        MRG_CUDA(cudaStreamSynchronize(ctx->c.st));
+        ctx->c.release(p);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dev_copy(mrg_ctx* ctx, void* dst, const void* src, size_t bytes, int kind)
+{
+    return guard([&] {
+        if (!ctx || (bytes && (!dst || !src))) return fail(MRG_E_INVALID, "NULL argument");
+        cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice
+                                     : (kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+        if (kind < 0 || kind > 2) return fail(MRG_E_INVALID, "unknown copy kind");
+        if (bytes) MRG_CUDA(cudaMemcpyAsync(dst, src, bytes, k, ctx->c.st));
+        MRG_CUDA(cudaStreamSynchronize(ctx->c.st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_event_record(mrg_ctx* ctx, int slot)
+{
+    return guard([&] {
+        if (!ctx || slot < 0 || slot >= 64) return fail(MRG_E_INVALID, "bad event slot");
+        cudaEvent_t& e = ctx->c.events[slot];
+        if (!e) MRG_CUDA(cudaEventCreate(&e));
+        MRG_CUDA(cudaEventRecord(e, ctx->c.st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_event_elapsed(mrg_ctx* ctx, int a, int b, float* ms)
+{
+    return guard([&] {
+        if (!ctx || !ms || a < 0 || b < 0 || a >= 64 || b >= 64) return fail(MRG_E_INVALID, "bad argument");
+        if (!ctx->c.events[a] || !ctx->c.events[b]) return fail(MRG_E_INVALID, "event slot not recorded");
+        MRG_CUDA(cudaEventSynchronize(ctx->c.events[b]));
+        MRG_CUDA(cudaEventElapsedTime(ms, ctx->c.events[a], ctx->c.events[b]));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_kernel_launches(uint64_t* count)
+{
+    if (!count) return fail(MRG_E_INVALID, "NULL argument");
+    *count = (uint64_t)launch_count();
+    return MRG_OK;
+}
+
+int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel, int reps, float* ms_per_launch)
+{
+    return guard([&] {
+        if (!mesh || !ms_per_launch) return fail(MRG_E_INVALID, "NULL argument");
+        Controls k = to_controls(controls);
+        *ms_per_launch = time_kernel(mesh->m, k, kernel, reps);
+        return (int)MRG_OK;
+    });
+}
+
 }  // extern "C"
 
 namespace mrg {

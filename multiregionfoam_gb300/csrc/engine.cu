@@ -51,6 +51,8 @@ void Ctx::release(void* p)
 Ctx::~Ctx()
 {
     if (st) cudaStreamSynchronize(st);
+    for (auto& e : events)
+        if (e) cudaEventDestroy(e);
     for (auto& kv : allocs) cudaFree(kv.first);
     allocs.clear();
     if (st) cudaStreamDestroy(st);
@@ -67,7 +69,7 @@ static T* upload(Ctx* c, const std::vector<T>& v)
 // ------------------------------------------------------------------ PlanState
 PlanState::~PlanState()
 {
-    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     // device memory is owned by ctx allocations and freed with the mesh
 }
 
@@ -357,7 +359,7 @@ static void record_iteration(PlanState& P, const Controls& cfg, int prec, cudaSt
     launch_rows(OP_UPDATE, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
 }
 
-static cudaGraphExec_t iteration_graph(PlanState& P, const Controls& cfg, int prec, int k)
+static PlanState::Graph iteration_graph(PlanState& P, const Controls& cfg, int prec, int k)
 {
     std::string key = std::to_string(cfg.solver) + "/" + std::to_string(cfg.pc) + "/" +
                       std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k);
@@ -365,15 +367,19 @@ static cudaGraphExec_t iteration_graph(PlanState& P, const Controls& cfg, int pr
     if (it != P.graphs.end()) return it->second;
     cudaStream_t st = P.ctx->st;
     cudaGraph_t g = nullptr;
+    const unsigned long long before = launch_count();
     MRG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < k; ++i) record_iteration(P, cfg, prec, st);
     cudaError_t e = cudaStreamEndCapture(st, &g);
+    const long long nodes = (long long)(launch_count() - before);
+    add_launches(-nodes);  // captured, not executed
     MRG_CUDA(e);
     cudaGraphExec_t ex = nullptr;
     MRG_CUDA(cudaGraphInstantiate(&ex, g, 0));
     cudaGraphDestroy(g);
-    P.graphs[key] = ex;
-    return ex;
+    PlanState::Graph gr{ex, nodes};
+    P.graphs[key] = gr;
+    return gr;
 }
 
 struct Poll {
@@ -406,12 +412,13 @@ static void run_iterations(PlanState& P, const Controls& cfg, int prec, int max_
 {
     Ctx* c = P.ctx;
     const int k = std::max(1, cfg.k_launch);
-    cudaGraphExec_t ex = iteration_graph(P, cfg, prec, k);
+    PlanState::Graph gr = iteration_graph(P, cfg, prec, k);
     poll(P, h);
     long launches = 0;
     const long cap = (long)max_iter / k + 2 + (long)cfg.min_iter / k;
     while (h->sc.active && launches <= cap) {
-        MRG_CUDA(cudaGraphLaunch(ex, c->st));
+        MRG_CUDA(cudaGraphLaunch(gr.exec, c->st));
+        add_launches(gr.nodes);
         ++launches;
         poll(P, h);
     }
@@ -612,6 +619,44 @@ void factor_diag_device(Mesh& m, int pc, int ordering, double* d_rD)
     MRG_CUDA(cudaGetLastError());
     Poll* h = pinned_poll();
     poll(P, h);
+}
+
+float time_kernel(Mesh& m, const Controls& cfg, int kernel, int reps)
+{
+    if (reps < 1) throw Error(MRG_E_INVALID, "reps must be >= 1");
+    if (kernel < 0 || kernel > 1) throw Error(MRG_E_INVALID, "unknown kernel id");
+    PlanState& P = prepare(m, cfg);
+    Ctx* c = m.ctx;
+    const int prec = cfg.precision;
+    const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    int one = 1;
+    MRG_CUDA(cudaMemcpyAsync((char*)P.sys.sc + offsetof(Scal, active), &one, sizeof one, cudaMemcpyHostToDevice,
+                             c->st));
+    if (kernel == 1 && cfg.pc >= PC_DIC && cfg.ordering == MRG_ORDER_EXACT) init_sentinels(P, cfg, prec);
+    auto once = [&] {
+        if (kernel == 0)
+            launch_rows(OP_SPMV_QP, prec, P.d_sys, P.d_tiles, P.ntiles, grid_rows(c, P.ntiles), pb, c->st);
+        else
+            record_precondition(P, cfg, prec, 0, c->st);
+    };
+    once();  // warm-up
+    cudaEvent_t e0, e1;
+    MRG_CUDA(cudaEventCreate(&e0));
+    MRG_CUDA(cudaEventCreate(&e1));
+    MRG_CUDA(cudaEventRecord(e0, c->st));
+    for (int i = 0; i < reps; ++i) once();
+    MRG_CUDA(cudaEventRecord(e1, c->st));
+    MRG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int zero = 0;
+    MRG_CUDA(cudaMemcpyAsync((char*)P.sys.sc + offsetof(Scal, active), &zero, sizeof zero, cudaMemcpyHostToDevice,
+                             c->st));
+    MRG_CUDA(cudaStreamSynchronize(c->st));
+    MRG_CUDA(cudaGetLastError());
+    return ms / reps;
 }
 
 }  // namespace mrg

@@ -29,6 +29,7 @@ struct Ctx {
     size_t budget = 0, used = 0;
     std::map<void*, size_t> allocs;
     Ctl* d_ctl = nullptr;
+    cudaEvent_t events[64] = {};
     void* alloc(size_t bytes);
     void release(void* p);
     ~Ctx();
@@ -54,7 +55,11 @@ struct PlanState {
     uint64_t factored = 0;    // coefficient version factored
     int factored_pc = -1;
     bool factored32 = false;
-    std::map<std::string, cudaGraphExec_t> graphs;
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        long long nodes = 0;  // kernels per replay (for the launch counter)
+    };
+    std::map<std::string, Graph> graphs;
     ~PlanState();
     void sync_sys();  // copy host mirror to device
 };
@@ -107,5 +112,8 @@ void amul_device(Mesh& m, const double* d_x, double* d_y, int transpose);
 void residual_device(Mesh& m, const double* d_b, const double* d_x, double* res, double* nfac);
 void precondition_device(Mesh& m, int pc, int ordering, const double* d_r, double* d_w, int transpose);
 void factor_diag_device(Mesh& m, int pc, int ordering, double* d_rD);
+// Mean ms per launch of one hot-path kernel (0: Amul + (q,p); 1: one
+// preconditioner application) on the current state.
+float time_kernel(Mesh& m, const Controls& c, int kernel, int reps);
 
 }  // namespace mrg

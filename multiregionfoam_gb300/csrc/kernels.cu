@@ -15,6 +15,7 @@
 // on padding.  Everything else is HBM- or latency-bound: no tensor cores.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "kernels.h"
@@ -644,11 +645,16 @@ __global__ void k_ggi(int n_dst, const int32_t* __restrict__ ptr, const int32_t*
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
+static std::atomic<unsigned long long> g_launches{0};
+unsigned long long launch_count() { return g_launches.load(); }
+void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }
+
 void launch_rows(RowOp op, int precision, const SysDev* d, const int2* tiles, int ntiles, int grid, int pb,
                  cudaStream_t st)
 {
     if (ntiles <= 0) return;
     if (grid > ntiles) grid = ntiles;
+    ++g_launches;
 #define MRG_CASE64(OPX) \
     case OPX: launch_one<double, OPX>(d, tiles, ntiles, grid, pb, st); break;
 #define MRG_CASE32(OPX) \
@@ -690,6 +696,7 @@ void launch_rows(RowOp op, int precision, const SysDev* d, const int2* tiles, in
 void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st)
 {
     if (n <= 0) return;
+    ++g_launches;
     int grid = (int)((n + 255) / 256);
     if (grid > 4096) grid = 4096;
     if (precision == 0)
@@ -700,12 +707,14 @@ void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st)
 
 void launch_factor(const SysDev* d, int nsys, int maxchunks, Ctl* ctl, int grid, int with32, cudaStream_t st)
 {
+    ++g_launches;
     k_factor<<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, with32);
 }
 
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const SysDev* d, int nsys,
                   int maxchunks, Ctl* ctl, int grid, cudaStream_t st)
 {
+    ++g_launches;
     if (syncfree) {
         if (precision == 0) {
             if (fwd)
@@ -735,6 +744,7 @@ void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, co
 
 void launch_iface_gather(int precision, int which, const SysDev* d, int nsys, int grid, cudaStream_t st)
 {
+    ++g_launches;
     if (precision == 0)
         k_iface_gather<double><<<grid, 256, 0, st>>>(d, nsys, which);
     else
@@ -743,6 +753,7 @@ void launch_iface_gather(int precision, int which, const SysDev* d, int nsys, in
 
 void launch_permute(int to_internal, const SysDev* d, int s, const double* src, double* dst, int n, cudaStream_t st)
 {
+    ++g_launches;
     int grid = (n + 255) / 256;
     if (grid > 2048) grid = 2048;
     if (grid < 1) grid = 1;
@@ -754,6 +765,7 @@ void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double
 {
     long long tot = (long long)n_dst * ncomp;
     if (tot <= 0) return;
+    ++g_launches;
     int grid = (int)((tot + 255) / 256);
     if (grid > 4096) grid = 4096;
     k_ggi<<<grid, 256, 0, st>>>(n_dst, ptr, addr, w, src, dst, ncomp);

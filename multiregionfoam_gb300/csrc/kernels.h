@@ -63,4 +63,9 @@ void launch_permute(int to_internal, const SysDev* d_sys, int sysidx, const doub
 void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double* w,
                 const double* src, double* dst, int ncomp, cudaStream_t st);
 
+// Kernels launched so far in this process (captured launches included;
+// the engine corrects for graph capture and replay).
+unsigned long long launch_count();
+void add_launches(long long d);
+
 }  // namespace mrg

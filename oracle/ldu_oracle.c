@@ -425,6 +425,175 @@ int or_pbicg(const or_ldu* m, const double* b, double* x, double tol,
     return 0;
 }
 
+/* ---- GPU reduction-order mirror ----------------------------------------
+ * The solvers above sum sequentially, as a serial foam run does.  The GPU
+ * library sums in a fixed tree instead: rows are renumbered into sweep-level
+ * order (level = 1 + max level of the lower neighbours, stable by cell),
+ * padded to tiles of 1024 rows; in each tile 256 threads accumulate their
+ * rows, a warp-shuffle tree and an 8-warp tree combine them, and the tile
+ * partials are summed per thread (stride 256) and tree-combined again.
+ * or_solve_mirror repeats the fused-mode solve with exactly that order, so
+ * the GPU's whole solve can be checked bit for bit.  Not foam semantics:
+ * a cross-check of the GPU's arithmetic only. */
+
+#define MR_TILE 1024
+#define MR_BLOCK 256
+
+typedef struct {
+    int n, npad;
+    int32_t* perm; /* internal -> cell */
+} mr_order;
+
+static void mr_order_init(const or_ldu* m, mr_order* o)
+{
+    int n = m->n;
+    int32_t* lvl = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+    int maxl = 0;
+    for (int f = 0; f < m->nf; ++f) { /* faces ascending: owner levels final */
+        int u = m->upper[f], l = m->lower[f];
+        if (lvl[l] + 1 > lvl[u]) lvl[u] = lvl[l] + 1;
+    }
+    for (int c = 0; c < n; ++c) if (lvl[c] > maxl) maxl = lvl[c];
+    int32_t* cnt = (int32_t*)calloc((size_t)maxl + 2, sizeof(int32_t));
+    for (int c = 0; c < n; ++c) cnt[lvl[c] + 1]++;
+    for (int k = 0; k <= maxl; ++k) cnt[k + 1] += cnt[k];
+    o->perm = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    for (int c = 0; c < n; ++c) o->perm[cnt[lvl[c]]++] = c;
+    o->n = n;
+    o->npad = ((n + MR_TILE - 1) / MR_TILE) * MR_TILE;
+    free(cnt);
+    free(lvl);
+}
+
+/* warp_sum of 32 lane values as __shfl_down_sync(16,8,4,2,1) leaves lane 0 */
+static double mr_warp(double* v)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        for (int i = 0; i < o; ++i) v[i] = v[i] + v[i + o];
+    return v[0];
+}
+
+static double mr_block(const double* acc /* [256] */)
+{
+    double sh[8], v[32];
+    for (int w = 0; w < 8; ++w) {
+        for (int l = 0; l < 32; ++l) v[l] = acc[w * 32 + l];
+        sh[w] = mr_warp(v);
+    }
+    for (int l = 0; l < 32; ++l) v[l] = l < 8 ? sh[l] : 0.0;
+    return mr_warp(v);
+}
+
+/* Row handled by thread t in its k-th step of tile `tile`.
+ * assign 0: elementwise (row0 + t + 256k); 1: sliced (warp = slice owner). */
+static int mr_row(int tile, int t, int k, int assign)
+{
+    int row0 = tile * MR_TILE;
+    if (assign == 0) return row0 + t + MR_BLOCK * k;
+    int w = t >> 5, lane = t & 31;
+    return ((row0 >> 5) + w + 8 * k) * 32 + lane;
+}
+
+/* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order) */
+static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)
+{
+    int ntiles = o->npad / MR_TILE;
+    double* part = (double*)malloc(sizeof(double) * (size_t)(ntiles ? ntiles : 1));
+    double acc[MR_BLOCK];
+    for (int tile = 0; tile < ntiles; ++tile) {
+        for (int t = 0; t < MR_BLOCK; ++t) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                int i = mr_row(tile, t, k, assign);
+                double av = 0.0, bv = 0.0;
+                if (i < o->n) {
+                    av = a[o->perm[i]];
+                    if (kind == 0) bv = b[o->perm[i]];
+                }
+                s = kind == 0 ? fma(av, bv, s) : s + av;
+            }
+            acc[t] = s;
+        }
+        part[tile] = mr_block(acc);
+    }
+    for (int t = 0; t < MR_BLOCK; ++t) {
+        double s = 0.0;
+        for (int k = t; k < ntiles; k += MR_BLOCK) s += part[k];
+        acc[t] = s;
+    }
+    free(part);
+    return mr_block(acc);
+}
+
+int or_solve_mirror(const or_ldu* m, const double* b, double* x, double tol,
+                    double rel_tol, int min_iter, int max_iter, int precon,
+                    int pbicg, or_perf* perf)
+{
+    int n = m->n;
+    size_t bytes = sizeof(double) * (size_t)(n ? n : 1);
+    double *wA = (double*)malloc(bytes), *rA = (double*)malloc(bytes), *pA = (double*)malloc(bytes);
+    double *wT = (double*)malloc(bytes), *rT = (double*)malloc(bytes), *pT = (double*)malloc(bytes);
+    double* t = (double*)malloc(bytes);
+    mr_order o;
+    mr_order_init(m, &o);
+    memset(perf, 0, sizeof(*perf));
+
+    or_amul(m, x, wA, 1);
+    if (pbicg) or_tmul(m, x, wT, 1);
+    double xbar = mr_reduce(&o, 0, 1, x, NULL) / (double)n;
+    or_sumA(m, t);
+    for (int c = 0; c < n; ++c) {
+        double tr = t[c] * xbar;
+        t[c] = fabs(wA[c] - tr) + fabs(b[c] - tr);
+        rA[c] = b[c] - wA[c];
+        if (pbicg) rT[c] = b[c] - wT[c];
+        wA[c] = fabs(rA[c]);
+    }
+    double nfac = mr_reduce(&o, 1, 1, t, NULL) + OR_SMALL;
+    perf->initial_residual = mr_reduce(&o, 1, 1, wA, NULL) / nfac;
+    perf->final_residual = perf->initial_residual;
+
+    if (min_iter > 0 || !check_convergence(perf, tol, rel_tol)) {
+        or_precon pc;
+        precon_init(&pc, m, precon);
+        double rho = OR_GREAT, rho_old;
+        do {
+            rho_old = rho;
+            precon_apply(&pc, m, rA, wA, 0, 1);
+            if (pbicg) precon_apply(&pc, m, rT, wT, 1, 1);
+            rho = mr_reduce(&o, 0, 0, wA, pbicg ? rT : rA);
+            if (perf->n_iter == 0) {
+                memcpy(pA, wA, bytes);
+                if (pbicg) memcpy(pT, wT, bytes);
+            } else {
+                double beta = rho / rho_old;
+                for (int c = 0; c < n; ++c) {
+                    pA[c] = fma(beta, pA[c], wA[c]);
+                    if (pbicg) pT[c] = fma(beta, pT[c], wT[c]);
+                }
+            }
+            or_amul(m, pA, wA, 1);
+            if (pbicg) or_tmul(m, pT, wT, 1);
+            double qp = mr_reduce(&o, 1, 0, wA, pbicg ? pT : pA);
+            if (fabs(qp) / nfac < OR_VSMALL) { perf->singular = 1; break; }
+            double alpha = rho / qp;
+            for (int c = 0; c < n; ++c) {
+                x[c] = fma(alpha, pA[c], x[c]);
+                rA[c] = fma(-alpha, wA[c], rA[c]);
+                if (pbicg) rT[c] = fma(-alpha, wT[c], rT[c]);
+                t[c] = fabs(rA[c]);
+            }
+            perf->final_residual = mr_reduce(&o, 0, 1, t, NULL) / nfac;
+            perf->n_iter++;
+        } while ((perf->n_iter < max_iter &&
+                  !check_convergence(perf, tol, rel_tol)) ||
+                 perf->n_iter < min_iter);
+        free(pc.rD);
+    }
+    free(wA); free(rA); free(pA); free(wT); free(rT); free(pT); free(t); free(o.perm);
+    return 0;
+}
+
 /* Foam-normalised residual of a given x (initial-residual formula). */
 double or_residual(const or_ldu* m, const double* b, const double* x)
 {

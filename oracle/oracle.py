@@ -51,7 +51,7 @@ def lib():
         L.or_dic_factor.argtypes = [pldu, dp]
         L.or_dilu_factor.argtypes = [pldu, dp]
         L.or_precondition.argtypes = [pldu, C.c_int, dp, dp, C.c_int, C.c_int]
-        for fn in (L.or_pcg, L.or_pbicg):
+        for fn in (L.or_pcg, L.or_pbicg, L.or_solve_mirror):
             fn.argtypes = [pldu, dp, dp, C.c_double, C.c_double, C.c_int, C.c_int,
                            C.c_int, C.c_int, C.POINTER(_Perf)]
         L.or_ggi_apply.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_int]
@@ -183,6 +183,20 @@ class OracleMatrix:
         fn = lib().or_pcg if solver == "PCG" else lib().or_pbicg
         fn(C.byref(self._s), _d(b), _d(x), tol, rel_tol, int(min_iter), int(max_iter),
            PRECONDITIONERS[precond], int(fused), C.byref(p))
+        return x, {"initial_residual": p.initial_residual, "final_residual": p.final_residual,
+                   "n_iter": p.n_iter, "converged": bool(p.converged), "singular": bool(p.singular)}
+
+    def solve_mirror(self, b, x0, solver="PCG", precond="DIC", tol=1e-8, rel_tol=0.0,
+                     min_iter=0, max_iter=1000):
+        """Fused-mode solve that sums in the GPU library's reduction tree.
+
+        Not foam semantics: it exists so the GPU's whole solve can be
+        compared bit for bit (see or_solve_mirror in ldu_oracle.c)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.array(x0, dtype=np.float64, copy=True)
+        p = _Perf()
+        lib().or_solve_mirror(C.byref(self._s), _d(b), _d(x), tol, rel_tol, int(min_iter), int(max_iter),
+                              PRECONDITIONERS[precond], int(solver == "PBiCG"), C.byref(p))
         return x, {"initial_residual": p.initial_residual, "final_residual": p.final_residual,
                    "n_iter": p.n_iter, "converged": bool(p.converged), "singular": bool(p.singular)}
 

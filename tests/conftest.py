@@ -47,6 +47,18 @@ def golden_small():
     return dict(np.load(os.path.join(GOLDEN, "oracle_small.npz")))
 
 
+def golden_system(g, name):
+    """Rebuild a golden system from its stored input arrays."""
+    from multiregionfoam_gb300 import cases
+    iface = None
+    if f"{name}_iface_cells" in g:
+        iface = {k: g[f"{name}_iface_{k}"] for k in ("cells", "bou", "ptr", "src", "w")}
+        iface["int"] = None
+    return cases.LduSystem(int(g[f"{name}_n"]), g[f"{name}_lower"], g[f"{name}_upper"], g[f"{name}_diag"],
+                           g[f"{name}_upper_c"], g.get(f"{name}_lower_c"), g[f"{name}_b"], g[f"{name}_x0"],
+                           iface, name=name)
+
+
 def oracle_matrix(O, s):
     return O.OracleMatrix(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.iface)
 

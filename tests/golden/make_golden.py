@@ -110,6 +110,17 @@ def oracle_fixture():
         "cd": cases.convdiff_system(10, 9, 8, seed=5),
     }
     for name, s in systems.items():
+        # inputs are stored too: numpy's exp/log may differ by an ulp across
+        # hosts, so tests rebuild the systems from these arrays, not from seeds
+        out[f"{name}_n"] = np.int64(s.n)
+        out[f"{name}_lower"], out[f"{name}_upper"] = s.lower, s.upper
+        out[f"{name}_diag"], out[f"{name}_upper_c"] = s.diag, s.upper_c
+        out[f"{name}_b"], out[f"{name}_x0"] = s.b, s.x0
+        if s.lower_c is not None:
+            out[f"{name}_lower_c"] = s.lower_c
+        if s.iface is not None:
+            for k in ("cells", "bou", "ptr", "src", "w"):
+                out[f"{name}_iface_{k}"] = s.iface[k]
         M = O.OracleMatrix(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.iface)
         rng = np.random.default_rng(99)
         xr = rng.standard_normal(s.n)
@@ -124,6 +135,14 @@ def oracle_fixture():
         x, perf = M.solve(s.b, s.x0, solver, kind, tol=1e-10)
         out[f"{name}_sol"] = x
         out[f"{name}_perf"] = np.array([perf["initial_residual"], perf["final_residual"], perf["n_iter"]])
+        # GPU-arithmetic mirrors (fused products, GPU reduction tree): the GPU
+        # must reproduce these bit for bit from the stored inputs
+        out[f"{name}_amul_fused"] = M.amul(xr, fused=True)
+        out[f"{name}_tmul_fused"] = M.tmul(xr, fused=True)
+        out[f"{name}_prec_fused"] = M.precondition(kind, xr, fused=True)
+        xm, pm = M.solve_mirror(s.b, s.x0, solver, kind, tol=1e-10)
+        out[f"{name}_sol_mirror"] = xm
+        out[f"{name}_perf_mirror"] = np.array([pm["initial_residual"], pm["final_residual"], pm["n_iter"]])
     np.savez_compressed(os.path.join(HERE, "oracle_small.npz"), **out)
     print("wrote oracle_small.npz", len(out), "arrays")
 

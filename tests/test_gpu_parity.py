@@ -82,17 +82,51 @@ def test_diagonal_and_none_preconditioners(mrg, ctx, oracle_mod):
 
 
 def check_solve(mrg, ctx, O, s, solver, pc, tol=1e-8, **kw):
+    """GPU solve vs the oracle.
+
+    * vs the GPU-order mirror (same IEEE operations, same reduction tree):
+      bit-identical solution, residuals and iteration count;
+    * vs foam's sequential-sum arithmetic: same iteration count, solution and
+      initial residual within 1e-10 relative, final residual within 1e-10 of
+      the initial residual (a converged residual is ~tol x the initial one,
+      so summation order alone moves it by ~1e-16/tol relative).
+    """
     A = oracle_matrix(O, s)
     xo, po = A.solve(s.b, s.x0, solver, pc, tol=tol, **kw)
+    xm, pm = A.solve_mirror(s.b, s.x0, solver, pc, tol=tol, **kw)
     m = gpu_mesh(mrg, ctx, s)
     xg, pg = m.solve(s.b, s.x0, tol=tol, solver=solver, precond=pc, **kw)
     m.close()
+    assert np.array_equal(xg, xm), rel_err(xg, xm)
+    assert (pg["initial_residual"], pg["final_residual"], pg["n_iter"]) == \
+        (pm["initial_residual"], pm["final_residual"], pm["n_iter"])
     assert pg["n_iter"] == po["n_iter"], (pg, po)
     assert pg["converged"] == po["converged"]
     assert abs(pg["initial_residual"] - po["initial_residual"]) <= REL * po["initial_residual"]
-    assert abs(pg["final_residual"] - po["final_residual"]) <= REL * max(po["final_residual"], 1e-300) + 1e-300
+    assert abs(pg["final_residual"] - po["final_residual"]) <= REL * po["initial_residual"]
     assert rel_err(xg, xo) <= REL, rel_err(xg, xo)
     return xg, pg, po
+
+
+def test_golden_fixtures_bitexact(mrg, ctx, golden_small):
+    """Vectors computed on the CPU (x86) and committed are reproduced bit for bit."""
+    from conftest import golden_system
+    g = golden_small
+    for name in ("cht", "chtc", "cd"):
+        s = golden_system(g, name)
+        m = gpu_mesh(mrg, ctx, s)
+        x = g[f"{name}_x"]
+        assert np.array_equal(m.amul(x), g[f"{name}_amul_fused"]), name
+        assert np.array_equal(m.amul(x, transpose=True), g[f"{name}_tmul_fused"]), name
+        kind = "DIC" if s.symmetric else "DILU"
+        solver = "PCG" if s.symmetric else "PBiCG"
+        assert np.array_equal(m.factor_diag(kind), g[f"{name}_rD"]), name
+        assert np.array_equal(m.precondition(kind, x), g[f"{name}_prec_fused"]), name
+        xs, p = m.solve(s.b, s.x0, tol=1e-10, solver=solver, precond=kind)
+        assert np.array_equal(xs, g[f"{name}_sol_mirror"]), name
+        assert [p["initial_residual"], p["final_residual"], p["n_iter"]] == g[f"{name}_perf_mirror"].tolist()
+        assert rel_err(xs, g[f"{name}_sol"]) <= REL
+        m.close()
 
 
 def test_pcg_dic_c1_plain_method(mrg, ctx, oracle_mod):

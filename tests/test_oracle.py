@@ -120,11 +120,10 @@ def test_maxiter_and_miniter(oracle_mod):
 
 
 def test_golden_regression(oracle_mod, golden_small):
+    from conftest import golden_system
     g = golden_small
-    systems = {"cht": cases.cht_system(12, 10, 8, 5, seed=11, form="global"),
-               "chtc": cases.cht_system(12, 10, 8, 5, seed=11, form="coupled"),
-               "cd": cases.convdiff_system(10, 9, 8, seed=5)}
-    for name, s in systems.items():
+    for name in ("cht", "chtc", "cd"):
+        s = golden_system(g, name)
         A = oracle_matrix(oracle_mod, s)
         x = g[f"{name}_x"]
         assert np.array_equal(A.amul(x), g[f"{name}_amul"]), name
@@ -133,6 +132,24 @@ def test_golden_regression(oracle_mod, golden_small):
         kind = "DIC" if s.symmetric else "DILU"
         assert np.array_equal(A.factor(kind), g[f"{name}_rD"]), name
         assert np.array_equal(A.precondition(kind, x), g[f"{name}_prec"]), name
+        solver = "PCG" if s.symmetric else "PBiCG"
+        xs, p = A.solve(s.b, s.x0, solver, kind, tol=1e-10)
+        assert np.array_equal(xs, g[f"{name}_sol"]), name
+        assert [p["initial_residual"], p["final_residual"], p["n_iter"]] == g[f"{name}_perf"].tolist()
+
+
+def test_mirror_mode_close_to_foam_order(oracle_mod, golden_small):
+    """The GPU-order mirror differs from foam's sequential sums only by rounding."""
+    from conftest import golden_system
+    for name in ("cht", "chtc", "cd"):
+        s = golden_system(golden_small, name)
+        A = oracle_matrix(oracle_mod, s)
+        solver, kind = ("PCG", "DIC") if s.symmetric else ("PBiCG", "DILU")
+        x1, p1 = A.solve(s.b, s.x0, solver, kind, tol=1e-10)
+        x2, p2 = A.solve_mirror(s.b, s.x0, solver, kind, tol=1e-10)
+        assert p1["n_iter"] == p2["n_iter"]
+        assert np.abs(x1 - x2).max() <= 1e-12 * np.abs(x1).max()
+        assert abs(p1["final_residual"] - p2["final_residual"]) <= 1e-12 * p1["initial_residual"]
 
 
 def test_real_mesh_directmap_and_solve(oracle_mod, fohp):

@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Coupled solves/s at 1e-8 relative residual on one GB300.
+
+Workload (BASELINE configuration "plain vs mixed-precision on GPU"): a
+two-region conjugate-heat-transfer temperature system, fluid 128^3 over solid
+128x128x64 (n = 3,145,728 cells, 9,371,648 faces incl. the 16,384-face
+interface), conductivity log-uniform in [0.1, 50] per cell (seeded), in
+monolithic LDU form.  One step = one solve to foam-normalised residual 1e-8
+(relTol 0): coefficient upload (views + DIC factor) and the Krylov solve.
+
+  value   mixed form (FP32 PCG + multi-colour DIC inside FP64 iterative
+          refinement) with coefficients, b and x0 already resident in HBM
+  e2e     the same through the host-pointer C ABI (mrg_coeffs_upload +
+          mrg_solve from pinned host memory; copies inside the timed region)
+  plain   the plain method, FP64 PCG+DIC in foam's order, reported beside
+
+The working set (~1 GB per solve) is far larger than the 129 MB L2, so no
+L2 flush is needed between steps.
+
+--impl reference times the reference algorithm's CPU implementation (the
+project's C oracle; foam-extend itself cannot be built here) on bounded
+samples of the same solve.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TOL = 1e-8
+SEED = 0
+
+
+def peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(name):
+    """dram bytes per launch from a committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_system(rank, scale):
+    from multiregionfoam_gb300 import cases
+    return cases.c2(form="global", seed=SEED + rank, scale=scale)
+
+
+def cpu_oracle_rate(s, iters_full, sample_iters, reps=1):
+    """Oracle PCG+DIC (single thread) on the full system: setup + per-iteration
+    cost measured on a bounded number of iterations, extrapolated to the
+    iteration count the solve needs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    A = O.OracleMatrix(s.n, s.lower, s.upper, s.diag, s.upper_c, None, None)
+    t1 = []
+    t2 = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        A.solve(s.b, s.x0, "PCG", "DIC", tol=0.0, max_iter=1)
+        t1.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        A.solve(s.b, s.x0, "PCG", "DIC", tol=0.0, max_iter=1 + sample_iters)
+        t2.append(time.perf_counter() - t)
+    a, b = min(t1), min(t2)
+    per_iter = (b - a) / sample_iters
+    setup = max(a - per_iter, 0.0)
+    solve_s = setup + iters_full * per_iter
+    return 1.0 / solve_s, solve_s, per_iter, a + b
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    s = make_system(0, args.scale)
+    iters_full = args.ref_iters
+    vals = []
+    tot_cpu = 0.0
+    for k in range(args.warmup + args.steps):
+        rate, solve_s, per_iter, spent = cpu_oracle_rate(s, iters_full, args.ref_sample)
+        tot_cpu += spent
+        if k >= args.warmup:
+            vals.append(rate)
+    v = float(np.median(vals))
+    sample = (f"oracle PCG+DIC FP64 on the full {s.n}-cell system: 1 and 1+{args.ref_sample} iterations "
+              f"timed per step, extrapolated to {iters_full} iterations (the plain method's count at 1e-8)")
+    line = {"metric": "coupled solves/s at 1e-8 rel. residual", "value": v, "unit": "solves/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded C2 system)",
+            "config": {"workload": "cht-2region-128^3+128x128x64", "n_cells": s.n, "n_faces": s.nf,
+                       "tolerance": TOL},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    from multiregionfoam_gb300 import _build, mrgpu
+    rank, world, local, dist = dist_setup(args.gpus)
+    _build.build()
+    L = mrgpu.load()
+    s = make_system(rank, args.scale)
+    n, nf = s.n, s.nf
+    ctx = mrgpu.Context(local)
+    mesh = mrgpu.Mesh(ctx, n, s.lower, s.upper)
+    d_diag, d_up = ctx.to_device(s.diag), ctx.to_device(s.upper_c)
+    d_b, d_x0 = ctx.to_device(s.b), ctx.to_device(s.x0)
+    d_x = ctx.dev_alloc(8 * n)
+    mixed = mrgpu.controls(tol=TOL, max_iter=20000, solver="PCG", precond="DIC", precision="mixed",
+                           ordering="colour", inner_rel_tol=args.inner_tol)
+    plain = mrgpu.controls(tol=TOL, max_iter=20000, solver="PCG", precond="DIC", precision="fp64",
+                           ordering="exact")
+
+    def step(ctl):
+        mesh.upload_device(d_diag, d_up)
+        ctx.copy_d2d(d_x, d_x0, 8 * n)
+        return mesh.solve_device(d_b, d_x, ctl)
+
+    def timed(ctl, k, slot0):
+        barrier(dist)
+        ctx.record(slot0)
+        perfs = []
+        for i in range(k):
+            perfs.append(step(ctl))
+            ctx.record(slot0 + 1 + i)
+        tot = ctx.elapsed_ms(slot0, slot0 + k)
+        per = [ctx.elapsed_ms(slot0 + i, slot0 + i + 1) for i in range(k)]
+        return tot, per, perfs
+
+    for _ in range(args.warmup):
+        step(mixed)
+    for _ in range(min(args.warmup, 2)):
+        step(plain)
+
+    clocks = Clocks(local)
+    l0 = mrgpu.kernel_launches()
+    tot_mixed, per_mixed, perf_mixed = timed(mixed, args.steps, 0)
+    launches = mrgpu.kernel_launches() - l0
+    x_mixed = ctx.from_device(d_x, np.empty(n))
+    k_plain = max(1, min(args.steps, args.plain_steps))
+    tot_plain, per_plain, perf_plain = timed(plain, k_plain, 20)
+    clk = clocks.stop()
+    x_plain = ctx.from_device(d_x, np.empty(n))
+    tot_mixed = max_over_ranks(dist, tot_mixed)
+    tot_plain = max_over_ranks(dist, tot_plain)
+
+    # e2e through the host-pointer ABI from pinned memory
+    h_diag = mrgpu.host_array(None, n); h_diag[:] = s.diag
+    h_up = mrgpu.host_array(None, nf); h_up[:] = s.upper_c
+    h_b = mrgpu.host_array(None, n); h_b[:] = s.b
+    h_x = mrgpu.host_array(None, n)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    perf = mrgpu.Perf()
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        h_x[:] = s.x0
+        barrier(dist)
+        ctx.record(40)
+        mrgpu._check(L.mrg_coeffs_upload(mesh.h, dp(h_diag), dp(h_up), None, None, None))
+        mrgpu._check(L.mrg_solve(mesh.h, dp(h_b), dp(h_x), C.byref(mixed), C.byref(perf)))
+        ctx.record(41)
+        if i >= args.warmup:
+            e2e_ms.append(ctx.elapsed_ms(40, 41))
+    e2e_tot = max_over_ranks(dist, float(np.sum(e2e_ms)))
+
+    # dominant-kernel roofline: Amul + (q,p) of the FP32 inner loop
+    peak, peak_kind = peaks()
+    step(mixed)
+    ms_spmv32 = mesh.time_kernel(mixed, 0, 50)
+    ms_prec32 = mesh.time_kernel(mixed, 1, 20)
+    step(plain)
+    ms_spmv64 = mesh.time_kernel(plain, 0, 50)
+    ms_prec64 = mesh.time_kernel(plain, 1, 5)
+    bytes32 = 12 * n + 12 * nf          # FP32 values, int32 addressing (sym)
+    bytes64 = 24 * n + 16 * nf
+    ach32 = bytes32 / (ms_spmv32 * 1e-3) / 1e9
+    ach64 = bytes64 / (ms_spmv64 * 1e-3) / 1e9
+    traffic = profile_traffic("spmv_fp32_c2.txt")
+
+    if rank != 0:
+        return
+    k = args.steps
+    value = world * k / (tot_mixed * 1e-3)
+    plain_rate = world * k_plain / (tot_plain * 1e-3)
+    err = float(np.abs(x_mixed - x_plain).max() / np.abs(x_plain).max())
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        rate, solve_s, per_iter, spent = cpu_oracle_rate(s, perf_plain[-1]["n_iter"], args.ref_sample)
+        cpu = {"value": rate, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle PCG+DIC FP64, full system, 1 and 1+{args.ref_sample} iterations timed, "
+                         f"extrapolated to {perf_plain[-1]['n_iter']} iterations ({solve_s:.1f} s/solve)"}
+    pm = perf_mixed[-1]
+    pp = perf_plain[-1]
+    line = {
+        "metric": "coupled solves/s at 1e-8 rel. residual", "value": value, "unit": "solves/s",
+        "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": tot_mixed / k,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64",
+        "data": "synthetic (seeded C2 system)",
+        "config": {"workload": "cht-2region-128^3+128x128x64", "n_cells": n, "n_faces": nf,
+                   "tolerance": TOL, "form": "mixed FP32 PCG + colour DIC inside FP64 refinement",
+                   "l2": "inputs larger than L2 (~1 GB working set)", "parallelism": f"replicas x{world}"},
+        "p50_ms": float(np.percentile(per_mixed, 50)), "p99_ms": float(np.percentile(per_mixed, 99)),
+        "mixed": {"iters": pm["n_iter"], "outer": pm["n_outer"], "final_residual": pm["final_residual"],
+                  "converged": pm["converged"], "rel_err_vs_fp64": err},
+        "plain_fp64": {"value": plain_rate, "unit": "solves/s", "ms_per_step": tot_plain / k_plain,
+                       "iters": pp["n_iter"], "final_residual": pp["final_residual"],
+                       "p50_ms": float(np.percentile(per_plain, 50)), "p99_ms": float(np.percentile(per_plain, 99)),
+                       "steps": k_plain},
+        "speedup_mixed_vs_plain": value / plain_rate,
+        "e2e": {"value": world * k / (e2e_tot * 1e-3), "unit": "solves/s",
+                "h2d_bytes_per_step": 8 * (n + nf) + 16 * n, "d2h_bytes_per_step": 8 * n,
+                "p99_ms": float(np.percentile(e2e_ms, 99))},
+        "roofline": {"kernel": "Amul+(q,p) FP32 (mixed inner loop)", "bound": "hbm", "achieved": ach32,
+                     "peak": peak, "unit": "GB/s", "frac": ach32 / peak, "traffic": traffic,
+                     "algorithmic_bytes": bytes32, "ms_per_launch": ms_spmv32, "peak_source": peak_kind},
+        "kernels": {"spmv_fp64": {"ms": ms_spmv64, "GB/s": ach64, "frac": ach64 / peak},
+                    "precondition_fp32_colour_ms": ms_prec32, "precondition_fp64_exact_ms": ms_prec64},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=1, help="divide the mesh dimensions (testing only)")
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--ref-sample", type=int, default=40)
+    ap.add_argument("--ref-iters", type=int, default=0, help="reference arm: iterations per solve (0 = measured)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        if args.ref_iters <= 0:
+            args.ref_iters = REF_ITERS
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+# Iterations the plain FP64 PCG+DIC needs on this workload at 1e-8 (identical
+# on CPU and GPU by parity); measured on GB300 and used by the reference arm.
+REF_ITERS = 600
+
+if __name__ == "__main__":
+    main()

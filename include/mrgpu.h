@@ -83,8 +83,10 @@ typedef struct {
     int preconditioner;    /* MRG_PRECOND_*                                 */
     int precision;         /* MRG_PRECISION_*                               */
     int ordering;          /* MRG_ORDER_*                                   */
-    double inner_rel_tol;  /* mixed: inner FP32 residual reduction per outer
-                              step (default 1e-4)                           */
+    double inner_rel_tol;  /* mixed: the most an FP32 inner solve is asked to
+                              reduce its residual per refinement step
+                              (default 1e-5); each step aims at 0.1 x the
+                              residual still to remove, never below this    */
     int inner_max_iter;    /* mixed: inner iterations per outer step (default
                               = max_iter)                                    */
     int max_outer;         /* mixed: refinement steps (default 50)          */

@@ -58,7 +58,7 @@ Controls to_controls(const mrg_controls* c)
     k.pc = c->preconditioner;
     k.precision = c->precision;
     k.ordering = c->ordering;
-    k.inner_rel_tol = c->inner_rel_tol > 0 ? c->inner_rel_tol : 1e-4;
+    k.inner_rel_tol = c->inner_rel_tol > 0 ? c->inner_rel_tol : 1e-5;
     k.inner_max_iter = c->inner_max_iter;
     k.max_outer = c->max_outer > 0 ? c->max_outer : 50;
     k.k_launch = c->iters_per_launch > 0 ? c->iters_per_launch : 16;
@@ -164,7 +164,7 @@ void mrg_controls_default(mrg_controls* c)
     c->preconditioner = MRG_PRECOND_DIC;
     c->precision = MRG_PRECISION_FP64;
     c->ordering = MRG_ORDER_EXACT;
-    c->inner_rel_tol = 1e-4;
+    c->inner_rel_tol = 1e-5;
     c->inner_max_iter = 0;
     c->max_outer = 50;
     c->iters_per_launch = 16;

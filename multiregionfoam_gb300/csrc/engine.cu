@@ -496,7 +496,13 @@ Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
             while ((!conv || inner_total < cfg.min_iter) && outer < cfg.max_outer && inner_total < cfg.max_iter) {
                 if (S.ngen) launch_iface_gather(0, 1, P.d_sys, 1, 64, st);
                 launch_rows(OP_RESID64, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
-                write_controls(P, cfg.inner_rel_tol, 0.0, 0, std::min(inner_max, cfg.max_iter - inner_total));
+                // Each refinement step aims past the target (0.1 x the residual
+                // still to remove) so the last step overshoots instead of
+                // landing just under the tolerance; the FP32 inner solve is not
+                // asked for more than inner_rel_tol per step.
+                const double goal = std::max(cfg.tol, cfg.rel_tol > 1e-20 ? cfg.rel_tol * res0 : 0.0);
+                const double inner_tol = std::min(0.5, std::max(cfg.inner_rel_tol, 0.1 * goal / res));
+                write_controls(P, inner_tol, 0.0, 0, std::min(inner_max, cfg.max_iter - inner_total));
                 launch_rows(OP_TO32, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
                 if (pb) {
                     // transpose residual of the correction system starts equal to r

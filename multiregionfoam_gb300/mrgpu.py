@@ -25,7 +25,8 @@ EXPORTED = [
     "mrg_ctx_mem_used", "mrg_host_alloc", "mrg_host_free", "mrg_mesh_upload", "mrg_mesh_destroy",
     "mrg_mesh_levels", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
     "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
-    "mrg_ggi_apply", "mrg_ggi_apply_device",
+    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
+    "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
 ]
 
 
@@ -93,6 +94,13 @@ def load(path: str = LIB_PATH):
     L.mrg_ggi_destroy.argtypes = [vp]
     L.mrg_ggi_apply.argtypes = [vp, dp, dp, C.c_int]
     L.mrg_ggi_apply_device.argtypes = [vp, vp, vp, C.c_int]
+    L.mrg_dev_alloc.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
+    L.mrg_dev_free.argtypes = [vp, vp]
+    L.mrg_dev_copy.argtypes = [vp, vp, vp, C.c_size_t, C.c_int]
+    L.mrg_event_record.argtypes = [vp, C.c_int]
+    L.mrg_event_elapsed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
+    L.mrg_kernel_launches.argtypes = [C.POINTER(C.c_uint64)]
+    L.mrg_time_kernel.argtypes = [vp, C.POINTER(Controls), C.c_int, C.c_int, C.POINTER(C.c_float)]
     _LIB = L
     return L
 
@@ -111,7 +119,7 @@ def _i(a):
 
 
 def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", precond="DIC",
-             precision="fp64", ordering="exact", inner_rel_tol=1e-4, inner_max_iter=0, max_outer=50,
+             precision="fp64", ordering="exact", inner_rel_tol=1e-5, inner_max_iter=0, max_outer=50,
              iters_per_launch=16) -> Controls:
     c = Controls()
     load().mrg_controls_default(C.byref(c))
@@ -137,6 +145,51 @@ class Context:
         v = C.c_size_t()
         _check(load().mrg_ctx_mem_used(self.h, C.byref(v)))
         return v.value
+
+    # -- resident buffers and device timing (no foam counterpart) ----------
+    def dev_alloc(self, nbytes: int) -> int:
+        p = C.c_void_p()
+        _check(load().mrg_dev_alloc(self.h, nbytes, C.byref(p)))
+        return p.value
+
+    def dev_free(self, p: int):
+        _check(load().mrg_dev_free(self.h, C.c_void_p(p)))
+
+    def to_device(self, arr: np.ndarray) -> int:
+        arr = np.ascontiguousarray(arr)
+        p = self.dev_alloc(arr.nbytes)
+        _check(load().mrg_dev_copy(self.h, C.c_void_p(p), arr.ctypes.data_as(C.c_void_p), arr.nbytes, 0))
+        return p
+
+    def from_device(self, p: int, out: np.ndarray) -> np.ndarray:
+        _check(load().mrg_dev_copy(self.h, out.ctypes.data_as(C.c_void_p), C.c_void_p(p), out.nbytes, 1))
+        return out
+
+    def copy_d2d(self, dst: int, src: int, nbytes: int):
+        _check(load().mrg_dev_copy(self.h, C.c_void_p(dst), C.c_void_p(src), nbytes, 2))
+
+    def record(self, slot: int):
+        _check(load().mrg_event_record(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        v = C.c_float()
+        _check(load().mrg_event_elapsed(self.h, a, b, C.byref(v)))
+        return v.value
+
+
+def kernel_launches() -> int:
+    v = C.c_uint64()
+    _check(load().mrg_kernel_launches(C.byref(v)))
+    return v.value
+
+
+def host_array(ctx_unused, n: int, dtype=np.float64) -> np.ndarray:
+    """A numpy array over pinned (page-locked) host memory."""
+    nbytes = int(n) * np.dtype(dtype).itemsize
+    p = C.c_void_p()
+    _check(load().mrg_host_alloc(nbytes, C.byref(p)))
+    buf = (C.c_char * nbytes).from_address(p.value)
+    return np.frombuffer(buf, dtype=dtype, count=int(n))  # lives until process exit
 
     def close(self):
         for m in self._meshes:
@@ -229,6 +282,16 @@ class Mesh:
         _check(load().mrg_precondition(self.h, PRECONDITIONERS[precond], ORDERINGS[ordering], _d(r), _d(w),
                                        int(transpose)))
         return w
+
+    def upload_device(self, d_diag, d_upper, d_lower=None, d_ibou=None, d_iint=None):
+        vp = lambda p: None if p is None else C.c_void_p(p)
+        _check(load().mrg_coeffs_upload_device(self.h, vp(d_diag), vp(d_upper), vp(d_lower), vp(d_ibou),
+                                               vp(d_iint)))
+
+    def time_kernel(self, ctl: Controls, kernel: int, reps: int) -> float:
+        v = C.c_float()
+        _check(load().mrg_time_kernel(self.h, C.byref(ctl), kernel, reps, C.byref(v)))
+        return v.value
 
     def factor_diag(self, precond, ordering="exact"):
         out = np.empty(self.n)

@@ -329,9 +329,12 @@ static void record_precondition(PlanState& P, const Controls& cfg, int prec, int
             launch_sweep(prec, 1, trans, 1, 0, P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), st);
             launch_sweep(prec, 0, trans, 1, 0, P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), st);
         } else {
+            // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if nl == 1)
             const int g = std::max(1, std::min(grid_sweep(c), (S.nchunks + 7) / 8));
-            for (int L = 0; L < S.nlevels; ++L) launch_sweep(prec, 1, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
-            for (int L = 0; L < S.nlevels; ++L) launch_sweep(prec, 0, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
+            const int nl = S.nlevels;
+            for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
+            for (int L = std::max(nl - 2, 0); L >= 0; --L)
+                launch_sweep(prec, 0, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
         }
     }
 }

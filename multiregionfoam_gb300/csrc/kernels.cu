@@ -153,19 +153,40 @@ template <> struct VP<float> {
 };
 
 // Sliced-ELL row product y_i = diag_i x_i + sum_k a_k x[col_k] (foam order).
+// All column indices of the row are loaded first, then every coefficient and
+// gathered x, then the FMA chain runs: the loads of one row are in flight
+// together instead of one dependent round trip per entry.  Padding (col -1)
+// is skipped, so no FP64 work is spent on it.
+constexpr int kMaxW = 8;
+constexpr int kRedGrid = 1024;  // CTAs of a reducing row kernel (fixes the sum order)
+
 template <typename V>
 __device__ __forceinline__ V ell_row(const SysDev& S, const V* __restrict__ val, const V* __restrict__ dg,
                                      const V* __restrict__ x, int i)
 {
     const int sl = i >> 5, lane = i & 31;
-    const int e0 = S.a_sptr[sl], W = (S.a_sptr[sl + 1] - e0) >> 5;
-    V y = vmul(dg[i], x[i]);
+    const int e0 = __ldg(S.a_sptr + sl), W = (__ldg(S.a_sptr + sl + 1) - e0) >> 5;
     const int* __restrict__ col = S.a_col + e0 + lane;
     const V* __restrict__ v = val + e0 + lane;
-    for (int k = 0; k < W; ++k) {
-        const int c = __ldg(col + k * 32);
-        if (c < 0) break;
-        y = vfma(__ldg(v + k * 32), x[c], y);
+    V y = vmul(__ldg(dg + i), __ldg(x + i));
+    if (W <= kMaxW) {
+        int c[kMaxW];
+        V a[kMaxW], xv[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) c[k] = k < W ? __ldg(col + k * 32) : -1;
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            a[k] = c[k] >= 0 ? __ldg(v + k * 32) : V(0);
+            xv[k] = c[k] >= 0 ? __ldg(x + c[k]) : V(0);
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k)
+            if (c[k] >= 0) y = vfma(a[k], xv[k], y);
+    } else {
+        for (int k = 0; k < W; ++k) {
+            const int ck = __ldg(col + k * 32);
+            if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldg(x + ck), y);
+        }
     }
     return y;
 }
@@ -236,27 +257,15 @@ __device__ void finalize(const SysDev& S, RowOp op, const double* sums)
 }
 
 // ---------------------------------------------------------------- row kernel
+// One 1024-row tile of a row operation.  Elementwise ops give thread t the
+// rows row0 + t + 256k; ELL ops give warp w the slices row0/32 + w + 8k.
+// Reductions accumulate into acc (FP64) in that row order.
 template <typename V, RowOp OP, bool PB>
-__global__ void __launch_bounds__(kBlock) k_rows(const SysDev* __restrict__ Ss, const int2* __restrict__ tiles,
-                                                 int ntiles)
+__device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&acc)[kMaxRed])
 {
-    constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
-                           OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32);
-    constexpr bool kNeedActive = !(OP == OP_SCATTER || OP == OP_SUMX || OP == OP_INIT_RES ||
-                                   OP == OP_AMUL || OP == OP_TMUL || OP == OP_DIAG_RD ||
-                                   OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
-    __shared__ double sh[(kBlock / 32) * kMaxRed];
-    __shared__ int s_last;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int2 tl = tiles[t];
-        const SysDev& S = Ss[tl.x];
-        if (kNeedActive && !S.sc->active) continue;
-        const int row0 = tl.y * kTileRows;
-        double acc[kMaxRed] = {0.0, 0.0};
-        const Vecs<V>& v = VP<V>::v(S);
-
+    const Vecs<V>& v = VP<V>::v(S);
+    {
         if constexpr (OP == OP_SCATTER) {
             // FP64 views (+ FP32 copies when allocated); one warp per slice.
             const bool asym = S.aT_val != S.a_val;
@@ -377,37 +386,101 @@ __global__ void __launch_bounds__(kBlock) k_rows(const SysDev* __restrict__ Ss, 
             }
         }
 
-        if constexpr (kRed) {
-            block_sum<kMaxRed>(acc, sh);
-            if (tid == 0) {
-                S.partials[tl.y * kMaxRed + 0] = acc[0];
-                S.partials[tl.y * kMaxRed + 1] = acc[1];
-                __threadfence();
-                const unsigned prev = atomicAdd(S.counter, 1u);
-                s_last = (prev == (unsigned)S.ntiles - 1u);
-            }
-            __syncthreads();
-            if (s_last) {
-                double tot[kMaxRed] = {0.0, 0.0};
-                for (int k = tid; k < S.ntiles; k += kBlock) {
-                    tot[0] += __ldcg(S.partials + k * kMaxRed + 0);
-                    tot[1] += __ldcg(S.partials + k * kMaxRed + 1);
-                }
-                block_sum<kMaxRed>(tot, sh);
-                if (tid == 0) {
-                    finalize(S, OP, tot);
-                    *S.counter = 0u;
-                    __threadfence();
-                }
-            }
-            __syncthreads();
+    }
+}
+
+template <RowOp OP>
+struct OpTraits {
+    static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
+                                  OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32);
+    static constexpr bool kNeedActive = !(OP == OP_SCATTER || OP == OP_SUMX || OP == OP_INIT_RES ||
+                                          OP == OP_AMUL || OP == OP_TMUL || OP == OP_DIAG_RD ||
+                                          OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
+};
+
+// Close one reduction segment (consecutive tiles [first, first+count) of one
+// system handled by this CTA): block tree, partial into slot `first`, and the
+// CTA that completes the system's tile count sums every slot in slot order
+// (unused slots hold zero) and finalises.  Deterministic for a given tile
+// table and grid size.
+template <RowOp OP>
+__device__ __forceinline__ void flush_segment(const SysDev& S, int first, int count, double (&acc)[kMaxRed],
+                                              double* sh, int* s_last)
+{
+    const int tid = threadIdx.x;
+    block_sum<kMaxRed>(acc, sh);
+    if (tid == 0) {
+        S.partials[first * kMaxRed + 0] = acc[0];
+        S.partials[first * kMaxRed + 1] = acc[1];
+        __threadfence();
+        const unsigned prev = atomicAdd(S.counter, (unsigned)count);
+        *s_last = (prev + (unsigned)count == (unsigned)S.ntiles);
+    }
+    __syncthreads();
+    if (*s_last) {
+        double tot[kMaxRed] = {0.0, 0.0};
+        for (int k = tid; k < S.ntiles; k += kBlock) {
+            tot[0] += __ldcg(S.partials + k * kMaxRed + 0);
+            tot[1] += __ldcg(S.partials + k * kMaxRed + 1);
+            S.partials[k * kMaxRed + 0] = 0.0;
+            S.partials[k * kMaxRed + 1] = 0.0;
         }
+        block_sum<kMaxRed>(tot, sh);
+        if (tid == 0) {
+            finalize(S, OP, tot);
+            *S.counter = 0u;
+            __threadfence();
+        }
+    }
+    __syncthreads();
+}
+
+// Row kernel.  Non-reducing ops: grid-stride over tiles.  Reducing ops: CTA b
+// owns the contiguous tiles [b*T/G, (b+1)*T/G) of the tile table (G =
+// gridDim.x, at most kRedGrid) and accumulates across them, so the
+// fence/atomic/tree cost is paid once per CTA and system, not per tile.
+template <typename V, RowOp OP, bool PB>
+__global__ void __launch_bounds__(kBlock) k_rows(const SysDev* __restrict__ Ss, const int2* __restrict__ tiles,
+                                                 int ntiles)
+{
+    __shared__ double sh[(kBlock / 32) * kMaxRed];
+    __shared__ int s_last;
+    if constexpr (!OpTraits<OP>::kRed) {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int2 tl = tiles[t];
+            const SysDev& S = Ss[tl.x];
+            if (OpTraits<OP>::kNeedActive && !S.sc->active) continue;
+            double acc[kMaxRed] = {0.0, 0.0};
+            tile_body<V, OP, PB>(S, tl.y * kTileRows, acc);
+        }
+    } else {
+        const int G = gridDim.x;
+        const int t0 = (int)((long long)blockIdx.x * ntiles / G);
+        const int t1 = (int)((long long)(blockIdx.x + 1) * ntiles / G);
+        int cur = -1, first = 0, count = 0;
+        bool live = false;
+        double acc[kMaxRed] = {0.0, 0.0};
+        for (int t = t0; t < t1; ++t) {
+            const int2 tl = tiles[t];
+            if (tl.x != cur) {
+                if (live) flush_segment<OP>(Ss[cur], first, count, acc, sh, &s_last);
+                cur = tl.x;
+                first = tl.y;
+                count = 0;
+                acc[0] = acc[1] = 0.0;
+                live = !OpTraits<OP>::kNeedActive || Ss[cur].sc->active;
+            }
+            ++count;
+            if (live) tile_body<V, OP, PB>(Ss[cur], tl.y * kTileRows, acc);
+        }
+        if (live) flush_segment<OP>(Ss[cur], first, count, acc, sh, &s_last);
     }
 }
 
 template <typename V, RowOp OP>
 void launch_one(const SysDev* d, const int2* tiles, int ntiles, int grid, int pb, cudaStream_t st)
 {
+    if (OpTraits<OP>::kRed) grid = ntiles < kRedGrid ? ntiles : kRedGrid;
     if (pb)
         k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(d, tiles, ntiles);
     else
@@ -498,12 +571,22 @@ __global__ void __launch_bounds__(kBlock) k_factor(const SysDev* __restrict__ Ss
 // ---------------------------------------------------------------- sweeps
 // Forward:  y_i = rD_i r_i - sum_{deps ascending} (rD_i A[i][d]) y_d
 // Backward: w_i = y_i     - sum_{deps descending} (rD_i A[i][d]) w_d
-// Sync-free variant: one launch covers every level; a warp claims chunks in
-// topological order from a counter and waits (bounded) for each dependency
-// to leave the sentinel state.  The forward sweep re-arms w with sentinels
-// for the backward sweep and vice versa.
+// The dependency indices and coefficients of a row are loaded before any
+// dependency value is read, so only the dependency values sit on the
+// critical path.
+//
+// Sync-free variant (exact ordering): one launch covers every level; a warp
+// claims chunks in topological order from a counter and waits (bounded) for
+// each dependency to leave the sentinel state.  The forward sweep re-arms w
+// with sentinels for the backward sweep and vice versa.
+//
+// Level variant (colour ordering): one launch per level, plain loads.  Level
+// 0 is never stored (its forward value rD r is recomputed where needed) and
+// the last level writes w directly (it has no backward dependencies), so a
+// two-colour sweep is two launches: forward level 1, backward level 0.
 template <typename V, bool FWD>
-__device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, bool syncfree, Ctl* ctl)
+__device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, bool syncfree, Ctl* ctl,
+                                            int lvl0_end, bool last_level, bool first_level)
 {
     const int lane = threadIdx.x & 31;
     const int r0 = S.chunk_start[c], r1 = S.chunk_start[c + 1];
@@ -513,34 +596,71 @@ __device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, 
     V* y = trans ? v.yT : v.y;
     V* w = trans ? v.wT : v.w;
     const V* r = trans ? v.rT : v.r;
+    const V* rD = VP<V>::rD(S);
     const int* sptr = FWD ? S.f_sptr : S.b_sptr;
     const int* colp = FWD ? S.f_col : S.b_col;
     const V* coef = FWD ? VP<V>::fc(S, trans) : VP<V>::bc(S, trans);
     V* dep = FWD ? y : w;
     const int e0 = sptr[c], W = (sptr[c + 1] - e0) >> 5;
-    V acc = FWD ? vmul(VP<V>::rD(S)[i], r[i]) : y[i];
-    for (int k = 0; k < W; ++k) {
-        const int e = e0 + k * 32 + lane;
-        const int col = __ldg(colp + e);
-        if (col < 0) break;
-        const V cf = __ldg(coef + e);
-        const V d = syncfree ? wait_ready(dep + col, ctl) : dep[col];
-        acc = vfma(-cf, d, acc);
-    }
-    if (FWD) {
+    V acc;
+    if (FWD || (!syncfree && first_level))
+        acc = vmul(rD[i], r[i]);
+    else
+        acc = y[i];
+    if (W <= kMaxW) {
+        int col[kMaxW];
+        V cf[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) col[k] = k < W ? __ldg(colp + e0 + k * 32 + lane) : -1;
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) cf[k] = col[k] >= 0 ? __ldg(coef + e0 + k * 32 + lane) : V(0);
         if (syncfree) {
+#pragma unroll
+            for (int k = 0; k < kMaxW; ++k)
+                if (col[k] >= 0) acc = vfma(-cf[k], wait_ready(dep + col[k], ctl), acc);
+        } else {
+            V d[kMaxW];
+#pragma unroll
+            for (int k = 0; k < kMaxW; ++k) {
+                const int ck = col[k];
+                if (FWD)
+                    d[k] = ck < 0 ? V(0) : (ck < lvl0_end ? vmul(rD[ck], r[ck]) : dep[ck]);
+                else
+                    d[k] = ck < 0 ? V(0) : dep[ck];
+            }
+#pragma unroll
+            for (int k = 0; k < kMaxW; ++k)
+                if (col[k] >= 0) acc = vfma(-cf[k], d[k], acc);
+        }
+    } else {
+        for (int k = 0; k < W; ++k) {
+            const int e = e0 + k * 32 + lane;
+            const int ck = __ldg(colp + e);
+            if (ck < 0) break;
+            const V cfk = __ldg(coef + e);
+            V d;
+            if (syncfree)
+                d = wait_ready(dep + ck, ctl);
+            else if (FWD && ck < lvl0_end)
+                d = vmul(rD[ck], r[ck]);
+            else
+                d = dep[ck];
+            acc = vfma(-cfk, d, acc);
+        }
+    }
+    if (syncfree) {
+        if (FWD) {
             st_relaxed(y + i, acc);
             w[i] = sent<V>();
         } else {
-            y[i] = acc;
-        }
-    } else {
-        if (syncfree) {
             st_relaxed(w + i, acc);
             y[i] = sent<V>();
-        } else {
-            w[i] = acc;
         }
+    } else {
+        if (FWD && !last_level)
+            y[i] = acc;
+        else
+            w[i] = acc;
     }
 }
 
@@ -559,7 +679,7 @@ __global__ void __launch_bounds__(kBlock) k_sweep_sf(const SysDev* __restrict__ 
         const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
         const SysDev& S = Ss[s];
         if (c >= S.nchunks || !S.sc->active) continue;
-        sweep_chunk<V, FWD>(S, FWD ? c : S.nchunks - 1 - c, trans != 0, true, ctl);
+        sweep_chunk<V, FWD>(S, FWD ? c : S.nchunks - 1 - c, trans != 0, true, ctl, 0, false, false);
     }
     if (lane == 0) {
         const unsigned nw = gridDim.x * (blockDim.x / 32);
@@ -572,17 +692,23 @@ __global__ void __launch_bounds__(kBlock) k_sweep_sf(const SysDev* __restrict__ 
     }
 }
 
+// One level L of a levelled sweep for every system that has it: forward
+// levels 1..nlevels-1, backward levels nlevels-2..0 (level 0 alone when
+// nlevels == 1).
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock) k_sweep_lvl(const SysDev* __restrict__ Ss, int nsys, int level, int trans)
+__global__ void __launch_bounds__(kBlock) k_sweep_lvl(const SysDev* __restrict__ Ss, int nsys, int L, int trans)
 {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int s = 0; s < nsys; ++s) {
         const SysDev& S = Ss[s];
-        if (!S.sc->active || level >= S.nlevels) continue;
-        const int L = FWD ? level : S.nlevels - 1 - level;
+        const int nl = S.nlevels;
+        if (!S.sc->active) continue;
+        if (FWD ? (L < 1 || L > nl - 1) : !(L <= nl - 2 || (nl == 1 && L == 0))) continue;
+        const int lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
+        const bool last = L == nl - 1, first = L == 0;
         for (int c = S.lvl_chunk[L] + gw; c < S.lvl_chunk[L + 1]; c += nw)
-            sweep_chunk<V, FWD>(S, c, trans != 0, false, nullptr);
+            sweep_chunk<V, FWD>(S, c, trans != 0, false, nullptr, lvl0_end, last, first);
     }
 }
 

@@ -494,27 +494,37 @@ static int mr_row(int tile, int t, int k, int assign)
     return ((row0 >> 5) + w + 8 * k) * 32 + lane;
 }
 
-/* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order) */
+#define MR_GRID 1024
+
+/* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order).
+ * CTA g of G = min(tiles, 1024) owns tiles [g*T/G, (g+1)*T/G) and keeps
+ * accumulating across them; its tree sum lands in the slot of its first tile
+ * (the other slots stay zero). */
 static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)
 {
     int ntiles = o->npad / MR_TILE;
-    double* part = (double*)malloc(sizeof(double) * (size_t)(ntiles ? ntiles : 1));
+    int G = ntiles < MR_GRID ? ntiles : MR_GRID;
+    double* part = (double*)calloc((size_t)(ntiles ? ntiles : 1), sizeof(double));
     double acc[MR_BLOCK];
-    for (int tile = 0; tile < ntiles; ++tile) {
-        for (int t = 0; t < MR_BLOCK; ++t) {
-            double s = 0.0;
-            for (int k = 0; k < 4; ++k) {
-                int i = mr_row(tile, t, k, assign);
-                double av = 0.0, bv = 0.0;
-                if (i < o->n) {
-                    av = a[o->perm[i]];
-                    if (kind == 0) bv = b[o->perm[i]];
+    for (int g = 0; g < G; ++g) {
+        int t0 = (int)((long long)g * ntiles / G), t1 = (int)((long long)(g + 1) * ntiles / G);
+        for (int t = 0; t < MR_BLOCK; ++t) acc[t] = 0.0;
+        for (int tile = t0; tile < t1; ++tile) {
+            for (int t = 0; t < MR_BLOCK; ++t) {
+                double s = acc[t];
+                for (int k = 0; k < 4; ++k) {
+                    int i = mr_row(tile, t, k, assign);
+                    double av = 0.0, bv = 0.0;
+                    if (i < o->n) {
+                        av = a[o->perm[i]];
+                        if (kind == 0) bv = b[o->perm[i]];
+                    }
+                    s = kind == 0 ? fma(av, bv, s) : s + av;
                 }
-                s = kind == 0 ? fma(av, bv, s) : s + av;
+                acc[t] = s;
             }
-            acc[t] = s;
         }
-        part[tile] = mr_block(acc);
+        if (t1 > t0) part[t0] = mr_block(acc);
     }
     for (int t = 0; t < MR_BLOCK; ++t) {
         double s = 0.0;

@@ -38,6 +38,24 @@ template <> __device__ __forceinline__ float sent<float>() { return __uint_as_fl
 __device__ __forceinline__ bool is_sent(double v) { return __double_as_longlong(v) == kSentBits64; }
 __device__ __forceinline__ bool is_sent(float v) { return __float_as_uint(v) == kSentBits32; }
 
+// float -> double on the integer pipe.  GB300 issues FP64 (conversions
+// included) at a small fraction of the FP32 rate, so the FP64 reductions of
+// the FP32 inner loop widen their operands with bit arithmetic: for a normal
+// float the double has the same sign and mantissa and the exponent rebiased
+// by 1023-127; zero, subnormal, inf and NaN take the hardware conversion.
+// The result is exactly (double)f.
+__device__ __forceinline__ double widen(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned long long m = (unsigned long long)(u & 0x007fffffu) << 29;
+    const unsigned long long ex = (unsigned long long)(e + 896u) << 52;
+    return __longlong_as_double((long long)(s | ex | m));
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
 __device__ __forceinline__ double vmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double vfma(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -291,7 +309,7 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
                 S.sumA[i] = s;
             }
         } else if constexpr (OP == OP_SUMX) {
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) acc[0] += (double)v.x[i];
+            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) acc[0] += widen(v.x[i]);
         } else if constexpr (OP == OP_INIT_RES) {
             const double xbar = S.sc->xsum / (double)S.n;
             for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
@@ -311,7 +329,7 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
         } else if constexpr (OP == OP_RHO) {
             const V* rr = PB ? v.rT : v.r;
             for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
-                acc[0] = __fma_rn((double)v.w[i], (double)rr[i], acc[0]);
+                acc[0] = __fma_rn(widen(v.w[i]), widen(rr[i]), acc[0]);
         } else if constexpr (OP == OP_PUPDATE) {
             const int it = S.sc->iter;
             const V beta = (V)S.sc->beta;
@@ -327,9 +345,9 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
                 if (PB) {
                     const V qt = ell_row<V>(S, VP<V>::aval(S, true), VP<V>::diag(S), v.pT, i);
                     v.qT[i] = qt;
-                    acc[0] = __fma_rn((double)q, (double)v.pT[i], acc[0]);
+                    acc[0] = __fma_rn(widen(q), widen(v.pT[i]), acc[0]);
                 } else {
-                    acc[0] = __fma_rn((double)q, (double)v.p[i], acc[0]);
+                    acc[0] = __fma_rn(widen(q), widen(v.p[i]), acc[0]);
                 }
             }
         } else if constexpr (OP == OP_UPDATE) {
@@ -339,7 +357,7 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
                 const V r = vfma(-alpha, v.q[i], v.r[i]);
                 v.r[i] = r;
                 if (PB) v.rT[i] = vfma(-alpha, v.qT[i], v.rT[i]);
-                acc[0] += fabs((double)r);
+                acc[0] += fabs(widen(r));
             }
         } else if constexpr (OP == OP_PRECOND_DIAG) {
             const V* rD = VP<V>::rD(S);
@@ -373,7 +391,7 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
                 const float r = (float)(S.v64.r[i] * s);
                 S.v32.r[i] = r;
                 S.v32.x[i] = 0.0f;
-                acc[0] += fabs((double)r);
+                acc[0] += fabs(widen(r));
             }
         } else if constexpr (OP == OP_CORRECT) {
             const double s = S.sc->inv_scale;

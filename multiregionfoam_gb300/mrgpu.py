@@ -176,6 +176,20 @@ class Context:
         _check(load().mrg_event_elapsed(self.h, a, b, C.byref(v)))
         return v.value
 
+    def close(self):
+        for m in self._meshes:
+            m.close()
+        self._meshes = []
+        if self.h:
+            _check(load().mrg_ctx_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 def kernel_launches() -> int:
     v = C.c_uint64()
@@ -190,20 +204,6 @@ def host_array(ctx_unused, n: int, dtype=np.float64) -> np.ndarray:
     _check(load().mrg_host_alloc(nbytes, C.byref(p)))
     buf = (C.c_char * nbytes).from_address(p.value)
     return np.frombuffer(buf, dtype=dtype, count=int(n))  # lives until process exit
-
-    def close(self):
-        for m in self._meshes:
-            m.close()
-        self._meshes = []
-        if self.h:
-            _check(load().mrg_ctx_destroy(self.h))
-            self.h = None
-
-    def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass
 
 
 class Mesh:

@@ -226,8 +226,9 @@ PlanState& Mesh::plan(int ordering)
 }
 
 // ------------------------------------------------------------------ prepare
-static int grid_rows(const Ctx* c, int ntiles) { return std::max(1, std::min(ntiles, c->nsm * 8)); }
-static int grid_sweep(const Ctx* c) { return c->nsm * 8; }
+// One wave of 256-thread CTAs at the 4 per SM the kernels are compiled for.
+static int grid_rows(const Ctx* c, int ntiles) { return std::max(1, std::min(ntiles, c->nsm * 4)); }
+static int grid_sweep(const Ctx* c) { return c->nsm * 4; }
 
 PlanState& prepare(Mesh& m, const Controls& cfg)
 {

@@ -176,15 +176,21 @@ template <> struct VP<float> {
 // together instead of one dependent round trip per entry.  Padding (col -1)
 // is skipped, so no FP64 work is spent on it.
 constexpr int kMaxW = 8;
-constexpr int kRedGrid = 1024;  // CTAs of a reducing row kernel (fixes the sum order)
+// Row and sweep kernels are compiled for at least 4 resident 256-thread CTAs
+// per SM; a reducing row kernel always runs on kRedGrid = 608 CTAs (one wave
+// on the 152 SMs of a GB300), a constant so that the reduction order -- and
+// therefore every result bit -- does not depend on the device.
+constexpr int kMinCtas = 4;
+constexpr int kRedGrid = 608;
 
 template <typename V>
-__device__ __forceinline__ V ell_row(const SysDev& S, const V* __restrict__ val, const V* __restrict__ dg,
-                                     const V* __restrict__ x, int i)
+__device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __restrict__ acol,
+                                     const V* __restrict__ val, const V* __restrict__ dg, const V* __restrict__ x,
+                                     int i)
 {
     const int sl = i >> 5, lane = i & 31;
-    const int e0 = __ldg(S.a_sptr + sl), W = (__ldg(S.a_sptr + sl + 1) - e0) >> 5;
-    const int* __restrict__ col = S.a_col + e0 + lane;
+    const int e0 = __ldg(sptr + sl), W = (__ldg(sptr + sl + 1) - e0) >> 5;
+    const int* __restrict__ col = acol + e0 + lane;
     const V* __restrict__ v = val + e0 + lane;
     V y = vmul(__ldg(dg + i), __ldg(x + i));
     if (W <= kMaxW) {
@@ -277,133 +283,199 @@ __device__ void finalize(const SysDev& S, RowOp op, const double* sums)
 // ---------------------------------------------------------------- row kernel
 // One 1024-row tile of a row operation.  Elementwise ops give thread t the
 // rows row0 + t + 256k; ELL ops give warp w the slices row0/32 + w + 8k.
-// Reductions accumulate into acc (FP64) in that row order.
+// Reductions accumulate into acc (FP64) in that row order.  The system's
+// pointers are read once into __restrict__ locals: the kernels store through
+// them, and reading them through the SysDev in global memory would force a
+// reload after every store.
 template <typename V, RowOp OP, bool PB>
 __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&acc)[kMaxRed])
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const Vecs<V>& v = VP<V>::v(S);
-    {
-        if constexpr (OP == OP_SCATTER) {
-            // FP64 views (+ FP32 copies when allocated); one warp per slice.
-            const bool asym = S.aT_val != S.a_val;
-            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
-                const int e0 = S.a_sptr[sl], e1 = S.a_sptr[sl + 1];
-                const int i = sl * 32 + lane;
-                double d = i < S.n ? S.raw_diag[S.perm[i]] : 0.0;
-                S.diag[i] = d;
-                if (S.diag32) S.diag32[i] = (float)d;
-                double s = d;
-                for (int e = e0 + lane; e < e1; e += 32) {
-                    const int sc = S.a_src[e];
-                    const double a = sc < 0 ? 0.0 : src_val(S, sc, false);
-                    S.a_val[e] = a;
-                    if (S.a_val32) S.a_val32[e] = (float)a;
-                    if (asym) {
-                        const double at = sc < 0 ? 0.0 : src_val(S, sc, true);
-                        S.aT_val[e] = at;
-                        if (S.aT_val32) S.aT_val32[e] = (float)at;
-                    }
-                    if (sc >= 0) s = __dadd_rn(s, a);
+    const int sl0 = row0 >> 5, sl1 = sl0 + kTileRows / 32;
+    const int* __restrict__ sptr = S.a_sptr;
+    const int* __restrict__ acol = S.a_col;
+    if constexpr (OP == OP_SCATTER) {
+        // FP64 views (+ FP32 copies when allocated); one warp per slice.
+        const bool asym = S.aT_val != S.a_val;
+        const int* __restrict__ asrc = S.a_src;
+        const int* __restrict__ perm = S.perm;
+        const double* __restrict__ rdiag = S.raw_diag;
+        double* __restrict__ dg = S.diag;
+        double* __restrict__ sA = S.sumA;
+        double* __restrict__ av = S.a_val;
+        double* __restrict__ atv = S.aT_val;
+        float* __restrict__ dg32 = S.diag32;
+        float* __restrict__ av32 = S.a_val32;
+        float* __restrict__ atv32 = S.aT_val32;
+        const int n = S.n;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int e0 = sptr[sl], e1 = sptr[sl + 1];
+            const int i = sl * 32 + lane;
+            const double d = i < n ? rdiag[perm[i]] : 0.0;
+            dg[i] = d;
+            if (dg32) dg32[i] = (float)d;
+            double s = d;
+            for (int e = e0 + lane; e < e1; e += 32) {
+                const int sc = asrc[e];
+                const double a = sc < 0 ? 0.0 : src_val(S, sc, false);
+                av[e] = a;
+                if (av32) av32[e] = (float)a;
+                if (asym) {
+                    const double at = sc < 0 ? 0.0 : src_val(S, sc, true);
+                    atv[e] = at;
+                    if (atv32) atv32[e] = (float)at;
                 }
-                S.sumA[i] = s;
+                if (sc >= 0) s = __dadd_rn(s, a);
             }
-        } else if constexpr (OP == OP_SUMX) {
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) acc[0] += widen(v.x[i]);
-        } else if constexpr (OP == OP_INIT_RES) {
-            const double xbar = S.sc->xsum / (double)S.n;
-            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
-                const int i = sl * 32 + lane;
-                const double ax = ell_row<double>(S, S.a_val, S.diag, S.v64.x, i);
-                const double b = S.v64.b[i];
-                const double tr = __dmul_rn(S.sumA[i], xbar);
-                acc[0] += fabs(ax - tr) + fabs(b - tr);
-                const double r = b - ax;
-                S.v64.r[i] = r;
-                acc[1] += fabs(r);
-                if (PB) {
-                    const double at = ell_row<double>(S, S.aT_val, S.diag, S.v64.x, i);
-                    S.v64.rT[i] = b - at;
-                }
-            }
-        } else if constexpr (OP == OP_RHO) {
-            const V* rr = PB ? v.rT : v.r;
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
-                acc[0] = __fma_rn(widen(v.w[i]), widen(rr[i]), acc[0]);
-        } else if constexpr (OP == OP_PUPDATE) {
-            const int it = S.sc->iter;
-            const V beta = (V)S.sc->beta;
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-                v.p[i] = it == 0 ? v.w[i] : vfma(beta, v.p[i], v.w[i]);
-                if (PB) v.pT[i] = it == 0 ? v.wT[i] : vfma(beta, v.pT[i], v.wT[i]);
-            }
-        } else if constexpr (OP == OP_SPMV_QP) {
-            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
-                const int i = sl * 32 + lane;
-                const V q = ell_row<V>(S, VP<V>::aval(S, false), VP<V>::diag(S), v.p, i);
-                v.q[i] = q;
-                if (PB) {
-                    const V qt = ell_row<V>(S, VP<V>::aval(S, true), VP<V>::diag(S), v.pT, i);
-                    v.qT[i] = qt;
-                    acc[0] = __fma_rn(widen(q), widen(v.pT[i]), acc[0]);
-                } else {
-                    acc[0] = __fma_rn(widen(q), widen(v.p[i]), acc[0]);
-                }
-            }
-        } else if constexpr (OP == OP_UPDATE) {
-            const V alpha = (V)S.sc->alpha;
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-                v.x[i] = vfma(alpha, v.p[i], v.x[i]);
-                const V r = vfma(-alpha, v.q[i], v.r[i]);
-                v.r[i] = r;
-                if (PB) v.rT[i] = vfma(-alpha, v.qT[i], v.rT[i]);
-                acc[0] += fabs(widen(r));
-            }
-        } else if constexpr (OP == OP_PRECOND_DIAG) {
-            const V* rD = VP<V>::rD(S);
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-                v.w[i] = vmul(rD[i], v.r[i]);
-                if (PB) v.wT[i] = vmul(rD[i], v.rT[i]);
-            }
-        } else if constexpr (OP == OP_PRECOND_NONE) {
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-                v.w[i] = v.r[i];
-                if (PB) v.wT[i] = v.rT[i];
-            }
-        } else if constexpr (OP == OP_DIAG_RD) {
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-                const double r = i < S.n ? __ddiv_rn(1.0, S.diag[i]) : 0.0;
-                S.rD[i] = r;
-                if (S.rD32) S.rD32[i] = (float)r;
-            }
-        } else if constexpr (OP == OP_RESID64) {
-            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
-                const int i = sl * 32 + lane;
-                const double ax = ell_row<double>(S, S.a_val, S.diag, S.v64.x, i);
-                const double r = S.v64.b[i] - ax;
-                S.v64.r[i] = r;
-                acc[0] += fabs(r);
-            }
-        } else if constexpr (OP == OP_TO32) {
-            // s scales the FP64 residual to O(1) per cell before rounding to FP32.
-            const double s = S.sc->osum > 0.0 ? (double)S.n / S.sc->osum : 1.0;
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-                const float r = (float)(S.v64.r[i] * s);
-                S.v32.r[i] = r;
-                S.v32.x[i] = 0.0f;
-                acc[0] += fabs(widen(r));
-            }
-        } else if constexpr (OP == OP_CORRECT) {
-            const double s = S.sc->inv_scale;
-            for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
-                S.v64.x[i] = __fma_rn((double)S.v32.x[i], s, S.v64.x[i]);
-        } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
-            for (int sl = (row0 >> 5) + wid; sl < (row0 >> 5) + kTileRows / 32; sl += kBlock / 32) {
-                const int i = sl * 32 + lane;
-                S.v64.q[i] = ell_row<double>(S, OP == OP_TMUL ? S.aT_val : S.a_val, S.diag, S.v64.p, i);
+            sA[i] = s;
+        }
+    } else if constexpr (OP == OP_SUMX) {
+        const V* __restrict__ x = VP<V>::v(S).x;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) acc[0] += widen(x[i]);
+    } else if constexpr (OP == OP_INIT_RES) {
+        const double xbar = S.sc->xsum / (double)S.n;
+        const double* __restrict__ av = S.a_val;
+        const double* __restrict__ atv = S.aT_val;
+        const double* __restrict__ dg = S.diag;
+        const double* __restrict__ sA = S.sumA;
+        const double* __restrict__ x = S.v64.x;
+        const double* __restrict__ b = S.v64.b;
+        double* __restrict__ r = S.v64.r;
+        double* __restrict__ rT = S.v64.rT;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            const double ax = ell_row<double>(sptr, acol, av, dg, x, i);
+            const double bi = b[i];
+            const double tr = __dmul_rn(sA[i], xbar);
+            acc[0] += fabs(ax - tr) + fabs(bi - tr);
+            const double ri = bi - ax;
+            r[i] = ri;
+            acc[1] += fabs(ri);
+            if (PB) rT[i] = bi - ell_row<double>(sptr, acol, atv, dg, x, i);
+        }
+    } else if constexpr (OP == OP_RHO) {
+        const Vecs<V>& v = VP<V>::v(S);
+        const V* __restrict__ w = v.w;
+        const V* __restrict__ rr = PB ? v.rT : v.r;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
+            acc[0] = __fma_rn(widen(w[i]), widen(rr[i]), acc[0]);
+    } else if constexpr (OP == OP_PUPDATE) {
+        const Vecs<V>& v = VP<V>::v(S);
+        const int it = S.sc->iter;
+        const V beta = (V)S.sc->beta;
+        V* __restrict__ p = v.p;
+        const V* __restrict__ w = v.w;
+        V* __restrict__ pT = v.pT;
+        const V* __restrict__ wT = v.wT;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+            p[i] = it == 0 ? w[i] : vfma(beta, p[i], w[i]);
+            if (PB) pT[i] = it == 0 ? wT[i] : vfma(beta, pT[i], wT[i]);
+        }
+    } else if constexpr (OP == OP_SPMV_QP) {
+        const Vecs<V>& v = VP<V>::v(S);
+        const V* __restrict__ av = VP<V>::aval(S, false);
+        const V* __restrict__ atv = VP<V>::aval(S, true);
+        const V* __restrict__ dg = VP<V>::diag(S);
+        const V* __restrict__ p = v.p;
+        const V* __restrict__ pT = v.pT;
+        V* __restrict__ q = v.q;
+        V* __restrict__ qT = v.qT;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            const V qi = ell_row<V>(sptr, acol, av, dg, p, i);
+            q[i] = qi;
+            if (PB) {
+                qT[i] = ell_row<V>(sptr, acol, atv, dg, pT, i);
+                acc[0] = __fma_rn(widen(qi), widen(pT[i]), acc[0]);
+            } else {
+                acc[0] = __fma_rn(widen(qi), widen(p[i]), acc[0]);
             }
         }
-
+    } else if constexpr (OP == OP_UPDATE) {
+        const Vecs<V>& v = VP<V>::v(S);
+        const V alpha = (V)S.sc->alpha;
+        V* __restrict__ x = v.x;
+        V* __restrict__ r = v.r;
+        V* __restrict__ rT = v.rT;
+        const V* __restrict__ p = v.p;
+        const V* __restrict__ q = v.q;
+        const V* __restrict__ qT = v.qT;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+            x[i] = vfma(alpha, p[i], x[i]);
+            const V ri = vfma(-alpha, q[i], r[i]);
+            r[i] = ri;
+            if (PB) rT[i] = vfma(-alpha, qT[i], rT[i]);
+            acc[0] += fabs(widen(ri));
+        }
+    } else if constexpr (OP == OP_PRECOND_DIAG) {
+        const Vecs<V>& v = VP<V>::v(S);
+        const V* __restrict__ rD = VP<V>::rD(S);
+        V* __restrict__ w = v.w;
+        V* __restrict__ wT = v.wT;
+        const V* __restrict__ r = v.r;
+        const V* __restrict__ rT = v.rT;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+            w[i] = vmul(rD[i], r[i]);
+            if (PB) wT[i] = vmul(rD[i], rT[i]);
+        }
+    } else if constexpr (OP == OP_PRECOND_NONE) {
+        const Vecs<V>& v = VP<V>::v(S);
+        V* __restrict__ w = v.w;
+        V* __restrict__ wT = v.wT;
+        const V* __restrict__ r = v.r;
+        const V* __restrict__ rT = v.rT;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+            w[i] = r[i];
+            if (PB) wT[i] = rT[i];
+        }
+    } else if constexpr (OP == OP_DIAG_RD) {
+        const double* __restrict__ dg = S.diag;
+        double* __restrict__ rD = S.rD;
+        float* __restrict__ rD32 = S.rD32;
+        const int n = S.n;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+            const double r = i < n ? __ddiv_rn(1.0, dg[i]) : 0.0;
+            rD[i] = r;
+            if (rD32) rD32[i] = (float)r;
+        }
+    } else if constexpr (OP == OP_RESID64) {
+        const double* __restrict__ av = S.a_val;
+        const double* __restrict__ dg = S.diag;
+        const double* __restrict__ x = S.v64.x;
+        const double* __restrict__ b = S.v64.b;
+        double* __restrict__ r = S.v64.r;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            const double ri = b[i] - ell_row<double>(sptr, acol, av, dg, x, i);
+            r[i] = ri;
+            acc[0] += fabs(ri);
+        }
+    } else if constexpr (OP == OP_TO32) {
+        // s scales the FP64 residual to O(1) per cell before rounding to FP32.
+        const double s = S.sc->osum > 0.0 ? (double)S.n / S.sc->osum : 1.0;
+        const double* __restrict__ r64 = S.v64.r;
+        float* __restrict__ r32 = S.v32.r;
+        float* __restrict__ x32 = S.v32.x;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
+            const float ri = (float)(r64[i] * s);
+            r32[i] = ri;
+            x32[i] = 0.0f;
+            acc[0] += fabs(widen(ri));
+        }
+    } else if constexpr (OP == OP_CORRECT) {
+        const double s = S.sc->inv_scale;
+        const float* __restrict__ d32 = S.v32.x;
+        double* __restrict__ x = S.v64.x;
+        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) x[i] = __fma_rn(widen(d32[i]), s, x[i]);
+    } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
+        const double* __restrict__ av = OP == OP_TMUL ? S.aT_val : S.a_val;
+        const double* __restrict__ dg = S.diag;
+        const double* __restrict__ p = S.v64.p;
+        double* __restrict__ q = S.v64.q;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            q[i] = ell_row<double>(sptr, acol, av, dg, p, i);
+        }
     }
 }
 
@@ -414,6 +486,9 @@ struct OpTraits {
     static constexpr bool kNeedActive = !(OP == OP_SCATTER || OP == OP_SUMX || OP == OP_INIT_RES ||
                                           OP == OP_AMUL || OP == OP_TMUL || OP == OP_DIAG_RD ||
                                           OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
+    // Values reduced: only the initial residual needs two (normFactor and
+    // sum|r|).  Every tree level costs one FP64 add per thread per value.
+    static constexpr int kNR = OP == OP_INIT_RES ? 2 : 1;
 };
 
 // Close one reduction segment (consecutive tiles [first, first+count) of one
@@ -425,27 +500,37 @@ template <RowOp OP>
 __device__ __forceinline__ void flush_segment(const SysDev& S, int first, int count, double (&acc)[kMaxRed],
                                               double* sh, int* s_last)
 {
+    constexpr int NR = OpTraits<OP>::kNR;
     const int tid = threadIdx.x;
-    block_sum<kMaxRed>(acc, sh);
+    double a[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) a[k] = acc[k];
+    block_sum<NR>(a, sh);
     if (tid == 0) {
-        S.partials[first * kMaxRed + 0] = acc[0];
-        S.partials[first * kMaxRed + 1] = acc[1];
+#pragma unroll
+        for (int k = 0; k < NR; ++k) S.partials[first * kMaxRed + k] = a[k];
         __threadfence();
         const unsigned prev = atomicAdd(S.counter, (unsigned)count);
         *s_last = (prev + (unsigned)count == (unsigned)S.ntiles);
     }
     __syncthreads();
     if (*s_last) {
-        double tot[kMaxRed] = {0.0, 0.0};
-        for (int k = tid; k < S.ntiles; k += kBlock) {
-            tot[0] += __ldcg(S.partials + k * kMaxRed + 0);
-            tot[1] += __ldcg(S.partials + k * kMaxRed + 1);
-            S.partials[k * kMaxRed + 0] = 0.0;
-            S.partials[k * kMaxRed + 1] = 0.0;
+        double tot[NR];
+#pragma unroll
+        for (int k = 0; k < NR; ++k) tot[k] = 0.0;
+        for (int j = tid; j < S.ntiles; j += kBlock) {
+#pragma unroll
+            for (int k = 0; k < NR; ++k) {
+                tot[k] += __ldcg(S.partials + j * kMaxRed + k);
+                S.partials[j * kMaxRed + k] = 0.0;
+            }
         }
-        block_sum<kMaxRed>(tot, sh);
+        block_sum<NR>(tot, sh);
         if (tid == 0) {
-            finalize(S, OP, tot);
+            double sums[kMaxRed] = {0.0, 0.0};
+#pragma unroll
+            for (int k = 0; k < NR; ++k) sums[k] = tot[k];
+            finalize(S, OP, sums);
             *S.counter = 0u;
             __threadfence();
         }
@@ -458,8 +543,8 @@ __device__ __forceinline__ void flush_segment(const SysDev& S, int first, int co
 // gridDim.x, at most kRedGrid) and accumulates across them, so the
 // fence/atomic/tree cost is paid once per CTA and system, not per tile.
 template <typename V, RowOp OP, bool PB>
-__global__ void __launch_bounds__(kBlock) k_rows(const SysDev* __restrict__ Ss, const int2* __restrict__ tiles,
-                                                 int ntiles)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const SysDev* __restrict__ Ss,
+                                                           const int2* __restrict__ tiles, int ntiles)
 {
     __shared__ double sh[(kBlock / 32) * kMaxRed];
     __shared__ int s_last;
@@ -559,7 +644,7 @@ __device__ __forceinline__ void factor_row(const SysDev& S, int c, int lane, Ctl
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_factor(const SysDev* __restrict__ Ss, int nsys, int maxchunks,
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_factor(const SysDev* __restrict__ Ss, int nsys, int maxchunks,
                                                    Ctl* ctl, int with32)
 {
     const int lane = threadIdx.x & 31;
@@ -602,24 +687,50 @@ __global__ void __launch_bounds__(kBlock) k_factor(const SysDev* __restrict__ Ss
 // 0 is never stored (its forward value rD r is recomputed where needed) and
 // the last level writes w directly (it has no backward dependencies), so a
 // two-colour sweep is two launches: forward level 1, backward level 0.
+// Pointers one sweep needs, copied into registers once per system so the
+// stores of the sweep cannot force them to be re-read from the SysDev.
+template <typename V>
+struct SweepPtrs {
+    const int* cstart;
+    const int* sptr;
+    const int* col;
+    const V* coef;
+    const V* rD;
+    const V* r;
+    V* y;
+    V* w;
+};
+
 template <typename V, bool FWD>
-__device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, bool syncfree, Ctl* ctl,
-                                            int lvl0_end, bool last_level, bool first_level)
+__device__ __forceinline__ SweepPtrs<V> sweep_ptrs(const SysDev& S, bool trans)
+{
+    const Vecs<V>& v = VP<V>::v(S);
+    SweepPtrs<V> P;
+    P.cstart = S.chunk_start;
+    P.sptr = FWD ? S.f_sptr : S.b_sptr;
+    P.col = FWD ? S.f_col : S.b_col;
+    P.coef = FWD ? VP<V>::fc(S, trans) : VP<V>::bc(S, trans);
+    P.rD = VP<V>::rD(S);
+    P.r = trans ? v.rT : v.r;
+    P.y = trans ? v.yT : v.y;
+    P.w = trans ? v.wT : v.w;
+    return P;
+}
+
+template <typename V, bool FWD>
+__device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool syncfree, Ctl* ctl, int lvl0_end,
+                                            bool last_level, bool first_level)
 {
     const int lane = threadIdx.x & 31;
-    const int r0 = S.chunk_start[c], r1 = S.chunk_start[c + 1];
+    const int r0 = __ldg(P.cstart + c), r1 = __ldg(P.cstart + c + 1);
     const int i = r0 + lane;
     if (i >= r1) return;
-    const Vecs<V>& v = VP<V>::v(S);
-    V* y = trans ? v.yT : v.y;
-    V* w = trans ? v.wT : v.w;
-    const V* r = trans ? v.rT : v.r;
-    const V* rD = VP<V>::rD(S);
-    const int* sptr = FWD ? S.f_sptr : S.b_sptr;
-    const int* colp = FWD ? S.f_col : S.b_col;
-    const V* coef = FWD ? VP<V>::fc(S, trans) : VP<V>::bc(S, trans);
+    V* __restrict__ y = P.y;
+    V* __restrict__ w = P.w;
+    const V* __restrict__ r = P.r;
+    const V* __restrict__ rD = P.rD;
     V* dep = FWD ? y : w;
-    const int e0 = sptr[c], W = (sptr[c + 1] - e0) >> 5;
+    const int e0 = __ldg(P.sptr + c), W = (__ldg(P.sptr + c + 1) - e0) >> 5;
     V acc;
     if (FWD || (!syncfree && first_level))
         acc = vmul(rD[i], r[i]);
@@ -629,9 +740,9 @@ __device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, 
         int col[kMaxW];
         V cf[kMaxW];
 #pragma unroll
-        for (int k = 0; k < kMaxW; ++k) col[k] = k < W ? __ldg(colp + e0 + k * 32 + lane) : -1;
+        for (int k = 0; k < kMaxW; ++k) col[k] = k < W ? __ldg(P.col + e0 + k * 32 + lane) : -1;
 #pragma unroll
-        for (int k = 0; k < kMaxW; ++k) cf[k] = col[k] >= 0 ? __ldg(coef + e0 + k * 32 + lane) : V(0);
+        for (int k = 0; k < kMaxW; ++k) cf[k] = col[k] >= 0 ? __ldg(P.coef + e0 + k * 32 + lane) : V(0);
         if (syncfree) {
 #pragma unroll
             for (int k = 0; k < kMaxW; ++k)
@@ -653,9 +764,9 @@ __device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, 
     } else {
         for (int k = 0; k < W; ++k) {
             const int e = e0 + k * 32 + lane;
-            const int ck = __ldg(colp + e);
+            const int ck = __ldg(P.col + e);
             if (ck < 0) break;
-            const V cfk = __ldg(coef + e);
+            const V cfk = __ldg(P.coef + e);
             V d;
             if (syncfree)
                 d = wait_ready(dep + ck, ctl);
@@ -683,8 +794,8 @@ __device__ __forceinline__ void sweep_chunk(const SysDev& S, int c, bool trans, 
 }
 
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock) k_sweep_sf(const SysDev* __restrict__ Ss, int nsys, int maxchunks,
-                                                     Ctl* ctl, int trans)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const SysDev* __restrict__ Ss, int nsys,
+                                                               int maxchunks, Ctl* ctl, int trans)
 {
     const int lane = threadIdx.x & 31;
     const unsigned total = (unsigned)nsys * (unsigned)maxchunks;
@@ -696,8 +807,10 @@ __global__ void __launch_bounds__(kBlock) k_sweep_sf(const SysDev* __restrict__ 
         if (t >= total) break;
         const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
         const SysDev& S = Ss[s];
-        if (c >= S.nchunks || !S.sc->active) continue;
-        sweep_chunk<V, FWD>(S, FWD ? c : S.nchunks - 1 - c, trans != 0, true, ctl, 0, false, false);
+        const int nch = S.nchunks;
+        if (c >= nch || !S.sc->active) continue;
+        const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans != 0);
+        sweep_chunk<V, FWD>(P, FWD ? c : nch - 1 - c, true, ctl, 0, false, false);
     }
     if (lane == 0) {
         const unsigned nw = gridDim.x * (blockDim.x / 32);
@@ -714,7 +827,8 @@ __global__ void __launch_bounds__(kBlock) k_sweep_sf(const SysDev* __restrict__ 
 // levels 1..nlevels-1, backward levels nlevels-2..0 (level 0 alone when
 // nlevels == 1).
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock) k_sweep_lvl(const SysDev* __restrict__ Ss, int nsys, int L, int trans)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const SysDev* __restrict__ Ss, int nsys, int L,
+                                                                int trans)
 {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -725,8 +839,9 @@ __global__ void __launch_bounds__(kBlock) k_sweep_lvl(const SysDev* __restrict__
         if (FWD ? (L < 1 || L > nl - 1) : !(L <= nl - 2 || (nl == 1 && L == 0))) continue;
         const int lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
         const bool last = L == nl - 1, first = L == 0;
-        for (int c = S.lvl_chunk[L] + gw; c < S.lvl_chunk[L + 1]; c += nw)
-            sweep_chunk<V, FWD>(S, c, trans != 0, false, nullptr, lvl0_end, last, first);
+        const int c0 = S.lvl_chunk[L], c1 = S.lvl_chunk[L + 1];
+        const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans != 0);
+        for (int c = c0 + gw; c < c1; c += nw) sweep_chunk<V, FWD>(P, c, false, nullptr, lvl0_end, last, first);
     }
 }
 

@@ -494,10 +494,10 @@ static int mr_row(int tile, int t, int k, int assign)
     return ((row0 >> 5) + w + 8 * k) * 32 + lane;
 }
 
-#define MR_GRID 1024
+#define MR_GRID 608
 
 /* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order).
- * CTA g of G = min(tiles, 1024) owns tiles [g*T/G, (g+1)*T/G) and keeps
+ * CTA g of G = min(tiles, 608) owns tiles [g*T/G, (g+1)*T/G) and keeps
  * accumulating across them; its tree sum lands in the slot of its first tile
  * (the other slots stay zero). */
 static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)

@@ -68,4 +68,23 @@ def build(force: bool = False, verbose: bool = False) -> str:
             list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         run([cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    build_adapter(force)
     return LIB
+
+
+FOAM = os.path.join(HERE, "foam")
+ADAPTER = os.path.join(OUT, "test_adapter")
+
+
+def build_adapter(force: bool = False) -> str:
+    """The lduMatrix::solver adapters + their driver, against the API shim."""
+    srcs = [os.path.join(FOAM, "gpuLduSolvers.C"), os.path.join(FOAM, "test_adapter.C")]
+    deps = srcs + [os.path.join(FOAM, "shim", "lduMatrix.H"), os.path.join(INCLUDE, "mrgpu.h"), LIB]
+    if force or _stale(ADAPTER, deps):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(FOAM, "shim"), "-I", INCLUDE] + srcs + \
+              ["-L", OUT, "-lmrgpu", "-Wl,-rpath," + OUT, "-o", ADAPTER]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("adapter build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return ADAPTER

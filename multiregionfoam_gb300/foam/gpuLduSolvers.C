@@ -76,7 +76,8 @@ public:
     {
     }
 
-    solverPerformance solve(scalarField& psi, const scalarField& source, const direction) const override
+    lduMatrix::solverPerformance solve(scalarField& psi, const scalarField& source,
+                                       const direction) const override
     {
         GpuState& S = state();
         std::lock_guard<std::mutex> g(S.lock);
@@ -136,7 +137,7 @@ public:
         c.inner_rel_tol = controls_.lookupOrDefault("innerRelTol", 1e-5);
         mrg_perf perf;
         check(mrg_solve(mesh, source.data(), psi.data(), &c, &perf), "mrg_solve");
-        solverPerformance out;
+        lduMatrix::solverPerformance out;
         out.solverName = solverKind_ == MRG_SOLVER_PCG ? (precision_ ? "gpuMixedPCG" : "gpuPCG")
                                                         : (precision_ ? "gpuMixedPBiCG" : "gpuPBiCG");
         out.fieldName = fieldName_;

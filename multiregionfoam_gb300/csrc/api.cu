@@ -3,6 +3,7 @@
 // throws across the ABI.
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -23,11 +24,13 @@ struct mrg_ggi {
 };
 
 namespace {
-thread_local std::string g_last_error;
+// A plain buffer, not std::string: callers may reach the ABI from static
+// destructors after thread-local objects with destructors are gone.
+thread_local char g_last_error[1024];
 
 int fail(int code, const std::string& msg)
 {
-    g_last_error = msg;
+    std::snprintf(g_last_error, sizeof g_last_error, "%s", msg.c_str());
     return code;
 }
 
@@ -35,7 +38,7 @@ template <typename F>
 int guard(F&& f)
 {
     try {
-        g_last_error.clear();
+        g_last_error[0] = '\0';
         return f();
     } catch (const Error& e) {
         return fail(e.code, e.what());
@@ -84,25 +87,18 @@ void fill_perf(mrg_perf* p, const Perf& r)
     p->solve_ms = r.ms;
 }
 
-// Scratch device buffers of a context for host-pointer entry points.
-struct HostStage {
-    double* d[3] = {nullptr, nullptr, nullptr};
-    size_t cap = 0;
-};
-thread_local std::map<Ctx*, HostStage> g_stage;
-
+// Device staging buffers of a context for the host-pointer entry points.
 double* stage(Ctx* c, int k, size_t n)
 {
-    HostStage& s = g_stage[c];
-    if (s.cap < n) {
-        for (auto& p : s.d) {
+    if (c->stage_cap < n) {
+        for (auto& p : c->stage) {
             c->release(p);
             p = nullptr;
         }
-        s.cap = n;
+        c->stage_cap = n;
     }
-    if (!s.d[k]) s.d[k] = (double*)c->alloc(8 * s.cap);
-    return s.d[k];
+    if (!c->stage[k]) c->stage[k] = (double*)c->alloc(8 * c->stage_cap);
+    return c->stage[k];
 }
 
 void h2d(Ctx* c, double* d, const double* h, size_t n)
@@ -148,7 +144,7 @@ void upload_coeffs(Mesh& m, const double* diag, const double* upper, const doubl
 
 extern "C" {
 
-const char* mrg_last_error(void) { return g_last_error.c_str(); }
+const char* mrg_last_error(void) { return g_last_error; }
 
 const char* mrg_version(void) { return "mrgpu 0.1 (sm_103a)"; }
 
@@ -200,7 +196,6 @@ int mrg_ctx_destroy(mrg_ctx* ctx)
 {
     return guard([&] {
         if (!ctx) return (int)MRG_OK;
-        g_stage.erase(&ctx->c);
         delete ctx;
         return (int)MRG_OK;
     });

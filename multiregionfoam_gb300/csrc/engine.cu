@@ -214,8 +214,7 @@ PlanState& Mesh::plan(int ordering)
     H.g_ptr.clear();
     H.g_src.clear();
     H.g_w.clear();
-    H.chunk_start.clear();
-    H.lvl_chunk.clear();
+    H.chunk_start.clear();  // lvl_chunk (one int per level) stays for launch sizing
     plans[ordering] = std::move(P);
     // entry counts for the lazily allocated FP32 / transpose arrays
     nnz_cache[ordering][0] = nnz;
@@ -330,9 +329,13 @@ static void record_precondition(PlanState& P, const Controls& cfg, int prec, int
             launch_sweep(prec, 1, trans, 1, 0, P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), st);
             launch_sweep(prec, 0, trans, 1, 0, P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), st);
         } else {
-            // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if nl == 1)
-            const int g = std::max(1, std::min(grid_sweep(c), (S.nchunks + 7) / 8));
+            // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
+            // nl == 1); one chunk per warp of the widest level
             const int nl = S.nlevels;
+            int widest = 1;
+            for (int L = 0; L < nl; ++L)
+                widest = std::max(widest, P.host.lvl_chunk[L + 1] - P.host.lvl_chunk[L]);
+            const int g = std::max(1, std::min(65535, (widest + 7) / 8));
             for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
             for (int L = std::max(nl - 2, 0); L >= 0; --L)
                 launch_sweep(prec, 0, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);

@@ -30,6 +30,8 @@ struct Ctx {
     std::map<void*, size_t> allocs;
     Ctl* d_ctl = nullptr;
     cudaEvent_t events[64] = {};
+    double* stage[3] = {nullptr, nullptr, nullptr};  // host-pointer entry points
+    size_t stage_cap = 0;
     void* alloc(size_t bytes);
     void release(void* p);
     ~Ctx();

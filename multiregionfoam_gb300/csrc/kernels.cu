@@ -128,22 +128,24 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-// Deterministic block sum of NR values (fixed tree).  Result valid in tid 0.
+// Deterministic block sum of NR values (fixed order).  Result valid in tid 0.
+// Lane l of warp 0 adds the eight warps' values at lane l in warp order, then
+// one shuffle tree finishes: 12 FP64 adds on 32 lanes instead of a shuffle
+// tree on all 256 threads (FP64 adds are scarce on GB300).
 template <int NR>
 __device__ __forceinline__ void block_sum(double (&a)[NR], double* sh)
 {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 #pragma unroll
-    for (int k = 0; k < NR; ++k) a[k] = warp_sum(a[k]);
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NR; ++k) sh[wid * NR + k] = a[k];
+    for (int k = 0; k < NR; ++k) sh[k * kBlock + tid] = a[k];
     __syncthreads();
     if (wid == 0) {
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            double v = lane < (kBlock / 32) ? sh[lane * NR + k] : 0.0;
-            a[k] = warp_sum(v);
+            double s = sh[k * kBlock + lane];
+#pragma unroll
+            for (int w = 1; w < kBlock / 32; ++w) s += sh[k * kBlock + w * 32 + lane];
+            a[k] = warp_sum(s);
         }
     }
     __syncthreads();
@@ -177,11 +179,12 @@ template <> struct VP<float> {
 // is skipped, so no FP64 work is spent on it.
 constexpr int kMaxW = 8;
 // Row and sweep kernels are compiled for at least 4 resident 256-thread CTAs
-// per SM; a reducing row kernel always runs on kRedGrid = 608 CTAs (one wave
-// on the 152 SMs of a GB300), a constant so that the reduction order -- and
-// therefore every result bit -- does not depend on the device.
+// per SM.  A reducing row kernel always runs on kRedGrid = 2432 CTAs (16 per
+// SM of a GB300, a few waves so that loads of many CTAs overlap), a constant
+// so that the reduction order -- and therefore every result bit -- does not
+// depend on the device.  Non-reducing row kernels take one tile per CTA.
 constexpr int kMinCtas = 4;
-constexpr int kRedGrid = 608;
+constexpr int kRedGrid = 2432;
 
 template <typename V>
 __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __restrict__ acol,
@@ -546,7 +549,7 @@ template <typename V, RowOp OP, bool PB>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const SysDev* __restrict__ Ss,
                                                            const int2* __restrict__ tiles, int ntiles)
 {
-    __shared__ double sh[(kBlock / 32) * kMaxRed];
+    __shared__ double sh[kBlock * kMaxRed];
     __shared__ int s_last;
     if constexpr (!OpTraits<OP>::kRed) {
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -912,7 +915,8 @@ void launch_rows(RowOp op, int precision, const SysDev* d, const int2* tiles, in
                  cudaStream_t st)
 {
     if (ntiles <= 0) return;
-    if (grid > ntiles) grid = ntiles;
+    (void)grid;
+    grid = ntiles < 65535 ? ntiles : 65535;
     ++g_launches;
 #define MRG_CASE64(OPX) \
     case OPX: launch_one<double, OPX>(d, tiles, ntiles, grid, pb, st); break;

@@ -473,14 +473,16 @@ static double mr_warp(double* v)
     return v[0];
 }
 
+/* block_sum: lane l adds the eight warps' values at lane l in warp order,
+ * then one warp shuffle tree. */
 static double mr_block(const double* acc /* [256] */)
 {
-    double sh[8], v[32];
-    for (int w = 0; w < 8; ++w) {
-        for (int l = 0; l < 32; ++l) v[l] = acc[w * 32 + l];
-        sh[w] = mr_warp(v);
+    double v[32];
+    for (int l = 0; l < 32; ++l) {
+        double s = acc[l];
+        for (int w = 1; w < 8; ++w) s += acc[w * 32 + l];
+        v[l] = s;
     }
-    for (int l = 0; l < 32; ++l) v[l] = l < 8 ? sh[l] : 0.0;
     return mr_warp(v);
 }
 
@@ -494,10 +496,10 @@ static int mr_row(int tile, int t, int k, int assign)
     return ((row0 >> 5) + w + 8 * k) * 32 + lane;
 }
 
-#define MR_GRID 608
+#define MR_GRID 2432
 
 /* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order).
- * CTA g of G = min(tiles, 608) owns tiles [g*T/G, (g+1)*T/G) and keeps
+ * CTA g of G = min(tiles, 2432) owns tiles [g*T/G, (g+1)*T/G) and keeps
  * accumulating across them; its tree sum lands in the slot of its first tile
  * (the other slots stay zero). */
 static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)

@@ -215,6 +215,26 @@ int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp);
 int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst,
                          int ncomp);
 
+/* ---- batched solves ----------------------------------------------------
+ * Many independent systems (meshes with their current coefficients) solved
+ * in lockstep: every iteration is one set of launches over all members, and
+ * each member stops when its own convergence test passes.  Replaces a loop
+ * of per-region fvMatrix::solve calls (multiRegionSystem.C:193-324,
+ * assembleAndSolveEqns) or of independent cases; each member's result is
+ * bit-identical to solving it alone.  `ordering` fixes which plan of each
+ * mesh the batch uses; the controls' ordering must match. */
+int mrg_batch_create(mrg_ctx* ctx, int n_meshes, mrg_mesh* const* meshes,
+                     int ordering, mrg_batch** out);
+int mrg_batch_destroy(mrg_batch* batch);
+/* b[s], x_inout[s]: host vectors of member s (its mesh's numbering);
+ * perfs: n_meshes records or NULL. */
+int mrg_batch_solve(mrg_batch* batch, const double* const* b,
+                    double* const* x_inout, const mrg_controls* controls,
+                    mrg_perf* perfs);
+int mrg_batch_solve_device(mrg_batch* batch, const double* const* d_b,
+                           double* const* d_x_inout,
+                           const mrg_controls* controls, mrg_perf* perfs);
+
 /* ---- device buffers, timing and diagnostics --------------------------
  * No counterpart in the reference (foam-extend times solves with
  * cpuTimeIncrement, multiRegionSystem.C:546-650).  They let a caller keep

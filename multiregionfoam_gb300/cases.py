@@ -177,6 +177,29 @@ def c2(form="global", seed=0, scale=1):
     return cht_system(s, s, s, s // 2, seed=seed, k_range=(0.1, 50.0), form=form)
 
 
+def batch_shapes(count: int, n_lo: int = 8000, n_hi: int = 260000, seed: int = 0):
+    """Block dimensions of `count` two-region CHT systems with log-uniform cell
+    counts in [n_lo, n_hi] and random aspect ratios (log-U[0.5, 2] per axis);
+    the solid is the lower third of each block."""
+    rng = np.random.default_rng(seed)
+    shapes = []
+    for _ in range(count):
+        n = float(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        a = np.exp(rng.uniform(np.log(0.5), np.log(2.0), 3))
+        s = (n / a.prod()) ** (1.0 / 3.0)
+        nx, ny, nz = (max(2, int(round(v))) for v in a * s)
+        nzs = max(1, nz // 3)
+        shapes.append((nx, ny, max(1, nz - nzs), nzs))
+    return shapes
+
+
+def c4(count: int = 512, seed: int = 0, n_lo: int = 8000, n_hi: int = 260000):
+    """Batched case: independent 2-region CHT systems of uneven size,
+    conductivity log-uniform in [0.1, 50] per cell."""
+    return [cht_system(nx, ny, nzf, nzs, seed=seed + 1 + i, k_range=(0.1, 50.0))
+            for i, (nx, ny, nzf, nzs) in enumerate(batch_shapes(count, n_lo, n_hi, seed))]
+
+
 def laplace_1d(n: int, dirichlet=(0.0, 1.0), k: float = 1.0):
     """1-D Laplacian with Dirichlet ends: exact solution is linear."""
     lower = np.arange(n - 1, dtype=np.int32)

@@ -22,6 +22,19 @@ struct mrg_mesh {
 struct mrg_ggi {
     Ggi g;
 };
+struct mrg_batch {
+    Ctx* ctx = nullptr;
+    int ordering = 0;
+    std::vector<Mesh*> meshes;
+    BatchHost bh;
+    double* d_stage = nullptr;    // caller-numbered b and x of every member
+    size_t stage_n = 0;
+    std::vector<size_t> offset;   // member s: b at offset[s], x at stage_n + offset[s]
+    ~mrg_batch()
+    {
+        if (ctx) ctx->release(d_stage);
+    }
+};
 
 namespace {
 // A plain buffer, not std::string: callers may reach the ABI from static
@@ -181,7 +194,6 @@ int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out)
             c->c.budget = hbm_budget_bytes;
             MRG_CUDA(cudaDeviceGetAttribute(&c->c.nsm, cudaDevAttrMultiProcessorCount, device));
             MRG_CUDA(cudaStreamCreateWithFlags(&c->c.st, cudaStreamNonBlocking));
-            c->c.d_ctl = (Ctl*)c->c.alloc(sizeof(Ctl));
             MRG_CUDA(cudaStreamSynchronize(c->c.st));
         } catch (...) {
             delete c;
@@ -470,6 +482,110 @@ int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp)
         MRG_CUDA(cudaMemcpyAsync(dst, g.d_dst, 8 * (size_t)g.n_dst * ncomp, cudaMemcpyDeviceToHost, c->st));
         MRG_CUDA(cudaStreamSynchronize(c->st));
         return (int)MRG_OK;
+    });
+}
+
+int mrg_batch_create(mrg_ctx* ctx, int n_meshes, mrg_mesh* const* meshes, int ordering, mrg_batch** out)
+{
+    return guard([&] {
+        if (!ctx || !out || n_meshes < 1 || !meshes) return fail(MRG_E_INVALID, "bad argument");
+        if (ordering < 0 || ordering > 1) return fail(MRG_E_INVALID, "unknown ordering");
+        *out = nullptr;
+        auto* b = new mrg_batch();
+        try {
+            b->ctx = &ctx->c;
+            b->ordering = ordering;
+            std::vector<PlanState*> plans;
+            size_t tot = 0;
+            for (int i = 0; i < n_meshes; ++i) {
+                if (!meshes[i] || meshes[i]->m.ctx != &ctx->c)
+                    throw Error(MRG_E_INVALID, "batch member " + std::to_string(i) + " is NULL or in another context");
+                for (int j = 0; j < i; ++j)
+                    if (meshes[j] == meshes[i])
+                        throw Error(MRG_E_INVALID, "a mesh appears twice in the batch");
+                b->meshes.push_back(&meshes[i]->m);
+                plans.push_back(&meshes[i]->m.plan(ordering));
+                b->offset.push_back(tot);
+                tot += (size_t)meshes[i]->m.n;
+            }
+            b->stage_n = tot;
+            b->d_stage = (double*)ctx->c.alloc(16 * tot);
+            b->bh.init(&ctx->c);
+            b->bh.set(plans);
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_batch_destroy(mrg_batch* batch)
+{
+    return guard([&] {
+        delete batch;
+        return (int)MRG_OK;
+    });
+}
+
+// Shared by the host and device variants: d_b[s], d_x[s] are device pointers.
+static int batch_solve_device(mrg_batch* batch, const double* const* d_b, double* const* d_x,
+                              const mrg_controls* controls, mrg_perf* perfs)
+{
+    Controls k = to_controls(controls);
+    if (k.ordering != batch->ordering) throw Error(MRG_E_INVALID, "controls.ordering differs from the batch's");
+    prepare_batch(batch->bh, batch->meshes, k);
+    for (size_t s = 0; s < batch->meshes.size(); ++s) {
+        PlanState* P = batch->bh.members[s];
+        P->sys.in_b = d_b[s];
+        P->sys.in_x = d_x[s];
+        P->sys.out_x = d_x[s];
+    }
+    batch->bh.sync_sys();
+    std::vector<Perf> r = solve_batch(batch->bh, k);
+    int status = MRG_OK;
+    for (size_t s = 0; s < r.size(); ++s) {
+        if (perfs) fill_perf(perfs + s, r[s]);
+        if (r[s].status != MRG_OK) status = r[s].status;
+    }
+    if (status != MRG_OK) return fail(status, "non-finite residual in a batch member (breakdown)");
+    return (int)MRG_OK;
+}
+
+int mrg_batch_solve_device(mrg_batch* batch, const double* const* d_b, double* const* d_x,
+                           const mrg_controls* controls, mrg_perf* perfs)
+{
+    return guard([&] {
+        if (!batch || !d_b || !d_x) return fail(MRG_E_INVALID, "NULL argument");
+        return batch_solve_device(batch, d_b, d_x, controls, perfs);
+    });
+}
+
+int mrg_batch_solve(mrg_batch* batch, const double* const* b, double* const* x, const mrg_controls* controls,
+                    mrg_perf* perfs)
+{
+    return guard([&] {
+        if (!batch || !b || !x) return fail(MRG_E_INVALID, "NULL argument");
+        Ctx* c = batch->ctx;
+        const size_t ns = batch->meshes.size();
+        std::vector<const double*> db(ns);
+        std::vector<double*> dx(ns);
+        for (size_t s = 0; s < ns; ++s) {
+            const size_t n = (size_t)batch->meshes[s]->n;
+            double* pb = batch->d_stage + batch->offset[s];
+            double* px = batch->d_stage + batch->stage_n + batch->offset[s];
+            if (!b[s] || !x[s]) return fail(MRG_E_INVALID, "NULL member vector");
+            MRG_CUDA(cudaMemcpyAsync(pb, b[s], 8 * n, cudaMemcpyHostToDevice, c->st));
+            MRG_CUDA(cudaMemcpyAsync(px, x[s], 8 * n, cudaMemcpyHostToDevice, c->st));
+            db[s] = pb;
+            dx[s] = px;
+        }
+        int rc = batch_solve_device(batch, db.data(), dx.data(), controls, perfs);
+        for (size_t s = 0; s < ns; ++s)
+            MRG_CUDA(cudaMemcpyAsync(x[s], dx[s], 8 * (size_t)batch->meshes[s]->n, cudaMemcpyDeviceToHost, c->st));
+        MRG_CUDA(cudaStreamSynchronize(c->st));
+        return rc;
     });
 }
 

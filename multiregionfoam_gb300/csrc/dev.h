@@ -1,10 +1,13 @@
 // dev.h -- plain-old-data views shared by host and device code.
 //
 // A "system" is one LDU matrix with its plan, coefficients, work vectors and
-// scalar solver state, all resident in HBM.  Kernels take an array of
-// SysDev (one entry for a single solve, many for a batch) and a tile table;
-// every per-system reduction is two-level and deterministic: one partial per
-// 1024-row tile, summed in tile order by the last tile to finish.
+// scalar solver state, all resident in HBM.  A "batch" is a set of systems
+// solved in lockstep: every kernel takes one device-resident Batch
+// descriptor (the system array, a tile table over all systems, the per-level
+// sweep work list and the control block), so a single solve is a batch of one
+// and a captured CUDA graph stays valid when the batch's membership changes.
+// Every per-system reduction is deterministic: one partial per contiguous
+// tile segment of a fixed-size grid, summed in slot order by the last CTA.
 #pragma once
 #include <cstdint>
 
@@ -12,8 +15,14 @@ namespace mrg {
 
 constexpr int kBlock = 256;   // threads per CTA for row kernels
 constexpr int kMaxRed = 2;    // values reduced per tile
+// A system of T tiles is reduced in G = min(T, kRedSegs) contiguous tile
+// segments, segment j = tiles [j*T/G, (j+1)*T/G): the summation order of
+// every per-system reduction depends only on the system itself -- not on
+// the device, the launch grid or the other members of a batch.
+constexpr int kRedSegs = 2432;
 
-// Scalar state of one solve (lduSolverPerformance + Krylov scalars).
+// Scalar state of one solve (lduSolverPerformance + Krylov scalars), plus
+// the FP64 outer state of a mixed-precision solve.
 struct Scal {
     double rho, rho_old, alpha, beta;
     double nfac, res0, res, xsum;
@@ -21,9 +30,15 @@ struct Scal {
     double red[kMaxRed];   // last finalised reduction sums (diagnostics)
     double osum;           // mixed: sum|b - A x| of the FP64 outer residual
     double inv_scale;      // mixed: FP32 inner system is scaled by 1/inv_scale
-    int min_iter, max_iter;
+    // mixed-precision outer (FP64) state and controls
+    double onfac, ores0, ores, obest;
+    double otol, orel_tol, inner_rel_tol;
+    int min_iter, max_iter;  // user controls (foam minIter / maxIter)
+    int kmin, kmax;          // bounds of the current Krylov loop
     int iter, active, converged, singular;
-    int status, pad;
+    int status, mixed;
+    int ostate, oconv, oiter, ostall;
+    int inner_total, inner_max, max_outer, pad;
 };
 
 template <typename V>
@@ -38,7 +53,7 @@ enum { PC_NONE = 0, PC_DIAG = 1, PC_DIC = 2, PC_DILU = 3 };
 struct SysDev {
     int n, npad, nsl, ntiles;
     int nchunks, nlevels, nf, ni, ngen, sym, pc;
-    int pad0;
+    int syncfree;          // exact ordering: sentinel-based sweeps
     // plan
     const int32_t *perm, *a_sptr, *a_col, *a_src, *chunk_start, *lvl_chunk;
     const int32_t *f_sptr, *f_col, *f_src, *b_sptr, *b_col, *b_src;
@@ -55,18 +70,36 @@ struct SysDev {
     float *f_c32, *f_cT32, *b_c32, *b_cT32, *rD32;
     Vecs<double> v64;
     Vecs<float> v32;
+    // caller-numbered input/output of the current solve
+    const double *in_b, *in_x;
+    double* out_x;
     // reductions / state
     double* partials;      // [ntiles * kMaxRed]
     unsigned* counter;     // [1]
     Scal* sc;
 };
 
-// Per-launch control block shared by the systems of one batch.
+// Control block of one batch.
 struct Ctl {
     unsigned ticket[8];    // sync-free sweep work counters
     unsigned err;          // error bits (1 = wait timeout)
-    unsigned n_active;
-    unsigned pad[6];
+    unsigned n_active;     // systems still in their Krylov loop
+    unsigned n_oactive;    // systems still in their mixed-precision outer loop
+    unsigned pad[5];
+    // controls written into every system's Scal by OP_BEGIN
+    double tol, rel_tol, inner_rel_tol;
+    int min_iter, max_iter, inner_max, max_outer, mixed, pad2;
+};
+
+// A batch of systems, resident on the device.
+struct Batch {
+    SysDev* sys;           // [nsys]
+    const int2* tiles;     // [ntiles] (system, tile within system), systems contiguous
+    const int2* segs;      // [nsegs] (system, reduction segment), see kRedSegs
+    const int2* items;     // level-sweep work: (system, chunk) grouped by level
+    const int* item_off;   // [maxlevels + 1]
+    Ctl* ctl;
+    int nsys, ntiles, nsegs, maxchunks, maxlevels, pad;
 };
 
 enum { ERR_TIMEOUT = 1u, ERR_BREAKDOWN = 2u };

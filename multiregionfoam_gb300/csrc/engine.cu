@@ -1,5 +1,5 @@
 // engine.cu -- host engine: device residency, plan upload, coefficient
-// views, CUDA-graph iteration loops, FP32/FP64 iterative refinement.
+// views, batches, CUDA-graph iteration loops, FP32/FP64 iterative refinement.
 #include "engine.h"
 
 #include <cuda_runtime.h>
@@ -66,12 +66,107 @@ static T* upload(Ctx* c, const std::vector<T>& v)
     return p;
 }
 
-// ------------------------------------------------------------------ PlanState
-PlanState::~PlanState()
+// One wave of 256-thread CTAs at the 4 per SM the kernels are compiled for.
+static int grid_sweep(const Ctx* c) { return c->nsm * 4; }
+
+// ------------------------------------------------------------------ BatchHost
+void BatchHost::init(Ctx* c)
+{
+    ctx = c;
+    d = (Batch*)c->alloc(sizeof(Batch));
+    d_ctl = (Ctl*)c->alloc(sizeof(Ctl));
+}
+
+BatchHost::~BatchHost()
 {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
-    // device memory is owned by ctx allocations and freed with the mesh
+    if (!ctx) return;
+    for (void* p : {(void*)d, (void*)d_ctl, (void*)d_sys, (void*)d_tiles, (void*)d_segs, (void*)d_items,
+                    (void*)d_item_off})
+        ctx->release(p);
 }
+
+template <typename T>
+static void ensure(Ctx* c, T*& p, size_t& cap, size_t n)
+{
+    if (cap >= n && p) return;
+    c->release(p);
+    cap = std::max<size_t>(n, 1);
+    p = (T*)c->alloc(sizeof(T) * cap);
+}
+
+void BatchHost::set(const std::vector<PlanState*>& systems)
+{
+    members = systems;
+    const int nsys = (int)systems.size();
+    std::vector<SysDev> sv(nsys);
+    std::vector<int2> tiles, segs;
+    int maxchunks = 0, maxlevels = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const PlanState* P = systems[s];
+        sv[s] = P->sys;
+        for (int t = 0; t < P->ntiles; ++t) tiles.push_back(make_int2(s, t));
+        for (int j = 0; j < std::min(P->ntiles, kRedSegs); ++j) segs.push_back(make_int2(s, j));
+        maxchunks = std::max(maxchunks, P->sys.nchunks);
+        if (!P->sys.syncfree) maxlevels = std::max(maxlevels, P->sys.nlevels);
+    }
+    // level-sweep work list (colour-ordered members): (system, chunk) by level
+    std::vector<int2> items;
+    std::vector<int> off(maxlevels + 1, 0);
+    widest_level = 1;
+    for (int L = 0; L < maxlevels; ++L) {
+        off[L] = (int)items.size();
+        for (int s = 0; s < nsys; ++s) {
+            const PlanState* P = systems[s];
+            if (P->sys.syncfree || L >= P->sys.nlevels) continue;
+            for (int c = P->host.lvl_chunk[L]; c < P->host.lvl_chunk[L + 1]; ++c) items.push_back(make_int2(s, c));
+        }
+        widest_level = std::max(widest_level, (int)items.size() - off[L]);
+    }
+    off[maxlevels] = (int)items.size();
+    ensure(ctx, d_sys, cap_sys, (size_t)nsys);
+    ensure(ctx, d_tiles, cap_tiles, tiles.size());
+    ensure(ctx, d_segs, cap_segs, segs.size());
+    ensure(ctx, d_items, cap_items, items.size());
+    ensure(ctx, d_item_off, cap_off, off.size());
+    cudaStream_t st = ctx->st;
+    if (nsys) MRG_CUDA(cudaMemcpyAsync(d_sys, sv.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, st));
+    if (!tiles.empty())
+        MRG_CUDA(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, st));
+    if (!segs.empty())
+        MRG_CUDA(cudaMemcpyAsync(d_segs, segs.data(), sizeof(int2) * segs.size(), cudaMemcpyHostToDevice, st));
+    if (!items.empty())
+        MRG_CUDA(cudaMemcpyAsync(d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, st));
+    MRG_CUDA(cudaMemcpyAsync(d_item_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
+    h.sys = d_sys;
+    h.tiles = d_tiles;
+    h.segs = d_segs;
+    h.nsegs = (int)segs.size();
+    h.items = d_items;
+    h.item_off = d_item_off;
+    h.ctl = d_ctl;
+    h.nsys = nsys;
+    h.ntiles = (int)tiles.size();
+    h.maxchunks = maxchunks;
+    h.maxlevels = maxlevels;
+    MRG_CUDA(cudaMemcpyAsync(d, &h, sizeof(Batch), cudaMemcpyHostToDevice, st));
+    // graphs sized for the previous membership are rebuilt lazily
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+    graphs.clear();
+    MRG_CUDA(cudaStreamSynchronize(st));
+}
+
+void BatchHost::sync_sys()
+{
+    const int nsys = (int)members.size();
+    std::vector<SysDev> sv(nsys);
+    for (int s = 0; s < nsys; ++s) sv[s] = members[s]->sys;
+    if (nsys)
+        MRG_CUDA(cudaMemcpyAsync(d_sys, sv.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, ctx->st));
+}
+
+// ------------------------------------------------------------------ PlanState
+PlanState::~PlanState() {}
 
 void PlanState::sync_sys()
 {
@@ -81,23 +176,19 @@ void PlanState::sync_sys()
 static void release_plan(Ctx* c, PlanState* P)
 {
     void* ptrs[] = {P->perm, P->a_sptr, P->a_col, P->a_src, P->chunk_start, P->lvl_chunk, P->f_sptr, P->f_col,
-                    P->f_src, P->b_sptr, P->b_col, P->b_src, P->g_ptr, P->g_src, P->g_w, P->g_w32,
-                    P->d_sys, P->d_tiles};
+                    P->f_src, P->b_sptr, P->b_col, P->b_src, P->g_ptr, P->g_src, P->g_w, P->g_w32, P->d_sys};
     for (void* p : ptrs) c->release(p);
     SysDev& S = P->sys;
     void* vals[] = {S.a_val, S.aT_val != S.a_val ? S.aT_val : nullptr, S.diag, S.sumA, S.f_c, S.f_cT, S.b_c,
                     S.b_cT, S.rD, S.D, S.a_val32, S.aT_val32 != S.a_val32 ? S.aT_val32 : nullptr, S.diag32,
                     S.f_c32, S.f_cT32, S.b_c32, S.b_cT32, S.rD32, S.partials, S.counter, S.sc};
     for (void* p : vals) c->release(p);
-    for (auto* V : {&S.v64}) {
-        void* vv[] = {V->x, V->b, V->r, V->w, V->y, V->p, V->q, V->rT, V->wT, V->yT, V->pT, V->qT};
-        for (void* p : vv) c->release(p);
-    }
-    {
-        auto* V = &S.v32;
-        void* vv[] = {V->x, V->b, V->r, V->w, V->y, V->p, V->q, V->rT, V->wT, V->yT, V->pT, V->qT};
-        for (void* p : vv) c->release(p);
-    }
+    for (void* p : {(void*)S.v64.x, (void*)S.v64.b, (void*)S.v64.r, (void*)S.v64.w, (void*)S.v64.y,
+                    (void*)S.v64.p, (void*)S.v64.q, (void*)S.v64.rT, (void*)S.v64.wT, (void*)S.v64.yT,
+                    (void*)S.v64.pT, (void*)S.v64.qT, (void*)S.v32.x, (void*)S.v32.b, (void*)S.v32.r,
+                    (void*)S.v32.w, (void*)S.v32.y, (void*)S.v32.p, (void*)S.v32.q, (void*)S.v32.rT,
+                    (void*)S.v32.wT, (void*)S.v32.yT, (void*)S.v32.pT, (void*)S.v32.qT})
+        c->release(p);
 }
 
 // ------------------------------------------------------------------ Mesh
@@ -140,9 +231,9 @@ PlanState& Mesh::plan(int ordering)
         P->g_w32 = upload(c, w32);
     }
     P->ntiles = H.npad / kTileRows;
-    std::vector<int2> tiles(P->ntiles);
-    for (int t = 0; t < P->ntiles; ++t) tiles[t] = make_int2(0, t);
-    P->d_tiles = upload(c, tiles);
+    P->nnz = H.a_col.size();
+    P->fnz = H.f_col.size();
+    P->bnz = H.b_col.size();
 
     SysDev& S = P->sys;
     std::memset(&S, 0, sizeof S);
@@ -157,6 +248,7 @@ PlanState& Mesh::plan(int ordering)
     S.ngen = H.ngen;
     S.sym = 1;
     S.pc = PC_NONE;
+    S.syncfree = ordering == 0 ? 1 : 0;
     S.perm = P->perm;
     S.a_sptr = P->a_sptr;
     S.a_col = P->a_col;
@@ -173,16 +265,15 @@ PlanState& Mesh::plan(int ordering)
     S.g_src = P->g_src;
     S.g_w = P->g_w;
     S.g_w32 = P->g_w32;
-    const size_t nnz = H.a_col.size(), fnz = H.f_col.size(), bnz = H.b_col.size();
     const size_t np = (size_t)H.npad, nx = (size_t)H.npad + H.ngen;
-    S.a_val = (double*)c->alloc(8 * nnz);
+    S.a_val = (double*)c->alloc(8 * P->nnz);
     S.aT_val = S.a_val;
     S.diag = (double*)c->alloc(8 * np);
     S.sumA = (double*)c->alloc(8 * np);
-    S.f_c = (double*)c->alloc(8 * fnz);
-    S.f_cT = (double*)c->alloc(8 * fnz);
-    S.b_c = (double*)c->alloc(8 * bnz);
-    S.b_cT = (double*)c->alloc(8 * bnz);
+    S.f_c = (double*)c->alloc(8 * P->fnz);
+    S.f_cT = (double*)c->alloc(8 * P->fnz);
+    S.b_c = (double*)c->alloc(8 * P->bnz);
+    S.b_cT = (double*)c->alloc(8 * P->bnz);
     S.rD = (double*)c->alloc(8 * np);
     S.D = (double*)c->alloc(8 * np);
     S.v64.x = (double*)c->alloc(8 * nx);
@@ -197,69 +288,59 @@ PlanState& Mesh::plan(int ordering)
     S.sc = (Scal*)c->alloc(sizeof(Scal));
     P->d_sys = (SysDev*)c->alloc(sizeof(SysDev));
     P->sync_sys();
-    // Keep only sizes on the host.
-    H.perm.clear(); H.perm.shrink_to_fit();
-    H.a_col.clear(); H.a_col.shrink_to_fit();
-    H.a_src.clear(); H.a_src.shrink_to_fit();
-    H.f_col.clear(); H.f_col.shrink_to_fit();
-    H.f_src.clear(); H.f_src.shrink_to_fit();
-    H.b_col.clear(); H.b_col.shrink_to_fit();
-    H.b_src.clear(); H.b_src.shrink_to_fit();
-    H.iperm.clear(); H.iperm.shrink_to_fit();
-    H.level_of_row.clear(); H.level_of_row.shrink_to_fit();
-    H.a_sptr.clear(); H.a_sptr.shrink_to_fit();
-    H.f_sptr.clear(); H.f_sptr.shrink_to_fit();
-    H.b_sptr.clear(); H.b_sptr.shrink_to_fit();
-    // sizes retained for workspace allocation
-    H.g_ptr.clear();
-    H.g_src.clear();
+    // Keep only sizes (and the per-level chunk offsets) on the host.
+    for (auto* v : {&H.perm, &H.a_col, &H.a_src, &H.f_col, &H.f_src, &H.b_col, &H.b_src, &H.iperm,
+                    &H.level_of_row, &H.a_sptr, &H.f_sptr, &H.b_sptr, &H.g_ptr, &H.g_src, &H.chunk_start}) {
+        v->clear();
+        v->shrink_to_fit();
+    }
     H.g_w.clear();
-    H.chunk_start.clear();  // lvl_chunk (one int per level) stays for launch sizing
+    H.g_w.shrink_to_fit();
+    P->single.init(c);
+    P->single.set({P.get()});
     plans[ordering] = std::move(P);
-    // entry counts for the lazily allocated FP32 / transpose arrays
-    nnz_cache[ordering][0] = nnz;
-    nnz_cache[ordering][1] = fnz;
-    nnz_cache[ordering][2] = bnz;
     MRG_CUDA(cudaStreamSynchronize(c->st));
     return *plans[ordering];
 }
 
 // ------------------------------------------------------------------ prepare
-// One wave of 256-thread CTAs at the 4 per SM the kernels are compiled for.
-static int grid_rows(const Ctx* c, int ntiles) { return std::max(1, std::min(ntiles, c->nsm * 4)); }
-static int grid_sweep(const Ctx* c) { return c->nsm * 4; }
-
-PlanState& prepare(Mesh& m, const Controls& cfg)
+// Allocations a system needs for these controls; returns true when its
+// SysDev changed (the batch arrays must be re-uploaded).
+static bool ensure_views(Mesh& m, PlanState& P, const Controls& cfg)
 {
-    if (!m.have_coeffs) throw Error(MRG_E_INVALID, "no coefficients uploaded for this mesh");
-    PlanState& P = m.plan(cfg.ordering);
     Ctx* c = m.ctx;
     SysDev& S = P.sys;
-    const size_t nnz = m.nnz_cache[cfg.ordering][0], fnz = m.nnz_cache[cfg.ordering][1],
-                 bnz = m.nnz_cache[cfg.ordering][2];
     const size_t np = (size_t)S.npad, nx = (size_t)S.npad + S.ngen;
-    bool rescatter = P.scattered != m.version;
     const bool asym = !m.sym || m.has_int;
-    const bool need32 = cfg.precision == 1;
+    const bool need32 = cfg.precision == MRG_PRECISION_MIXED;
     const bool needT = cfg.solver == MRG_SOLVER_PBICG;
-    S.sym = m.sym ? 1 : 0;
-    S.raw_diag = m.raw_diag;
-    S.raw_upper = m.raw_upper;
-    S.raw_lower = m.raw_lower;
-    S.raw_ibou = m.raw_ibou;
-    S.raw_iint = m.raw_iint;
+    bool changed = false;
+    auto setp = [&](auto& field, auto value) {
+        if (field != value) {
+            field = value;
+            changed = true;
+        }
+    };
+    setp(S.sym, m.sym ? 1 : 0);
+    setp(S.raw_diag, (const double*)m.raw_diag);
+    setp(S.raw_upper, (const double*)m.raw_upper);
+    setp(S.raw_lower, (const double*)m.raw_lower);
+    setp(S.raw_ibou, (const double*)m.raw_ibou);
+    setp(S.raw_iint, (const double*)m.raw_iint);
+    setp(S.pc, cfg.pc);
     if (asym && S.aT_val == S.a_val) {
-        S.aT_val = (double*)c->alloc(8 * nnz);
-        rescatter = true;
+        S.aT_val = (double*)c->alloc(8 * P.nnz);
+        P.scattered = 0;
+        changed = true;
     }
     if (need32 && !P.have32) {
-        S.a_val32 = (float*)c->alloc(4 * nnz);
-        S.aT_val32 = asym ? (float*)c->alloc(4 * nnz) : S.a_val32;
+        S.a_val32 = (float*)c->alloc(4 * P.nnz);
+        S.aT_val32 = asym ? (float*)c->alloc(4 * P.nnz) : S.a_val32;
         S.diag32 = (float*)c->alloc(4 * np);
-        S.f_c32 = (float*)c->alloc(4 * fnz);
-        S.f_cT32 = (float*)c->alloc(4 * fnz);
-        S.b_c32 = (float*)c->alloc(4 * bnz);
-        S.b_cT32 = (float*)c->alloc(4 * bnz);
+        S.f_c32 = (float*)c->alloc(4 * P.fnz);
+        S.f_cT32 = (float*)c->alloc(4 * P.fnz);
+        S.b_c32 = (float*)c->alloc(4 * P.bnz);
+        S.b_cT32 = (float*)c->alloc(4 * P.bnz);
         S.rD32 = (float*)c->alloc(4 * np);
         S.v32.x = (float*)c->alloc(4 * nx);
         S.v32.p = (float*)c->alloc(4 * nx);
@@ -268,11 +349,13 @@ PlanState& prepare(Mesh& m, const Controls& cfg)
         S.v32.y = (float*)c->alloc(4 * np);
         S.v32.q = (float*)c->alloc(4 * np);
         P.have32 = true;
-        rescatter = true;
+        P.scattered = 0;
+        changed = true;
     }
     if (need32 && asym && S.aT_val32 == S.a_val32) {
-        S.aT_val32 = (float*)c->alloc(4 * nnz);
-        rescatter = true;
+        S.aT_val32 = (float*)c->alloc(4 * P.nnz);
+        P.scattered = 0;
+        changed = true;
     }
     if (needT && !P.haveT) {
         S.v64.rT = (double*)c->alloc(8 * np);
@@ -281,102 +364,133 @@ PlanState& prepare(Mesh& m, const Controls& cfg)
         S.v64.pT = (double*)c->alloc(8 * nx);
         S.v64.qT = (double*)c->alloc(8 * np);
         P.haveT = true;
+        changed = true;
     }
-    if (needT && need32 && !S.v32.rT) {
+    if (needT && need32 && !P.haveT32) {
         S.v32.rT = (float*)c->alloc(4 * np);
         S.v32.wT = (float*)c->alloc(4 * np);
         S.v32.yT = (float*)c->alloc(4 * np);
         S.v32.pT = (float*)c->alloc(4 * nx);
         S.v32.qT = (float*)c->alloc(4 * np);
+        P.haveT32 = true;
+        changed = true;
     }
-    S.pc = cfg.pc;
-    P.sync_sys();
-    if (rescatter) {
-        launch_rows(OP_SCATTER, 0, P.d_sys, P.d_tiles, P.ntiles, grid_rows(c, P.ntiles), 0, c->st);
+    if (changed) P.sync_sys();
+    return changed;
+}
+
+void prepare_batch(BatchHost& bh, const std::vector<Mesh*>& meshes, const Controls& cfg)
+{
+    Ctx* c = bh.ctx;
+    bool changed = false, rescatter = false, refactor = false;
+    const bool want32 = cfg.precision == MRG_PRECISION_MIXED;
+    for (size_t s = 0; s < meshes.size(); ++s) {
+        Mesh& m = *meshes[s];
+        PlanState& P = *bh.members[s];
+        if (!m.have_coeffs) throw Error(MRG_E_INVALID, "no coefficients uploaded for a mesh of the batch");
+        changed |= ensure_views(m, P, cfg);
+        if (P.scattered != m.version) rescatter = true;
+        if (cfg.pc >= PC_DIAG &&
+            (P.factored != m.version || P.factored_pc != cfg.pc || (want32 && !P.factored32)))
+            refactor = true;
+    }
+    if (changed) {
+        bh.sync_sys();
+        // the single-system batches of the members see the same SysDev
+        for (PlanState* P : bh.members)
+            if (&P->single != &bh) P->single.sync_sys();
+    }
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    // the factor re-arms from the scatter (which writes D's sentinels)
+    if (rescatter || (refactor && cfg.pc >= PC_DIC)) {
+        launch_rows(OP_SCATTER, 0, bh.d, nt, ns, 0, c->st);
         MRG_CUDA(cudaGetLastError());
-        P.scattered = m.version;
-        P.factored = 0;
     }
-    const bool want32 = need32;
-    if (cfg.pc >= PC_DIC) {
-        if (P.factored != m.version || P.factored_pc != cfg.pc || (want32 && !P.factored32)) {
-            launch_fill_sentinel(S.D, S.n, 0, c->st);
-            launch_factor(P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), want32 ? 1 : 0, c->st);
-            MRG_CUDA(cudaGetLastError());
-            P.factored = m.version;
-            P.factored_pc = cfg.pc;
-            P.factored32 = want32;
-        }
-    } else if (cfg.pc == PC_DIAG) {
-        if (P.factored != m.version || P.factored_pc != cfg.pc || (want32 && !P.factored32)) {
-            launch_rows(OP_DIAG_RD, 0, P.d_sys, P.d_tiles, P.ntiles, grid_rows(c, P.ntiles), 0, c->st);
-            MRG_CUDA(cudaGetLastError());
-            P.factored = m.version;
+    if (refactor) {
+        if (cfg.pc >= PC_DIC)
+            launch_factor(bh.d, grid_sweep(c), want32 ? 1 : 0, c->st);
+        else
+            launch_rows(OP_DIAG_RD, 0, bh.d, nt, ns, 0, c->st);
+        MRG_CUDA(cudaGetLastError());
+    }
+    for (size_t s = 0; s < meshes.size(); ++s) {
+        PlanState& P = *bh.members[s];
+        P.scattered = meshes[s]->version;
+        if (refactor) {
+            P.factored = meshes[s]->version;
             P.factored_pc = cfg.pc;
             P.factored32 = want32;
         }
     }
+}
+
+PlanState& prepare(Mesh& m, const Controls& cfg)
+{
+    if (!m.have_coeffs) throw Error(MRG_E_INVALID, "no coefficients uploaded for this mesh");
+    PlanState& P = m.plan(cfg.ordering);
+    std::vector<Mesh*> ms{&m};
+    prepare_batch(P.single, ms, cfg);
     return P;
 }
 
 // ------------------------------------------------------------------ graphs
-static void record_precondition(PlanState& P, const Controls& cfg, int prec, int trans, cudaStream_t st)
+static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, int trans, cudaStream_t st)
 {
-    Ctx* c = P.ctx;
-    const SysDev& S = P.sys;
-    if (cfg.pc >= PC_DIC) {
-        if (cfg.ordering == MRG_ORDER_EXACT) {
-            launch_sweep(prec, 1, trans, 1, 0, P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), st);
-            launch_sweep(prec, 0, trans, 1, 0, P.d_sys, 1, S.nchunks, c->d_ctl, grid_sweep(c), st);
-        } else {
-            // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
-            // nl == 1); one chunk per warp of the widest level
-            const int nl = S.nlevels;
-            int widest = 1;
-            for (int L = 0; L < nl; ++L)
-                widest = std::max(widest, P.host.lvl_chunk[L + 1] - P.host.lvl_chunk[L]);
-            const int g = std::max(1, std::min(65535, (widest + 7) / 8));
-            for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
-            for (int L = std::max(nl - 2, 0); L >= 0; --L)
-                launch_sweep(prec, 0, trans, 0, L, P.d_sys, 1, 0, nullptr, g, st);
-        }
-    }
-}
-
-static void record_iteration(PlanState& P, const Controls& cfg, int prec, cudaStream_t st)
-{
-    Ctx* c = P.ctx;
-    const int pb = cfg.solver == MRG_SOLVER_PBICG;
-    const int g = grid_rows(c, P.ntiles);
-    if (cfg.pc >= PC_DIC) {
-        record_precondition(P, cfg, prec, 0, st);
-        if (pb) record_precondition(P, cfg, prec, 1, st);
-    } else if (cfg.pc == PC_DIAG) {
-        launch_rows(OP_PRECOND_DIAG, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
+    Ctx* c = bh.ctx;
+    if (cfg.pc < PC_DIC) return;
+    if (cfg.ordering == MRG_ORDER_EXACT) {
+        launch_sweep(prec, 1, trans, 1, 0, bh.d, grid_sweep(c), st);
+        launch_sweep(prec, 0, trans, 1, 0, bh.d, grid_sweep(c), st);
     } else {
-        launch_rows(OP_PRECOND_NONE, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
+        // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
+        // nl == 1); one chunk per warp of the widest level
+        const int nl = bh.h.maxlevels;
+        const int g = std::max(1, std::min(65535, (bh.widest_level + 7) / 8));
+        for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, bh.d, g, st);
+        for (int L = std::max(nl - 2, 0); L >= 0; --L) launch_sweep(prec, 0, trans, 0, L, bh.d, g, st);
     }
-    launch_rows(OP_RHO, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
-    launch_rows(OP_PUPDATE, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
-    if (P.sys.ngen) {
-        launch_iface_gather(prec, 0, P.d_sys, 1, 64, st);
-        if (pb) launch_iface_gather(prec, 2, P.d_sys, 1, 64, st);
-    }
-    launch_rows(OP_SPMV_QP, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
-    launch_rows(OP_UPDATE, prec, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
 }
 
-static PlanState::Graph iteration_graph(PlanState& P, const Controls& cfg, int prec, int k)
+static bool any_general_iface(const BatchHost& bh)
+{
+    for (const PlanState* P : bh.members)
+        if (P->sys.ngen) return true;
+    return false;
+}
+
+static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaStream_t st)
+{
+    const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    if (cfg.pc >= PC_DIC) {
+        record_precondition(bh, cfg, prec, 0, st);
+        if (pb) record_precondition(bh, cfg, prec, 1, st);
+    } else if (cfg.pc == PC_DIAG) {
+        launch_rows(OP_PRECOND_DIAG, prec, bh.d, nt, ns, pb, st);
+    } else {
+        launch_rows(OP_PRECOND_NONE, prec, bh.d, nt, ns, pb, st);
+    }
+    launch_rows(OP_RHO, prec, bh.d, nt, ns, pb, st);
+    launch_rows(OP_PUPDATE, prec, bh.d, nt, ns, pb, st);
+    if (any_general_iface(bh)) {
+        launch_iface_gather(prec, 0, bh.d, 64, st);
+        if (pb) launch_iface_gather(prec, 2, bh.d, 64, st);
+    }
+    launch_rows(OP_SPMV_QP, prec, bh.d, nt, ns, pb, st);
+    launch_rows(OP_UPDATE, prec, bh.d, nt, ns, pb, st);
+}
+
+static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int prec, int k)
 {
     std::string key = std::to_string(cfg.solver) + "/" + std::to_string(cfg.pc) + "/" +
                       std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k);
-    auto it = P.graphs.find(key);
-    if (it != P.graphs.end()) return it->second;
-    cudaStream_t st = P.ctx->st;
+    auto it = bh.graphs.find(key);
+    if (it != bh.graphs.end()) return it->second;
+    cudaStream_t st = bh.ctx->st;
     cudaGraph_t g = nullptr;
     const unsigned long long before = launch_count();
     MRG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < k; ++i) record_iteration(P, cfg, prec, st);
+    for (int i = 0; i < k; ++i) record_iteration(bh, cfg, prec, st);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     const long long nodes = (long long)(launch_count() - before);
     add_launches(-nodes);  // captured, not executed
@@ -384,166 +498,123 @@ static PlanState::Graph iteration_graph(PlanState& P, const Controls& cfg, int p
     cudaGraphExec_t ex = nullptr;
     MRG_CUDA(cudaGraphInstantiate(&ex, g, 0));
     cudaGraphDestroy(g);
-    PlanState::Graph gr{ex, nodes};
-    P.graphs[key] = gr;
+    BatchHost::Graph gr{ex, nodes};
+    bh.graphs[key] = gr;
     return gr;
 }
 
-struct Poll {
-    Scal sc;
-    Ctl ctl;
-};
-
-static Poll* pinned_poll()
+static Ctl* pinned_ctl()
 {
-    static thread_local Poll* p = nullptr;
-    if (!p) MRG_CUDA(cudaMallocHost((void**)&p, sizeof(Poll)));
+    static thread_local Ctl* p = nullptr;
+    if (!p) MRG_CUDA(cudaMallocHost((void**)&p, sizeof(Ctl)));
     return p;
 }
 
-static void poll(PlanState& P, Poll* h)
+static void poll(BatchHost& bh, Ctl* h)
 {
-    Ctx* c = P.ctx;
-    MRG_CUDA(cudaMemcpyAsync(&h->sc, P.sys.sc, sizeof(Scal), cudaMemcpyDeviceToHost, c->st));
-    MRG_CUDA(cudaMemcpyAsync(&h->ctl, c->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->st));
+    Ctx* c = bh.ctx;
+    MRG_CUDA(cudaMemcpyAsync(h, bh.d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->st));
     MRG_CUDA(cudaStreamSynchronize(c->st));
-    if (h->ctl.err) {
+    if (h->err) {
         unsigned zero = 0;
-        MRG_CUDA(cudaMemcpy(&c->d_ctl->err, &zero, sizeof zero, cudaMemcpyHostToDevice));
+        MRG_CUDA(cudaMemcpy(&bh.d_ctl->err, &zero, sizeof zero, cudaMemcpyHostToDevice));
         throw Error(MRG_E_TIMEOUT, "device wait timed out in a preconditioner sweep");
     }
 }
 
-// Runs Krylov iterations until the device state says stop.
-static void run_iterations(PlanState& P, const Controls& cfg, int prec, int max_iter, Poll* h)
+// Replays the iteration graph until no member is in its Krylov loop.
+static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long cap_iters, Ctl* h)
 {
-    Ctx* c = P.ctx;
     const int k = std::max(1, cfg.k_launch);
-    PlanState::Graph gr = iteration_graph(P, cfg, prec, k);
-    poll(P, h);
+    BatchHost::Graph gr = iteration_graph(bh, cfg, prec, k);
+    poll(bh, h);
     long launches = 0;
-    const long cap = (long)max_iter / k + 2 + (long)cfg.min_iter / k;
-    while (h->sc.active && launches <= cap) {
-        MRG_CUDA(cudaGraphLaunch(gr.exec, c->st));
+    const long cap = cap_iters / k + 2;
+    while (h->n_active > 0 && launches <= cap) {
+        MRG_CUDA(cudaGraphLaunch(gr.exec, bh.ctx->st));
         add_launches(gr.nodes);
         ++launches;
-        poll(P, h);
+        poll(bh, h);
     }
 }
 
-static void write_controls(PlanState& P, double tol, double rel_tol, int min_iter, int max_iter)
+static void write_ctl_controls(BatchHost& bh, const Controls& cfg)
 {
-    struct {
-        double tol, rel_tol;
-    } d{tol, rel_tol};
-    struct {
-        int min_iter, max_iter;
-    } i{min_iter, max_iter};
-    Ctx* c = P.ctx;
-    char* base = (char*)P.sys.sc;
-    MRG_CUDA(cudaMemcpyAsync(base + offsetof(Scal, tol), &d, sizeof d, cudaMemcpyHostToDevice, c->st));
-    MRG_CUDA(cudaMemcpyAsync(base + offsetof(Scal, min_iter), &i, sizeof i, cudaMemcpyHostToDevice, c->st));
-    MRG_CUDA(cudaStreamSynchronize(c->st));
+    Ctl host{};
+    host.tol = cfg.tol;
+    host.rel_tol = cfg.rel_tol;
+    host.inner_rel_tol = cfg.inner_rel_tol;
+    host.min_iter = cfg.min_iter;
+    host.max_iter = cfg.max_iter;
+    host.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : cfg.max_iter;
+    host.max_outer = cfg.max_outer;
+    host.mixed = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
+    // tickets, error bits and active counts start at zero
+    MRG_CUDA(cudaMemcpyAsync(bh.d_ctl, &host, sizeof(Ctl), cudaMemcpyHostToDevice, bh.ctx->st));
 }
 
-static void init_sentinels(PlanState& P, const Controls& cfg, int prec)
+std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
 {
-    if (cfg.pc < PC_DIC || cfg.ordering != MRG_ORDER_EXACT) return;
-    const SysDev& S = P.sys;
-    Ctx* c = P.ctx;
-    if (prec == 0) {
-        launch_fill_sentinel(S.v64.y, S.n, 0, c->st);
-        if (cfg.solver == MRG_SOLVER_PBICG) launch_fill_sentinel(S.v64.yT, S.n, 0, c->st);
-    } else {
-        launch_fill_sentinel(S.v32.y, S.n, 1, c->st);
-        if (cfg.solver == MRG_SOLVER_PBICG) launch_fill_sentinel(S.v32.yT, S.n, 1, c->st);
-    }
-}
-
-Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
-{
-    Ctx* c = m.ctx;
-    PlanState& P = prepare(m, cfg);
-    const SysDev& S = P.sys;
+    Ctx* c = bh.ctx;
     cudaStream_t st = c->st;
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
-    const int g = grid_rows(c, P.ntiles);
-    Poll* h = pinned_poll();
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    const bool gen = any_general_iface(bh);
+    Ctl* h = pinned_ctl();
     cudaEvent_t e0, e1;
     MRG_CUDA(cudaEventCreate(&e0));
     MRG_CUDA(cudaEventCreate(&e1));
-    MRG_CUDA(cudaEventRecord(e0, st));
-    Perf perf;
+    std::vector<Perf> out(bh.members.size());
     try {
-        launch_permute(1, P.d_sys, 0, d_b, S.v64.b, S.n, st);
-        launch_permute(1, P.d_sys, 0, d_x, S.v64.x, S.n, st);
-        write_controls(P, cfg.tol, cfg.rel_tol, cfg.min_iter, cfg.max_iter);
-        if (S.ngen) launch_iface_gather(0, 1, P.d_sys, 1, 64, st);
-        launch_rows(OP_SUMX, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
-        launch_rows(OP_INIT_RES, 0, P.d_sys, P.d_tiles, P.ntiles, g, pb, st);
+        MRG_CUDA(cudaEventRecord(e0, st));
+        write_ctl_controls(bh, cfg);
+        launch_rows(OP_PERMUTE_IN, 0, bh.d, nt, ns, 0, st);
+        launch_rows(OP_BEGIN, 0, bh.d, nt, ns, pb, st);
+        if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+        launch_rows(OP_SUMX, 0, bh.d, nt, ns, 0, st);
+        launch_rows(OP_INIT_RES, 0, bh.d, nt, ns, pb, st);
         MRG_CUDA(cudaGetLastError());
         if (cfg.precision == MRG_PRECISION_FP64) {
-            init_sentinels(P, cfg, 0);
-            run_iterations(P, cfg, 0, cfg.max_iter, h);
-            perf.res0 = h->sc.res0;
-            perf.res = h->sc.res;
-            perf.iters = h->sc.iter;
-            perf.converged = h->sc.converged;
-            perf.singular = h->sc.singular;
+            run_iterations(bh, cfg, 0, cfg.max_iter + cfg.min_iter, h);
         } else {
-            poll(P, h);
-            const double nfac = h->sc.nfac, res0 = h->sc.res0;
-            perf.res0 = res0;
-            double res = res0;
-            bool conv = h->sc.converged;
-            int inner_total = 0, outer = 0;
-            const int inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : cfg.max_iter;
-            double best = res;
-            int stall = 0;
-            while ((!conv || inner_total < cfg.min_iter) && outer < cfg.max_outer && inner_total < cfg.max_iter) {
-                if (S.ngen) launch_iface_gather(0, 1, P.d_sys, 1, 64, st);
-                launch_rows(OP_RESID64, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
-                // Each refinement step aims past the target (0.1 x the residual
-                // still to remove) so the last step overshoots instead of
-                // landing just under the tolerance; the FP32 inner solve is not
-                // asked for more than inner_rel_tol per step.
-                const double goal = std::max(cfg.tol, cfg.rel_tol > 1e-20 ? cfg.rel_tol * res0 : 0.0);
-                const double inner_tol = std::min(0.5, std::max(cfg.inner_rel_tol, 0.1 * goal / res));
-                write_controls(P, inner_tol, 0.0, 0, std::min(inner_max, cfg.max_iter - inner_total));
-                launch_rows(OP_TO32, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
-                if (pb) {
-                    // transpose residual of the correction system starts equal to r
-                    MRG_CUDA(cudaMemcpyAsync(S.v32.rT, S.v32.r, 4 * (size_t)S.npad, cudaMemcpyDeviceToDevice, st));
-                }
-                init_sentinels(P, cfg, 1);
-                run_iterations(P, cfg, 1, inner_max, h);
-                inner_total += h->sc.iter;
-                ++outer;
-                launch_rows(OP_CORRECT, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
-                if (S.ngen) launch_iface_gather(0, 1, P.d_sys, 1, 64, st);
-                launch_rows(OP_RESID64, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, st);
-                poll(P, h);
-                res = h->sc.osum / nfac;
-                conv = res < cfg.tol || (cfg.rel_tol > 1e-20 && res < cfg.rel_tol * res0);
-                if (!(res < best * 0.999)) {
-                    if (++stall >= 3) break;
-                } else {
-                    stall = 0;
-                    best = res;
-                }
-                if (h->sc.iter == 0) break;
+            for (int outer = 0; outer <= cfg.max_outer + 1; ++outer) {
+                if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+                launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
+                poll(bh, h);
+                if (h->n_oactive == 0) break;
+                launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
+                run_iterations(bh, cfg, 1, cfg.max_iter, h);
+                launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
             }
-            perf.res = res;
-            perf.iters = inner_total;
-            perf.outer = outer;
-            perf.converged = conv;
         }
-        launch_permute(0, P.d_sys, 0, S.v64.x, d_x, S.n, st);
+        launch_rows(OP_PERMUTE_OUT, 0, bh.d, nt, ns, 0, st);
         MRG_CUDA(cudaEventRecord(e1, st));
         MRG_CUDA(cudaEventSynchronize(e1));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
-        perf.ms = ms;
+        std::vector<Scal> sc(bh.members.size());
+        for (size_t s = 0; s < bh.members.size(); ++s)
+            MRG_CUDA(cudaMemcpyAsync(&sc[s], bh.members[s]->sys.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+        MRG_CUDA(cudaStreamSynchronize(st));
+        for (size_t s = 0; s < bh.members.size(); ++s) {
+            Perf& p = out[s];
+            const Scal& q = sc[s];
+            if (cfg.precision == MRG_PRECISION_FP64) {
+                p.res0 = q.res0;
+                p.res = q.res;
+                p.iters = q.iter;
+                p.converged = q.converged;
+                p.singular = q.singular;
+            } else {
+                p.res0 = q.ores0;
+                p.res = q.ores;
+                p.iters = q.inner_total;
+                p.outer = q.oiter;
+                p.converged = q.oconv;
+            }
+            p.ms = ms;
+            if (!std::isfinite(p.res0) || !std::isfinite(p.res)) p.status = MRG_E_BREAKDOWN;
+        }
     } catch (...) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -551,8 +622,18 @@ Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (!std::isfinite(perf.res0) || !std::isfinite(perf.res)) perf.status = MRG_E_BREAKDOWN;
-    return perf;
+    return out;
+}
+
+Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
+{
+    PlanState& P = prepare(m, cfg);
+    P.sys.in_b = d_b;
+    P.sys.in_x = d_x;
+    P.sys.out_x = d_x;
+    P.sync_sys();
+    P.single.sync_sys();
+    return solve_batch(P.single, cfg)[0];
 }
 
 // ------------------------------------------------------------------ building blocks
@@ -565,8 +646,8 @@ void amul_device(Mesh& m, const double* d_x, double* d_y, int transpose)
     const SysDev& S = P.sys;
     Ctx* c = m.ctx;
     launch_permute(1, P.d_sys, 0, d_x, S.v64.p, S.n, c->st);
-    if (S.ngen) launch_iface_gather(0, 3, P.d_sys, 1, 64, c->st);
-    launch_rows(transpose ? OP_TMUL : OP_AMUL, 0, P.d_sys, P.d_tiles, P.ntiles, grid_rows(c, P.ntiles), 0, c->st);
+    if (S.ngen) launch_iface_gather(0, 3, P.single.d, 64, c->st);
+    launch_rows(transpose ? OP_TMUL : OP_AMUL, 0, P.single.d, P.ntiles, P.single.h.nsegs, 0, c->st);
     launch_permute(0, P.d_sys, 0, S.v64.q, d_y, S.n, c->st);
     MRG_CUDA(cudaGetLastError());
     MRG_CUDA(cudaStreamSynchronize(c->st));
@@ -576,20 +657,33 @@ void residual_device(Mesh& m, const double* d_b, const double* d_x, double* res,
 {
     Controls cfg;
     cfg.pc = PC_NONE;
+    cfg.tol = 0.0;
+    cfg.max_iter = 0;
     PlanState& P = prepare(m, cfg);
-    const SysDev& S = P.sys;
     Ctx* c = m.ctx;
-    launch_permute(1, P.d_sys, 0, d_b, S.v64.b, S.n, c->st);
-    launch_permute(1, P.d_sys, 0, d_x, S.v64.x, S.n, c->st);
-    write_controls(P, 0.0, 0.0, 0, 0);
-    if (S.ngen) launch_iface_gather(0, 1, P.d_sys, 1, 64, c->st);
-    const int g = grid_rows(c, P.ntiles);
-    launch_rows(OP_SUMX, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, c->st);
-    launch_rows(OP_INIT_RES, 0, P.d_sys, P.d_tiles, P.ntiles, g, 0, c->st);
-    Poll* h = pinned_poll();
-    poll(P, h);
-    if (res) *res = h->sc.res0;
-    if (nfac) *nfac = h->sc.nfac;
+    P.sys.in_b = d_b;
+    P.sys.in_x = d_x;
+    P.sys.out_x = nullptr;
+    P.sync_sys();
+    P.single.sync_sys();
+    BatchHost& bh = P.single;
+    write_ctl_controls(bh, cfg);
+    launch_rows(OP_PERMUTE_IN, 0, bh.d, P.ntiles, P.single.h.nsegs, 0, c->st);
+    launch_rows(OP_BEGIN, 0, bh.d, P.ntiles, P.single.h.nsegs, 0, c->st);
+    if (P.sys.ngen) launch_iface_gather(0, 1, bh.d, 64, c->st);
+    launch_rows(OP_SUMX, 0, bh.d, P.ntiles, P.single.h.nsegs, 0, c->st);
+    launch_rows(OP_INIT_RES, 0, bh.d, P.ntiles, P.single.h.nsegs, 0, c->st);
+    Scal sc;
+    MRG_CUDA(cudaMemcpyAsync(&sc, P.sys.sc, sizeof(Scal), cudaMemcpyDeviceToHost, c->st));
+    MRG_CUDA(cudaStreamSynchronize(c->st));
+    if (res) *res = sc.res0;
+    if (nfac) *nfac = sc.nfac;
+}
+
+static void set_active_flag(PlanState& P, int on)
+{
+    MRG_CUDA(cudaMemcpyAsync((char*)P.sys.sc + offsetof(Scal, active), &on, sizeof on, cudaMemcpyHostToDevice,
+                             P.ctx->st));
 }
 
 void precondition_device(Mesh& m, int pc, int ordering, const double* d_r, double* d_w, int transpose)
@@ -602,23 +696,17 @@ void precondition_device(Mesh& m, int pc, int ordering, const double* d_r, doubl
     const SysDev& S = P.sys;
     Ctx* c = m.ctx;
     launch_permute(1, P.d_sys, 0, d_r, transpose ? S.v64.rT : S.v64.r, S.n, c->st);
-    // mark the system active so the sweeps run
-    {
-        int one = 1;
-        MRG_CUDA(cudaMemcpyAsync((char*)S.sc + offsetof(Scal, active), &one, sizeof one, cudaMemcpyHostToDevice,
-                                 c->st));
-    }
+    set_active_flag(P, 1);
     if (pc >= PC_DIC) {
         if (ordering == MRG_ORDER_EXACT) launch_fill_sentinel(transpose ? S.v64.yT : S.v64.y, S.n, 0, c->st);
-        record_precondition(P, cfg, 0, transpose, c->st);
+        record_precondition(P.single, cfg, 0, transpose, c->st);
     } else {
-        launch_rows(pc == PC_DIAG ? OP_PRECOND_DIAG : OP_PRECOND_NONE, 0, P.d_sys, P.d_tiles, P.ntiles,
-                    grid_rows(c, P.ntiles), transpose, c->st);
+        launch_rows(pc == PC_DIAG ? OP_PRECOND_DIAG : OP_PRECOND_NONE, 0, P.single.d, P.ntiles, P.single.h.nsegs, transpose, c->st);
     }
     launch_permute(0, P.d_sys, 0, transpose ? S.v64.wT : S.v64.w, d_w, S.n, c->st);
+    set_active_flag(P, 0);
     MRG_CUDA(cudaGetLastError());
-    Poll* h = pinned_poll();
-    poll(P, h);
+    poll(P.single, pinned_ctl());
 }
 
 void factor_diag_device(Mesh& m, int pc, int ordering, double* d_rD)
@@ -630,8 +718,7 @@ void factor_diag_device(Mesh& m, int pc, int ordering, double* d_rD)
     Ctx* c = m.ctx;
     launch_permute(0, P.d_sys, 0, P.sys.rD, d_rD, P.sys.n, c->st);
     MRG_CUDA(cudaGetLastError());
-    Poll* h = pinned_poll();
-    poll(P, h);
+    poll(P.single, pinned_ctl());
 }
 
 float time_kernel(Mesh& m, const Controls& cfg, int kernel, int reps)
@@ -642,15 +729,19 @@ float time_kernel(Mesh& m, const Controls& cfg, int kernel, int reps)
     Ctx* c = m.ctx;
     const int prec = cfg.precision;
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
-    int one = 1;
-    MRG_CUDA(cudaMemcpyAsync((char*)P.sys.sc + offsetof(Scal, active), &one, sizeof one, cudaMemcpyHostToDevice,
-                             c->st));
-    if (kernel == 1 && cfg.pc >= PC_DIC && cfg.ordering == MRG_ORDER_EXACT) init_sentinels(P, cfg, prec);
+    set_active_flag(P, 1);
+    if (kernel == 1 && cfg.pc >= PC_DIC && cfg.ordering == MRG_ORDER_EXACT) {
+        const SysDev& S = P.sys;
+        if (prec == 0)
+            launch_fill_sentinel(S.v64.y, S.n, 0, c->st);
+        else
+            launch_fill_sentinel(S.v32.y, S.n, 1, c->st);
+    }
     auto once = [&] {
         if (kernel == 0)
-            launch_rows(OP_SPMV_QP, prec, P.d_sys, P.d_tiles, P.ntiles, grid_rows(c, P.ntiles), pb, c->st);
+            launch_rows(OP_SPMV_QP, prec, P.single.d, P.ntiles, P.single.h.nsegs, pb, c->st);
         else
-            record_precondition(P, cfg, prec, 0, c->st);
+            record_precondition(P.single, cfg, prec, 0, c->st);
     };
     once();  // warm-up
     cudaEvent_t e0, e1;
@@ -664,9 +755,7 @@ float time_kernel(Mesh& m, const Controls& cfg, int kernel, int reps)
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int zero = 0;
-    MRG_CUDA(cudaMemcpyAsync((char*)P.sys.sc + offsetof(Scal, active), &zero, sizeof zero, cudaMemcpyHostToDevice,
-                             c->st));
+    set_active_flag(P, 0);
     MRG_CUDA(cudaStreamSynchronize(c->st));
     MRG_CUDA(cudaGetLastError());
     return ms / reps;

@@ -28,13 +28,57 @@ struct Ctx {
     cudaStream_t st = nullptr;
     size_t budget = 0, used = 0;
     std::map<void*, size_t> allocs;
-    Ctl* d_ctl = nullptr;
     cudaEvent_t events[64] = {};
     double* stage[3] = {nullptr, nullptr, nullptr};  // host-pointer entry points
     size_t stage_cap = 0;
     void* alloc(size_t bytes);
     void release(void* p);
     ~Ctx();
+};
+
+struct Controls {
+    double tol = 1e-6, rel_tol = 0.0;
+    int min_iter = 0, max_iter = 1000;
+    int solver = 0, pc = 2, precision = 0, ordering = 0;
+    double inner_rel_tol = 1e-5;
+    int inner_max_iter = 0, max_outer = 50, k_launch = 16;
+};
+
+struct Perf {
+    double res0 = 0, res = 0;
+    int iters = 0, converged = 0, singular = 0, status = 0, outer = 0;
+    double ms = 0;
+};
+
+struct PlanState;
+
+// A device-resident batch: the Batch descriptor, the system array, the tile
+// table, the per-level sweep work list and the control block.  Captured
+// iteration graphs refer only to the descriptor's address.
+struct BatchHost {
+    Ctx* ctx = nullptr;
+    Batch h{};
+    Batch* d = nullptr;
+    Ctl* d_ctl = nullptr;
+    SysDev* d_sys = nullptr;
+    int2* d_tiles = nullptr;
+    int2* d_segs = nullptr;
+    int2* d_items = nullptr;
+    int* d_item_off = nullptr;
+    size_t cap_sys = 0, cap_tiles = 0, cap_segs = 0, cap_items = 0, cap_off = 0;
+    int widest_level = 1;      // items of the widest sweep level (grid sizing)
+    std::vector<PlanState*> members;
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        long long nodes = 0;   // kernels per replay (for the launch counter)
+    };
+    std::map<std::string, Graph> graphs;
+    void init(Ctx* c);
+    // (Re)build the arrays for these systems; the order fixes the tile table.
+    void set(const std::vector<PlanState*>& systems);
+    // Re-upload the system array (after a member's SysDev changed).
+    void sync_sys();
+    ~BatchHost();
 };
 
 // Device copy of one plan + coefficient views + workspaces for one ordering.
@@ -50,20 +94,16 @@ struct PlanState {
     float* g_w32 = nullptr;
     SysDev sys{};           // host mirror
     SysDev* d_sys = nullptr;
-    int2* d_tiles = nullptr;
     int ntiles = 0;
-    bool have32 = false, haveT = false;
+    size_t nnz = 0, fnz = 0, bnz = 0;
+    bool have32 = false, haveT = false, haveT32 = false;
     uint64_t scattered = 0;   // coefficient version scattered into the views
     uint64_t factored = 0;    // coefficient version factored
     int factored_pc = -1;
     bool factored32 = false;
-    struct Graph {
-        cudaGraphExec_t exec = nullptr;
-        long long nodes = 0;  // kernels per replay (for the launch counter)
-    };
-    std::map<std::string, Graph> graphs;
+    BatchHost single;         // this system alone
     ~PlanState();
-    void sync_sys();  // copy host mirror to device
+    void sync_sys();          // copy host mirror to device
 };
 
 struct Mesh {
@@ -75,7 +115,6 @@ struct Mesh {
     double *raw_ibou = nullptr, *raw_iint = nullptr;
     bool sym = true, has_int = false, have_coeffs = false;
     uint64_t version = 0;
-    size_t nnz_cache[2][3] = {};  // per ordering: Amul, forward, backward entries
     std::unique_ptr<PlanState> plans[2];
     PlanState& plan(int ordering);
     ~Mesh();
@@ -91,23 +130,15 @@ struct Ggi {
     ~Ggi();
 };
 
-struct Controls {
-    double tol = 1e-6, rel_tol = 0.0;
-    int min_iter = 0, max_iter = 1000;
-    int solver = 0, pc = 2, precision = 0, ordering = 0;
-    double inner_rel_tol = 1e-4;
-    int inner_max_iter = 0, max_outer = 50, k_launch = 16;
-};
+// Make views, FP32 copies, transpose vectors and factors of every member
+// current for these controls (one scatter and one factor launch per batch).
+void prepare_batch(BatchHost& bh, const std::vector<Mesh*>& meshes, const Controls& c);
+// Solve every member of the batch; each member's SysDev in_b/in_x/out_x point
+// at its caller-numbered device vectors.  Returns one Perf per member.
+std::vector<Perf> solve_batch(BatchHost& bh, const Controls& c);
 
-struct Perf {
-    double res0 = 0, res = 0;
-    int iters = 0, converged = 0, singular = 0, status = 0, outer = 0;
-    double ms = 0;
-};
-
-// Prepare views (+FP32 copies) and factor for a solve; returns the plan.
+// Single-system conveniences (batch of one).
 PlanState& prepare(Mesh& m, const Controls& c);
-// Solve with device-resident b and x (caller numbering).
 Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& c);
 
 void amul_device(Mesh& m, const double* d_x, double* d_y, int transpose);

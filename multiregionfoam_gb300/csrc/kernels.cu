@@ -179,12 +179,9 @@ template <> struct VP<float> {
 // is skipped, so no FP64 work is spent on it.
 constexpr int kMaxW = 8;
 // Row and sweep kernels are compiled for at least 4 resident 256-thread CTAs
-// per SM.  A reducing row kernel always runs on kRedGrid = 2432 CTAs (16 per
-// SM of a GB300, a few waves so that loads of many CTAs overlap), a constant
-// so that the reduction order -- and therefore every result bit -- does not
-// depend on the device.  Non-reducing row kernels take one tile per CTA.
+// per SM.  Reducing row kernels walk the batch's segment table (kRedSegs in
+// dev.h), non-reducing row kernels take one tile per CTA.
 constexpr int kMinCtas = 4;
-constexpr int kRedGrid = 2432;
 
 template <typename V>
 __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __restrict__ acol,
@@ -218,10 +215,28 @@ __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __
     return y;
 }
 
-// Per-system finalisation, executed by thread 0 of the last tile.
-__device__ void finalize(const SysDev& S, RowOp op, const double* sums)
+// Per-system finalisation, executed by thread 0 of the CTA that completes the
+// system's reduction.  Systems entering or leaving a Krylov loop (or the
+// mixed-precision outer loop) are counted in the batch's control block, which
+// is all the host polls.
+__device__ __forceinline__ void set_active(Ctl* ctl, Scal* sc, int on)
+{
+    if (sc->active == on) return;
+    sc->active = on;
+    atomicAdd(&ctl->n_active, on ? 1u : 0xffffffffu);
+}
+
+__device__ __forceinline__ void set_outer(Ctl* ctl, Scal* sc, int on)
+{
+    if (sc->ostate == on) return;
+    sc->ostate = on;
+    atomicAdd(&ctl->n_oactive, on ? 1u : 0xffffffffu);
+}
+
+__device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double* sums)
 {
     Scal* sc = S.sc;
+    Ctl* ctl = B.ctl;
     sc->red[0] = sums[0];
     sc->red[1] = sums[1];
     switch (op) {
@@ -237,7 +252,24 @@ __device__ void finalize(const SysDev& S, RowOp op, const double* sums)
         sc->rho = 1.0e20;
         const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
         sc->converged = conv;
-        sc->active = (sc->min_iter > 0 || !conv) ? 1 : 0;
+        sc->kmin = sc->min_iter;
+        sc->kmax = sc->max_iter;
+        const int go = (sc->min_iter > 0 || !conv) ? 1 : 0;
+        if (sc->mixed) {
+            // FP64 outer state of iterative refinement; the FP32 Krylov loop
+            // starts at OP_TO32.
+            sc->onfac = sc->nfac;
+            sc->ores0 = sc->res0;
+            sc->ores = sc->res0;
+            sc->obest = sc->res0;
+            sc->oconv = conv;
+            sc->oiter = 0;
+            sc->ostall = 0;
+            sc->inner_total = 0;
+            set_outer(ctl, sc, go);
+        } else {
+            set_active(ctl, sc, go);
+        }
         break;
     }
     case OP_RHO:
@@ -248,8 +280,8 @@ __device__ void finalize(const SysDev& S, RowOp op, const double* sums)
     case OP_SPMV_QP:
         if (fabs(sums[0]) / sc->nfac < 1.0e-300) {
             sc->singular = 1;
-            sc->active = 0;
             sc->alpha = 0.0;
+            set_active(ctl, sc, 0);
         } else {
             sc->alpha = sc->rho / sums[0];
         }
@@ -259,31 +291,55 @@ __device__ void finalize(const SysDev& S, RowOp op, const double* sums)
         sc->iter += 1;
         const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
         sc->converged = conv;
-        const bool more = (sc->iter < sc->max_iter && !conv) || sc->iter < sc->min_iter;
-        if (!more) sc->active = 0;
+        const bool more = (sc->iter < sc->kmax && !conv) || sc->iter < sc->kmin;
+        if (!more) set_active(ctl, sc, 0);
         break;
     }
-    case OP_RESID64:
+    case OP_RESID64: {
+        // true FP64 residual of the refined solution: foam's convergence test
         sc->osum = sums[0];
+        sc->ores = sums[0] / sc->onfac;
+        const bool conv = sc->ores < sc->otol || (sc->orel_tol > 1.0e-20 && sc->ores < sc->orel_tol * sc->ores0);
+        sc->oconv = conv;
+        if (sc->ores < 0.999 * sc->obest) {
+            sc->obest = sc->ores;
+            sc->ostall = 0;
+        } else if (sc->oiter > 0) {
+            sc->ostall += 1;
+        }
+        const bool more = ((!conv || sc->inner_total < sc->min_iter) && sc->oiter < sc->max_outer &&
+                           sc->inner_total < sc->max_iter && sc->ostall < 3);
+        if (!more) set_outer(ctl, sc, 0);
         break;
-    case OP_TO32:
-        // inner solve state: residual measured relative to the start
+    }
+    case OP_TO32: {
+        // inner FP32 solve of A d = r: residual measured relative to its start;
+        // it aims at 0.1x the FP64 residual still to remove (overshooting the
+        // tolerance on the last step), never asked for less than inner_rel_tol
+        const double goal = fmax(sc->otol, sc->orel_tol > 1.0e-20 ? sc->orel_tol * sc->ores0 : 0.0);
+        double itol = 0.1 * goal / fmax(sc->ores, 1.0e-300);
+        itol = fmin(0.5, fmax(sc->inner_rel_tol, itol));
         sc->inv_scale = sc->osum > 0.0 ? sc->osum / (double)S.n : 1.0;
         sc->nfac = sums[0] > 0.0 ? sums[0] : 1.0;
         sc->res0 = sums[0] / sc->nfac;
         sc->res = sc->res0;
+        sc->tol = itol;
+        sc->rel_tol = 0.0;
+        sc->kmin = 0;
+        const int left = sc->max_iter - sc->inner_total;
+        sc->kmax = sc->inner_max < left ? sc->inner_max : left;
         sc->iter = 0;
         sc->singular = 0;
         sc->rho = 1.0e20;
         sc->converged = 0;
-        sc->active = sums[0] > 0.0 ? 1 : 0;
+        set_active(ctl, sc, sums[0] > 0.0 ? 1 : 0);
         break;
+    }
     default:
         break;
     }
 }
 
-// ---------------------------------------------------------------- row kernel
 // One 1024-row tile of a row operation.  Elementwise ops give thread t the
 // rows row0 + t + 256k; ELL ops give warp w the slices row0/32 + w + 8k.
 // Reductions accumulate into acc (FP64) in that row order.  The system's
@@ -291,13 +347,67 @@ __device__ void finalize(const SysDev& S, RowOp op, const double* sums)
 // them, and reading them through the SysDev in global memory would force a
 // reload after every store.
 template <typename V, RowOp OP, bool PB>
-__device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&acc)[kMaxRed])
+__device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int row0, double (&acc)[kMaxRed])
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int sl0 = row0 >> 5, sl1 = sl0 + kTileRows / 32;
     const int* __restrict__ sptr = S.a_sptr;
     const int* __restrict__ acol = S.a_col;
-    if constexpr (OP == OP_SCATTER) {
+    if constexpr (OP == OP_BEGIN) {
+        // Start of a solve: arm the sync-free sweep sentinels and copy the
+        // batch's controls into the system's scalar state.
+        const int n = S.n;
+        if (S.syncfree && S.pc >= PC_DIC) {
+            double* __restrict__ y = S.v64.y;
+            double* __restrict__ yT = S.v64.yT;
+            for (int i = row0 + tid; i < row0 + kTileRows && i < n; i += kBlock) {
+                y[i] = sent<double>();
+                if (PB) yT[i] = sent<double>();
+            }
+        }
+        if (row0 == 0 && tid == 0) {
+            const Ctl* c = B.ctl;
+            Scal* sc = S.sc;
+            sc->tol = c->tol;
+            sc->rel_tol = c->rel_tol;
+            sc->otol = c->tol;
+            sc->orel_tol = c->rel_tol;
+            sc->inner_rel_tol = c->inner_rel_tol;
+            sc->min_iter = c->min_iter;
+            sc->max_iter = c->max_iter;
+            sc->kmin = c->min_iter;
+            sc->kmax = c->max_iter;
+            sc->inner_max = c->inner_max;
+            sc->max_outer = c->max_outer;
+            sc->mixed = c->mixed;
+            sc->active = 0;
+            sc->ostate = 0;
+            sc->iter = 0;
+            sc->oiter = 0;
+            sc->inner_total = 0;
+            sc->converged = 0;
+            sc->oconv = 0;
+            sc->singular = 0;
+        }
+    } else if constexpr (OP == OP_PERMUTE_IN) {
+        const int* __restrict__ perm = S.perm;
+        const double* __restrict__ ib = S.in_b;
+        const double* __restrict__ ix = S.in_x;
+        double* __restrict__ b = S.v64.b;
+        double* __restrict__ x = S.v64.x;
+        const int n = S.n;
+        for (int i = row0 + tid; i < row0 + kTileRows && i < n; i += kBlock) {
+            const int c = perm[i];
+            b[i] = ib[c];
+            x[i] = ix[c];
+        }
+    } else if constexpr (OP == OP_PERMUTE_OUT) {
+        const int* __restrict__ perm = S.perm;
+        const double* __restrict__ x = S.v64.x;
+        double* __restrict__ ox = S.out_x;
+        const int n = S.n;
+        for (int i = row0 + tid; i < row0 + kTileRows && i < n; i += kBlock) ox[perm[i]] = x[i];
+    } else if constexpr (OP == OP_SCATTER) {
         // FP64 views (+ FP32 copies when allocated); one warp per slice.
         const bool asym = S.aT_val != S.a_val;
         const int* __restrict__ asrc = S.a_src;
@@ -311,11 +421,13 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
         float* __restrict__ av32 = S.a_val32;
         float* __restrict__ atv32 = S.aT_val32;
         const int n = S.n;
+        double* __restrict__ Dfac = S.D;
         for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
             const int e0 = sptr[sl], e1 = sptr[sl + 1];
             const int i = sl * 32 + lane;
             const double d = i < n ? rdiag[perm[i]] : 0.0;
             dg[i] = d;
+            if (i < n) Dfac[i] = sent<double>();  // arms the sync-free factorisation
             if (dg32) dg32[i] = (float)d;
             double s = d;
             for (int e = e0 + lane; e < e1; e += 32) {
@@ -458,11 +570,21 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
         const double s = S.sc->osum > 0.0 ? (double)S.n / S.sc->osum : 1.0;
         const double* __restrict__ r64 = S.v64.r;
         float* __restrict__ r32 = S.v32.r;
+        float* __restrict__ rT32 = S.v32.rT;
         float* __restrict__ x32 = S.v32.x;
+        float* __restrict__ y32 = S.v32.y;
+        float* __restrict__ yT32 = S.v32.yT;
+        const bool arm = S.syncfree && S.pc >= PC_DIC;
+        const int n = S.n;
         for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
             const float ri = (float)(r64[i] * s);
             r32[i] = ri;
+            if (PB) rT32[i] = ri;  // the correction system starts from d = 0
             x32[i] = 0.0f;
+            if (arm && i < n) {
+                y32[i] = sent<float>();
+                if (PB) yT32[i] = sent<float>();
+            }
             acc[0] += fabs(widen(ri));
         }
     } else if constexpr (OP == OP_CORRECT) {
@@ -470,6 +592,12 @@ __device__ __forceinline__ void tile_body(const SysDev& S, int row0, double (&ac
         const float* __restrict__ d32 = S.v32.x;
         double* __restrict__ x = S.v64.x;
         for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) x[i] = __fma_rn(widen(d32[i]), s, x[i]);
+        if (row0 == 0 && tid == 0) {
+            Scal* sc = S.sc;
+            sc->inner_total += sc->iter;
+            sc->oiter += 1;
+            if (sc->iter == 0) set_outer(B.ctl, sc, 0);  // the inner solve made no progress
+        }
     } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
         const double* __restrict__ av = OP == OP_TMUL ? S.aT_val : S.a_val;
         const double* __restrict__ dg = S.diag;
@@ -486,13 +614,23 @@ template <RowOp OP>
 struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
                                   OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32);
-    static constexpr bool kNeedActive = !(OP == OP_SCATTER || OP == OP_SUMX || OP == OP_INIT_RES ||
-                                          OP == OP_AMUL || OP == OP_TMUL || OP == OP_DIAG_RD ||
-                                          OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
+    // Krylov-loop ops run only for systems whose loop is active; the
+    // refinement ops only for systems whose outer loop is active.
+    static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
+                                         OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE);
+    static constexpr bool kNeedOuter = (OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
     // Values reduced: only the initial residual needs two (normFactor and
     // sum|r|).  Every tree level costs one FP64 add per thread per value.
     static constexpr int kNR = OP == OP_INIT_RES ? 2 : 1;
 };
+
+template <RowOp OP>
+__device__ __forceinline__ bool system_live(const SysDev& S)
+{
+    if (OpTraits<OP>::kNeedActive) return S.sc->active != 0;
+    if (OpTraits<OP>::kNeedOuter) return S.sc->ostate != 0;
+    return true;
+}
 
 // Close one reduction segment (consecutive tiles [first, first+count) of one
 // system handled by this CTA): block tree, partial into slot `first`, and the
@@ -500,8 +638,8 @@ struct OpTraits {
 // (unused slots hold zero) and finalises.  Deterministic for a given tile
 // table and grid size.
 template <RowOp OP>
-__device__ __forceinline__ void flush_segment(const SysDev& S, int first, int count, double (&acc)[kMaxRed],
-                                              double* sh, int* s_last)
+__device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, int first, int count,
+                                              double (&acc)[kMaxRed], double* sh, int* s_last)
 {
     constexpr int NR = OpTraits<OP>::kNR;
     const int tid = threadIdx.x;
@@ -533,7 +671,7 @@ __device__ __forceinline__ void flush_segment(const SysDev& S, int first, int co
             double sums[kMaxRed] = {0.0, 0.0};
 #pragma unroll
             for (int k = 0; k < NR; ++k) sums[k] = tot[k];
-            finalize(S, OP, sums);
+            finalize(B, S, OP, sums);
             *S.counter = 0u;
             __threadfence();
         }
@@ -541,56 +679,50 @@ __device__ __forceinline__ void flush_segment(const SysDev& S, int first, int co
     __syncthreads();
 }
 
-// Row kernel.  Non-reducing ops: grid-stride over tiles.  Reducing ops: CTA b
-// owns the contiguous tiles [b*T/G, (b+1)*T/G) of the tile table (G =
-// gridDim.x, at most kRedGrid) and accumulates across them, so the
-// fence/atomic/tree cost is paid once per CTA and system, not per tile.
+// Row kernel over a batch.  Non-reducing ops: grid-stride over the tile
+// table.  Reducing ops: grid-stride over the segment table; a segment
+// (system s, j) covers the contiguous tiles [j*T/G, (j+1)*T/G) of s (T its
+// tile count, G = min(T, kRedSegs)), accumulates across them and pays the
+// fence/atomic/tree cost once.
 template <typename V, RowOp OP, bool PB>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const SysDev* __restrict__ Ss,
-                                                           const int2* __restrict__ tiles, int ntiles)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restrict__ pB)
 {
     __shared__ double sh[kBlock * kMaxRed];
     __shared__ int s_last;
+    const Batch B = *pB;
     if constexpr (!OpTraits<OP>::kRed) {
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            const int2 tl = tiles[t];
-            const SysDev& S = Ss[tl.x];
-            if (OpTraits<OP>::kNeedActive && !S.sc->active) continue;
+        for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
+            const int2 tl = B.tiles[t];
+            const SysDev& S = B.sys[tl.x];
+            if (!system_live<OP>(S)) continue;
             double acc[kMaxRed] = {0.0, 0.0};
-            tile_body<V, OP, PB>(S, tl.y * kTileRows, acc);
+            tile_body<V, OP, PB>(B, S, tl.y * kTileRows, acc);
         }
     } else {
-        const int G = gridDim.x;
-        const int t0 = (int)((long long)blockIdx.x * ntiles / G);
-        const int t1 = (int)((long long)(blockIdx.x + 1) * ntiles / G);
-        int cur = -1, first = 0, count = 0;
-        bool live = false;
-        double acc[kMaxRed] = {0.0, 0.0};
-        for (int t = t0; t < t1; ++t) {
-            const int2 tl = tiles[t];
-            if (tl.x != cur) {
-                if (live) flush_segment<OP>(Ss[cur], first, count, acc, sh, &s_last);
-                cur = tl.x;
-                first = tl.y;
-                count = 0;
-                acc[0] = acc[1] = 0.0;
-                live = !OpTraits<OP>::kNeedActive || Ss[cur].sc->active;
-            }
-            ++count;
-            if (live) tile_body<V, OP, PB>(Ss[cur], tl.y * kTileRows, acc);
+        for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
+            const int2 sg = B.segs[g];
+            const SysDev& S = B.sys[sg.x];
+            if (!system_live<OP>(S)) continue;  // uniform over all of S's segments
+            const int T = S.ntiles, G = T < kRedSegs ? T : kRedSegs;
+            const int t0 = (int)((long long)sg.y * T / G), t1 = (int)((long long)(sg.y + 1) * T / G);
+            double acc[kMaxRed] = {0.0, 0.0};
+            for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, S, t * kTileRows, acc);
+            flush_segment<OP>(B, S, t0, t1 - t0, acc, sh, &s_last);
         }
-        if (live) flush_segment<OP>(Ss[cur], first, count, acc, sh, &s_last);
     }
 }
 
 template <typename V, RowOp OP>
-void launch_one(const SysDev* d, const int2* tiles, int ntiles, int grid, int pb, cudaStream_t st)
+void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
 {
-    if (OpTraits<OP>::kRed) grid = ntiles < kRedGrid ? ntiles : kRedGrid;
+    // ntiles / nsegs: the host's upper bounds on the batch's table sizes
+    int grid = OpTraits<OP>::kRed ? nsegs : ntiles;
+    grid = grid < 65535 ? grid : 65535;
+    if (grid < 1) grid = 1;
     if (pb)
-        k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(d, tiles, ntiles);
+        k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(dB);
     else
-        k_rows<V, OP, false><<<grid, kBlock, 0, st>>>(d, tiles, ntiles);
+        k_rows<V, OP, false><<<grid, kBlock, 0, st>>>(dB);
 }
 
 // ---------------------------------------------------------------- factor
@@ -647,11 +779,14 @@ __device__ __forceinline__ void factor_row(const SysDev& S, int c, int lane, Ctl
     }
 }
 
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_factor(const SysDev* __restrict__ Ss, int nsys, int maxchunks,
-                                                   Ctl* ctl, int with32)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_factor(const Batch* __restrict__ pB, int with32)
 {
+    const Batch B = *pB;
+    const SysDev* __restrict__ Ss = B.sys;
+    const int nsys = B.nsys;
+    Ctl* ctl = B.ctl;
     const int lane = threadIdx.x & 31;
-    const unsigned total = (unsigned)nsys * (unsigned)maxchunks;
+    const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
     for (;;) {
         unsigned t = 0;
         if (lane == 0) t = atomicAdd(&ctl->ticket[0], 1u);
@@ -797,11 +932,14 @@ __device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool s
 }
 
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const SysDev* __restrict__ Ss, int nsys,
-                                                               int maxchunks, Ctl* ctl, int trans)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __restrict__ pB, int trans)
 {
+    const Batch B = *pB;
+    const SysDev* __restrict__ Ss = B.sys;
+    const int nsys = B.nsys;
+    Ctl* ctl = B.ctl;
     const int lane = threadIdx.x & 31;
-    const unsigned total = (unsigned)nsys * (unsigned)maxchunks;
+    const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
     const int slot = FWD ? 2 : 4;
     for (;;) {
         unsigned t = 0;
@@ -811,7 +949,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const SysDev* __r
         const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
         const SysDev& S = Ss[s];
         const int nch = S.nchunks;
-        if (c >= nch || !S.sc->active) continue;
+        if (c >= nch || !S.sc->active || !S.syncfree || S.pc < PC_DIC) continue;
         const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans != 0);
         sweep_chunk<V, FWD>(P, FWD ? c : nch - 1 - c, true, ctl, 0, false, false);
     }
@@ -828,23 +966,36 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const SysDev* __r
 
 // One level L of a levelled sweep for every system that has it: forward
 // levels 1..nlevels-1, backward levels nlevels-2..0 (level 0 alone when
-// nlevels == 1).
+// nlevels == 1).  Work comes from the batch's per-level list of (system,
+// chunk) items, one chunk per warp.
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const SysDev* __restrict__ Ss, int nsys, int L,
-                                                                int trans)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
 {
+    const Batch B = *pB;
+    if (L >= B.maxlevels) return;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int s = 0; s < nsys; ++s) {
-        const SysDev& S = Ss[s];
-        const int nl = S.nlevels;
-        if (!S.sc->active) continue;
-        if (FWD ? (L < 1 || L > nl - 1) : !(L <= nl - 2 || (nl == 1 && L == 0))) continue;
-        const int lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
-        const bool last = L == nl - 1, first = L == 0;
-        const int c0 = S.lvl_chunk[L], c1 = S.lvl_chunk[L + 1];
-        const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans != 0);
-        for (int c = c0 + gw; c < c1; c += nw) sweep_chunk<V, FWD>(P, c, false, nullptr, lvl0_end, last, first);
+    const int i0 = B.item_off[L], i1 = B.item_off[L + 1];
+    int cur = -1;
+    bool ok = false, last = false, first = false;
+    int lvl0_end = 0;
+    SweepPtrs<V> P;
+    for (int it = i0 + gw; it < i1; it += nw) {
+        const int2 item = B.items[it];
+        if (item.x != cur) {
+            cur = item.x;
+            const SysDev& S = B.sys[cur];
+            const int nl = S.nlevels;
+            ok = S.sc->active && S.pc >= PC_DIC && !S.syncfree &&
+                 (FWD ? (L >= 1 && L <= nl - 1) : (L <= nl - 2 || (nl == 1 && L == 0)));
+            if (ok) {
+                lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
+                last = L == nl - 1;
+                first = L == 0;
+                P = sweep_ptrs<V, FWD>(S, trans != 0);
+            }
+        }
+        if (ok) sweep_chunk<V, FWD>(P, item.y, false, nullptr, lvl0_end, last, first);
     }
 }
 
@@ -857,8 +1008,10 @@ __global__ void k_fill_sent(V* p, long long n)
 }
 
 template <typename V>
-__global__ void k_iface_gather(const SysDev* __restrict__ Ss, int nsys, int which)
+__global__ void k_iface_gather(const Batch* __restrict__ pB, int which)
 {
+    const SysDev* __restrict__ Ss = pB->sys;
+    const int nsys = pB->nsys;
     for (int s = 0; s < nsys; ++s) {
         const SysDev& S = Ss[s];
         if (S.ngen == 0) continue;
@@ -911,17 +1064,14 @@ static std::atomic<unsigned long long> g_launches{0};
 unsigned long long launch_count() { return g_launches.load(); }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }
 
-void launch_rows(RowOp op, int precision, const SysDev* d, const int2* tiles, int ntiles, int grid, int pb,
-                 cudaStream_t st)
+void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
 {
     if (ntiles <= 0) return;
-    (void)grid;
-    grid = ntiles < 65535 ? ntiles : 65535;
     ++g_launches;
 #define MRG_CASE64(OPX) \
-    case OPX: launch_one<double, OPX>(d, tiles, ntiles, grid, pb, st); break;
+    case OPX: launch_one<double, OPX>(dB, ntiles, nsegs, pb, st); break;
 #define MRG_CASE32(OPX) \
-    case OPX: launch_one<float, OPX>(d, tiles, ntiles, grid, pb, st); break;
+    case OPX: launch_one<float, OPX>(dB, ntiles, nsegs, pb, st); break;
     if (precision == 0) {
         switch (op) {
             MRG_CASE64(OP_SCATTER)
@@ -939,6 +1089,9 @@ void launch_rows(RowOp op, int precision, const SysDev* d, const int2* tiles, in
             MRG_CASE64(OP_AMUL)
             MRG_CASE64(OP_TMUL)
             MRG_CASE64(OP_DIAG_RD)
+            MRG_CASE64(OP_BEGIN)
+            MRG_CASE64(OP_PERMUTE_IN)
+            MRG_CASE64(OP_PERMUTE_OUT)
         default: break;
         }
     } else {
@@ -968,50 +1121,51 @@ void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st)
         k_fill_sent<float><<<grid, 256, 0, st>>>((float*)p, n);
 }
 
-void launch_factor(const SysDev* d, int nsys, int maxchunks, Ctl* ctl, int grid, int with32, cudaStream_t st)
+void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st)
 {
     ++g_launches;
-    k_factor<<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, with32);
+    k_factor<<<grid, kBlock, 0, st>>>(dB, with32);
 }
 
-void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const SysDev* d, int nsys,
-                  int maxchunks, Ctl* ctl, int grid, cudaStream_t st)
+void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
+                  cudaStream_t st)
 {
     ++g_launches;
+    if (grid < 1) grid = 1;
     if (syncfree) {
         if (precision == 0) {
             if (fwd)
-                k_sweep_sf<double, true><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+                k_sweep_sf<double, true><<<grid, kBlock, 0, st>>>(dB, trans);
             else
-                k_sweep_sf<double, false><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+                k_sweep_sf<double, false><<<grid, kBlock, 0, st>>>(dB, trans);
         } else {
             if (fwd)
-                k_sweep_sf<float, true><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+                k_sweep_sf<float, true><<<grid, kBlock, 0, st>>>(dB, trans);
             else
-                k_sweep_sf<float, false><<<grid, kBlock, 0, st>>>(d, nsys, maxchunks, ctl, trans);
+                k_sweep_sf<float, false><<<grid, kBlock, 0, st>>>(dB, trans);
         }
     } else {
         if (precision == 0) {
             if (fwd)
-                k_sweep_lvl<double, true><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+                k_sweep_lvl<double, true><<<grid, kBlock, 0, st>>>(dB, level, trans);
             else
-                k_sweep_lvl<double, false><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+                k_sweep_lvl<double, false><<<grid, kBlock, 0, st>>>(dB, level, trans);
         } else {
             if (fwd)
-                k_sweep_lvl<float, true><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+                k_sweep_lvl<float, true><<<grid, kBlock, 0, st>>>(dB, level, trans);
             else
-                k_sweep_lvl<float, false><<<grid, kBlock, 0, st>>>(d, nsys, level, trans);
+                k_sweep_lvl<float, false><<<grid, kBlock, 0, st>>>(dB, level, trans);
         }
     }
 }
 
-void launch_iface_gather(int precision, int which, const SysDev* d, int nsys, int grid, cudaStream_t st)
+void launch_iface_gather(int precision, int which, const Batch* dB, int grid, cudaStream_t st)
 {
     ++g_launches;
     if (precision == 0)
-        k_iface_gather<double><<<grid, 256, 0, st>>>(d, nsys, which);
+        k_iface_gather<double><<<grid, 256, 0, st>>>(dB, which);
     else
-        k_iface_gather<float><<<grid, 256, 0, st>>>(d, nsys, which);
+        k_iface_gather<float><<<grid, 256, 0, st>>>(dB, which);
 }
 
 void launch_permute(int to_internal, const SysDev* d, int s, const double* src, double* dst, int n, cudaStream_t st)

@@ -1,4 +1,9 @@
 // kernels.h -- launchers for the sm_103a kernels in kernels.cu.
+//
+// Every launcher takes a device-resident Batch descriptor (dev.h); the
+// kernels read the batch's sizes from it at run time, so a captured graph of
+// launches stays valid when the batch's contents change.  Host-side sizes
+// passed here are upper bounds used only to size grids.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,9 +11,9 @@
 
 namespace mrg {
 
-// Row-kernel operations (one tile of 1024 rows per CTA iteration).
+// Row-kernel operations (tiles of 1024 rows).
 enum RowOp {
-    OP_SCATTER = 0,     // raw coefficients -> internal views (+ sumA)
+    OP_SCATTER = 0,     // raw coefficients -> internal views (+ sumA), arms the factor
     OP_SUMX,            // xsum = sum(x)
     OP_INIT_RES,        // r = b - A x (rT = b - A^T x), normFactor, initial residual
     OP_RHO,             // rho = (w, r)  [PBiCG: (w, rT)], beta
@@ -17,45 +22,41 @@ enum RowOp {
     OP_UPDATE,          // x += alpha p, r -= alpha q [+ rT], final residual, convergence
     OP_PRECOND_DIAG,    // w = rD r  [+ wT]
     OP_PRECOND_NONE,    // w = r     [+ wT]
-    OP_RESID64,         // mixed: r64 = b - A x (FP64), sum|r64| -> res
-    OP_TO32,            // mixed: r32 = float(s * r64), inner state reset
+    OP_RESID64,         // mixed: r64 = b - A x (FP64), outer convergence test
+    OP_TO32,            // mixed: r32 = float(s * r64), inner state
     OP_CORRECT,         // mixed: x64 += d32 / s
     OP_AMUL,            // y = A x (test hook; x in v64.p, y in v64.q)
     OP_TMUL,            // y = A^T x (test hook)
     OP_DIAG_RD,         // rD = 1/diag (diagonal preconditioner)
+    OP_BEGIN,           // start of a solve: controls into Scal, sweep sentinels
+    OP_PERMUTE_IN,      // b, x from the caller's numbering (in_b, in_x)
+    OP_PERMUTE_OUT,     // x to the caller's numbering (out_x)
     OP_COUNT
 };
 
-struct LaunchCfg {
-    int grid_rows;     // CTAs for row kernels
-    int grid_sweep;    // CTAs for sync-free sweeps
-};
-
-// precision: 0 = FP64 vectors/coefficients, 1 = FP32 (mixed inner loop)
-void launch_rows(RowOp op, int precision, const SysDev* d_sys, const int2* d_tiles,
-                 int ntiles, int grid, int pbicg, cudaStream_t st);
+// precision: 0 = FP64 vectors/coefficients, 1 = FP32 (mixed inner loop).
+// ntiles, nsegs: upper bounds on the batch's tile and segment counts.
+void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st);
 
 // Sentinel fill of a vector (sync-free readiness marker).
 void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st);
 
-// Level-scheduled DIC/DILU factor, sync-free over chunks (forward order).
+// Level-scheduled DIC/DILU factor, sync-free over chunks (forward order), for
+// every system of the batch with a DIC/DILU preconditioner.
 // with32: also write FP32 copies of rD and sweep coefficients.
-void launch_factor(const SysDev* d_sys, int nsys, int maxchunks, Ctl* ctl, int grid,
-                   int with32, cudaStream_t st);
+void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st);
 
 // One triangular sweep.  fwd: y = forward(r); else w = backward(y).
 // trans selects DILU's preconditionT coefficients and the T vectors.
 // syncfree=1: all levels in one launch (exact ordering); else one level.
-void launch_sweep(int precision, int fwd, int trans, int syncfree, int level,
-                  const SysDev* d_sys, int nsys, int maxchunks, Ctl* ctl, int grid,
+void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
                   cudaStream_t st);
 
 // GGI gather of the general interface faces: x[npad + j] = sum w x[src]
 // (which: 0 = p, 1 = x, 2 = pT; 0 and 2 skip inactive systems, 3 = p always).
-void launch_iface_gather(int precision, int which, const SysDev* d_sys, int nsys,
-                         int grid, cudaStream_t st);
+void launch_iface_gather(int precision, int which, const Batch* dB, int grid, cudaStream_t st);
 
-// Internal <-> caller numbering (FP64).
+// Internal <-> caller numbering (FP64) of one system (test hooks).
 void launch_permute(int to_internal, const SysDev* d_sys, int sysidx, const double* src,
                     double* dst, int n, cudaStream_t st);
 

@@ -27,6 +27,7 @@ EXPORTED = [
     "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
     "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
+    "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
 ]
 
 
@@ -101,6 +102,10 @@ def load(path: str = LIB_PATH):
     L.mrg_event_elapsed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.mrg_kernel_launches.argtypes = [C.POINTER(C.c_uint64)]
     L.mrg_time_kernel.argtypes = [vp, C.POINTER(Controls), C.c_int, C.c_int, C.POINTER(C.c_float)]
+    L.mrg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp), C.c_int, C.POINTER(vp)]
+    L.mrg_batch_destroy.argtypes = [vp]
+    L.mrg_batch_solve.argtypes = [vp, C.POINTER(dp), C.POINTER(dp), C.POINTER(Controls), C.POINTER(Perf)]
+    L.mrg_batch_solve_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Perf)]
     _LIB = L
     return L
 
@@ -297,6 +302,43 @@ class Mesh:
         out = np.empty(self.n)
         _check(load().mrg_factor_diag(self.h, PRECONDITIONERS[precond], ORDERINGS[ordering], _d(out)))
         return out
+
+
+class Batch:
+    """Independent systems solved in lockstep (each with its current coefficients)."""
+
+    def __init__(self, ctx: Context, meshes, ordering="exact"):
+        self.meshes = list(meshes)
+        self.ordering = ordering
+        arr = (C.c_void_p * len(self.meshes))(*[m.h.value for m in self.meshes])
+        h = C.c_void_p()
+        _check(load().mrg_batch_create(ctx.h, len(self.meshes), arr, ORDERINGS[ordering], C.byref(h)))
+        self.h = h
+
+    def solve(self, bs, x0s, ctl: Controls | None = None, **kw):
+        kw.setdefault("ordering", self.ordering)
+        ctl = ctl if ctl is not None else controls(**kw)
+        ns = len(self.meshes)
+        bs = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+        xs = [np.array(x, dtype=np.float64, copy=True) for x in x0s]
+        pb = (C.POINTER(C.c_double) * ns)(*[_d(b) for b in bs])
+        px = (C.POINTER(C.c_double) * ns)(*[_d(x) for x in xs])
+        perfs = (Perf * ns)()
+        _check(load().mrg_batch_solve(self.h, pb, px, C.byref(ctl), perfs))
+        return xs, [p.as_dict() for p in perfs]
+
+    def solve_device(self, d_bs, d_xs, ctl: Controls):
+        ns = len(self.meshes)
+        pb = (C.c_void_p * ns)(*d_bs)
+        px = (C.c_void_p * ns)(*d_xs)
+        perfs = (Perf * ns)()
+        _check(load().mrg_batch_solve_device(self.h, pb, px, C.byref(ctl), perfs))
+        return [p.as_dict() for p in perfs]
+
+    def close(self):
+        if self.h:
+            _check(load().mrg_batch_destroy(self.h))
+            self.h = None
 
 
 class Ggi:

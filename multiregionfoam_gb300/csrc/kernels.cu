@@ -340,17 +340,52 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
     }
 }
 
+// 4-row vector access: thread t of a tile owns the rows row0 + 4t .. 4t+3
+// (one 16-byte load per FP32 array, two per FP64 array).
+__device__ __forceinline__ void ld4(const float* __restrict__ p, float (&o)[4])
+{
+    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double* __restrict__ p, double (&o)[4])
+{
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+// Plain (coherent) loads for arrays the same kernel also writes.
+__device__ __forceinline__ void ld4w(const float* p, float (&o)[4])
+{
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+}
+__device__ __forceinline__ void ld4w(const double* p, double (&o)[4])
+{
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&v)[4])
+{
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&v)[4])
+{
+    reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
 // One 1024-row tile of a row operation.  Elementwise ops give thread t the
-// rows row0 + t + 256k; ELL ops give warp w the slices row0/32 + w + 8k.
-// Reductions accumulate into acc (FP64) in that row order.  The system's
-// pointers are read once into __restrict__ locals: the kernels store through
-// them, and reading them through the SysDev in global memory would force a
-// reload after every store.
+// four consecutive rows row0 + 4t .. 4t+3 (vector loads); ELL ops give warp w
+// the slices row0/32 + w + 8k, k = 0..3.  Reductions accumulate into acc
+// (FP64) in that row order.  S is the CTA's shared-memory copy of the system
+// descriptor; pointers are taken into __restrict__ locals.
 template <typename V, RowOp OP, bool PB>
 __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int row0, double (&acc)[kMaxRed])
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int sl0 = row0 >> 5, sl1 = sl0 + kTileRows / 32;
+    const int r4 = row0 + 4 * tid;  // first of this thread's four elementwise rows
     const int* __restrict__ sptr = S.a_sptr;
     const int* __restrict__ acol = S.a_col;
     if constexpr (OP == OP_BEGIN) {
@@ -360,10 +395,12 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         if (S.syncfree && S.pc >= PC_DIC) {
             double* __restrict__ y = S.v64.y;
             double* __restrict__ yT = S.v64.yT;
-            for (int i = row0 + tid; i < row0 + kTileRows && i < n; i += kBlock) {
-                y[i] = sent<double>();
-                if (PB) yT[i] = sent<double>();
-            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (r4 + k < n) {
+                    y[r4 + k] = sent<double>();
+                    if (PB) yT[r4 + k] = sent<double>();
+                }
         }
         if (row0 == 0 && tid == 0) {
             const Ctl* c = B.ctl;
@@ -396,17 +433,25 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         double* __restrict__ b = S.v64.b;
         double* __restrict__ x = S.v64.x;
         const int n = S.n;
-        for (int i = row0 + tid; i < row0 + kTileRows && i < n; i += kBlock) {
-            const int c = perm[i];
-            b[i] = ib[c];
-            x[i] = ix[c];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = r4 + k;
+            if (i < n) {
+                const int c = __ldg(perm + i);
+                b[i] = __ldg(ib + c);
+                x[i] = __ldg(ix + c);
+            }
         }
     } else if constexpr (OP == OP_PERMUTE_OUT) {
         const int* __restrict__ perm = S.perm;
         const double* __restrict__ x = S.v64.x;
         double* __restrict__ ox = S.out_x;
         const int n = S.n;
-        for (int i = row0 + tid; i < row0 + kTileRows && i < n; i += kBlock) ox[perm[i]] = x[i];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = r4 + k;
+            if (i < n) ox[__ldg(perm + i)] = x[i];
+        }
     } else if constexpr (OP == OP_SCATTER) {
         // FP64 views (+ FP32 copies when allocated); one warp per slice.
         const bool asym = S.aT_val != S.a_val;
@@ -445,8 +490,10 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             sA[i] = s;
         }
     } else if constexpr (OP == OP_SUMX) {
-        const V* __restrict__ x = VP<V>::v(S).x;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) acc[0] += widen(x[i]);
+        V x[4];
+        ld4(VP<V>::v(S).x + r4, x);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[0] += widen(x[k]);
     } else if constexpr (OP == OP_INIT_RES) {
         const double xbar = S.sc->xsum / (double)S.n;
         const double* __restrict__ av = S.a_val;
@@ -470,21 +517,36 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         }
     } else if constexpr (OP == OP_RHO) {
         const Vecs<V>& v = VP<V>::v(S);
-        const V* __restrict__ w = v.w;
-        const V* __restrict__ rr = PB ? v.rT : v.r;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock)
-            acc[0] = __fma_rn(widen(w[i]), widen(rr[i]), acc[0]);
+        V w[4], rr[4];
+        ld4(v.w + r4, w);
+        ld4((PB ? v.rT : v.r) + r4, rr);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[0] = __fma_rn(widen(w[k]), widen(rr[k]), acc[0]);
     } else if constexpr (OP == OP_PUPDATE) {
         const Vecs<V>& v = VP<V>::v(S);
         const int it = S.sc->iter;
         const V beta = (V)S.sc->beta;
-        V* __restrict__ p = v.p;
-        const V* __restrict__ w = v.w;
-        V* __restrict__ pT = v.pT;
-        const V* __restrict__ wT = v.wT;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-            p[i] = it == 0 ? w[i] : vfma(beta, p[i], w[i]);
-            if (PB) pT[i] = it == 0 ? wT[i] : vfma(beta, pT[i], wT[i]);
+        V w[4], p[4];
+        ld4(v.w + r4, w);
+        if (it == 0) {
+            st4(v.p + r4, w);
+        } else {
+            ld4w(v.p + r4, p);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) p[k] = vfma(beta, p[k], w[k]);
+            st4(v.p + r4, p);
+        }
+        if (PB) {
+            V wT[4], pT[4];
+            ld4(v.wT + r4, wT);
+            if (it == 0) {
+                st4(v.pT + r4, wT);
+            } else {
+                ld4w(v.pT + r4, pT);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) pT[k] = vfma(beta, pT[k], wT[k]);
+                st4(v.pT + r4, pT);
+            }
         }
     } else if constexpr (OP == OP_SPMV_QP) {
         const Vecs<V>& v = VP<V>::v(S);
@@ -509,49 +571,61 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
     } else if constexpr (OP == OP_UPDATE) {
         const Vecs<V>& v = VP<V>::v(S);
         const V alpha = (V)S.sc->alpha;
-        V* __restrict__ x = v.x;
-        V* __restrict__ r = v.r;
-        V* __restrict__ rT = v.rT;
-        const V* __restrict__ p = v.p;
-        const V* __restrict__ q = v.q;
-        const V* __restrict__ qT = v.qT;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-            x[i] = vfma(alpha, p[i], x[i]);
-            const V ri = vfma(-alpha, q[i], r[i]);
-            r[i] = ri;
-            if (PB) rT[i] = vfma(-alpha, qT[i], rT[i]);
-            acc[0] += fabs(widen(ri));
+        V x[4], r[4], p[4], q[4];
+        ld4w(v.x + r4, x);
+        ld4w(v.r + r4, r);
+        ld4(v.p + r4, p);
+        ld4(v.q + r4, q);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x[k] = vfma(alpha, p[k], x[k]);
+            r[k] = vfma(-alpha, q[k], r[k]);
         }
+        st4(v.x + r4, x);
+        st4(v.r + r4, r);
+        if (PB) {
+            V rT[4], qT[4];
+            ld4w(v.rT + r4, rT);
+            ld4(v.qT + r4, qT);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) rT[k] = vfma(-alpha, qT[k], rT[k]);
+            st4(v.rT + r4, rT);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[0] += fabs(widen(r[k]));
     } else if constexpr (OP == OP_PRECOND_DIAG) {
         const Vecs<V>& v = VP<V>::v(S);
-        const V* __restrict__ rD = VP<V>::rD(S);
-        V* __restrict__ w = v.w;
-        V* __restrict__ wT = v.wT;
-        const V* __restrict__ r = v.r;
-        const V* __restrict__ rT = v.rT;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-            w[i] = vmul(rD[i], r[i]);
-            if (PB) wT[i] = vmul(rD[i], rT[i]);
+        V d[4], r[4], w[4];
+        ld4(VP<V>::rD(S) + r4, d);
+        ld4(v.r + r4, r);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) w[k] = vmul(d[k], r[k]);
+        st4(v.w + r4, w);
+        if (PB) {
+            ld4(v.rT + r4, r);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) w[k] = vmul(d[k], r[k]);
+            st4(v.wT + r4, w);
         }
     } else if constexpr (OP == OP_PRECOND_NONE) {
         const Vecs<V>& v = VP<V>::v(S);
-        V* __restrict__ w = v.w;
-        V* __restrict__ wT = v.wT;
-        const V* __restrict__ r = v.r;
-        const V* __restrict__ rT = v.rT;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-            w[i] = r[i];
-            if (PB) wT[i] = rT[i];
+        V r[4];
+        ld4(v.r + r4, r);
+        st4(v.w + r4, r);
+        if (PB) {
+            ld4(v.rT + r4, r);
+            st4(v.wT + r4, r);
         }
     } else if constexpr (OP == OP_DIAG_RD) {
-        const double* __restrict__ dg = S.diag;
-        double* __restrict__ rD = S.rD;
-        float* __restrict__ rD32 = S.rD32;
         const int n = S.n;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-            const double r = i < n ? __ddiv_rn(1.0, dg[i]) : 0.0;
-            rD[i] = r;
-            if (rD32) rD32[i] = (float)r;
+        double d[4], rd[4];
+        ld4(S.diag + r4, d);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rd[k] = r4 + k < n ? __ddiv_rn(1.0, d[k]) : 0.0;
+        st4(S.rD + r4, rd);
+        if (S.rD32) {
+            float f[4] = {(float)rd[0], (float)rd[1], (float)rd[2], (float)rd[3]};
+            st4(S.rD32 + r4, f);
         }
     } else if constexpr (OP == OP_RESID64) {
         const double* __restrict__ av = S.a_val;
@@ -568,30 +642,36 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
     } else if constexpr (OP == OP_TO32) {
         // s scales the FP64 residual to O(1) per cell before rounding to FP32.
         const double s = S.sc->osum > 0.0 ? (double)S.n / S.sc->osum : 1.0;
-        const double* __restrict__ r64 = S.v64.r;
-        float* __restrict__ r32 = S.v32.r;
-        float* __restrict__ rT32 = S.v32.rT;
-        float* __restrict__ x32 = S.v32.x;
-        float* __restrict__ y32 = S.v32.y;
-        float* __restrict__ yT32 = S.v32.yT;
         const bool arm = S.syncfree && S.pc >= PC_DIC;
         const int n = S.n;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) {
-            const float ri = (float)(r64[i] * s);
-            r32[i] = ri;
-            if (PB) rT32[i] = ri;  // the correction system starts from d = 0
-            x32[i] = 0.0f;
-            if (arm && i < n) {
-                y32[i] = sent<float>();
-                if (PB) yT32[i] = sent<float>();
-            }
-            acc[0] += fabs(widen(ri));
+        double r64[4];
+        ld4(S.v64.r + r4, r64);
+        float r32[4];
+        const float zero[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r32[k] = (float)(r64[k] * s);
+        st4(S.v32.r + r4, r32);
+        if (PB) st4(S.v32.rT + r4, r32);  // the correction system starts from d = 0
+        st4(S.v32.x + r4, zero);
+        if (arm) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (r4 + k < n) {
+                    S.v32.y[r4 + k] = sent<float>();
+                    if (PB) S.v32.yT[r4 + k] = sent<float>();
+                }
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[0] += fabs(widen(r32[k]));
     } else if constexpr (OP == OP_CORRECT) {
         const double s = S.sc->inv_scale;
-        const float* __restrict__ d32 = S.v32.x;
-        double* __restrict__ x = S.v64.x;
-        for (int i = row0 + tid; i < row0 + kTileRows; i += kBlock) x[i] = __fma_rn(widen(d32[i]), s, x[i]);
+        float d32[4];
+        double x[4];
+        ld4(S.v32.x + r4, d32);
+        ld4w(S.v64.x + r4, x);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = __fma_rn(widen(d32[k]), s, x[k]);
+        st4(S.v64.x + r4, x);
         if (row0 == 0 && tid == 0) {
             Scal* sc = S.sc;
             sc->inner_total += sc->iter;
@@ -683,31 +763,55 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
 // table.  Reducing ops: grid-stride over the segment table; a segment
 // (system s, j) covers the contiguous tiles [j*T/G, (j+1)*T/G) of s (T its
 // tile count, G = min(T, kRedSegs)), accumulates across them and pays the
-// fence/atomic/tree cost once.
+// fence/atomic/tree cost once.  The system's descriptor is copied into
+// shared memory once per CTA and system, so threads read its pointers from
+// shared memory instead of each issuing ~40 global loads.
+static_assert(sizeof(SysDev) % 8 == 0, "SysDev is copied as 8-byte words");
+
+__device__ __forceinline__ void load_sys(SysDev* dst, const SysDev* src)
+{
+    __syncthreads();  // the previous system's copy is no longer in use
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(SysDev) / 8); k += blockDim.x) d[k] = s[k];
+    __syncthreads();
+}
+
 template <typename V, RowOp OP, bool PB>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restrict__ pB)
 {
     __shared__ double sh[kBlock * kMaxRed];
     __shared__ int s_last;
+    __shared__ __align__(16) SysDev sS;
     const Batch B = *pB;
+    int cur = -1;
+    bool live = false;
     if constexpr (!OpTraits<OP>::kRed) {
         for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
             const int2 tl = B.tiles[t];
-            const SysDev& S = B.sys[tl.x];
-            if (!system_live<OP>(S)) continue;
+            if (tl.x != cur) {
+                cur = tl.x;
+                load_sys(&sS, B.sys + cur);
+                live = system_live<OP>(sS);
+            }
+            if (!live) continue;
             double acc[kMaxRed] = {0.0, 0.0};
-            tile_body<V, OP, PB>(B, S, tl.y * kTileRows, acc);
+            tile_body<V, OP, PB>(B, sS, tl.y * kTileRows, acc);
         }
     } else {
         for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
             const int2 sg = B.segs[g];
-            const SysDev& S = B.sys[sg.x];
-            if (!system_live<OP>(S)) continue;  // uniform over all of S's segments
-            const int T = S.ntiles, G = T < kRedSegs ? T : kRedSegs;
-            const int t0 = (int)((long long)sg.y * T / G), t1 = (int)((long long)(sg.y + 1) * T / G);
+            if (sg.x != cur) {
+                cur = sg.x;
+                load_sys(&sS, B.sys + cur);
+                live = system_live<OP>(sS);  // uniform over all of the system's segments
+            }
+            if (!live) continue;
+            const unsigned T = (unsigned)sS.ntiles, G = T < (unsigned)kRedSegs ? T : (unsigned)kRedSegs;
+            const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
-            for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, S, t * kTileRows, acc);
-            flush_segment<OP>(B, S, t0, t1 - t0, acc, sh, &s_last);
+            for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+            flush_segment<OP>(B, sS, t0, t1 - t0, acc, sh, &s_last);
         }
     }
 }

@@ -487,11 +487,12 @@ static double mr_block(const double* acc /* [256] */)
 }
 
 /* Row handled by thread t in its k-th step of tile `tile`.
- * assign 0: elementwise (row0 + t + 256k); 1: sliced (warp = slice owner). */
+ * assign 0: elementwise (four consecutive rows row0 + 4t + k);
+ * assign 1: sliced (warp w owns slices row0/32 + w + 8k). */
 static int mr_row(int tile, int t, int k, int assign)
 {
     int row0 = tile * MR_TILE;
-    if (assign == 0) return row0 + t + MR_BLOCK * k;
+    if (assign == 0) return row0 + 4 * t + k;
     int w = t >> 5, lane = t & 31;
     return ((row0 >> 5) + w + 8 * k) * 32 + lane;
 }

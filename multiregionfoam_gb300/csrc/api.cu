@@ -193,6 +193,7 @@ int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out)
             c->c.device = device;
             c->c.budget = hbm_budget_bytes;
             MRG_CUDA(cudaDeviceGetAttribute(&c->c.nsm, cudaDevAttrMultiProcessorCount, device));
+            set_device_sms(c->c.nsm);
             MRG_CUDA(cudaStreamCreateWithFlags(&c->c.st, cudaStreamNonBlocking));
             MRG_CUDA(cudaStreamSynchronize(c->c.st));
         } catch (...) {

@@ -15,11 +15,19 @@ namespace mrg {
 
 constexpr int kBlock = 256;   // threads per CTA for row kernels
 constexpr int kMaxRed = 2;    // values reduced per tile
-// A system of T tiles is reduced in G = min(T, kRedSegs) contiguous tile
-// segments, segment j = tiles [j*T/G, (j+1)*T/G): the summation order of
-// every per-system reduction depends only on the system itself -- not on
-// the device, the launch grid or the other members of a batch.
-constexpr int kRedSegs = 2432;
+// A system of T tiles is reduced in G = min(kRedSegs, ceil(T / kSegTiles))
+// contiguous tile segments, segment j = tiles [j*T/G, (j+1)*T/G): the
+// summation order of every per-system reduction depends only on the system
+// itself -- not on the device, the launch grid or the other members of a
+// batch.  Segments of >= 4 tiles keep the per-segment tree and flush small
+// against the per-row work.
+constexpr int kRedSegs = 608;
+constexpr int kSegTiles = 4;
+__host__ __device__ inline int red_segments(int tiles)
+{
+    const int g = (tiles + kSegTiles - 1) / kSegTiles;
+    return g < kRedSegs ? (g > 0 ? g : 1) : kRedSegs;
+}
 
 // Scalar state of one solve (lduSolverPerformance + Krylov scalars), plus
 // the FP64 outer state of a mixed-precision solve.

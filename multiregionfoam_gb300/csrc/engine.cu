@@ -106,7 +106,7 @@ void BatchHost::set(const std::vector<PlanState*>& systems)
         const PlanState* P = systems[s];
         sv[s] = P->sys;
         for (int t = 0; t < P->ntiles; ++t) tiles.push_back(make_int2(s, t));
-        for (int j = 0; j < std::min(P->ntiles, kRedSegs); ++j) segs.push_back(make_int2(s, j));
+        for (int j = 0; j < red_segments(P->ntiles); ++j) segs.push_back(make_int2(s, j));
         maxchunks = std::max(maxchunks, P->sys.nchunks);
         if (!P->sys.syncfree) maxlevels = std::max(maxlevels, P->sys.nlevels);
     }
@@ -445,7 +445,7 @@ static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, in
         // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
         // nl == 1); one chunk per warp of the widest level
         const int nl = bh.h.maxlevels;
-        const int g = std::max(1, std::min(65535, (bh.widest_level + 7) / 8));
+        const int g = std::max(1, std::min(persistent_grid(), (bh.widest_level + 7) / 8));
         for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, bh.d, g, st);
         for (int L = std::max(nl - 2, 0); L >= 0; --L) launch_sweep(prec, 0, trans, 0, L, bh.d, g, st);
     }

@@ -807,7 +807,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
                 live = system_live<OP>(sS);  // uniform over all of the system's segments
             }
             if (!live) continue;
-            const unsigned T = (unsigned)sS.ntiles, G = T < (unsigned)kRedSegs ? T : (unsigned)kRedSegs;
+            const unsigned T = (unsigned)sS.ntiles, G = (unsigned)red_segments(sS.ntiles);
             const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
             for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
@@ -816,12 +816,17 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
     }
 }
 
+// CTAs of a persistent launch: one wave of kMinCtas CTAs per SM.
+static int g_grid_cap = 152 * kMinCtas;
+
 template <typename V, RowOp OP>
 void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
 {
     // ntiles / nsegs: the host's upper bounds on the batch's table sizes
+    // Persistent grid: one wave that walks the tiles / segments, so each CTA
+    // pays its prologue (descriptor and system copy) once.
     int grid = OpTraits<OP>::kRed ? nsegs : ntiles;
-    grid = grid < 65535 ? grid : 65535;
+    grid = grid < g_grid_cap ? grid : g_grid_cap;
     if (grid < 1) grid = 1;
     if (pb)
         k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(dB);
@@ -1166,6 +1171,8 @@ __global__ void k_ggi(int n_dst, const int32_t* __restrict__ ptr, const int32_t*
 // ---------------------------------------------------------------- launchers
 static std::atomic<unsigned long long> g_launches{0};
 unsigned long long launch_count() { return g_launches.load(); }
+void set_device_sms(int nsm) { g_grid_cap = (nsm > 0 ? nsm : 152) * kMinCtas; }
+int persistent_grid() { return g_grid_cap; }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }
 
 void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)

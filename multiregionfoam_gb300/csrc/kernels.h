@@ -67,6 +67,9 @@ void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double
 // Kernels launched so far in this process (captured launches included;
 // the engine corrects for graph capture and replay).
 unsigned long long launch_count();
+// SM count of the device in use (sizes the persistent grids).
+void set_device_sms(int nsm);
+int persistent_grid();
 void add_launches(long long d);
 
 }  // namespace mrg

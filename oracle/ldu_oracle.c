@@ -497,16 +497,19 @@ static int mr_row(int tile, int t, int k, int assign)
     return ((row0 >> 5) + w + 8 * k) * 32 + lane;
 }
 
-#define MR_GRID 2432
+#define MR_GRID 608
+#define MR_SEG_TILES 4
 
 /* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order).
- * CTA g of G = min(tiles, 2432) owns tiles [g*T/G, (g+1)*T/G) and keeps
+ * Segment g of G = min(608, ceil(tiles/4)) owns tiles [g*T/G, (g+1)*T/G) and keeps
  * accumulating across them; its tree sum lands in the slot of its first tile
  * (the other slots stay zero). */
 static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)
 {
     int ntiles = o->npad / MR_TILE;
-    int G = ntiles < MR_GRID ? ntiles : MR_GRID;
+    int G = (ntiles + MR_SEG_TILES - 1) / MR_SEG_TILES;
+    if (G > MR_GRID) G = MR_GRID;
+    if (G < 1) G = 1;
     double* part = (double*)calloc((size_t)(ntiles ? ntiles : 1), sizeof(double));
     double acc[MR_BLOCK];
     for (int g = 0; g < G; ++g) {

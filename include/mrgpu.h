@@ -259,6 +259,37 @@ int mrg_kernel_launches(uint64_t* count);
 int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel,
                     int reps, float* ms_per_launch);
 
+/* ---- residual without device allocation -------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory where they need a residual: code inside a host application whose
+ * own allocator already holds the GPU's memory (a caching pool, or an MPS
+ * client under a hard memory limit), or monitoring code beside asynchronous
+ * solves, where cudaMalloc / cudaFree would synchronise the device.
+ *
+ * The same residual and norm factor as mrg_residual, for a matrix without
+ * interfaces held in the caller's device arrays in foam's lduAddressing:
+ * lowerAddr, upperAddr [n_faces]; ownerStartAddr, losortStartAddr
+ * [n_cells + 1]; losortAddr [n_faces]; diag [n_cells], upper, lower
+ * [n_faces] (d_lower NULL: symmetric); b, x [n_cells].  Runs on `stream` (a
+ * cudaStream_t of the current device, NULL = the default stream) and
+ * returns after it; residual and norm_factor are host pointers (either may
+ * be NULL).  It allocates nothing: its reduction scratch is a fixed
+ * 393,472-byte device array inside the library, held on every GPU that
+ * loads it until the process exits, so n_cells is limited to 16,777,216
+ * (larger: MRG_E_INVALID).  The first call on a device looks up that array
+ * and loads the library's device code there if needed: make it before any
+ * stream capture.  Every call shares the array: calls that overlap on the
+ * GPU (other host threads, or streams that do not wait for each other)
+ * race and give undefined results.  Addressing that points outside its
+ * arrays is not read and returns MRG_E_INVALID. */
+int mrg_residual_noalloc(int n_cells, int n_faces,
+                         const int* d_lower_addr, const int* d_upper_addr,
+                         const int* d_owner_start, const int* d_losort,
+                         const int* d_losort_start, const double* d_diag,
+                         const double* d_upper, const double* d_lower,
+                         const double* d_b, const double* d_x, void* stream,
+                         double* residual, double* norm_factor);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,6 +10,7 @@
 #include "../../include/mrgpu.h"
 #include "engine.h"
 #include "kernels.h"
+#include "noalloc.h"
 
 using namespace mrg;
 
@@ -658,6 +659,18 @@ int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel, in
         if (!mesh || !ms_per_launch) return fail(MRG_E_INVALID, "NULL argument");
         Controls k = to_controls(controls);
         *ms_per_launch = time_kernel(mesh->m, k, kernel, reps);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_residual_noalloc(int n_cells, int n_faces, const int* d_lower_addr, const int* d_upper_addr,
+                         const int* d_owner_start, const int* d_losort, const int* d_losort_start,
+                         const double* d_diag, const double* d_upper, const double* d_lower, const double* d_b,
+                         const double* d_x, void* stream, double* residual, double* norm_factor)
+{
+    return guard([&] {
+        residual_noalloc(n_cells, n_faces, d_lower_addr, d_upper_addr, d_owner_start, d_losort, d_losort_start,
+                         d_diag, d_upper, d_lower, d_b, d_x, stream, residual, norm_factor);
         return (int)MRG_OK;
     });
 }

@@ -28,6 +28,7 @@ EXPORTED = [
     "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
+    "mrg_residual_noalloc",
 ]
 
 
@@ -106,6 +107,7 @@ def load(path: str = LIB_PATH):
     L.mrg_batch_destroy.argtypes = [vp]
     L.mrg_batch_solve.argtypes = [vp, C.POINTER(dp), C.POINTER(dp), C.POINTER(Controls), C.POINTER(Perf)]
     L.mrg_batch_solve_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Perf)]
+    L.mrg_residual_noalloc.argtypes = [C.c_int, C.c_int] + [vp] * 11 + [dp, dp]
     _LIB = L
     return L
 
@@ -200,6 +202,18 @@ def kernel_launches() -> int:
     v = C.c_uint64()
     _check(load().mrg_kernel_launches(C.byref(v)))
     return v.value
+
+
+def residual_noalloc(n_cells: int, n_faces: int, d_lower_addr: int, d_upper_addr: int, d_owner_start: int,
+                     d_losort: int, d_losort_start: int, d_diag: int, d_upper: int, d_lower: int | None,
+                     d_b: int, d_x: int, stream: int | None = None) -> tuple[float, float]:
+    """mrg_residual_noalloc on device arrays (integer device addresses):
+    returns (residual, norm_factor) without allocating device memory."""
+    r, nf = C.c_double(), C.c_double()
+    _check(load().mrg_residual_noalloc(int(n_cells), int(n_faces), *[C.c_void_p(p) for p in (
+        d_lower_addr, d_upper_addr, d_owner_start, d_losort, d_losort_start, d_diag, d_upper, d_lower, d_b, d_x,
+        stream)], C.byref(r), C.byref(nf)))
+    return r.value, nf.value
 
 
 def host_array(ctx_unused, n: int, dtype=np.float64) -> np.ndarray:

@@ -40,19 +40,30 @@ __device__ __forceinline__ bool is_sent(float v) { return __float_as_uint(v) == 
 
 // float -> double on the integer pipe.  GB300 issues FP64 (conversions
 // included) at a small fraction of the FP32 rate, so the FP64 reductions of
-// the FP32 inner loop widen their operands with bit arithmetic: for a normal
-// float the double has the same sign and mantissa and the exponent rebiased
-// by 1023-127; zero, subnormal, inf and NaN take the hardware conversion.
-// The result is exactly (double)f.
+// the FP32 inner loop widen their operands with bit arithmetic only (a
+// hardware-conversion fallback for rare cases would be if-converted by the
+// compiler and then run for every element):
+//   normal     same sign and mantissa, exponent rebiased by 1023 - 127
+//   subnormal  m * 2^-149 = 1.f * 2^(p - 149), p = index of m's top bit
+//   zero       signed zero
+//   inf / NaN  exponent 0x7ff, mantissa shifted, NaN made quiet
+// The result equals (double)f for every float (checked over all 2^32 bit
+// patterns; NaN maps to NaN).
 __device__ __forceinline__ double widen(float f)
 {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)f;
-    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
-    const unsigned long long m = (unsigned long long)(u & 0x007fffffu) << 29;
-    const unsigned long long ex = (unsigned long long)(e + 896u) << 52;
-    return __longlong_as_double((long long)(s | ex | m));
+    const unsigned m = u & 0x007fffffu;
+    unsigned long long bits = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e - 1u < 0xfeu) {
+        bits |= ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    } else if (e == 0xffu) {
+        bits |= (0x7ffull << 52) | ((unsigned long long)m << 29) | (m ? (1ull << 51) : 0ull);
+    } else if (m) {
+        const int p = 31 - __clz((int)m);
+        bits |= ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull);
+    }
+    return __longlong_as_double((long long)bits);
 }
 __device__ __forceinline__ double widen(double d) { return d; }
 
@@ -213,6 +224,76 @@ __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __
         }
     }
     return y;
+}
+
+// Sliced-ELL product of one 1024-row tile, warp w taking the tile's slices
+// w, w+8, w+16, w+24.  The arithmetic of each row is ell_row's (diagonal
+// first, then entries in slot order, padding skipped), but the latency chain
+// is shorter: the 33 slice bounds of the tile are one coalesced load per warp
+// (handed out by shuffles), and the next slice's column indexes are fetched
+// while the current slice's coefficients and gathered x are in flight, so a
+// slice costs about one dependent round trip instead of three.
+// emit(i, y, x_i) consumes row i's product and its own x value.
+template <typename V, typename Emit>
+__device__ __forceinline__ void ell_tile(const int* __restrict__ sptr, const int* __restrict__ acol,
+                                         const V* __restrict__ val, const V* __restrict__ dg,
+                                         const V* __restrict__ x, int sl0, Emit&& emit)
+{
+    constexpr int kWarps = kBlock / 32, kPer = 32 / kWarps;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int sp = __ldg(sptr + sl0 + lane);
+    const int spend = __ldg(sptr + sl0 + 32);
+    int e0 = __shfl_sync(kFull, sp, wid);
+    int W = (__shfl_sync(kFull, sp, wid + 1) - e0) >> 5;
+    int c[kMaxW];
+    if (W <= kMaxW) {
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) c[k] = k < W ? __ldg(acol + e0 + lane + k * 32) : -1;
+    }
+#pragma unroll 1
+    for (int j = 0; j < kPer; ++j) {
+        const int s = wid + kWarps * j;
+        const int i = (sl0 + s) * 32 + lane;
+        int ne0 = 0, nW = kMaxW + 1;
+        if (j + 1 < kPer) {
+            ne0 = __shfl_sync(kFull, sp, s + kWarps);
+            const int ne1 = (s + kWarps + 1 < 32) ? __shfl_sync(kFull, sp, s + kWarps + 1) : spend;
+            nW = (ne1 - ne0) >> 5;
+        }
+        const V xi = __ldg(x + i);
+        V y = vmul(__ldg(dg + i), xi);
+        const V* __restrict__ v = val + e0 + lane;
+        if (W <= kMaxW) {
+            V a[kMaxW], xv[kMaxW];
+            unsigned live = 0;
+#pragma unroll
+            for (int k = 0; k < kMaxW; ++k) {
+                live |= (c[k] >= 0 ? 1u : 0u) << k;
+                a[k] = c[k] >= 0 ? __ldg(v + k * 32) : V(0);
+                xv[k] = c[k] >= 0 ? __ldg(x + c[k]) : V(0);
+            }
+            if (nW <= kMaxW) {
+#pragma unroll
+                for (int k = 0; k < kMaxW; ++k) c[k] = k < nW ? __ldg(acol + ne0 + lane + k * 32) : -1;
+            }
+#pragma unroll
+            for (int k = 0; k < kMaxW; ++k)
+                if (live & (1u << k)) y = vfma(a[k], xv[k], y);
+        } else {
+            const int* __restrict__ col = acol + e0 + lane;
+            for (int k = 0; k < W; ++k) {
+                const int ck = __ldg(col + k * 32);
+                if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldg(x + ck), y);
+            }
+            if (nW <= kMaxW) {
+#pragma unroll
+                for (int k = 0; k < kMaxW; ++k) c[k] = k < nW ? __ldg(acol + ne0 + lane + k * 32) : -1;
+            }
+        }
+        emit(i, y, xi);
+        e0 = ne0;
+        W = nW;
+    }
 }
 
 // Per-system finalisation, executed by thread 0 of the CTA that completes the
@@ -557,15 +638,18 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         const V* __restrict__ pT = v.pT;
         V* __restrict__ q = v.q;
         V* __restrict__ qT = v.qT;
-        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
-            const int i = sl * 32 + lane;
-            const V qi = ell_row<V>(sptr, acol, av, dg, p, i);
-            q[i] = qi;
-            if (PB) {
+        if constexpr (!PB) {
+            ell_tile<V>(sptr, acol, av, dg, p, sl0, [&](int i, V qi, V pi) {
+                q[i] = qi;
+                acc[0] = __fma_rn(widen(qi), widen(pi), acc[0]);
+            });
+        } else {
+            for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+                const int i = sl * 32 + lane;
+                const V qi = ell_row<V>(sptr, acol, av, dg, p, i);
+                q[i] = qi;
                 qT[i] = ell_row<V>(sptr, acol, atv, dg, pT, i);
                 acc[0] = __fma_rn(widen(qi), widen(pT[i]), acc[0]);
-            } else {
-                acc[0] = __fma_rn(widen(qi), widen(p[i]), acc[0]);
             }
         }
     } else if constexpr (OP == OP_UPDATE) {
@@ -964,12 +1048,13 @@ __device__ __forceinline__ SweepPtrs<V> sweep_ptrs(const SysDev& S, bool trans)
     return P;
 }
 
+// Rows i = r0 + lane < r1 of one chunk whose sweep entries start at e0 and
+// are W wide.
 template <typename V, bool FWD>
-__device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool syncfree, Ctl* ctl, int lvl0_end,
-                                            bool last_level, bool first_level)
+__device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1, int e0, int W, bool syncfree,
+                                           Ctl* ctl, int lvl0_end, bool last_level, bool first_level)
 {
     const int lane = threadIdx.x & 31;
-    const int r0 = __ldg(P.cstart + c), r1 = __ldg(P.cstart + c + 1);
     const int i = r0 + lane;
     if (i >= r1) return;
     V* __restrict__ y = P.y;
@@ -977,7 +1062,6 @@ __device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool s
     const V* __restrict__ r = P.r;
     const V* __restrict__ rD = P.rD;
     V* dep = FWD ? y : w;
-    const int e0 = __ldg(P.sptr + c), W = (__ldg(P.sptr + c + 1) - e0) >> 5;
     V acc;
     if (FWD || (!syncfree && first_level))
         acc = vmul(rD[i], r[i]);
@@ -1041,6 +1125,15 @@ __device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool s
 }
 
 template <typename V, bool FWD>
+__device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool syncfree, Ctl* ctl, int lvl0_end,
+                                            bool last_level, bool first_level)
+{
+    const int r0 = __ldg(P.cstart + c), r1 = __ldg(P.cstart + c + 1);
+    const int e0 = __ldg(P.sptr + c), W = (__ldg(P.sptr + c + 1) - e0) >> 5;
+    sweep_rows<V, FWD>(P, r0, r1, e0, W, syncfree, ctl, lvl0_end, last_level, first_level);
+}
+
+template <typename V, bool FWD>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __restrict__ pB, int trans)
 {
     const Batch B = *pB;
@@ -1076,12 +1169,16 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __re
 // One level L of a levelled sweep for every system that has it: forward
 // levels 1..nlevels-1, backward levels nlevels-2..0 (level 0 alone when
 // nlevels == 1).  Work comes from the batch's per-level list of (system,
-// chunk) items, one chunk per warp.
+// chunk) items, one chunk per warp, warp g taking items g, g + nw, ...
+// Lane k of a warp fetches the item and the row / entry bounds of the
+// warp's k-th next chunk, so 32 chunks' metadata costs one chain of
+// dependent loads instead of one chain per chunk.
 template <typename V, bool FWD>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
 {
     const Batch B = *pB;
     if (L >= B.maxlevels) return;
+    const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int i0 = B.item_off[L], i1 = B.item_off[L + 1];
@@ -1089,22 +1186,41 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __r
     bool ok = false, last = false, first = false;
     int lvl0_end = 0;
     SweepPtrs<V> P;
-    for (int it = i0 + gw; it < i1; it += nw) {
-        const int2 item = B.items[it];
-        if (item.x != cur) {
-            cur = item.x;
-            const SysDev& S = B.sys[cur];
-            const int nl = S.nlevels;
-            ok = S.sc->active && S.pc >= PC_DIC && !S.syncfree &&
-                 (FWD ? (L >= 1 && L <= nl - 1) : (L <= nl - 2 || (nl == 1 && L == 0)));
-            if (ok) {
-                lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
-                last = L == nl - 1;
-                first = L == 0;
-                P = sweep_ptrs<V, FWD>(S, trans != 0);
-            }
+    for (int base = i0 + gw; base < i1; base += 32 * nw) {
+        const int my = base + lane * nw;
+        int ms = -1, mc = 0, mr0 = 0, mr1 = 0, me0 = 0, mW = 0;
+        if (my < i1) {
+            const int2 item = B.items[my];
+            ms = item.x;
+            mc = item.y;
+            const SysDev& S = B.sys[ms];
+            const int* __restrict__ cs = S.chunk_start;
+            const int* __restrict__ sp = FWD ? S.f_sptr : S.b_sptr;
+            mr0 = __ldg(cs + mc);
+            mr1 = __ldg(cs + mc + 1);
+            me0 = __ldg(sp + mc);
+            mW = (__ldg(sp + mc + 1) - me0) >> 5;
         }
-        if (ok) sweep_chunk<V, FWD>(P, item.y, false, nullptr, lvl0_end, last, first);
+        const int cnt = min(32, (i1 - base + nw - 1) / nw);
+        for (int j = 0; j < cnt; ++j) {
+            const int s = __shfl_sync(kFull, ms, j);
+            const int r0 = __shfl_sync(kFull, mr0, j), r1 = __shfl_sync(kFull, mr1, j);
+            const int e0 = __shfl_sync(kFull, me0, j), W = __shfl_sync(kFull, mW, j);
+            if (s != cur) {
+                cur = s;
+                const SysDev& S = B.sys[cur];
+                const int nl = S.nlevels;
+                ok = S.sc->active && S.pc >= PC_DIC && !S.syncfree &&
+                     (FWD ? (L >= 1 && L <= nl - 1) : (L <= nl - 2 || (nl == 1 && L == 0)));
+                if (ok) {
+                    lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
+                    last = L == nl - 1;
+                    first = L == 0;
+                    P = sweep_ptrs<V, FWD>(S, trans != 0);
+                }
+            }
+            if (ok) sweep_rows<V, FWD>(P, r0, r1, e0, W, false, nullptr, lvl0_end, last, first);
+        }
     }
 }
 

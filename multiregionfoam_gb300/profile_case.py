@@ -1,0 +1,45 @@
+"""One solve of a named workload, for profiling the hot-path kernels.
+
+    python -m multiregionfoam_gb300.profile_case --case c2 --precision mixed
+    python -m multiregionfoam_gb300.profile_case --case c2 --precision fp64 --max-iter 6
+
+The case is built and uploaded once and solved once (PCG + DIC at 1e-8;
+mixed: colour ordering, fp64: exact foam order), so a kernel profiler sees
+every kernel of one solve -- or, with ``--max-iter``, of a few Krylov
+iterations after a short prologue.  Prints the solve's performance record.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import _build, cases, mrgpu
+
+CASES = {
+    "c1": lambda seed: cases.c1(form="global", seed=seed),
+    "c2": lambda seed: cases.c2(form="global", seed=seed),
+}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--case", default="c2", choices=sorted(CASES))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--max-iter", type=int, default=20000)
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args(argv)
+    _build.build()
+    s = CASES[args.case](args.seed)
+    ctx = mrgpu.Context(0)
+    m = mrgpu.Mesh(ctx, s.n, s.lower, s.upper)
+    m.upload(s.diag, s.upper_c)
+    ordering = "colour" if args.precision == "mixed" else "exact"
+    _, perf = m.solve(s.b, s.x0, tol=1e-8, precision=args.precision, ordering=ordering,
+                      max_iter=args.max_iter, iters_per_launch=2 if args.max_iter < 100 else 16)
+    print(json.dumps({"case": args.case, "n": s.n, "precision": args.precision, **perf}), flush=True)
+    m.close()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -235,6 +235,50 @@ int mrg_batch_solve_device(mrg_batch* batch, const double* const* d_b,
                            double* const* d_x_inout,
                            const mrg_controls* controls, mrg_perf* perfs);
 
+/* ---- serving: continuous batching of solve requests -------------------
+ * No counterpart in the reference, which solves each region's equation in
+ * turn inside its time loop (multiRegionSystem.C:193-324).  A server keeps
+ * the meshes' addressing resident and takes requests "solve this mesh with
+ * these new coefficients, b and x0" from any host thread; its own thread
+ * admits them into a running batch (one for PCG requests, one for PBiCG)
+ * between iteration-graph launches, while batch slots and the HBM budget
+ * on in-flight working sets allow, and completes each when it converges.
+ * A mesh has at most one request in flight; its next one waits.  Results
+ * are bit-identical to mrg_solve with the same controls.  While a server
+ * runs, only mrg_server_* calls may use its context; destroy it before its
+ * meshes and context. */
+typedef struct {
+    uint64_t submitted, completed;
+    int running, queued, peak_running, reserved;
+    size_t inflight_bytes, peak_inflight_bytes;
+} mrg_server_stats;
+/* sym_controls: PCG requests (preconditioner/precision/ordering/tolerance);
+ * asym_controls: PBiCG requests, or NULL to refuse them.  hbm_budget: bytes
+ * of in-flight working sets (0 = only the context's budget); max_active:
+ * members per running batch (0 = 256). */
+int mrg_server_create(mrg_ctx* ctx, const mrg_controls* sym_controls,
+                      const mrg_controls* asym_controls, size_t hbm_budget,
+                      int max_active, mrg_server** out);
+int mrg_server_destroy(mrg_server* server);
+/* Queue one solve of `mesh` (asym != 0: PBiCG family).  The host arrays
+ * (mrg_coeffs_upload's, plus b, x0 and x_out) must stay valid and unchanged
+ * until the request completes; pinned memory (mrg_host_alloc) copies
+ * fastest.  MRG_E_BUSY when the queue is full. */
+int mrg_server_submit(mrg_server* server, mrg_mesh* mesh, int asym,
+                      const double* diag, const double* upper,
+                      const double* lower_or_null, const double* iface_bou,
+                      const double* iface_int_or_null, const double* b,
+                      const double* x0, double* x_out, uint64_t* request_id);
+/* *done = 1 once the request finished (x_out written, perf filled); the
+ * record is then released and the return value is the request's status.
+ * latency_ms: submit to completion. */
+int mrg_server_poll(mrg_server* server, uint64_t request_id, int* done,
+                    mrg_perf* perf, double* latency_ms);
+/* As poll, blocking up to timeout_ms (< 0: no limit). */
+int mrg_server_wait(mrg_server* server, uint64_t request_id, double timeout_ms,
+                    int* done, mrg_perf* perf, double* latency_ms);
+int mrg_server_get_stats(mrg_server* server, mrg_server_stats* out);
+
 /* ---- device buffers, timing and diagnostics --------------------------
  * No counterpart in the reference (foam-extend times solves with
  * cpuTimeIncrement, multiRegionSystem.C:546-650).  They let a caller keep

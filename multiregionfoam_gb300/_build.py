@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_lib")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libmrgpu.so")
 
-SOURCES = ["kernels.cu", "engine.cu", "api.cu", "noalloc.cu", "plan.cpp"]
+SOURCES = ["kernels.cu", "engine.cu", "api.cu", "noalloc.cu", "plan.cpp", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
 
@@ -67,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
-        run([cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+        run([cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"])
     build_adapter(force)
     return LIB
 

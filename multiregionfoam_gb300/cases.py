@@ -200,6 +200,48 @@ def c4(count: int = 512, seed: int = 0, n_lo: int = 8000, n_hi: int = 260000):
             for i, (nx, ny, nzf, nzs) in enumerate(batch_shapes(count, n_lo, n_hi, seed))]
 
 
+def perturb_step(sys: LduSystem, rng, scale: float = 0.05) -> LduSystem:
+    """The next time step of a recurring mesh: every off-diagonal coefficient
+    and the diagonal's excess over the row's off-diagonal magnitudes are
+    multiplied by 1 + scale*N(0,1) (clipped positive), so a diagonally
+    dominant matrix stays so; b is perturbed the same way, x0 is kept."""
+    def f(k):
+        return np.clip(1.0 + scale * rng.standard_normal(k), 0.2, None)
+
+    def rowsum(up, lo):
+        s = np.zeros(sys.n)
+        np.add.at(s, sys.lower, np.abs(up))
+        np.add.at(s, sys.upper, np.abs(lo))
+        return s
+
+    lo_old = sys.upper_c if sys.lower_c is None else sys.lower_c
+    excess = sys.diag - rowsum(sys.upper_c, lo_old)
+    up = sys.upper_c * f(sys.nf)
+    lo = None if sys.lower_c is None else sys.lower_c * f(sys.nf)
+    diag = excess * f(sys.n) + rowsum(up, up if lo is None else lo)
+    return dataclasses.replace(sys, diag=diag, upper_c=up, lower_c=lo, b=sys.b * f(sys.n))
+
+
+def c5_meshes(count: int = 100, seed: int = 0, n_lo: int = 10000, n_hi: int = 2000000, asym_frac: float = 0.3):
+    """Served case: `count` meshes of log-uniform size in [n_lo, n_hi] cells,
+    a fraction `asym_frac` asymmetric convection-diffusion (PBiCG+DILU), the
+    rest two-region CHT (PCG+DIC).  Returns [(system, asym)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = float(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        a = np.exp(rng.uniform(np.log(0.5), np.log(2.0), 3))
+        a = a / np.cbrt(a.prod())
+        asym = bool(rng.uniform() < asym_frac)
+        nx, ny, nz = (max(4, int(round(np.cbrt(n) * a[k]))) for k in range(3))
+        if asym:
+            out.append((convdiff_system(nx, ny, nz, seed=seed + 1 + i), True))
+        else:
+            nzs = max(2, nz // 3)
+            out.append((cht_system(nx, ny, max(2, nz - nzs), nzs, seed=seed + 1 + i, k_range=(0.1, 50.0)), False))
+    return out
+
+
 def laplace_1d(n: int, dirichlet=(0.0, 1.0), k: float = 1.0):
     """1-D Laplacian with Dirichlet ends: exact solution is linear."""
     lower = np.arange(n - 1, dtype=np.int32)

@@ -5,12 +5,14 @@
 
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 
 #include "../../include/mrgpu.h"
 #include "engine.h"
 #include "kernels.h"
 #include "noalloc.h"
+#include "server.h"
 
 using namespace mrg;
 
@@ -22,6 +24,9 @@ struct mrg_mesh {
 };
 struct mrg_ggi {
     Ggi g;
+};
+struct mrg_server {
+    std::unique_ptr<Server> s;
 };
 struct mrg_batch {
     Ctx* ctx = nullptr;
@@ -123,35 +128,6 @@ void d2h(Ctx* c, double* h, const double* d, size_t n)
 {
     MRG_CUDA(cudaMemcpyAsync(h, d, 8 * n, cudaMemcpyDeviceToHost, c->st));
     MRG_CUDA(cudaStreamSynchronize(c->st));
-}
-
-void upload_coeffs(Mesh& m, const double* diag, const double* upper, const double* lower, const double* ibou,
-                   const double* iint, cudaMemcpyKind kind)
-{
-    if (!diag || (m.nf > 0 && !upper)) throw Error(MRG_E_INVALID, "diag/upper must not be NULL");
-    if (m.ni > 0 && !ibou) throw Error(MRG_E_INVALID, "interface coefficients must not be NULL");
-    Ctx* c = m.ctx;
-    if (!m.raw_diag) m.raw_diag = (double*)c->alloc(8 * (size_t)m.n);
-    if (!m.raw_upper) m.raw_upper = (double*)c->alloc(8 * (size_t)std::max(m.nf, 1));
-    if (lower && !m.raw_lower) m.raw_lower = (double*)c->alloc(8 * (size_t)std::max(m.nf, 1));
-    if (m.ni && !m.raw_ibou) m.raw_ibou = (double*)c->alloc(8 * (size_t)m.ni);
-    if (iint && !m.raw_iint) m.raw_iint = (double*)c->alloc(8 * (size_t)m.ni);
-    MRG_CUDA(cudaMemcpyAsync(m.raw_diag, diag, 8 * (size_t)m.n, kind, c->st));
-    if (m.nf) MRG_CUDA(cudaMemcpyAsync(m.raw_upper, upper, 8 * (size_t)m.nf, kind, c->st));
-    if (lower && m.nf) MRG_CUDA(cudaMemcpyAsync(m.raw_lower, lower, 8 * (size_t)m.nf, kind, c->st));
-    if (m.ni) MRG_CUDA(cudaMemcpyAsync(m.raw_ibou, ibou, 8 * (size_t)m.ni, kind, c->st));
-    if (iint && m.ni) MRG_CUDA(cudaMemcpyAsync(m.raw_iint, iint, 8 * (size_t)m.ni, kind, c->st));
-    const bool new_sym = lower == nullptr, new_int = iint != nullptr;
-    if (m.have_coeffs && (new_sym != m.sym || new_int != m.has_int)) {
-        // symmetry changed: the transposed views must be rebuilt
-        for (auto& p : m.plans)
-            if (p) p->scattered = 0;
-    }
-    m.sym = new_sym;
-    m.has_int = new_int;
-    m.have_coeffs = true;
-    ++m.version;
-    if (kind == cudaMemcpyHostToDevice) MRG_CUDA(cudaStreamSynchronize(c->st));
 }
 
 }  // namespace
@@ -302,7 +278,7 @@ int mrg_coeffs_upload(mrg_mesh* mesh, const double* diag, const double* upper, c
 {
     return guard([&] {
         if (!mesh) return fail(MRG_E_INVALID, "mesh is NULL");
-        upload_coeffs(mesh->m, diag, upper, lower_or_null, iface_bou, iface_int_or_null, cudaMemcpyHostToDevice);
+        upload_coeffs(mesh->m, diag, upper, lower_or_null, iface_bou, iface_int_or_null, cudaMemcpyHostToDevice, true);
         return (int)MRG_OK;
     });
 }
@@ -312,7 +288,7 @@ int mrg_coeffs_upload_device(mrg_mesh* mesh, const double* diag, const double* u
 {
     return guard([&] {
         if (!mesh) return fail(MRG_E_INVALID, "mesh is NULL");
-        upload_coeffs(mesh->m, diag, upper, lower_or_null, iface_bou, iface_int_or_null, cudaMemcpyDeviceToDevice);
+        upload_coeffs(mesh->m, diag, upper, lower_or_null, iface_bou, iface_int_or_null, cudaMemcpyDeviceToDevice, false);
         return (int)MRG_OK;
     });
 }
@@ -659,6 +635,102 @@ int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel, in
         if (!mesh || !ms_per_launch) return fail(MRG_E_INVALID, "NULL argument");
         Controls k = to_controls(controls);
         *ms_per_launch = time_kernel(mesh->m, k, kernel, reps);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_server_create(mrg_ctx* ctx, const mrg_controls* sym_controls, const mrg_controls* asym_controls,
+                      size_t hbm_budget, int max_active, mrg_server** out)
+{
+    return guard([&] {
+        if (!ctx || !sym_controls || !out) return fail(MRG_E_INVALID, "NULL argument");
+        *out = nullptr;
+        Controls sym = to_controls(sym_controls), asym;
+        if (asym_controls) asym = to_controls(asym_controls);
+        auto* s = new mrg_server();
+        try {
+            s->s.reset(new Server(&ctx->c, sym, asym_controls ? &asym : nullptr, hbm_budget, max_active));
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = s;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_server_destroy(mrg_server* server)
+{
+    return guard([&] {
+        delete server;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_server_submit(mrg_server* server, mrg_mesh* mesh, int asym, const double* diag, const double* upper,
+                      const double* lower_or_null, const double* iface_bou, const double* iface_int_or_null,
+                      const double* b, const double* x0, double* x_out, uint64_t* request_id)
+{
+    return guard([&] {
+        if (!server || !mesh || !request_id) return fail(MRG_E_INVALID, "NULL argument");
+        if (mesh->m.ni > 0 && !iface_bou) return fail(MRG_E_INVALID, "interface coefficients must not be NULL");
+        *request_id = server->s->submit(&mesh->m, asym, diag, upper, lower_or_null, iface_bou, iface_int_or_null, b,
+                                        x0, x_out);
+        return (int)MRG_OK;
+    });
+}
+
+static int server_result(int status, bool done, const Perf& p, const std::string& err, int* done_out,
+                         mrg_perf* perf, double lat, double* latency_ms)
+{
+    if (done_out) *done_out = done ? 1 : 0;
+    if (!done) return (int)MRG_OK;
+    fill_perf(perf, p);
+    if (latency_ms) *latency_ms = lat;
+    if (status != MRG_OK) return fail(status, err.empty() ? "request failed" : err);
+    return (int)MRG_OK;
+}
+
+int mrg_server_poll(mrg_server* server, uint64_t request_id, int* done, mrg_perf* perf, double* latency_ms)
+{
+    return guard([&] {
+        if (!server || !done) return fail(MRG_E_INVALID, "NULL argument");
+        bool d = false;
+        Perf p;
+        double lat = 0;
+        std::string err;
+        const int st = server->s->poll(request_id, &d, &p, &lat, &err);
+        return server_result(st, d, p, err, done, perf, lat, latency_ms);
+    });
+}
+
+int mrg_server_wait(mrg_server* server, uint64_t request_id, double timeout_ms, int* done, mrg_perf* perf,
+                    double* latency_ms)
+{
+    return guard([&] {
+        if (!server || !done) return fail(MRG_E_INVALID, "NULL argument");
+        bool d = false;
+        Perf p;
+        double lat = 0;
+        std::string err;
+        const int st = server->s->wait(request_id, timeout_ms, &d, &p, &lat, &err);
+        return server_result(st, d, p, err, done, perf, lat, latency_ms);
+    });
+}
+
+int mrg_server_get_stats(mrg_server* server, mrg_server_stats* out)
+{
+    return guard([&] {
+        if (!server || !out) return fail(MRG_E_INVALID, "NULL argument");
+        const ServerStats s = server->s->stats();
+        std::memset(out, 0, sizeof *out);
+        out->submitted = s.submitted;
+        out->completed = s.completed;
+        out->running = s.running;
+        out->queued = s.queued;
+        out->peak_running = s.peak_running;
+        out->inflight_bytes = s.inflight_bytes;
+        out->peak_inflight_bytes = s.peak_inflight_bytes;
         return (int)MRG_OK;
     });
 }

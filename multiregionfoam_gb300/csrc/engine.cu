@@ -82,7 +82,7 @@ BatchHost::~BatchHost()
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     if (!ctx) return;
     for (void* p : {(void*)d, (void*)d_ctl, (void*)d_sys, (void*)d_tiles, (void*)d_segs, (void*)d_items,
-                    (void*)d_item_off})
+                    (void*)d_item_off, (void*)d_scal})
         ctx->release(p);
 }
 
@@ -150,9 +150,13 @@ void BatchHost::set(const std::vector<PlanState*>& systems)
     h.maxchunks = maxchunks;
     h.maxlevels = maxlevels;
     MRG_CUDA(cudaMemcpyAsync(d, &h, sizeof(Batch), cudaMemcpyHostToDevice, st));
-    // graphs sized for the previous membership are rebuilt lazily
-    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
-    graphs.clear();
+    // Graphs refer to the descriptor's address only; their key holds the
+    // launch shapes (grids, level count), so one captured for an earlier
+    // membership stays valid while the shapes match.
+    if (graphs.size() > 32) {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+    }
     MRG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -192,6 +196,39 @@ static void release_plan(Ctx* c, PlanState* P)
 }
 
 // ------------------------------------------------------------------ Mesh
+
+// Copy a mesh's coefficients into its raw device arrays (caller numbering)
+// and bump its coefficient version; views and factors follow lazily.
+void upload_coeffs(Mesh& m, const double* diag, const double* upper, const double* lower, const double* ibou,
+                   const double* iint, cudaMemcpyKind kind, bool sync)
+{
+    if (!diag || (m.nf > 0 && !upper)) throw Error(MRG_E_INVALID, "diag/upper must not be NULL");
+    if (m.ni > 0 && !ibou) throw Error(MRG_E_INVALID, "interface coefficients must not be NULL");
+    Ctx* c = m.ctx;
+    if (!m.raw_diag) m.raw_diag = (double*)c->alloc(8 * (size_t)m.n);
+    if (!m.raw_upper) m.raw_upper = (double*)c->alloc(8 * (size_t)std::max(m.nf, 1));
+    if (lower && !m.raw_lower) m.raw_lower = (double*)c->alloc(8 * (size_t)std::max(m.nf, 1));
+    if (m.ni && !m.raw_ibou) m.raw_ibou = (double*)c->alloc(8 * (size_t)m.ni);
+    if (iint && !m.raw_iint) m.raw_iint = (double*)c->alloc(8 * (size_t)m.ni);
+    MRG_CUDA(cudaMemcpyAsync(m.raw_diag, diag, 8 * (size_t)m.n, kind, c->st));
+    if (m.nf) MRG_CUDA(cudaMemcpyAsync(m.raw_upper, upper, 8 * (size_t)m.nf, kind, c->st));
+    if (lower && m.nf) MRG_CUDA(cudaMemcpyAsync(m.raw_lower, lower, 8 * (size_t)m.nf, kind, c->st));
+    if (m.ni) MRG_CUDA(cudaMemcpyAsync(m.raw_ibou, ibou, 8 * (size_t)m.ni, kind, c->st));
+    if (iint && m.ni) MRG_CUDA(cudaMemcpyAsync(m.raw_iint, iint, 8 * (size_t)m.ni, kind, c->st));
+    const bool new_sym = lower == nullptr, new_int = iint != nullptr;
+    if (m.have_coeffs && (new_sym != m.sym || new_int != m.has_int)) {
+        // symmetry changed: the transposed views must be rebuilt
+        for (auto& p : m.plans)
+            if (p) p->scattered = 0;
+    }
+    m.sym = new_sym;
+    m.has_int = new_int;
+    m.have_coeffs = true;
+    ++m.version;
+    if (sync) MRG_CUDA(cudaStreamSynchronize(c->st));
+}
+
+
 Mesh::~Mesh()
 {
     if (!ctx) return;
@@ -482,8 +519,13 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
 
 static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int prec, int k)
 {
+    const int cap = persistent_grid();
+    const int g_rows = std::min(std::max(bh.h.ntiles, 1), cap), g_red = std::min(std::max(bh.h.nsegs, 1), cap);
+    const int g_sweep = std::max(1, std::min(cap, (bh.widest_level + 7) / 8));
     std::string key = std::to_string(cfg.solver) + "/" + std::to_string(cfg.pc) + "/" +
-                      std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k);
+                      std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k) + "/" +
+                      std::to_string(g_rows) + "/" + std::to_string(g_red) + "/" + std::to_string(g_sweep) + "/" +
+                      std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0);
     auto it = bh.graphs.find(key);
     if (it != bh.graphs.end()) return it->second;
     cudaStream_t st = bh.ctx->st;
@@ -553,6 +595,26 @@ static void write_ctl_controls(BatchHost& bh, const Controls& cfg)
     MRG_CUDA(cudaMemcpyAsync(bh.d_ctl, &host, sizeof(Ctl), cudaMemcpyHostToDevice, bh.ctx->st));
 }
 
+Perf perf_of(const Scal& q, int precision)
+{
+    Perf p;
+    if (precision == MRG_PRECISION_FP64) {
+        p.res0 = q.res0;
+        p.res = q.res;
+        p.iters = q.iter;
+        p.converged = q.converged;
+        p.singular = q.singular;
+    } else {
+        p.res0 = q.ores0;
+        p.res = q.ores;
+        p.iters = q.inner_total;
+        p.outer = q.oiter;
+        p.converged = q.oconv;
+    }
+    if (!std::isfinite(p.res0) || !std::isfinite(p.res)) p.status = MRG_E_BREAKDOWN;
+    return p;
+}
+
 std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
 {
     Ctx* c = bh.ctx;
@@ -597,23 +659,8 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
             MRG_CUDA(cudaMemcpyAsync(&sc[s], bh.members[s]->sys.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
         MRG_CUDA(cudaStreamSynchronize(st));
         for (size_t s = 0; s < bh.members.size(); ++s) {
-            Perf& p = out[s];
-            const Scal& q = sc[s];
-            if (cfg.precision == MRG_PRECISION_FP64) {
-                p.res0 = q.res0;
-                p.res = q.res;
-                p.iters = q.iter;
-                p.converged = q.converged;
-                p.singular = q.singular;
-            } else {
-                p.res0 = q.ores0;
-                p.res = q.ores;
-                p.iters = q.inner_total;
-                p.outer = q.oiter;
-                p.converged = q.oconv;
-            }
-            p.ms = ms;
-            if (!std::isfinite(p.res0) || !std::isfinite(p.res)) p.status = MRG_E_BREAKDOWN;
+            out[s] = perf_of(sc[s], cfg.precision);
+            out[s].ms = ms;
         }
     } catch (...) {
         cudaEventDestroy(e0);
@@ -634,6 +681,77 @@ Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
     P.sync_sys();
     P.single.sync_sys();
     return solve_batch(P.single, cfg)[0];
+}
+
+// ------------------------------------------------------------------ serving steps
+// The steps of solve_batch, one at a time, for a server that changes a
+// running batch's membership between iteration launches.  Each step works on
+// whichever members the given batch holds; per-system state decides what a
+// member does (Krylov-loop ops skip inactive members, refinement ops skip
+// members outside the outer loop), so a member sees the same sequence of
+// operations, and gets the same bits, as in solve_batch.
+void batch_begin(BatchHost& bh, const Controls& cfg)
+{
+    cudaStream_t st = bh.ctx->st;
+    const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    const bool gen = any_general_iface(bh);
+    write_ctl_controls(bh, cfg);
+    launch_rows(OP_PERMUTE_IN, 0, bh.d, nt, ns, 0, st);
+    launch_rows(OP_BEGIN, 0, bh.d, nt, ns, pb, st);
+    if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+    launch_rows(OP_SUMX, 0, bh.d, nt, ns, 0, st);
+    launch_rows(OP_INIT_RES, 0, bh.d, nt, ns, pb, st);
+    if (cfg.precision == MRG_PRECISION_MIXED) {
+        if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+        launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
+        launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
+    }
+    MRG_CUDA(cudaGetLastError());
+}
+
+void batch_iterate(BatchHost& bh, const Controls& cfg)
+{
+    const int prec = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
+    BatchHost::Graph gr = iteration_graph(bh, cfg, prec, std::max(1, cfg.k_launch));
+    MRG_CUDA(cudaGraphLaunch(gr.exec, bh.ctx->st));
+    add_launches(gr.nodes);
+}
+
+void batch_outer(BatchHost& bh, const Controls& cfg)
+{
+    cudaStream_t st = bh.ctx->st;
+    const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
+    if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, st);
+    launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
+    launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
+    MRG_CUDA(cudaGetLastError());
+}
+
+void batch_finish(BatchHost& bh)
+{
+    launch_rows(OP_PERMUTE_OUT, 0, bh.d, bh.h.ntiles, bh.h.nsegs, 0, bh.ctx->st);
+    MRG_CUDA(cudaGetLastError());
+}
+
+void batch_recount(BatchHost& bh)
+{
+    launch_recount(bh.d, bh.ctx->st);
+    MRG_CUDA(cudaGetLastError());
+}
+
+void batch_status(BatchHost& bh, std::vector<Scal>& out)
+{
+    const int nsys = (int)bh.members.size();
+    out.resize(nsys);
+    if (nsys == 0) return;
+    ensure(bh.ctx, bh.d_scal, bh.cap_scal, (size_t)nsys);
+    Ctl* h = pinned_ctl();
+    launch_gather_scal(bh.d, bh.d_scal, bh.ctx->st);
+    MRG_CUDA(cudaMemcpyAsync(out.data(), bh.d_scal, sizeof(Scal) * nsys, cudaMemcpyDeviceToHost, bh.ctx->st));
+    poll(bh, h);
 }
 
 // ------------------------------------------------------------------ building blocks

@@ -65,7 +65,8 @@ struct BatchHost {
     int2* d_segs = nullptr;
     int2* d_items = nullptr;
     int* d_item_off = nullptr;
-    size_t cap_sys = 0, cap_tiles = 0, cap_segs = 0, cap_items = 0, cap_off = 0;
+    Scal* d_scal = nullptr;    // gathered member states (serving)
+    size_t cap_sys = 0, cap_tiles = 0, cap_segs = 0, cap_items = 0, cap_off = 0, cap_scal = 0;
     int widest_level = 1;      // items of the widest sweep level (grid sizing)
     std::vector<PlanState*> members;
     struct Graph {
@@ -136,6 +137,28 @@ void prepare_batch(BatchHost& bh, const std::vector<Mesh*>& meshes, const Contro
 // Solve every member of the batch; each member's SysDev in_b/in_x/out_x point
 // at its caller-numbered device vectors.  Returns one Perf per member.
 std::vector<Perf> solve_batch(BatchHost& bh, const Controls& c);
+
+// Solve record of one member from its scalar state.
+Perf perf_of(const Scal& q, int precision);
+
+// Serving steps (the stages of solve_batch, for a batch whose membership
+// changes between them): begin = permute in + initial residual (+ first
+// refinement step when mixed); iterate = one launch of the captured K-iteration
+// graph; outer = correction + FP64 residual + next inner start (mixed);
+// finish = permute the solution out; recount = recompute the control block's
+// active counts after a membership change; status = gather every member's
+// scalar state to the host (checks the device error bits).
+void batch_begin(BatchHost& bh, const Controls& c);
+void batch_iterate(BatchHost& bh, const Controls& c);
+void batch_outer(BatchHost& bh, const Controls& c);
+void batch_finish(BatchHost& bh);
+void batch_recount(BatchHost& bh);
+void batch_status(BatchHost& bh, std::vector<Scal>& out);
+
+// Copy coefficients into a mesh's raw device arrays (caller numbering) and
+// bump its version; `sync` waits for the copies.
+void upload_coeffs(Mesh& m, const double* diag, const double* upper, const double* lower, const double* ibou,
+                   const double* iint, cudaMemcpyKind kind, bool sync);
 
 // Single-system conveniences (batch of one).
 PlanState& prepare(Mesh& m, const Controls& c);

@@ -1282,6 +1282,37 @@ __global__ void k_ggi(int n_dst, const int32_t* __restrict__ ptr, const int32_t*
     }
 }
 
+
+// Serving support.
+__global__ void k_gather_scal(const Batch* __restrict__ pB, Scal* __restrict__ out)
+{
+    const int nsys = pB->nsys;
+    const SysDev* __restrict__ Ss = pB->sys;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsys; s += gridDim.x * blockDim.x) out[s] = *Ss[s].sc;
+}
+
+// n_active / n_oactive of the batch's control block from its members' flags
+// (one CTA; counts are small integers, so the order of the sums is free).
+__global__ void k_recount(const Batch* __restrict__ pB)
+{
+    __shared__ unsigned na, no;
+    if (threadIdx.x == 0) na = no = 0u;
+    __syncthreads();
+    const int nsys = pB->nsys;
+    unsigned a = 0, o = 0;
+    for (int s = threadIdx.x; s < nsys; s += blockDim.x) {
+        const Scal* sc = pB->sys[s].sc;
+        a += sc->active ? 1u : 0u;
+        o += sc->ostate ? 1u : 0u;
+    }
+    atomicAdd(&na, a);
+    atomicAdd(&no, o);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        pB->ctl->n_active = na;
+        pB->ctl->n_oactive = no;
+    }
+}
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
@@ -1402,6 +1433,18 @@ void launch_permute(int to_internal, const SysDev* d, int s, const double* src, 
     if (grid > 2048) grid = 2048;
     if (grid < 1) grid = 1;
     k_permute<<<grid, 256, 0, st>>>(d, s, to_internal, src, dst, n);
+}
+
+void launch_gather_scal(const Batch* dB, Scal* out, cudaStream_t st)
+{
+    ++g_launches;
+    k_gather_scal<<<8, 128, 0, st>>>(dB, out);
+}
+
+void launch_recount(const Batch* dB, cudaStream_t st)
+{
+    ++g_launches;
+    k_recount<<<1, 256, 0, st>>>(dB);
 }
 
 void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double* w, const double* src, double* dst,

@@ -66,6 +66,11 @@ void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double
 
 // Kernels launched so far in this process (captured launches included;
 // the engine corrects for graph capture and replay).
+// Serving support: copy every member's Scal into out[nsys]; recompute the
+// control block's n_active / n_oactive from the members' flags.
+void launch_gather_scal(const Batch* dB, Scal* out, cudaStream_t st);
+void launch_recount(const Batch* dB, cudaStream_t st);
+
 unsigned long long launch_count();
 // SM count of the device in use (sizes the persistent grids).
 void set_device_sms(int nsm);

@@ -1,0 +1,366 @@
+// server.cpp -- continuous batching of solve requests (see server.h).
+//
+// The server thread owns the context's stream while it runs.  Each pass of
+// its loop: admit queued requests in arrival order while batch slots and the
+// HBM budget allow (a mesh has at most one step in flight: its next time
+// step waits for the previous one); start the admitted ones (coefficients,
+// b and x0 uploaded, views and factor, initial residual) in a side batch and
+// add them to their family's running batch; launch each running batch's
+// captured K-iteration graph once; gather every member's state; run the
+// mixed-precision outer step for members whose inner loop ended; copy out
+// and complete the members that converged.  New requests therefore join
+// while others are mid-solve, and all members share every kernel launch.
+#include "server.h"
+
+#include <algorithm>
+#include <chrono>
+
+#include "../../include/mrgpu.h"
+
+namespace mrg {
+
+namespace {
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+Server::Server(Ctx* ctx, const Controls& sym, const Controls* asym, size_t budget, int max_active)
+    : ctx_(ctx), budget_(budget), max_active_(max_active > 0 ? max_active : 256)
+{
+    if (sym.solver != MRG_SOLVER_PCG) throw Error(MRG_E_INVALID, "symmetric controls must select PCG");
+    if (asym && asym->solver != MRG_SOLVER_PBICG) throw Error(MRG_E_INVALID, "asymmetric controls must select PBiCG");
+    fam_[0].cfg = sym;
+    fam_[0].enabled = true;
+    if (asym) {
+        fam_[1].cfg = *asym;
+        fam_[1].enabled = true;
+    }
+    for (Family& F : fam_) {
+        F.main.init(ctx_);
+        F.sub.init(ctx_);
+    }
+    MRG_CUDA(cudaStreamSynchronize(ctx_->st));
+    thread_ = std::thread([this] { loop(); });
+}
+
+Server::~Server()
+{
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stopping_ = true;
+    }
+    cv_work_.notify_all();
+    if (thread_.joinable()) thread_.join();
+    cudaStreamSynchronize(ctx_->st);
+    std::vector<Request*> left;
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        for (auto& kv : reqs_)
+            if (kv.second->state != 2) left.push_back(kv.second);
+    }
+    for (Request* r : left) complete(r, MRG_E_INVALID, "server destroyed before the request completed");
+    for (auto& kv : reqs_) delete kv.second;
+    for (auto& kv : slots_) ctx_->release(kv.second.d_bx);
+}
+
+size_t Server::estimate(const Mesh& m) const
+{
+    // FP64 and FP32 work vectors, plan, coefficient views and their FP32
+    // copies (about 224 B per cell and 128 B per face for a symmetric
+    // matrix; asymmetric ones keep transposed views too).
+    const size_t per_cell = 224, per_face = m.sym ? 128 : 192;
+    return per_cell * (size_t)m.n + per_face * (size_t)m.nf + 16 * (size_t)m.n;
+}
+
+uint64_t Server::submit(Mesh* m, int asym, const double* diag, const double* upper, const double* lower,
+                        const double* ibou, const double* iint, const double* b, const double* x0, double* x_out)
+{
+    if (!m || !diag || (m->nf > 0 && !upper) || !b || !x0 || !x_out) throw Error(MRG_E_INVALID, "NULL argument");
+    if (m->ctx != ctx_) throw Error(MRG_E_INVALID, "the mesh belongs to another context");
+    const int f = asym ? 1 : 0;
+    if (!fam_[f].enabled) throw Error(MRG_E_INVALID, "this server takes no asymmetric (PBiCG) requests");
+    if (asym && !lower) throw Error(MRG_E_INVALID, "an asymmetric request needs lower coefficients");
+    auto* r = new Request();
+    r->mesh = m;
+    r->fam = f;
+    r->diag = diag;
+    r->upper = upper;
+    r->lower = lower;
+    r->ibou = ibou;
+    r->iint = iint;
+    r->b = b;
+    r->x0 = x0;
+    r->x_out = x_out;
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (stopping_) {
+            delete r;
+            throw Error(MRG_E_INVALID, "server is stopping");
+        }
+        if (queue_.size() >= 1u << 20) {
+            delete r;
+            throw Error(MRG_E_BUSY, "server queue full");
+        }
+        r->id = next_id_++;
+        r->t_submit = now_ms();
+        reqs_[r->id] = r;
+        slots_[m];   // create the mesh's slot here, under the lock
+        queue_.push_back(r);
+        ++st_.submitted;
+        st_.queued = (int)queue_.size();
+    }
+    cv_work_.notify_one();
+    return r->id;
+}
+
+int Server::poll(uint64_t id, bool* done, Perf* perf, double* latency_ms, std::string* err)
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) throw Error(MRG_E_INVALID, "unknown request id (or already collected)");
+    Request* r = it->second;
+    if (r->state != 2) {
+        *done = false;
+        return MRG_OK;
+    }
+    *done = true;
+    if (perf) *perf = r->perf;
+    if (latency_ms) *latency_ms = r->t_done - r->t_submit;
+    if (err) *err = r->err;
+    const int status = r->status;
+    reqs_.erase(it);
+    delete r;
+    return status;
+}
+
+int Server::wait(uint64_t id, double timeout_ms, bool* done, Perf* perf, double* latency_ms, std::string* err)
+{
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        auto it = reqs_.find(id);
+        if (it == reqs_.end()) throw Error(MRG_E_INVALID, "unknown request id (or already collected)");
+        Request* r = it->second;
+        auto ready = [r] { return r->state == 2; };
+        if (timeout_ms < 0)
+            cv_done_.wait(lk, ready);
+        else
+            cv_done_.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready);
+    }
+    return poll(id, done, perf, latency_ms, err);
+}
+
+ServerStats Server::stats()
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    return st_;
+}
+
+void Server::complete(Request* r, int status, const std::string& err)
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    r->state = 2;
+    r->status = status;
+    r->err = err;
+    r->t_done = now_ms();
+    st_.inflight_bytes -= std::min(st_.inflight_bytes, r->charged);
+    r->charged = 0;
+    auto it = slots_.find(r->mesh);
+    if (it != slots_.end()) it->second.busy = false;
+    ++st_.completed;
+    cv_done_.notify_all();
+}
+
+void Server::loop()
+{
+    cudaSetDevice(ctx_->device);
+    for (;;) {
+        std::vector<Request*> admitted[2], rejected;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            const bool idle = fam_[0].running.empty() && fam_[1].running.empty();
+            if (idle) cv_work_.wait(lk, [this] { return stopping_ || !queue_.empty(); });
+            if (stopping_) break;
+            for (auto it = queue_.begin(); it != queue_.end();) {
+                Request* r = *it;
+                Slot& sl = slots_[r->mesh];
+                if (sl.busy) {   // the mesh's previous step is still in flight
+                    ++it;
+                    continue;
+                }
+                const int f = r->fam;
+                if ((int)(fam_[f].running.size() + admitted[f].size()) >= max_active_) {
+                    ++it;
+                    continue;
+                }
+                const size_t need = sl.bytes ? sl.bytes : estimate(*r->mesh);
+                if (budget_ && need > budget_) {
+                    rejected.push_back(r);
+                    it = queue_.erase(it);
+                    continue;
+                }
+                if (budget_ && st_.inflight_bytes + need > budget_) break;   // first come, first served
+                sl.busy = true;
+                r->charged = need;
+                r->state = 1;
+                st_.inflight_bytes += need;
+                st_.peak_inflight_bytes = std::max(st_.peak_inflight_bytes, st_.inflight_bytes);
+                admitted[f].push_back(r);
+                it = queue_.erase(it);
+            }
+            st_.queued = (int)queue_.size();
+        }
+        for (Request* r : rejected)
+            complete(r, MRG_E_OOM, "the request's working set exceeds the server's HBM budget");
+        for (int f = 0; f < 2; ++f) {
+            try {
+                if (!admitted[f].empty()) start(f, admitted[f]);
+                if (!fam_[f].running.empty()) batch_iterate(fam_[f].main, fam_[f].cfg);
+            } catch (const Error& e) {
+                fail_family(f, e.code, e.what());
+            }
+        }
+        for (int f = 0; f < 2; ++f) {
+            try {
+                if (!fam_[f].running.empty()) harvest(f);
+            } catch (const Error& e) {
+                fail_family(f, e.code, e.what());
+            }
+        }
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.running = (int)(fam_[0].running.size() + fam_[1].running.size());
+        st_.peak_running = std::max(st_.peak_running, st_.running);
+    }
+}
+
+static std::vector<PlanState*> plans_of(const std::vector<Mesh*>& ms, int ordering)
+{
+    std::vector<PlanState*> ps;
+    for (Mesh* m : ms) ps.push_back(&m->plan(ordering));
+    return ps;
+}
+
+void Server::start(int f, std::vector<Request*>& rs)
+{
+    Family& F = fam_[f];
+    cudaStream_t st = ctx_->st;
+    for (Request* r : rs) {
+        try {
+            Mesh& m = *r->mesh;
+            Slot* sl;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                sl = &slots_[&m];
+            }
+            const bool had_plan = m.plans[F.cfg.ordering] != nullptr;
+            const size_t before = ctx_->used;
+            upload_coeffs(m, r->diag, r->upper, r->lower, r->ibou, r->iint, cudaMemcpyHostToDevice, false);
+            const size_t n = (size_t)m.n;
+            if (!sl->d_bx) sl->d_bx = (double*)ctx_->alloc(16 * n);
+            MRG_CUDA(cudaMemcpyAsync(sl->d_bx, r->b, 8 * n, cudaMemcpyHostToDevice, st));
+            MRG_CUDA(cudaMemcpyAsync(sl->d_bx + n, r->x0, 8 * n, cudaMemcpyHostToDevice, st));
+            PlanState& P = m.plan(F.cfg.ordering);
+            P.sys.in_b = sl->d_bx;
+            P.sys.in_x = sl->d_bx + n;
+            P.sys.out_x = sl->d_bx + n;
+            F.sub.set({&P});
+            std::vector<Mesh*> ms{&m};
+            prepare_batch(F.sub, ms, F.cfg);
+            F.sub.sync_sys();
+            batch_begin(F.sub, F.cfg);
+            const size_t grew = ctx_->used - before;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (!sl->bytes) {
+                    // measured when this admission built the working set
+                    sl->bytes = had_plan ? std::max(grew, estimate(m)) : grew;
+                    st_.inflight_bytes += sl->bytes;
+                    st_.inflight_bytes -= std::min(st_.inflight_bytes, r->charged);
+                    r->charged = sl->bytes;
+                    st_.peak_inflight_bytes = std::max(st_.peak_inflight_bytes, st_.inflight_bytes);
+                }
+            }
+            F.running.push_back(r);
+        } catch (const Error& e) {
+            complete(r, e.code, e.what());
+        }
+    }
+    std::vector<Mesh*> ms;
+    for (Request* r : F.running) ms.push_back(r->mesh);
+    F.main.set(plans_of(ms, F.cfg.ordering));
+    batch_recount(F.main);
+}
+
+void Server::harvest(int f)
+{
+    Family& F = fam_[f];
+    std::vector<Scal> sc;
+    batch_status(F.main, sc);
+    const bool mixed = F.cfg.precision == MRG_PRECISION_MIXED;
+    std::vector<Request*> outer, done;
+    for (size_t s = 0; s < F.running.size(); ++s) {
+        if (sc[s].active) continue;
+        if (mixed && sc[s].ostate)
+            outer.push_back(F.running[s]);
+        else
+            done.push_back(F.running[s]);
+    }
+    if (outer.empty() && done.empty()) return;
+    if (!outer.empty()) {
+        // correction, FP64 residual and the next inner start of the members
+        // whose FP32 loop ended; those whose refinement ended are complete
+        std::vector<Mesh*> ms;
+        for (Request* r : outer) ms.push_back(r->mesh);
+        F.sub.set(plans_of(ms, F.cfg.ordering));
+        batch_outer(F.sub, F.cfg);
+        std::vector<Scal> s2;
+        batch_status(F.sub, s2);
+        for (size_t i = 0; i < outer.size(); ++i)
+            if (!s2[i].ostate) done.push_back(outer[i]);
+    }
+    if (!done.empty()) {
+        std::vector<Mesh*> ms;
+        for (Request* r : done) ms.push_back(r->mesh);
+        F.sub.set(plans_of(ms, F.cfg.ordering));
+        batch_finish(F.sub);
+        std::vector<Scal> s3;
+        batch_status(F.sub, s3);
+        for (Request* r : done) {
+            Slot* sl;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                sl = &slots_[r->mesh];
+            }
+            const size_t n = (size_t)r->mesh->n;
+            MRG_CUDA(cudaMemcpyAsync(r->x_out, sl->d_bx + n, 8 * n, cudaMemcpyDeviceToHost, ctx_->st));
+        }
+        MRG_CUDA(cudaStreamSynchronize(ctx_->st));
+        for (size_t i = 0; i < done.size(); ++i) {
+            Perf p = perf_of(s3[i], F.cfg.precision);
+            done[i]->perf = p;
+            F.running.erase(std::find(F.running.begin(), F.running.end(), done[i]));
+            complete(done[i], p.status, p.status ? "non-finite residual (breakdown)" : "");
+        }
+    }
+    std::vector<Mesh*> ms;
+    for (Request* r : F.running) ms.push_back(r->mesh);
+    F.main.set(plans_of(ms, F.cfg.ordering));
+    batch_recount(F.main);
+}
+
+void Server::fail_family(int f, int code, const std::string& msg)
+{
+    Family& F = fam_[f];
+    cudaStreamSynchronize(ctx_->st);
+    std::vector<Request*> rs;
+    rs.swap(F.running);
+    for (Request* r : rs) complete(r, code, msg);
+    try {
+        F.main.set({});
+    } catch (const Error&) {
+    }
+}
+
+}  // namespace mrg

@@ -28,7 +28,8 @@ EXPORTED = [
     "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
-    "mrg_residual_noalloc",
+    "mrg_residual_noalloc", "mrg_server_create", "mrg_server_destroy", "mrg_server_submit", "mrg_server_poll",
+    "mrg_server_wait", "mrg_server_get_stats",
 ]
 
 
@@ -54,6 +55,12 @@ class Perf(C.Structure):
         return {"initial_residual": self.initial_residual, "final_residual": self.final_residual,
                 "n_iter": self.n_iter, "converged": bool(self.converged), "singular": bool(self.singular),
                 "status": self.status, "n_outer": self.n_outer, "solve_ms": self.solve_ms}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("running", C.c_int), ("queued", C.c_int),
+                ("peak_running", C.c_int), ("reserved", C.c_int), ("inflight_bytes", C.c_size_t),
+                ("peak_inflight_bytes", C.c_size_t)]
 
 
 class IfaceDesc(C.Structure):
@@ -108,6 +115,14 @@ def load(path: str = LIB_PATH):
     L.mrg_batch_solve.argtypes = [vp, C.POINTER(dp), C.POINTER(dp), C.POINTER(Controls), C.POINTER(Perf)]
     L.mrg_batch_solve_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Perf)]
     L.mrg_residual_noalloc.argtypes = [C.c_int, C.c_int] + [vp] * 11 + [dp, dp]
+    L.mrg_server_create.argtypes = [vp, C.POINTER(Controls), C.POINTER(Controls), C.c_size_t, C.c_int,
+                                    C.POINTER(vp)]
+    L.mrg_server_destroy.argtypes = [vp]
+    L.mrg_server_submit.argtypes = [vp, vp, C.c_int] + [vp] * 8 + [C.POINTER(C.c_uint64)]
+    L.mrg_server_poll.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int), C.POINTER(Perf), C.POINTER(C.c_double)]
+    L.mrg_server_wait.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(C.c_int), C.POINTER(Perf),
+                                  C.POINTER(C.c_double)]
+    L.mrg_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
     _LIB = L
     return L
 
@@ -379,3 +394,60 @@ class Ggi:
         if self.h:
             _check(load().mrg_ggi_destroy(self.h))
             self.h = None
+
+
+class Server:
+    """Continuous-batching solve server (mrg_server_*).
+
+    While it runs, use the context only through this object.  submit() keeps
+    references to the request's arrays until the request is collected."""
+
+    def __init__(self, ctx: Context, sym: Controls, asym: Controls | None = None, hbm_budget: int = 0,
+                 max_active: int = 0):
+        h = C.c_void_p()
+        _check(load().mrg_server_create(ctx.h, C.byref(sym), C.byref(asym) if asym is not None else None,
+                                        int(hbm_budget), int(max_active), C.byref(h)))
+        self.h = h
+        self._live = {}
+
+    def submit(self, mesh: "Mesh", b, x0, diag, upper, lower=None, iface_bou=None, iface_int=None,
+               asym: bool = False, x_out=None) -> int:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (diag, upper, lower, iface_bou, iface_int, b, x0)]
+        x = np.empty(mesh.n) if x_out is None else x_out
+        rid = C.c_uint64()
+        _check(load().mrg_server_submit(self.h, mesh.h, int(bool(asym)),
+                                        *[None if a is None else a.ctypes.data_as(C.c_void_p) for a in arrs],
+                                        x.ctypes.data_as(C.c_void_p), C.byref(rid)))
+        self._live[rid.value] = (arrs, x)
+        return rid.value
+
+    def _result(self, rid, fn, *extra):
+        done = C.c_int()
+        p = Perf()
+        lat = C.c_double()
+        rc = fn(self.h, C.c_uint64(rid), *extra, C.byref(done), C.byref(p), C.byref(lat))
+        if done.value:
+            _, x = self._live.pop(rid)
+            _check(rc)
+            return x, p.as_dict(), lat.value
+        _check(rc)
+        return None
+
+    def poll(self, rid: int):
+        """(x, perf, latency_ms) once the request finished, else None."""
+        return self._result(rid, load().mrg_server_poll)
+
+    def wait(self, rid: int, timeout_ms: float = -1.0):
+        return self._result(rid, load().mrg_server_wait, C.c_double(timeout_ms))
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(load().mrg_server_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_ if k != "reserved"}
+
+    def close(self):
+        if self.h:
+            _check(load().mrg_server_destroy(self.h))
+            self.h = None
+            self._live.clear()

@@ -17,6 +17,14 @@ monolithic LDU form.  One step = one solve to foam-normalised residual 1e-8
 The working set (~1 GB per solve) is far larger than the 129 MB L2, so no
 L2 flush is needed between steps.
 
+Beside the headline, the line carries the other two forms of the metric:
+  batched   512 independent CHT systems (8k-260k cells) in one batch, mixed
+            vs plain FP64, solves/s (--batched N, 0 skips)
+  served    Poisson-arriving requests over recurring meshes (10k-2M cells,
+            70% PCG+DIC / 30% PBiCG+DILU, 5% coefficient drift per step)
+            through the continuous-batching server: solves/s, p50/p99 ms
+            (--served-meshes/--served-steps/--served-rate, 0 meshes skips)
+
 --impl reference times the reference algorithm's CPU implementation (the
 project's C oracle; foam-extend itself cannot be built here) on bounded
 samples of the same solve.
@@ -218,6 +226,102 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, ctx, mrgpu):
+    """Batched configuration: `args.batched` independent two-region CHT
+    systems (cells log-uniform in [8k, 260k], random aspect ratios,
+    conductivity log-uniform in [0.1, 50]) solved in one batch, device
+    resident; mixed (colour) and plain FP64 (exact order)."""
+    from multiregionfoam_gb300 import cases
+    systems = cases.c4(args.batched, seed=SEED)
+    meshes = []
+    for s in systems:
+        m = mrgpu.Mesh(ctx, s.n, s.lower, s.upper)
+        m.upload(s.diag, s.upper_c)
+        meshes.append(m)
+    d_b = [ctx.to_device(s.b) for s in systems]
+    d_x0 = [ctx.to_device(s.x0) for s in systems]
+    d_x = [ctx.dev_alloc(8 * s.n) for s in systems]
+    out = {"systems": len(systems), "cells": int(sum(s.n for s in systems)),
+           "faces": int(sum(s.nf for s in systems))}
+    for name, prec, order in (("mixed", "mixed", "colour"), ("plain_fp64", "fp64", "exact")):
+        bt = mrgpu.Batch(ctx, meshes, order)
+        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="PCG", precond="DIC", precision=prec, ordering=order,
+                             inner_rel_tol=args.inner_tol)
+        ms = []
+        for rep in range(1 + args.batched_reps):
+            for sy, a, b in zip(systems, d_x, d_x0):
+                ctx.copy_d2d(a, b, 8 * sy.n)
+            ctx.record(50)
+            perfs = bt.solve_device(d_b, d_x, ctl)
+            ctx.record(51)
+            if rep:
+                ms.append(ctx.elapsed_ms(50, 51))
+        bt.close()
+        its = [p["n_iter"] for p in perfs]
+        best = min(ms)
+        out[name] = {"solves_per_s": len(systems) / (best * 1e-3), "ms_per_batch": best,
+                     "iters_max": int(max(its)), "iters_mean": float(np.mean(its)),
+                     "converged": int(sum(p["converged"] for p in perfs))}
+    out["speedup_mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    for a in d_b + d_x0 + d_x:
+        ctx.dev_free(a)
+    for m in meshes:
+        m.close()
+    return out
+
+
+def run_served(args, ctx, mrgpu):
+    """Served configuration: Poisson arrivals at `args.served_rate`/s of
+    solve requests over `args.served_meshes` meshes (cells log-uniform in
+    [10k, 2M], 70% CHT with PCG+DIC, 30% convection-diffusion with
+    PBiCG+DILU), each mesh recurring `args.served_steps` time steps with its
+    coefficients re-drawn at 5% perturbation per step; 150 GB HBM budget.
+    Mixed (colour) and plain FP64 (exact) servers in turn."""
+    from multiregionfoam_gb300 import cases
+    ms = cases.c5_meshes(args.served_meshes, seed=SEED)
+    rng = np.random.default_rng(SEED + 7)
+    meshes, steps = [], []
+    for s, a in ms:
+        meshes.append(mrgpu.Mesh(ctx, s.n, s.lower, s.upper))
+        cur, seq = s, []
+        for k in range(args.served_steps):
+            seq.append(cur)
+            cur = cases.perturb_step(cur, rng)
+        steps.append(seq)
+    reqs = [(i, steps[i][k], ms[i][1]) for k in range(args.served_steps) for i in range(len(ms))]
+    arrivals = np.cumsum(np.random.default_rng(SEED + 11).exponential(1.0 / args.served_rate, len(reqs)))
+    out = {"requests": len(reqs), "meshes": len(ms), "rate_per_s": args.served_rate,
+           "cells_mean": float(np.mean([s.n for s, _ in ms])), "asym_meshes": int(sum(a for _, a in ms)),
+           "hbm_budget_gb": 150}
+    for name, prec, order in (("mixed", "mixed", "colour"), ("plain_fp64", "fp64", "exact")):
+        kw = dict(tol=TOL, max_iter=20000, precision=prec, ordering=order, inner_rel_tol=args.inner_tol,
+                  iters_per_launch=8)
+        srv = mrgpu.Server(ctx, mrgpu.controls(solver="PCG", precond="DIC", **kw),
+                           mrgpu.controls(solver="PBiCG", precond="DILU", **kw), hbm_budget=150 * 2**30)
+        ids = []
+        t0 = time.perf_counter()
+        for (i, s, a), ta in zip(reqs, arrivals):
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(meshes[i], s.b, s.x0, s.diag, s.upper_c, s.lower_c, asym=a))
+        lat, conv = [], 0
+        for r in ids:
+            x, p, l = srv.wait(r, 600000.0)
+            lat.append(l)
+            conv += p["converged"]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        out[name] = {"solves_per_s": len(ids) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                     "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv),
+                     "peak_running": st["peak_running"], "peak_inflight_gb": st["peak_inflight_bytes"] / 2**30}
+    out["speedup_mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    for m in meshes:
+        m.close()
+    return out
+
+
 def run_gpu(args):
     from multiregionfoam_gb300 import _build, mrgpu
     rank, world, local, dist = dist_setup(args.gpus)
@@ -301,6 +405,9 @@ def run_gpu(args):
     ach64 = bytes64 / (ms_spmv64 * 1e-3) / 1e9
     traffic = profile_traffic("spmv_fp32_c2.txt")
 
+    batched = run_batched(args, ctx, mrgpu) if args.batched > 0 else None
+    served = run_served(args, ctx, mrgpu) if args.served_meshes > 0 else None
+
     if rank != 0:
         return
     k = args.steps
@@ -342,6 +449,8 @@ def run_gpu(args):
                      "algorithmic_bytes": bytes32, "ms_per_launch": ms_spmv32, "peak_source": peak_kind},
         "kernels": {"spmv_fp64": {"ms": ms_spmv64, "GB/s": ach64, "frac": ach64 / peak},
                     "precondition_fp32_colour_ms": ms_prec32, "precondition_fp64_exact_ms": ms_prec64},
+        "batched": batched,
+        "served": served,
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": int(launches),
@@ -361,6 +470,11 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=40)
     ap.add_argument("--ref-iters", type=int, default=0, help="reference arm: iterations per solve (0 = measured)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batched", type=int, default=512, help="systems of the batched configuration (0: skip)")
+    ap.add_argument("--batched-reps", type=int, default=2)
+    ap.add_argument("--served-meshes", type=int, default=24, help="meshes of the served configuration (0: skip)")
+    ap.add_argument("--served-steps", type=int, default=8)
+    ap.add_argument("--served-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -87,8 +87,10 @@ typedef struct {
                               reduce its residual per refinement step
                               (default 1e-5); each step aims at 0.1 x the
                               residual still to remove, never below this    */
-    int inner_max_iter;    /* mixed: inner iterations per outer step (default
-                              = max_iter)                                    */
+    int inner_max_iter;    /* mixed: inner iterations per outer step; 0 =
+                              max_iter for PCG, 150 for PBiCG (an FP32 BiCG
+                              recurrence can drift and diverge; restarting
+                              it from the FP64 residual keeps it stable)     */
     int max_outer;         /* mixed: refinement steps (default 50)          */
     int iters_per_launch;  /* iterations per CUDA-graph launch (default 16) */
 } mrg_controls;

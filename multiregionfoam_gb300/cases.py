@@ -209,10 +209,8 @@ def perturb_step(sys: LduSystem, rng, scale: float = 0.05) -> LduSystem:
         return np.clip(1.0 + scale * rng.standard_normal(k), 0.2, None)
 
     def rowsum(up, lo):
-        s = np.zeros(sys.n)
-        np.add.at(s, sys.lower, np.abs(up))
-        np.add.at(s, sys.upper, np.abs(lo))
-        return s
+        return (np.bincount(sys.lower, np.abs(up), minlength=sys.n) +
+                np.bincount(sys.upper, np.abs(lo), minlength=sys.n))
 
     lo_old = sys.upper_c if sys.lower_c is None else sys.lower_c
     excess = sys.diag - rowsum(sys.upper_c, lo_old)

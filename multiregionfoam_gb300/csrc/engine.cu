@@ -588,7 +588,10 @@ static void write_ctl_controls(BatchHost& bh, const Controls& cfg)
     host.inner_rel_tol = cfg.inner_rel_tol;
     host.min_iter = cfg.min_iter;
     host.max_iter = cfg.max_iter;
-    host.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : cfg.max_iter;
+    // FP32 BiCG restarts from the FP64 residual every 150 iterations unless
+    // told otherwise: its unstabilised recurrence can drift in FP32
+    const int auto_inner = cfg.solver == MRG_SOLVER_PBICG ? std::min(cfg.max_iter, 150) : cfg.max_iter;
+    host.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : auto_inner;
     host.max_outer = cfg.max_outer;
     host.mixed = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
     // tickets, error bits and active counts start at zero

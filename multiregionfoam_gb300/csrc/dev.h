@@ -93,7 +93,9 @@ struct Ctl {
     unsigned err;          // error bits (1 = wait timeout)
     unsigned n_active;     // systems still in their Krylov loop
     unsigned n_oactive;    // systems still in their mixed-precision outer loop
-    unsigned pad[5];
+    unsigned bar_count;    // persistent iteration kernel: CTAs at the grid barrier
+    unsigned bar_gen;      // persistent iteration kernel: barrier generation
+    unsigned pad[3];
     // controls written into every system's Scal by OP_BEGIN
     double tol, rel_tol, inner_rel_tol;
     int min_iter, max_iter, inner_max, max_outer, mixed, pad2;

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 
 #include "../../include/mrgpu.h"
@@ -517,32 +518,82 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
     launch_rows(OP_UPDATE, prec, bh.d, nt, ns, pb, st);
 }
 
+// How K iterations are launched: K copies of the separate launches of
+// record_iteration captured in one graph (the default: measured faster on
+// GB300, a kernel boundary inside a graph costs about what a grid barrier
+// does), or one persistent cooperative kernel whose phases are those
+// launches (MRG_ITERATION=persistent).  Both give the same bits.
+static bool persistent_iteration()
+{
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = std::getenv("MRG_ITERATION");
+        mode = (e && std::string(e) == "persistent") ? 1 : 0;
+    }
+    return mode == 1;
+}
+
+static void record_persistent(BatchHost& bh, const Controls& cfg, int prec, int k, cudaStream_t st)
+{
+    const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int sf = cfg.ordering == MRG_ORDER_EXACT && cfg.pc >= PC_DIC;
+    MRG_CUDA(launch_iterate(prec, pb, sf, bh.d, k, cfg.pc, any_general_iface(bh) ? 1 : 0, st));
+}
+
+// The captured graph of K iterations.  A persistent launch that the driver
+// refuses to capture is launched directly instead (exec stays null).
 static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int prec, int k)
 {
+    const bool pers = persistent_iteration();
     const int cap = persistent_grid();
     const int g_rows = std::min(std::max(bh.h.ntiles, 1), cap), g_red = std::min(std::max(bh.h.nsegs, 1), cap);
     const int g_sweep = std::max(1, std::min(cap, (bh.widest_level + 7) / 8));
     std::string key = std::to_string(cfg.solver) + "/" + std::to_string(cfg.pc) + "/" +
                       std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k) + "/" +
                       std::to_string(g_rows) + "/" + std::to_string(g_red) + "/" + std::to_string(g_sweep) + "/" +
-                      std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0);
+                      std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0) +
+                      (pers ? "/p" : "/l");
     auto it = bh.graphs.find(key);
     if (it != bh.graphs.end()) return it->second;
     cudaStream_t st = bh.ctx->st;
     cudaGraph_t g = nullptr;
     const unsigned long long before = launch_count();
     MRG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < k; ++i) record_iteration(bh, cfg, prec, st);
+    cudaError_t rec = cudaSuccess;
+    if (pers) {
+        const int pb = cfg.solver == MRG_SOLVER_PBICG;
+        const int sf = cfg.ordering == MRG_ORDER_EXACT && cfg.pc >= PC_DIC;
+        rec = launch_iterate(prec, pb, sf, bh.d, k, cfg.pc, any_general_iface(bh) ? 1 : 0, st);
+    } else {
+        for (int i = 0; i < k; ++i) record_iteration(bh, cfg, prec, st);
+    }
     cudaError_t e = cudaStreamEndCapture(st, &g);
     const long long nodes = (long long)(launch_count() - before);
     add_launches(-nodes);  // captured, not executed
-    MRG_CUDA(e);
     cudaGraphExec_t ex = nullptr;
-    MRG_CUDA(cudaGraphInstantiate(&ex, g, 0));
-    cudaGraphDestroy(g);
+    if (rec == cudaSuccess && e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (pers && (rec != cudaSuccess || e != cudaSuccess)) {
+        cudaGetLastError();   // capture refused: launch directly
+        ex = nullptr;
+    } else {
+        MRG_CUDA(rec);
+        MRG_CUDA(e);
+    }
     BatchHost::Graph gr{ex, nodes};
     bh.graphs[key] = gr;
     return gr;
+}
+
+// One launch of K iterations (graph replay, or the persistent kernel).
+static void launch_iterations(BatchHost& bh, const Controls& cfg, int prec, const BatchHost::Graph& gr)
+{
+    if (gr.exec) {
+        MRG_CUDA(cudaGraphLaunch(gr.exec, bh.ctx->st));
+        add_launches(gr.nodes);
+    } else {
+        record_persistent(bh, cfg, prec, std::max(1, cfg.k_launch), bh.ctx->st);
+    }
 }
 
 static Ctl* pinned_ctl()
@@ -558,9 +609,12 @@ static void poll(BatchHost& bh, Ctl* h)
     MRG_CUDA(cudaMemcpyAsync(h, bh.d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->st));
     MRG_CUDA(cudaStreamSynchronize(c->st));
     if (h->err) {
-        unsigned zero = 0;
-        MRG_CUDA(cudaMemcpy(&bh.d_ctl->err, &zero, sizeof zero, cudaMemcpyHostToDevice));
-        throw Error(MRG_E_TIMEOUT, "device wait timed out in a preconditioner sweep");
+        // clear the error bit and the persistent kernel's barrier counter (a
+        // launch that gave up may have left CTAs counted at a barrier)
+        unsigned zero[3] = {0, 0, 0};
+        MRG_CUDA(cudaMemcpy(&bh.d_ctl->err, zero, sizeof(unsigned), cudaMemcpyHostToDevice));
+        MRG_CUDA(cudaMemcpy(&bh.d_ctl->bar_count, zero, sizeof(unsigned), cudaMemcpyHostToDevice));
+        throw Error(MRG_E_TIMEOUT, "a device-side wait timed out (sweep dependency or grid barrier)");
     }
 }
 
@@ -573,8 +627,7 @@ static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long ca
     long launches = 0;
     const long cap = cap_iters / k + 2;
     while (h->n_active > 0 && launches <= cap) {
-        MRG_CUDA(cudaGraphLaunch(gr.exec, bh.ctx->st));
-        add_launches(gr.nodes);
+        launch_iterations(bh, cfg, prec, gr);
         ++launches;
         poll(bh, h);
     }
@@ -717,8 +770,7 @@ void batch_iterate(BatchHost& bh, const Controls& cfg)
 {
     const int prec = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
     BatchHost::Graph gr = iteration_graph(bh, cfg, prec, std::max(1, cfg.k_launch));
-    MRG_CUDA(cudaGraphLaunch(gr.exec, bh.ctx->st));
-    add_launches(gr.nodes);
+    launch_iterations(bh, cfg, prec, gr);
 }
 
 void batch_outer(BatchHost& bh, const Controls& cfg)

@@ -203,7 +203,7 @@ __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __
     const int e0 = __ldg(sptr + sl), W = (__ldg(sptr + sl + 1) - e0) >> 5;
     const int* __restrict__ col = acol + e0 + lane;
     const V* __restrict__ v = val + e0 + lane;
-    V y = vmul(__ldg(dg + i), __ldg(x + i));
+    V y = vmul(__ldg(dg + i), __ldca(x + i));
     if (W <= kMaxW) {
         int c[kMaxW];
         V a[kMaxW], xv[kMaxW];
@@ -212,7 +212,7 @@ __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __
 #pragma unroll
         for (int k = 0; k < kMaxW; ++k) {
             a[k] = c[k] >= 0 ? __ldg(v + k * 32) : V(0);
-            xv[k] = c[k] >= 0 ? __ldg(x + c[k]) : V(0);
+            xv[k] = c[k] >= 0 ? __ldca(x + c[k]) : V(0);
         }
 #pragma unroll
         for (int k = 0; k < kMaxW; ++k)
@@ -220,7 +220,7 @@ __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __
     } else {
         for (int k = 0; k < W; ++k) {
             const int ck = __ldg(col + k * 32);
-            if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldg(x + ck), y);
+            if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldca(x + ck), y);
         }
     }
     return y;
@@ -260,7 +260,7 @@ __device__ __forceinline__ void ell_tile(const int* __restrict__ sptr, const int
             const int ne1 = (s + kWarps + 1 < 32) ? __shfl_sync(kFull, sp, s + kWarps + 1) : spend;
             nW = (ne1 - ne0) >> 5;
         }
-        const V xi = __ldg(x + i);
+        const V xi = __ldca(x + i);
         V y = vmul(__ldg(dg + i), xi);
         const V* __restrict__ v = val + e0 + lane;
         if (W <= kMaxW) {
@@ -270,7 +270,7 @@ __device__ __forceinline__ void ell_tile(const int* __restrict__ sptr, const int
             for (int k = 0; k < kMaxW; ++k) {
                 live |= (c[k] >= 0 ? 1u : 0u) << k;
                 a[k] = c[k] >= 0 ? __ldg(v + k * 32) : V(0);
-                xv[k] = c[k] >= 0 ? __ldg(x + c[k]) : V(0);
+                xv[k] = c[k] >= 0 ? __ldca(x + c[k]) : V(0);
             }
             if (nW <= kMaxW) {
 #pragma unroll
@@ -283,7 +283,7 @@ __device__ __forceinline__ void ell_tile(const int* __restrict__ sptr, const int
             const int* __restrict__ col = acol + e0 + lane;
             for (int k = 0; k < W; ++k) {
                 const int ck = __ldg(col + k * 32);
-                if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldg(x + ck), y);
+                if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldca(x + ck), y);
             }
             if (nW <= kMaxW) {
 #pragma unroll
@@ -425,13 +425,13 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
 // (one 16-byte load per FP32 array, two per FP64 array).
 __device__ __forceinline__ void ld4(const float* __restrict__ p, float (&o)[4])
 {
-    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    const float4 t = __ldca(reinterpret_cast<const float4*>(p));
     o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
 }
 __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&o)[4])
 {
-    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
-    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    const double2 a = __ldca(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldca(reinterpret_cast<const double2*>(p) + 1);
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
 }
 // Plain (coherent) loads for arrays the same kernel also writes.
@@ -861,21 +861,25 @@ __device__ __forceinline__ void load_sys(SysDev* dst, const SysDev* src)
     __syncthreads();
 }
 
+// One row operation over the whole batch by this CTA: grid-stride over the
+// tile table (non-reducing ops) or the segment table (reducing ops).  `cur`
+// names the system whose descriptor sS holds, so a persistent kernel that
+// runs several operations in turn copies it only when the system changes;
+// whether the system takes part is re-read on every call.
 template <typename V, RowOp OP, bool PB>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restrict__ pB)
+__device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* sh, int* s_last, int& cur)
 {
-    __shared__ double sh[kBlock * kMaxRed];
-    __shared__ int s_last;
-    __shared__ __align__(16) SysDev sS;
-    const Batch B = *pB;
-    int cur = -1;
+    int lcur = -1;
     bool live = false;
     if constexpr (!OpTraits<OP>::kRed) {
         for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
             const int2 tl = B.tiles[t];
-            if (tl.x != cur) {
-                cur = tl.x;
-                load_sys(&sS, B.sys + cur);
+            if (tl.x != lcur) {
+                lcur = tl.x;
+                if (tl.x != cur) {
+                    cur = tl.x;
+                    load_sys(&sS, B.sys + cur);
+                }
                 live = system_live<OP>(sS);
             }
             if (!live) continue;
@@ -885,9 +889,12 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
     } else {
         for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
             const int2 sg = B.segs[g];
-            if (sg.x != cur) {
-                cur = sg.x;
-                load_sys(&sS, B.sys + cur);
+            if (sg.x != lcur) {
+                lcur = sg.x;
+                if (sg.x != cur) {
+                    cur = sg.x;
+                    load_sys(&sS, B.sys + cur);
+                }
                 live = system_live<OP>(sS);  // uniform over all of the system's segments
             }
             if (!live) continue;
@@ -895,9 +902,20 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
             const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
             for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
-            flush_segment<OP>(B, sS, t0, t1 - t0, acc, sh, &s_last);
+            flush_segment<OP>(B, sS, t0, t1 - t0, acc, sh, s_last);
         }
     }
+}
+
+template <typename V, RowOp OP, bool PB>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restrict__ pB)
+{
+    __shared__ double sh[kBlock * kMaxRed];
+    __shared__ int s_last;
+    __shared__ __align__(16) SysDev sS;
+    const Batch B = *pB;
+    int cur = -1;
+    rows_phase<V, OP, PB>(B, sS, sh, &s_last, cur);
 }
 
 // CTAs of a persistent launch: one wave of kMinCtas CTAs per SM.
@@ -1064,9 +1082,9 @@ __device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1
     V* dep = FWD ? y : w;
     V acc;
     if (FWD || (!syncfree && first_level))
-        acc = vmul(rD[i], r[i]);
+        acc = vmul(__ldg(rD + i), __ldca(r + i));
     else
-        acc = y[i];
+        acc = __ldca(y + i);
     if (W <= kMaxW) {
         int col[kMaxW];
         V cf[kMaxW];
@@ -1084,9 +1102,9 @@ __device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1
             for (int k = 0; k < kMaxW; ++k) {
                 const int ck = col[k];
                 if (FWD)
-                    d[k] = ck < 0 ? V(0) : (ck < lvl0_end ? vmul(rD[ck], r[ck]) : dep[ck]);
+                    d[k] = ck < 0 ? V(0) : (ck < lvl0_end ? vmul(__ldg(rD + ck), __ldca(r + ck)) : __ldca(dep + ck));
                 else
-                    d[k] = ck < 0 ? V(0) : dep[ck];
+                    d[k] = ck < 0 ? V(0) : __ldca(dep + ck);
             }
 #pragma unroll
             for (int k = 0; k < kMaxW; ++k)
@@ -1102,9 +1120,9 @@ __device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1
             if (syncfree)
                 d = wait_ready(dep + ck, ctl);
             else if (FWD && ck < lvl0_end)
-                d = vmul(rD[ck], r[ck]);
+                d = vmul(__ldg(rD + ck), __ldca(r + ck));
             else
-                d = dep[ck];
+                d = __ldca(dep + ck);
             acc = vfma(-cfk, d, acc);
         }
     }
@@ -1134,9 +1152,8 @@ __device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool s
 }
 
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __restrict__ pB, int trans)
+__device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
 {
-    const Batch B = *pB;
     const SysDev* __restrict__ Ss = B.sys;
     const int nsys = B.nsys;
     Ctl* ctl = B.ctl;
@@ -1166,6 +1183,13 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __re
     }
 }
 
+template <typename V, bool FWD>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __restrict__ pB, int trans)
+{
+    const Batch B = *pB;
+    sweep_sf_phase<V, FWD>(B, trans);
+}
+
 // One level L of a levelled sweep for every system that has it: forward
 // levels 1..nlevels-1, backward levels nlevels-2..0 (level 0 alone when
 // nlevels == 1).  Work comes from the batch's per-level list of (system,
@@ -1174,9 +1198,8 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __re
 // warp's k-th next chunk, so 32 chunks' metadata costs one chain of
 // dependent loads instead of one chain per chunk.
 template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
+__device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans)
 {
-    const Batch B = *pB;
     if (L >= B.maxlevels) return;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1224,6 +1247,13 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __r
     }
 }
 
+template <typename V, bool FWD>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
+{
+    const Batch B = *pB;
+    sweep_lvl_phase<V, FWD>(B, L, trans);
+}
+
 // ---------------------------------------------------------------- misc
 template <typename V>
 __global__ void k_fill_sent(V* p, long long n)
@@ -1233,10 +1263,10 @@ __global__ void k_fill_sent(V* p, long long n)
 }
 
 template <typename V>
-__global__ void k_iface_gather(const Batch* __restrict__ pB, int which)
+__device__ __forceinline__ void iface_phase(const Batch& B, int which)
 {
-    const SysDev* __restrict__ Ss = pB->sys;
-    const int nsys = pB->nsys;
+    const SysDev* __restrict__ Ss = B.sys;
+    const int nsys = B.nsys;
     for (int s = 0; s < nsys; ++s) {
         const SysDev& S = Ss[s];
         if (S.ngen == 0) continue;
@@ -1246,10 +1276,17 @@ __global__ void k_iface_gather(const Batch* __restrict__ pB, int which)
         const V* w = VP<V>::gw(S);
         for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < S.ngen; j += gridDim.x * blockDim.x) {
             V acc = V(0);
-            for (int k = S.g_ptr[j]; k < S.g_ptr[j + 1]; ++k) acc = vfma(w[k], x[S.g_src[k]], acc);
+            for (int k = S.g_ptr[j]; k < S.g_ptr[j + 1]; ++k) acc = vfma(w[k], __ldca(x + S.g_src[k]), acc);
             x[S.npad + j] = acc;
         }
     }
+}
+
+template <typename V>
+__global__ void k_iface_gather(const Batch* __restrict__ pB, int which)
+{
+    const Batch B = *pB;
+    iface_phase<V>(B, which);
 }
 
 __global__ void k_permute(const SysDev* __restrict__ Ss, int s, int to_internal, const double* __restrict__ src,
@@ -1311,6 +1348,120 @@ __global__ void k_recount(const Batch* __restrict__ pB)
     if (threadIdx.x == 0) {
         pB->ctl->n_active = na;
         pB->ctl->n_oactive = no;
+    }
+}
+
+// ---------------------------------------------------------------- persistent iteration
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier of a cooperative launch (every CTA is resident).
+// Thread 0 of each CTA reads the generation, then arrives on the batch's
+// counter; the last to arrive resets the counter and publishes the next
+// generation (release), the others wait for it (acquire), so every write
+// made before the barrier is visible to every load after it.  The wait is
+// bounded: on timeout, or when another wait has already failed, it sets the
+// error bit and returns false, and the kernel leaves.
+__device__ bool grid_barrier(Ctl* ctl)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned gen = ld_acquire_u32(&ctl->bar_gen);
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1u) {
+            atomicExch(&ctl->bar_count, 0u);
+            __threadfence();
+            st_release_u32(&ctl->bar_gen, gen + 1u);
+        } else {
+            const long long t0 = clock64();
+            for (int it = 1; ld_acquire_u32(&ctl->bar_gen) == gen; ++it) {
+                if (it > 16) __nanosleep(32);
+                if ((it & 127) == 0) {
+                    if (*(volatile unsigned*)&ctl->err) {
+                        ok = 0;
+                        break;
+                    }
+                    if (clock64() - t0 > kWaitCycles) {
+                        atomicOr(&ctl->err, ERR_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        __threadfence();   // acquire side for the last arriver as well
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// K Krylov iterations of every active member of the batch in one
+// cooperative launch: the kernels of record_iteration (precondition, rho,
+// p update, interface gather, q = A p, x/r update) run as phases separated
+// by grid barriers, with the same per-row arithmetic and the same
+// per-system reduction order, so the results are bit-identical to the
+// separate launches.  Stops early once no member is active.
+template <typename V, bool PB, bool SF>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __restrict__ pB, int K, int pc, int gen)
+{
+    __shared__ double sh[kBlock * kMaxRed];
+    __shared__ int s_last;
+    __shared__ __align__(16) SysDev sS;
+    const Batch B = *pB;
+    Ctl* ctl = B.ctl;
+    const int nl = B.maxlevels;
+    int cur = -1;
+    for (int it = 0; it < K; ++it) {
+        if (pc >= PC_DIC) {
+            for (int tr = 0; tr < (PB ? 2 : 1); ++tr) {
+                if constexpr (SF) {
+                    sweep_sf_phase<V, true>(B, tr);
+                    if (!grid_barrier(ctl)) return;
+                    sweep_sf_phase<V, false>(B, tr);
+                    if (!grid_barrier(ctl)) return;
+                } else {
+                    for (int L = 1; L < nl; ++L) {
+                        sweep_lvl_phase<V, true>(B, L, tr);
+                        if (!grid_barrier(ctl)) return;
+                    }
+                    for (int L = nl - 2 > 0 ? nl - 2 : 0; L >= 0; --L) {
+                        sweep_lvl_phase<V, false>(B, L, tr);
+                        if (!grid_barrier(ctl)) return;
+                    }
+                }
+            }
+        } else if (pc == PC_DIAG) {
+            rows_phase<V, OP_PRECOND_DIAG, PB>(B, sS, sh, &s_last, cur);
+            if (!grid_barrier(ctl)) return;
+        } else {
+            rows_phase<V, OP_PRECOND_NONE, PB>(B, sS, sh, &s_last, cur);
+            if (!grid_barrier(ctl)) return;
+        }
+        rows_phase<V, OP_RHO, PB>(B, sS, sh, &s_last, cur);
+        if (!grid_barrier(ctl)) return;
+        rows_phase<V, OP_PUPDATE, PB>(B, sS, sh, &s_last, cur);
+        if (!grid_barrier(ctl)) return;
+        if (gen) {
+            iface_phase<V>(B, 0);
+            if (PB) iface_phase<V>(B, 2);
+            if (!grid_barrier(ctl)) return;
+        }
+        rows_phase<V, OP_SPMV_QP, PB>(B, sS, sh, &s_last, cur);
+        if (!grid_barrier(ctl)) return;
+        rows_phase<V, OP_UPDATE, PB>(B, sS, sh, &s_last, cur);
+        if (!grid_barrier(ctl)) return;
+        if (*(volatile unsigned*)&ctl->n_active == 0u) break;
     }
 }
 }  // namespace
@@ -1433,6 +1584,39 @@ void launch_permute(int to_internal, const SysDev* d, int s, const double* src, 
     if (grid > 2048) grid = 2048;
     if (grid < 1) grid = 1;
     k_permute<<<grid, 256, 0, st>>>(d, s, to_internal, src, dst, n);
+}
+
+template <typename V, bool PB, bool SF>
+static cudaError_t launch_iterate_t(const Batch* dB, int K, int pc, int gen, cudaStream_t st)
+{
+    static int per_sm = 0;
+    auto kern = k_iterate<V, PB, SF>;
+    if (!per_sm) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
+        if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+        if (per_sm > kMinCtas) per_sm = kMinCtas;
+    }
+    const int grid = per_sm * (g_grid_cap / kMinCtas);
+    void* args[] = {(void*)&dB, (void*)&K, (void*)&pc, (void*)&gen};
+    return cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kBlock), args, 0, st);
+}
+
+cudaError_t launch_iterate(int precision, int pb, int syncfree, const Batch* dB, int K, int pc, int gen,
+                           cudaStream_t st)
+{
+    ++g_launches;
+    if (precision == 0) {
+        if (pb)
+            return syncfree ? launch_iterate_t<double, true, true>(dB, K, pc, gen, st)
+                            : launch_iterate_t<double, true, false>(dB, K, pc, gen, st);
+        return syncfree ? launch_iterate_t<double, false, true>(dB, K, pc, gen, st)
+                        : launch_iterate_t<double, false, false>(dB, K, pc, gen, st);
+    }
+    if (pb)
+        return syncfree ? launch_iterate_t<float, true, true>(dB, K, pc, gen, st)
+                        : launch_iterate_t<float, true, false>(dB, K, pc, gen, st);
+    return syncfree ? launch_iterate_t<float, false, true>(dB, K, pc, gen, st)
+                    : launch_iterate_t<float, false, false>(dB, K, pc, gen, st);
 }
 
 void launch_gather_scal(const Batch* dB, Scal* out, cudaStream_t st)

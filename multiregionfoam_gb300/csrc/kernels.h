@@ -66,6 +66,14 @@ void launch_ggi(int n_dst, const int32_t* ptr, const int32_t* addr, const double
 
 // Kernels launched so far in this process (captured launches included;
 // the engine corrects for graph capture and replay).
+// K Krylov iterations of the batch in one cooperative (persistent) launch
+// whose phases are the launches of one iteration, separated by grid
+// barriers; grid = every resident CTA.  syncfree: exact-order sweeps;
+// otherwise levelled (colour) sweeps.  gen: members have general
+// interfaces.  Returns the launch status.
+cudaError_t launch_iterate(int precision, int pb, int syncfree, const Batch* dB, int K, int pc, int gen,
+                           cudaStream_t st);
+
 // Serving support: copy every member's Scal into out[nsys]; recompute the
 // control block's n_active / n_oactive from the members' flags.
 void launch_gather_scal(const Batch* dB, Scal* out, cudaStream_t st);

@@ -237,6 +237,27 @@ int mrg_batch_solve_device(mrg_batch* batch, const double* const* d_b,
                            double* const* d_x_inout,
                            const mrg_controls* controls, mrg_perf* perfs);
 
+/* ---- autotuner ---------------------------------------------------------
+ * No counterpart in the reference.  Times the Krylov loop of a mesh or batch
+ * on its current coefficients under each candidate launch shape and keeps
+ * the fastest for later solves with the same ordering: the iteration mode
+ * (a captured graph of separate launches, or one persistent cooperative
+ * kernel with grid barriers), the iterations per launch, and the number of
+ * level-sweep chunks per CTA.  A launch shape never changes a result bit.
+ * b and x as for a solve (device pointers); x is not modified. */
+typedef struct {
+    int mode;                  /* 0: graph of launches, 1: persistent kernel */
+    int iters_per_launch;
+    int sweep_chunks_per_cta;  /* colour ordering only                       */
+    int candidates;            /* shapes timed                               */
+    double us_per_iter;        /* of the chosen shape                        */
+} mrg_tuning;
+int mrg_mesh_tune(mrg_mesh* mesh, const double* d_b, const double* d_x,
+                  const mrg_controls* controls, mrg_tuning* out);
+int mrg_batch_tune(mrg_batch* batch, const double* const* d_b,
+                   const double* const* d_x, const mrg_controls* controls,
+                   mrg_tuning* out);
+
 /* ---- serving: continuous batching of solve requests -------------------
  * No counterpart in the reference, which solves each region's equation in
  * turn inside its time loop (multiRegionSystem.C:193-324).  A server keeps

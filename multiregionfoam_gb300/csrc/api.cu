@@ -639,6 +639,57 @@ int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel, in
     });
 }
 
+static void fill_tuning(mrg_tuning* out, const Tuning& t)
+{
+    if (!out) return;
+    std::memset(out, 0, sizeof *out);
+    out->mode = t.mode;
+    out->iters_per_launch = t.k;
+    out->sweep_chunks_per_cta = t.sweep_div;
+    out->candidates = t.candidates;
+    out->us_per_iter = t.us_per_iter;
+}
+
+int mrg_mesh_tune(mrg_mesh* mesh, const double* d_b, const double* d_x, const mrg_controls* controls,
+                  mrg_tuning* out)
+{
+    return guard([&] {
+        if (!mesh || !d_b || !d_x) return fail(MRG_E_INVALID, "NULL argument");
+        Controls k = to_controls(controls);
+        PlanState& P = prepare(mesh->m, k);
+        P.sys.in_b = d_b;
+        P.sys.in_x = d_x;
+        P.sys.out_x = nullptr;
+        P.sync_sys();
+        P.single.sync_sys();
+        fill_tuning(out, tune_batch(P.single, k));
+        MRG_CUDA(cudaStreamSynchronize(mesh->m.ctx->st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_batch_tune(mrg_batch* batch, const double* const* d_b, const double* const* d_x,
+                   const mrg_controls* controls, mrg_tuning* out)
+{
+    return guard([&] {
+        if (!batch || !d_b || !d_x) return fail(MRG_E_INVALID, "NULL argument");
+        Controls k = to_controls(controls);
+        if (k.ordering != batch->ordering) throw Error(MRG_E_INVALID, "controls.ordering differs from the batch's");
+        prepare_batch(batch->bh, batch->meshes, k);
+        for (size_t s = 0; s < batch->meshes.size(); ++s) {
+            PlanState* P = batch->bh.members[s];
+            if (!d_b[s] || !d_x[s]) throw Error(MRG_E_INVALID, "NULL member vector");
+            P->sys.in_b = d_b[s];
+            P->sys.in_x = d_x[s];
+            P->sys.out_x = nullptr;
+        }
+        batch->bh.sync_sys();
+        fill_tuning(out, tune_batch(batch->bh, k));
+        MRG_CUDA(cudaStreamSynchronize(batch->ctx->st));
+        return (int)MRG_OK;
+    });
+}
+
 int mrg_server_create(mrg_ctx* ctx, const mrg_controls* sym_controls, const mrg_controls* asym_controls,
                       size_t hbm_budget, int max_active, mrg_server** out)
 {

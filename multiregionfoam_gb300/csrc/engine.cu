@@ -483,7 +483,8 @@ static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, in
         // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
         // nl == 1); one chunk per warp of the widest level
         const int nl = bh.h.maxlevels;
-        const int g = std::max(1, std::min(persistent_grid(), (bh.widest_level + 7) / 8));
+        const int div = std::max(1, bh.tune.sweep_div);
+        const int g = std::max(1, std::min(persistent_grid(), (bh.widest_level + div - 1) / div));
         for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, bh.d, g, st);
         for (int L = std::max(nl - 2, 0); L >= 0; --L) launch_sweep(prec, 0, trans, 0, L, bh.d, g, st);
     }
@@ -523,14 +524,19 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
 // GB300, a kernel boundary inside a graph costs about what a grid barrier
 // does), or one persistent cooperative kernel whose phases are those
 // launches (MRG_ITERATION=persistent).  Both give the same bits.
-static bool persistent_iteration()
+static bool persistent_iteration(const BatchHost& bh)
 {
-    static int mode = -1;
-    if (mode < 0) {
+    static int env = -1;
+    if (env < 0) {
         const char* e = std::getenv("MRG_ITERATION");
-        mode = (e && std::string(e) == "persistent") ? 1 : 0;
+        env = (e && std::string(e) == "persistent") ? 1 : 0;
     }
-    return mode == 1;
+    return env == 1 || bh.tune.mode == 1;
+}
+
+static int iters_per_launch(const BatchHost& bh, const Controls& cfg)
+{
+    return std::max(1, bh.tune.k > 0 ? bh.tune.k : cfg.k_launch);
 }
 
 static void record_persistent(BatchHost& bh, const Controls& cfg, int prec, int k, cudaStream_t st)
@@ -544,10 +550,11 @@ static void record_persistent(BatchHost& bh, const Controls& cfg, int prec, int 
 // refuses to capture is launched directly instead (exec stays null).
 static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int prec, int k)
 {
-    const bool pers = persistent_iteration();
+    const bool pers = persistent_iteration(bh);
     const int cap = persistent_grid();
     const int g_rows = std::min(std::max(bh.h.ntiles, 1), cap), g_red = std::min(std::max(bh.h.nsegs, 1), cap);
-    const int g_sweep = std::max(1, std::min(cap, (bh.widest_level + 7) / 8));
+    const int div = std::max(1, bh.tune.sweep_div);
+    const int g_sweep = std::max(1, std::min(cap, (bh.widest_level + div - 1) / div));
     std::string key = std::to_string(cfg.solver) + "/" + std::to_string(cfg.pc) + "/" +
                       std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k) + "/" +
                       std::to_string(g_rows) + "/" + std::to_string(g_red) + "/" + std::to_string(g_sweep) + "/" +
@@ -592,7 +599,7 @@ static void launch_iterations(BatchHost& bh, const Controls& cfg, int prec, cons
         MRG_CUDA(cudaGraphLaunch(gr.exec, bh.ctx->st));
         add_launches(gr.nodes);
     } else {
-        record_persistent(bh, cfg, prec, std::max(1, cfg.k_launch), bh.ctx->st);
+        record_persistent(bh, cfg, prec, iters_per_launch(bh, cfg), bh.ctx->st);
     }
 }
 
@@ -621,7 +628,7 @@ static void poll(BatchHost& bh, Ctl* h)
 // Replays the iteration graph until no member is in its Krylov loop.
 static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long cap_iters, Ctl* h)
 {
-    const int k = std::max(1, cfg.k_launch);
+    const int k = iters_per_launch(bh, cfg);
     BatchHost::Graph gr = iteration_graph(bh, cfg, prec, k);
     poll(bh, h);
     long launches = 0;
@@ -769,7 +776,7 @@ void batch_begin(BatchHost& bh, const Controls& cfg)
 void batch_iterate(BatchHost& bh, const Controls& cfg)
 {
     const int prec = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
-    BatchHost::Graph gr = iteration_graph(bh, cfg, prec, std::max(1, cfg.k_launch));
+    BatchHost::Graph gr = iteration_graph(bh, cfg, prec, iters_per_launch(bh, cfg));
     launch_iterations(bh, cfg, prec, gr);
 }
 
@@ -807,6 +814,79 @@ void batch_status(BatchHost& bh, std::vector<Scal>& out)
     launch_gather_scal(bh.d, bh.d_scal, bh.ctx->st);
     MRG_CUDA(cudaMemcpyAsync(out.data(), bh.d_scal, sizeof(Scal) * nsys, cudaMemcpyDeviceToHost, bh.ctx->st));
     poll(bh, h);
+}
+
+// ------------------------------------------------------------------ autotuner
+Tuning tune_batch(BatchHost& bh, const Controls& cfg)
+{
+    Ctx* c = bh.ctx;
+    cudaStream_t st = c->st;
+    // the loop keeps iterating while being timed: no convergence, no limit
+    Controls run = cfg;
+    run.tol = 0.0;
+    run.rel_tol = 0.0;
+    run.min_iter = 0;
+    run.max_iter = 1 << 30;
+    run.inner_max_iter = 1 << 30;
+    run.inner_rel_tol = 1e-30;
+    const int prec = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
+    const bool levels = cfg.ordering == MRG_ORDER_COLOUR && cfg.pc >= PC_DIC;
+    std::vector<Tuning> cands;
+    for (int mode : {0, 1})
+        for (int k : {4, 16})
+            for (int div : {4, 8, 16}) {
+                if (!levels && div != 8) continue;
+                Tuning t;
+                t.mode = mode;
+                t.k = k;
+                t.sweep_div = div;
+                cands.push_back(t);
+            }
+    const Tuning saved = bh.tune;
+    Ctl* h = pinned_ctl();
+    cudaEvent_t e0, e1;
+    MRG_CUDA(cudaEventCreate(&e0));
+    MRG_CUDA(cudaEventCreate(&e1));
+    Tuning best;
+    best.us_per_iter = 1e300;
+    try {
+        for (Tuning t : cands) {
+            bh.tune = t;
+            bh.tune.tuned = 1;
+            batch_begin(bh, run);
+            BatchHost::Graph gr = iteration_graph(bh, run, prec, t.k);
+            launch_iterations(bh, run, prec, gr);   // warm-up (and capture)
+            poll(bh, h);
+            if (h->n_active == 0) continue;
+            const int reps = std::max(2, 64 / t.k);
+            MRG_CUDA(cudaEventRecord(e0, st));
+            for (int r = 0; r < reps; ++r) {
+                launch_iterations(bh, run, prec, gr);
+                poll(bh, h);   // the host loop polls after every launch
+            }
+            MRG_CUDA(cudaEventRecord(e1, st));
+            MRG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            MRG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            t.us_per_iter = 1e3 * ms / (reps * t.k);
+            if (t.us_per_iter < best.us_per_iter) best = t;
+        }
+    } catch (...) {
+        bh.tune = saved;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best.us_per_iter >= 1e300) {
+        bh.tune = saved;
+        return saved;
+    }
+    best.tuned = 1;
+    best.candidates = (int)cands.size();
+    bh.tune = best;
+    return best;
 }
 
 // ------------------------------------------------------------------ building blocks

@@ -52,6 +52,18 @@ struct Perf {
 
 struct PlanState;
 
+// Launch shapes of a batch's Krylov loop, chosen by tune_batch (or the
+// defaults).  None of them changes a result bit: they decide how the same
+// kernels are launched, never what they compute.
+struct Tuning {
+    int tuned = 0;
+    int mode = 0;        // 0: graph of separate launches, 1: persistent cooperative kernel
+    int k = 0;           // iterations per launch (0: the controls' iters_per_launch)
+    int sweep_div = 8;   // level-sweep grid: one CTA per sweep_div chunks of the widest level
+    double us_per_iter = 0.0;
+    int candidates = 0;
+};
+
 // A device-resident batch: the Batch descriptor, the system array, the tile
 // table, the per-level sweep work list and the control block.  Captured
 // iteration graphs refer only to the descriptor's address.
@@ -74,6 +86,7 @@ struct BatchHost {
         long long nodes = 0;   // kernels per replay (for the launch counter)
     };
     std::map<std::string, Graph> graphs;
+    Tuning tune;
     void init(Ctx* c);
     // (Re)build the arrays for these systems; the order fixes the tile table.
     void set(const std::vector<PlanState*>& systems);
@@ -154,6 +167,12 @@ void batch_outer(BatchHost& bh, const Controls& c);
 void batch_finish(BatchHost& bh);
 void batch_recount(BatchHost& bh);
 void batch_status(BatchHost& bh, std::vector<Scal>& out);
+
+// Autotuner: time the Krylov loop of the prepared batch (members' in_b/in_x
+// set) under each candidate launch shape -- iteration mode, iterations per
+// launch, level-sweep grid -- and keep the fastest in bh.tune.  The members'
+// outputs are not written.
+Tuning tune_batch(BatchHost& bh, const Controls& c);
 
 // Copy coefficients into a mesh's raw device arrays (caller numbering) and
 // bump its version; `sync` waits for the copies.

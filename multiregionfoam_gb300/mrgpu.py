@@ -29,7 +29,7 @@ EXPORTED = [
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
     "mrg_residual_noalloc", "mrg_server_create", "mrg_server_destroy", "mrg_server_submit", "mrg_server_poll",
-    "mrg_server_wait", "mrg_server_get_stats",
+    "mrg_server_wait", "mrg_server_get_stats", "mrg_mesh_tune", "mrg_batch_tune",
 ]
 
 
@@ -61,6 +61,14 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("running", C.c_int), ("queued", C.c_int),
                 ("peak_running", C.c_int), ("reserved", C.c_int), ("inflight_bytes", C.c_size_t),
                 ("peak_inflight_bytes", C.c_size_t)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("mode", C.c_int), ("iters_per_launch", C.c_int), ("sweep_chunks_per_cta", C.c_int),
+                ("candidates", C.c_int), ("us_per_iter", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class IfaceDesc(C.Structure):
@@ -123,6 +131,8 @@ def load(path: str = LIB_PATH):
     L.mrg_server_wait.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(C.c_int), C.POINTER(Perf),
                                   C.POINTER(C.c_double)]
     L.mrg_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+    L.mrg_mesh_tune.argtypes = [vp, vp, vp, C.POINTER(Controls), C.POINTER(Tuning)]
+    L.mrg_batch_tune.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Tuning)]
     _LIB = L
     return L
 
@@ -322,6 +332,12 @@ class Mesh:
         _check(load().mrg_coeffs_upload_device(self.h, vp(d_diag), vp(d_upper), vp(d_lower), vp(d_ibou),
                                                vp(d_iint)))
 
+    def tune(self, d_b: int, d_x: int, ctl: Controls) -> dict:
+        """Autotune the launch shapes of this mesh's Krylov loop (device b, x)."""
+        t = Tuning()
+        _check(load().mrg_mesh_tune(self.h, C.c_void_p(d_b), C.c_void_p(d_x), C.byref(ctl), C.byref(t)))
+        return t.as_dict()
+
     def time_kernel(self, ctl: Controls, kernel: int, reps: int) -> float:
         v = C.c_float()
         _check(load().mrg_time_kernel(self.h, C.byref(ctl), kernel, reps, C.byref(v)))
@@ -355,6 +371,14 @@ class Batch:
         perfs = (Perf * ns)()
         _check(load().mrg_batch_solve(self.h, pb, px, C.byref(ctl), perfs))
         return xs, [p.as_dict() for p in perfs]
+
+    def tune(self, d_bs, d_xs, ctl: Controls) -> dict:
+        """Autotune the launch shapes of this batch's Krylov loop."""
+        ns = len(self.meshes)
+        t = Tuning()
+        _check(load().mrg_batch_tune(self.h, (C.c_void_p * ns)(*d_bs), (C.c_void_p * ns)(*d_xs), C.byref(ctl),
+                                     C.byref(t)))
+        return t.as_dict()
 
     def solve_device(self, d_bs, d_xs, ctl: Controls):
         ns = len(self.meshes)

@@ -105,7 +105,8 @@ typedef struct {
     int singular;
     int status;            /* MRG_OK or MRG_E_*                              */
     int n_outer;           /* mixed: refinement steps                       */
-    int reserved;
+    int fallback;          /* mixed: 1 = the refinement stalled and the solve
+                              finished with FP64 Krylov from its best iterate */
     double solve_ms;       /* device time of the solve (CUDA events)        */
 } mrg_perf;
 

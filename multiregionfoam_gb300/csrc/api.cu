@@ -103,6 +103,7 @@ void fill_perf(mrg_perf* p, const Perf& r)
     p->singular = r.singular;
     p->status = r.status;
     p->n_outer = r.outer;
+    p->fallback = r.fallback;
     p->solve_ms = r.ms;
 }
 

@@ -40,13 +40,18 @@ struct Scal {
     double inv_scale;      // mixed: FP32 inner system is scaled by 1/inv_scale
     // mixed-precision outer (FP64) state and controls
     double onfac, ores0, ores, obest;
+    double obest_sum;      // mixed: sum|b - A x| of the best refined iterate
     double otol, orel_tol, inner_rel_tol;
     int min_iter, max_iter;  // user controls (foam minIter / maxIter)
     int kmin, kmax;          // bounds of the current Krylov loop
     int iter, active, converged, singular;
     int status, mixed;
     int ostate, oconv, oiter, ostall;
-    int inner_total, inner_max, max_outer, pad;
+    int inner_total, inner_max, max_outer;
+    int okeep;             // mixed: 1 = the last refinement improved (keep x), 0 = roll back
+    int fallback;          // mixed: 1 = refinement stalled, FP64 Krylov requested; 2 = running it;
+                           // 3 = done (true residual checked)
+    int pad;
 };
 
 template <typename V>
@@ -78,6 +83,8 @@ struct SysDev {
     float *f_c32, *f_cT32, *b_c32, *b_cT32, *rD32;
     Vecs<double> v64;
     Vecs<float> v32;
+    // mixed precision: best refined iterate and its FP64 residual
+    double *xb, *rb;
     // caller-numbered input/output of the current solve
     const double *in_b, *in_x;
     double* out_x;

@@ -186,7 +186,7 @@ static void release_plan(Ctx* c, PlanState* P)
     SysDev& S = P->sys;
     void* vals[] = {S.a_val, S.aT_val != S.a_val ? S.aT_val : nullptr, S.diag, S.sumA, S.f_c, S.f_cT, S.b_c,
                     S.b_cT, S.rD, S.D, S.a_val32, S.aT_val32 != S.a_val32 ? S.aT_val32 : nullptr, S.diag32,
-                    S.f_c32, S.f_cT32, S.b_c32, S.b_cT32, S.rD32, S.partials, S.counter, S.sc};
+                    S.f_c32, S.f_cT32, S.b_c32, S.b_cT32, S.rD32, S.partials, S.counter, S.sc, S.xb, S.rb};
     for (void* p : vals) c->release(p);
     for (void* p : {(void*)S.v64.x, (void*)S.v64.b, (void*)S.v64.r, (void*)S.v64.w, (void*)S.v64.y,
                     (void*)S.v64.p, (void*)S.v64.q, (void*)S.v64.rT, (void*)S.v64.wT, (void*)S.v64.yT,
@@ -386,6 +386,8 @@ static bool ensure_views(Mesh& m, PlanState& P, const Controls& cfg)
         S.v32.w = (float*)c->alloc(4 * np);
         S.v32.y = (float*)c->alloc(4 * np);
         S.v32.q = (float*)c->alloc(4 * np);
+        S.xb = (double*)c->alloc(8 * np);
+        S.rb = (double*)c->alloc(8 * np);
         P.have32 = true;
         P.scattered = 0;
         changed = true;
@@ -667,6 +669,15 @@ Perf perf_of(const Scal& q, int precision)
         p.iters = q.iter;
         p.converged = q.converged;
         p.singular = q.singular;
+    } else if (q.fallback >= 2) {
+        // refinement stalled and the solve finished with FP64 Krylov
+        p.res0 = q.ores0;
+        p.res = q.res;
+        p.iters = q.inner_total + q.iter;
+        p.outer = q.oiter;
+        p.converged = q.converged;
+        p.singular = q.singular;
+        p.fallback = 1;
     } else {
         p.res0 = q.ores0;
         p.res = q.ores;
@@ -705,11 +716,21 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
             for (int outer = 0; outer <= cfg.max_outer + 1; ++outer) {
                 if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
                 launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
+                launch_rows(OP_KEEPBEST, 0, bh.d, nt, ns, 0, st);
                 poll(bh, h);
                 if (h->n_oactive == 0) break;
                 launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
                 run_iterations(bh, cfg, 1, cfg.max_iter, h);
                 launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
+            }
+            // members whose refinement stalled finish with FP64 Krylov
+            if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+            launch_rows(OP_FALLBACK64, 0, bh.d, nt, ns, pb, st);
+            poll(bh, h);
+            if (h->n_active > 0) {
+                run_iterations(bh, cfg, 0, cfg.max_iter, h);
+                if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+                launch_rows(OP_FALLBACK64, 0, bh.d, nt, ns, 0, st);   // true residual of the result
             }
         }
         launch_rows(OP_PERMUTE_OUT, 0, bh.d, nt, ns, 0, st);
@@ -768,14 +789,22 @@ void batch_begin(BatchHost& bh, const Controls& cfg)
     if (cfg.precision == MRG_PRECISION_MIXED) {
         if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
         launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
+        launch_rows(OP_KEEPBEST, 0, bh.d, nt, ns, 0, st);
         launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
     }
     MRG_CUDA(cudaGetLastError());
 }
 
-void batch_iterate(BatchHost& bh, const Controls& cfg)
+void batch_fallback(BatchHost& bh, const Controls& cfg)
 {
-    const int prec = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
+    if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, bh.ctx->st);
+    launch_rows(OP_FALLBACK64, 0, bh.d, bh.h.ntiles, bh.h.nsegs, cfg.solver == MRG_SOLVER_PBICG, bh.ctx->st);
+    MRG_CUDA(cudaGetLastError());
+}
+
+void batch_iterate(BatchHost& bh, const Controls& cfg, int prec)
+{
+    if (prec < 0) prec = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
     BatchHost::Graph gr = iteration_graph(bh, cfg, prec, iters_per_launch(bh, cfg));
     launch_iterations(bh, cfg, prec, gr);
 }
@@ -788,6 +817,7 @@ void batch_outer(BatchHost& bh, const Controls& cfg)
     launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
     if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, st);
     launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
+    launch_rows(OP_KEEPBEST, 0, bh.d, nt, ns, 0, st);
     launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
     MRG_CUDA(cudaGetLastError());
 }

@@ -47,6 +47,7 @@ struct Controls {
 struct Perf {
     double res0 = 0, res = 0;
     int iters = 0, converged = 0, singular = 0, status = 0, outer = 0;
+    int fallback = 0;   // mixed: finished with FP64 Krylov after the refinement stalled
     double ms = 0;
 };
 
@@ -162,7 +163,10 @@ Perf perf_of(const Scal& q, int precision);
 // active counts after a membership change; status = gather every member's
 // scalar state to the host (checks the device error bits).
 void batch_begin(BatchHost& bh, const Controls& c);
-void batch_iterate(BatchHost& bh, const Controls& c);
+void batch_iterate(BatchHost& bh, const Controls& c, int prec = -1);
+// Mixed members whose refinement stalled (fallback requested): FP64 residual
+// of the best iterate and the start of an FP64 Krylov loop.
+void batch_fallback(BatchHost& bh, const Controls& c);
 void batch_outer(BatchHost& bh, const Controls& c);
 void batch_finish(BatchHost& bh);
 void batch_recount(BatchHost& bh);

@@ -343,6 +343,8 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
             sc->ores0 = sc->res0;
             sc->ores = sc->res0;
             sc->obest = sc->res0;
+            sc->obest_sum = sums[1];
+            sc->okeep = 1;
             sc->oconv = conv;
             sc->oiter = 0;
             sc->ostall = 0;
@@ -377,20 +379,64 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
         break;
     }
     case OP_RESID64: {
-        // true FP64 residual of the refined solution: foam's convergence test
-        sc->osum = sums[0];
-        sc->ores = sums[0] / sc->onfac;
+        // true FP64 residual of the refined solution: foam's convergence test.
+        // A refinement step that made the residual worse (an FP32 BiCG
+        // recurrence that drifted) is rolled back by OP_KEEPBEST and the
+        // next inner solve restarts sooner; the solve never returns an
+        // iterate worse than the best it has seen.
+        const double o = sums[0] / sc->onfac;
+        const bool improved = sc->oiter == 0 || o < sc->obest;
+        if (improved) {
+            if (o < 0.999 * sc->obest || sc->oiter == 0)
+                sc->ostall = 0;
+            else
+                sc->ostall += 1;
+            sc->obest = o;
+            sc->obest_sum = sums[0];
+            sc->okeep = 1;
+        } else {
+            sc->ostall += 1;
+            sc->okeep = 0;
+            sc->inner_max = sc->inner_max / 2 > 25 ? sc->inner_max / 2 : 25;
+        }
+        sc->osum = sc->obest_sum;
+        sc->ores = sc->obest;
         const bool conv = sc->ores < sc->otol || (sc->orel_tol > 1.0e-20 && sc->ores < sc->orel_tol * sc->ores0);
         sc->oconv = conv;
-        if (sc->ores < 0.999 * sc->obest) {
-            sc->obest = sc->ores;
-            sc->ostall = 0;
-        } else if (sc->oiter > 0) {
-            sc->ostall += 1;
-        }
         const bool more = ((!conv || sc->inner_total < sc->min_iter) && sc->oiter < sc->max_outer &&
                            sc->inner_total < sc->max_iter && sc->ostall < 3);
-        if (!more) set_outer(ctl, sc, 0);
+        if (!more) {
+            set_outer(ctl, sc, 0);
+            if (!conv) sc->fallback = 1;   // refinement stalled: finish in FP64
+        }
+        break;
+    }
+    case OP_FALLBACK64: {
+        if (sc->fallback == 2) {
+            // after the FP64 loop: the true FP64 residual of x is what the
+            // mixed form reports and tests
+            sc->fallback = 3;
+            sc->res = sums[0] / sc->onfac;
+            sc->converged = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
+            break;
+        }
+        // FP64 Krylov from the best refined iterate, with the solve's own
+        // normFactor and initial residual, so the convergence test and the
+        // reported residuals mean what they mean for the plain method
+        sc->fallback = 2;
+        sc->tol = sc->otol;
+        sc->rel_tol = sc->orel_tol;
+        sc->nfac = sc->onfac;
+        sc->res0 = sc->ores0;
+        sc->res = sums[0] / sc->onfac;
+        sc->iter = 0;
+        sc->singular = 0;
+        sc->rho = 1.0e20;
+        sc->kmin = 0;
+        sc->kmax = sc->max_iter;
+        const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
+        sc->converged = conv;
+        set_active(ctl, sc, conv ? 0 : 1);
         break;
     }
     case OP_TO32: {
@@ -505,6 +551,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             sc->inner_total = 0;
             sc->converged = 0;
             sc->oconv = 0;
+            sc->fallback = 0;
             sc->singular = 0;
         }
     } else if constexpr (OP == OP_PERMUTE_IN) {
@@ -711,17 +758,40 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             float f[4] = {(float)rd[0], (float)rd[1], (float)rd[2], (float)rd[3]};
             st4(S.rD32 + r4, f);
         }
-    } else if constexpr (OP == OP_RESID64) {
+    } else if constexpr (OP == OP_KEEPBEST) {
+        if (!S.xb) return;
+        const int keep = S.sc->okeep;
+        double* __restrict__ x = S.v64.x;
+        double* __restrict__ r = S.v64.r;
+        double* __restrict__ xb = S.xb;
+        double* __restrict__ rb = S.rb;
+        double a[4], b[4];
+        if (keep) {
+            ld4w(x + r4, a);
+            ld4w(r + r4, b);
+            st4(xb + r4, a);
+            st4(rb + r4, b);
+        } else {
+            ld4w(xb + r4, a);
+            ld4w(rb + r4, b);
+            st4(x + r4, a);
+            st4(r + r4, b);
+        }
+    } else if constexpr (OP == OP_RESID64 || OP == OP_FALLBACK64) {
         const double* __restrict__ av = S.a_val;
+        const double* __restrict__ atv = S.aT_val;
         const double* __restrict__ dg = S.diag;
         const double* __restrict__ x = S.v64.x;
         const double* __restrict__ b = S.v64.b;
         double* __restrict__ r = S.v64.r;
+        double* __restrict__ rT = S.v64.rT;
         for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
             const int i = sl * 32 + lane;
-            const double ri = b[i] - ell_row<double>(sptr, acol, av, dg, x, i);
+            const double bi = __ldca(b + i);
+            const double ri = bi - ell_row<double>(sptr, acol, av, dg, x, i);
             r[i] = ri;
             acc[0] += fabs(ri);
+            if (OP == OP_FALLBACK64 && PB) rT[i] = bi - ell_row<double>(sptr, acol, atv, dg, x, i);
         }
     } else if constexpr (OP == OP_TO32) {
         // s scales the FP64 residual to O(1) per cell before rounding to FP32.
@@ -777,7 +847,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
 template <RowOp OP>
 struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
-                                  OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32);
+                                  OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32 || OP == OP_FALLBACK64);
     // Krylov-loop ops run only for systems whose loop is active; the
     // refinement ops only for systems whose outer loop is active.
     static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
@@ -793,6 +863,7 @@ __device__ __forceinline__ bool system_live(const SysDev& S)
 {
     if (OpTraits<OP>::kNeedActive) return S.sc->active != 0;
     if (OpTraits<OP>::kNeedOuter) return S.sc->ostate != 0;
+    if (OP == OP_FALLBACK64) return S.sc->fallback == 1 || S.sc->fallback == 2;
     return true;
 }
 
@@ -1501,6 +1572,8 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE64(OP_BEGIN)
             MRG_CASE64(OP_PERMUTE_IN)
             MRG_CASE64(OP_PERMUTE_OUT)
+            MRG_CASE64(OP_KEEPBEST)
+            MRG_CASE64(OP_FALLBACK64)
         default: break;
         }
     } else {

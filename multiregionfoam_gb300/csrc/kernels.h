@@ -31,6 +31,8 @@ enum RowOp {
     OP_BEGIN,           // start of a solve: controls into Scal, sweep sentinels
     OP_PERMUTE_IN,      // b, x from the caller's numbering (in_b, in_x)
     OP_PERMUTE_OUT,     // x to the caller's numbering (out_x)
+    OP_KEEPBEST,        // mixed: after RESID64, keep (x, r) as the best or roll back to it
+    OP_FALLBACK64,      // mixed, refinement stalled: FP64 Krylov restart from the best x
     OP_COUNT
 };
 

@@ -41,6 +41,7 @@ Server::Server(Ctx* ctx, const Controls& sym, const Controls* asym, size_t budge
     for (Family& F : fam_) {
         F.main.init(ctx_);
         F.sub.init(ctx_);
+        F.fb.init(ctx_);
     }
     MRG_CUDA(cudaStreamSynchronize(ctx_->st));
     thread_ = std::thread([this] { loop(); });
@@ -180,7 +181,8 @@ void Server::loop()
         std::vector<Request*> admitted[2], rejected;
         {
             std::unique_lock<std::mutex> lk(mu_);
-            const bool idle = fam_[0].running.empty() && fam_[1].running.empty();
+            const bool idle = fam_[0].running.empty() && fam_[1].running.empty() && fam_[0].fbrun.empty() &&
+                              fam_[1].fbrun.empty();
             if (idle) cv_work_.wait(lk, [this] { return stopping_ || !queue_.empty(); });
             if (stopping_) break;
             for (auto it = queue_.begin(); it != queue_.end();) {
@@ -218,19 +220,21 @@ void Server::loop()
             try {
                 if (!admitted[f].empty()) start(f, admitted[f]);
                 if (!fam_[f].running.empty()) batch_iterate(fam_[f].main, fam_[f].cfg);
+                if (!fam_[f].fbrun.empty()) batch_iterate(fam_[f].fb, fam_[f].cfg, 0);
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }
         }
         for (int f = 0; f < 2; ++f) {
             try {
-                if (!fam_[f].running.empty()) harvest(f);
+                if (!fam_[f].running.empty() || !fam_[f].fbrun.empty()) harvest(f);
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }
         }
         std::lock_guard<std::mutex> lk(mu_);
-        st_.running = (int)(fam_[0].running.size() + fam_[1].running.size());
+        st_.running = (int)(fam_[0].running.size() + fam_[1].running.size() + fam_[0].fbrun.size() +
+                            fam_[1].fbrun.size());
         st_.peak_running = std::max(st_.peak_running, st_.running);
     }
 }
@@ -296,58 +300,117 @@ void Server::start(int f, std::vector<Request*>& rs)
 void Server::harvest(int f)
 {
     Family& F = fam_[f];
-    std::vector<Scal> sc;
-    batch_status(F.main, sc);
     const bool mixed = F.cfg.precision == MRG_PRECISION_MIXED;
-    std::vector<Request*> outer, done;
-    for (size_t s = 0; s < F.running.size(); ++s) {
-        if (sc[s].active) continue;
-        if (mixed && sc[s].ostate)
-            outer.push_back(F.running[s]);
-        else
-            done.push_back(F.running[s]);
+    std::vector<Request*> outer, fallback, done;
+    if (!F.running.empty()) {
+        std::vector<Scal> sc;
+        batch_status(F.main, sc);
+        for (size_t s = 0; s < F.running.size(); ++s) {
+            if (sc[s].active) continue;
+            if (mixed && sc[s].ostate)
+                outer.push_back(F.running[s]);
+            else if (mixed && sc[s].fallback == 1)
+                fallback.push_back(F.running[s]);
+            else
+                done.push_back(F.running[s]);
+        }
     }
-    if (outer.empty() && done.empty()) return;
+    if (!F.fbrun.empty()) {
+        std::vector<Scal> sc;
+        batch_status(F.fb, sc);
+        std::vector<Request*> ended;
+        for (size_t s = 0; s < F.fbrun.size(); ++s)
+            if (!sc[s].active) ended.push_back(F.fbrun[s]);
+        if (!ended.empty()) {
+            // the true FP64 residual of each finished FP64 continuation
+            std::vector<Mesh*> ms;
+            for (Request* r : ended) ms.push_back(r->mesh);
+            F.sub.set(plans_of(ms, F.cfg.ordering));
+            batch_fallback(F.sub, F.cfg);
+            done.insert(done.end(), ended.begin(), ended.end());
+        }
+    }
+    if (outer.empty() && fallback.empty() && done.empty()) return;
     if (!outer.empty()) {
         // correction, FP64 residual and the next inner start of the members
         // whose FP32 loop ended; those whose refinement ended are complete
+        // or, when it stalled, continue in FP64
         std::vector<Mesh*> ms;
         for (Request* r : outer) ms.push_back(r->mesh);
         F.sub.set(plans_of(ms, F.cfg.ordering));
         batch_outer(F.sub, F.cfg);
         std::vector<Scal> s2;
         batch_status(F.sub, s2);
-        for (size_t i = 0; i < outer.size(); ++i)
-            if (!s2[i].ostate) done.push_back(outer[i]);
+        for (size_t i = 0; i < outer.size(); ++i) {
+            if (s2[i].ostate) continue;
+            if (s2[i].fallback == 1)
+                fallback.push_back(outer[i]);
+            else
+                done.push_back(outer[i]);
+        }
     }
-    if (!done.empty()) {
+    if (!fallback.empty()) {
         std::vector<Mesh*> ms;
-        for (Request* r : done) ms.push_back(r->mesh);
+        for (Request* r : fallback) ms.push_back(r->mesh);
         F.sub.set(plans_of(ms, F.cfg.ordering));
-        batch_finish(F.sub);
-        std::vector<Scal> s3;
-        batch_status(F.sub, s3);
-        for (Request* r : done) {
-            Slot* sl;
-            {
-                std::lock_guard<std::mutex> lk(mu_);
-                sl = &slots_[r->mesh];
-            }
-            const size_t n = (size_t)r->mesh->n;
-            MRG_CUDA(cudaMemcpyAsync(r->x_out, sl->d_bx + n, 8 * n, cudaMemcpyDeviceToHost, ctx_->st));
-        }
-        MRG_CUDA(cudaStreamSynchronize(ctx_->st));
-        for (size_t i = 0; i < done.size(); ++i) {
-            Perf p = perf_of(s3[i], F.cfg.precision);
-            done[i]->perf = p;
-            F.running.erase(std::find(F.running.begin(), F.running.end(), done[i]));
-            complete(done[i], p.status, p.status ? "non-finite residual (breakdown)" : "");
+        batch_fallback(F.sub, F.cfg);
+        std::vector<Scal> s4;
+        batch_status(F.sub, s4);
+        for (size_t i = 0; i < fallback.size(); ++i) {
+            Request* r = fallback[i];
+            F.running.erase(std::find(F.running.begin(), F.running.end(), r));
+            if (s4[i].active)
+                F.fbrun.push_back(r);
+            else
+                done.push_back(r);
         }
     }
+    if (!done.empty()) finish(f, done);
+    rebuild(f);
+}
+
+void Server::finish(int f, std::vector<Request*>& done)
+{
+    Family& F = fam_[f];
+    std::vector<Mesh*> ms;
+    for (Request* r : done) ms.push_back(r->mesh);
+    F.sub.set(plans_of(ms, F.cfg.ordering));
+    batch_finish(F.sub);
+    std::vector<Scal> s3;
+    batch_status(F.sub, s3);
+    for (Request* r : done) {
+        Slot* sl;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            sl = &slots_[r->mesh];
+        }
+        const size_t n = (size_t)r->mesh->n;
+        MRG_CUDA(cudaMemcpyAsync(r->x_out, sl->d_bx + n, 8 * n, cudaMemcpyDeviceToHost, ctx_->st));
+    }
+    MRG_CUDA(cudaStreamSynchronize(ctx_->st));
+    for (size_t i = 0; i < done.size(); ++i) {
+        Request* r = done[i];
+        Perf p = perf_of(s3[i], F.cfg.precision);
+        r->perf = p;
+        auto it = std::find(F.running.begin(), F.running.end(), r);
+        if (it != F.running.end()) F.running.erase(it);
+        it = std::find(F.fbrun.begin(), F.fbrun.end(), r);
+        if (it != F.fbrun.end()) F.fbrun.erase(it);
+        complete(r, p.status, p.status ? "non-finite residual (breakdown)" : "");
+    }
+}
+
+void Server::rebuild(int f)
+{
+    Family& F = fam_[f];
     std::vector<Mesh*> ms;
     for (Request* r : F.running) ms.push_back(r->mesh);
     F.main.set(plans_of(ms, F.cfg.ordering));
     batch_recount(F.main);
+    ms.clear();
+    for (Request* r : F.fbrun) ms.push_back(r->mesh);
+    F.fb.set(plans_of(ms, F.cfg.ordering));
+    batch_recount(F.fb);
 }
 
 void Server::fail_family(int f, int code, const std::string& msg)
@@ -356,9 +419,12 @@ void Server::fail_family(int f, int code, const std::string& msg)
     cudaStreamSynchronize(ctx_->st);
     std::vector<Request*> rs;
     rs.swap(F.running);
+    rs.insert(rs.end(), F.fbrun.begin(), F.fbrun.end());
+    F.fbrun.clear();
     for (Request* r : rs) complete(r, code, msg);
     try {
         F.main.set({});
+        F.fb.set({});
     } catch (const Error&) {
     }
 }

@@ -70,8 +70,9 @@ private:
     struct Family {
         Controls cfg;
         bool enabled = false;
-        BatchHost main, sub;
-        std::vector<Request*> running;
+        BatchHost main, sub, fb;
+        std::vector<Request*> running;   // in main (the family's precision)
+        std::vector<Request*> fbrun;     // in fb: mixed solves finishing in FP64
     };
 
     Ctx* ctx_;
@@ -91,6 +92,8 @@ private:
     void loop();
     void start(int f, std::vector<Request*>& reqs);
     void harvest(int f);
+    void finish(int f, std::vector<Request*>& done);
+    void rebuild(int f);
     void fail_family(int f, int code, const std::string& msg);
     void complete(Request* r, int status, const std::string& err);
     size_t estimate(const Mesh& m) const;

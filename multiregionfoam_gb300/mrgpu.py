@@ -49,12 +49,13 @@ class Controls(C.Structure):
 class Perf(C.Structure):
     _fields_ = [("initial_residual", C.c_double), ("final_residual", C.c_double), ("n_iter", C.c_int),
                 ("converged", C.c_int), ("singular", C.c_int), ("status", C.c_int), ("n_outer", C.c_int),
-                ("reserved", C.c_int), ("solve_ms", C.c_double)]
+                ("fallback", C.c_int), ("solve_ms", C.c_double)]
 
     def as_dict(self):
         return {"initial_residual": self.initial_residual, "final_residual": self.final_residual,
                 "n_iter": self.n_iter, "converged": bool(self.converged), "singular": bool(self.singular),
-                "status": self.status, "n_outer": self.n_outer, "solve_ms": self.solve_ms}
+                "status": self.status, "n_outer": self.n_outer, "fallback": bool(self.fallback),
+                "solve_ms": self.solve_ms}
 
 
 class ServerStats(C.Structure):

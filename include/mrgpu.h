@@ -238,6 +238,66 @@ int mrg_batch_solve_device(mrg_batch* batch, const double* const* d_b,
                            double* const* d_x_inout,
                            const mrg_controls* controls, mrg_perf* perfs);
 
+/* ---- partitioned Dirichlet-Neumann coupling ----------------------------
+ * One interface coupled by the partitioned (DN) method, the reference's
+ * alternative to the monolithic solve: region A carries the jump
+ * (Dirichlet) patch, region B the flux (Neumann) patch.  The patch states,
+ * the relaxation history and the Aitken factors stay on the device.
+ * Replaces, per coupling iteration, genericRegionCoupledJumpFvPatchField::
+ * updateCoeffs (.C:164-217), genericRegionCoupledFluxFvPatchField::
+ * updateCoeffs (.C:172-239), their rawResidual/normResidual (Jump .C:244-332,
+ * Flux .C:241-409), fixedRelaxation / aitkenRelaxation::relax
+ * (fixedRelaxation.C:76-101, aitkenRelaxation.C:74-100,
+ * aitkenRelaxationTemplates.C:105-165) and dnaControl::criteriaSatisfied
+ * (dnaControl.C:582-635) for a scalar field with
+ * regionCoupledTemperatureJump (value jump (K-1) * nbr) and
+ * regionCoupledHeatFlux (flux jump 0). */
+typedef struct mrg_dn mrg_dn;
+typedef struct {
+    int n_cells;                 /* cells of the patch's region               */
+    int n_faces;                 /* faces of the patch                        */
+    const int32_t* face_cells;   /* [n_faces] faceCells                       */
+    const double* delta_coeffs;  /* [n_faces] 1 / cell-to-face distance       */
+    const double* k;             /* [n_faces] diffusivity at the face         */
+    const double* area;          /* [n_faces] face area |Sf|                  */
+    const int32_t* src_ptr;      /* [n_faces+1] this patch's faces from the   */
+    const int32_t* src_face;     /*   other patch's faces: GGI CSR (or        */
+    const double* src_weight;    /*   directMap: one weight 1 per face)       */
+} mrg_dn_patch;
+typedef struct {
+    double K;          /* regionCoupledTemperatureJump: value = K * nbr      */
+    double flux_jump;  /* regionCoupledHeatFlux: 0                           */
+    double relax;      /* fixed factor, or Aitken's initial factor           */
+    int relax_model;   /* 0 fixedRelaxation, 1 aitkenRelaxation              */
+    int reserved;
+} mrg_dn_config;
+int mrg_dn_create(mrg_ctx* ctx, const mrg_dn_patch* a, const mrg_dn_patch* b,
+                  const mrg_dn_config* config, mrg_dn** out);
+int mrg_dn_destroy(mrg_dn* dn);
+/* Initial patch value on A and gradient on B (host arrays); resets the
+ * relaxation history. */
+int mrg_dn_set_state(mrg_dn* dn, const double* value_a, const double* grad_b);
+/* A new time step restarts the relaxation's corrector count. */
+int mrg_dn_new_time_step(mrg_dn* dn);
+/* Jump update of A from region B's cell field (device), and flux update of
+ * B from region A's cell field (device). */
+int mrg_dn_update_jump(mrg_dn* dn, const double* d_t_b);
+int mrg_dn_update_flux(mrg_dn* dn, const double* d_t_a);
+/* d_b = d_b0 + the patch's source terms for region `side` (0: A, Dirichlet
+ * k|Sf|deltaCoeffs value; 1: B, Neumann k|Sf| gradient).  The matching
+ * Dirichlet diagonal term k|Sf|deltaCoeffs belongs to A's matrix. */
+int mrg_dn_rhs(mrg_dn* dn, int side, const double* d_b0, double* d_b);
+/* Normalised jump (A) and flux (B) residuals of the current state. */
+int mrg_dn_residuals(mrg_dn* dn, const double* d_t_a, const double* d_t_b,
+                     double* jump_res, double* flux_res);
+/* Host copies of the patch states and the two Aitken factors (any may be
+ * NULL). */
+int mrg_dn_get_state(mrg_dn* dn, double* value_a, double* grad_b, double* aitken);
+/* dnaControl::criteriaSatisfied: 0 on the first coupling iteration, else 1
+ * when both residuals are within their limits. */
+int mrg_dn_criteria(int corr, double jump_res, double flux_res, double max_jump_res,
+                    double max_flux_res);
+
 /* ---- autotuner ---------------------------------------------------------
  * No counterpart in the reference.  Times the Krylov loop of a mesh or batch
  * on its current coefficients under each candidate launch shape and keeps

@@ -141,7 +141,7 @@ def cht_system(nx: int, ny: int, nz_fluid: int, nz_solid: int, *, seed: int = 0,
     b[f_lid] += gb_f * t_top
 
     meta = dict(nx=nx, ny=ny, nz_fluid=nz_fluid, nz_solid=nz_solid, seed=seed, h=h,
-                n_solid=ns, n_fluid=nfl, n_iface=nx * ny, rc=rc)
+                n_solid=ns, n_fluid=nfl, n_iface=nx * ny, rc=rc, k_cell=kc)
     if form == "global":
         lo2, up2, g2 = upper_triangular(np.concatenate([lower, s_top]),
                                         np.concatenate([upper, f_bot]),
@@ -161,6 +161,48 @@ def cht_system(nx: int, ny: int, nz_fluid: int, nz_solid: int, *, seed: int = 0,
     }
     return LduSystem(n, lower.astype(np.int32), upper.astype(np.int32), diag, -g_int, None,
                      b, t_old, iface, name="cht-coupled", meta=meta)
+
+
+def partitioned_cht(nx: int, ny: int, nz_fluid: int, nz_solid: int, **kw):
+    """The two-region CHT problem of cht_system split for partitioned
+    Dirichlet-Neumann coupling: region A = fluid (jump / Dirichlet patch on
+    its bottom faces), region B = solid (flux / Neumann patch on its top
+    faces), conformal face-to-face map.  Returns a dict with the monolithic
+    global system, the two region systems (interface faces removed; the
+    Dirichlet patch's diagonal term k|Sf|deltaCoeffs = 2 k h added to A),
+    and the two patches (faceCells, deltaCoeffs = 2/h, face k = cell k,
+    |Sf| = h^2, identity interpolation).  Converged DN coupling reproduces
+    the monolithic solution: the harmonic-mean interface conductance of the
+    monolithic matrix is what continuity of value and flux gives."""
+    mono = cht_system(nx, ny, nz_fluid, nz_solid, form="global", **kw)
+    m = mono.meta
+    h, ns, n = m["h"], m["n_solid"], mono.n
+    kc = m["k_cell"]
+    nif = nx * ny
+    s_top = np.arange(nif) + (nz_solid - 1) * nif
+    f_bot = np.arange(nif) + ns
+    lo, up = mono.lower.astype(np.int64), mono.upper.astype(np.int64)
+    in_s = up < ns
+    in_f = lo >= ns
+    iface = ~(in_s | in_f)
+    g_if = -mono.upper_c[iface]
+    diag = mono.diag.copy()
+    np.subtract.at(diag, lo[iface], g_if)
+    np.subtract.at(diag, up[iface], g_if)
+    fluid_diag = diag[ns:].copy()
+    fluid_diag[f_bot - ns] += 2.0 * kc[f_bot] * h
+    solid = LduSystem(ns, lo[in_s].astype(np.int32), up[in_s].astype(np.int32), diag[:ns].copy(),
+                      mono.upper_c[in_s].copy(), None, mono.b[:ns].copy(), mono.x0[:ns].copy(), None,
+                      name="cht-solid")
+    fluid = LduSystem(n - ns, (lo[in_f] - ns).astype(np.int32), (up[in_f] - ns).astype(np.int32), fluid_diag,
+                      mono.upper_c[in_f].copy(), None, mono.b[ns:].copy(), mono.x0[ns:].copy(), None,
+                      name="cht-fluid")
+    ident = dict(ptr=np.arange(nif + 1, dtype=np.int32), addr=np.arange(nif, dtype=np.int32), w=np.ones(nif))
+    patch_a = dict(n_cells=n - ns, face_cells=(f_bot - ns).astype(np.int32), delta=np.full(nif, 2.0 / h),
+                   k=kc[f_bot].copy(), area=np.full(nif, h * h), **ident)
+    patch_b = dict(n_cells=ns, face_cells=s_top.astype(np.int32), delta=np.full(nif, 2.0 / h),
+                   k=kc[s_top].copy(), area=np.full(nif, h * h), **ident)
+    return dict(mono=mono, fluid=fluid, solid=solid, a=patch_a, b=patch_b, s_top=s_top, f_bot=f_bot)
 
 
 def c1(form="global", seed=0):

@@ -7,10 +7,12 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "../../include/mrgpu.h"
 #include "engine.h"
 #include "kernels.h"
+#include "dn.h"
 #include "noalloc.h"
 #include "server.h"
 
@@ -27,6 +29,9 @@ struct mrg_ggi {
 };
 struct mrg_server {
     std::unique_ptr<Server> s;
+};
+struct mrg_dn {
+    std::unique_ptr<Dn> d;
 };
 struct mrg_batch {
     Ctx* ctx = nullptr;
@@ -689,6 +694,117 @@ int mrg_batch_tune(mrg_batch* batch, const double* const* d_b, const double* con
         MRG_CUDA(cudaStreamSynchronize(batch->ctx->st));
         return (int)MRG_OK;
     });
+}
+
+int mrg_dn_create(mrg_ctx* ctx, const mrg_dn_patch* a, const mrg_dn_patch* b, const mrg_dn_config* cfg,
+                  mrg_dn** out)
+{
+    return guard([&] {
+        if (!ctx || !a || !b || !cfg || !out) return fail(MRG_E_INVALID, "NULL argument");
+        *out = nullptr;
+        if (!a->src_ptr || !b->src_ptr) return fail(MRG_E_INVALID, "NULL interpolation CSR");
+        std::vector<double> wa, wb;
+        const double* pwa = a->src_weight;
+        const double* pwb = b->src_weight;
+        if (!pwa) {
+            wa.assign((size_t)std::max(a->src_ptr[a->n_faces], 0), 1.0);
+            pwa = wa.data();
+        }
+        if (!pwb) {
+            wb.assign((size_t)std::max(b->src_ptr[b->n_faces], 0), 1.0);
+            pwb = wb.data();
+        }
+        auto* d = new mrg_dn();
+        try {
+            d->d.reset(dn_create(&ctx->c, a->n_cells, a->n_faces, a->face_cells, a->delta_coeffs, a->k, a->area,
+                                 b->n_cells, b->n_faces, b->face_cells, b->delta_coeffs, b->k, b->area, a->src_ptr,
+                                 a->src_face, pwa, b->src_ptr, b->src_face, pwb, cfg->K, cfg->flux_jump,
+                                 cfg->relax_model, cfg->relax));
+        } catch (...) {
+            delete d;
+            throw;
+        }
+        *out = d;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_destroy(mrg_dn* dn)
+{
+    return guard([&] {
+        delete dn;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_set_state(mrg_dn* dn, const double* value_a, const double* grad_b)
+{
+    return guard([&] {
+        if (!dn || !value_a || !grad_b) return fail(MRG_E_INVALID, "NULL argument");
+        dn_set_state(*dn->d, value_a, grad_b);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_new_time_step(mrg_dn* dn)
+{
+    return guard([&] {
+        if (!dn) return fail(MRG_E_INVALID, "NULL argument");
+        dn_new_time_step(*dn->d);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_update_jump(mrg_dn* dn, const double* d_t_b)
+{
+    return guard([&] {
+        if (!dn || !d_t_b) return fail(MRG_E_INVALID, "NULL argument");
+        dn_update_a(*dn->d, d_t_b);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_update_flux(mrg_dn* dn, const double* d_t_a)
+{
+    return guard([&] {
+        if (!dn || !d_t_a) return fail(MRG_E_INVALID, "NULL argument");
+        dn_update_b(*dn->d, d_t_a);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_rhs(mrg_dn* dn, int side, const double* d_b0, double* d_b)
+{
+    return guard([&] {
+        if (!dn || !d_b0 || !d_b) return fail(MRG_E_INVALID, "NULL argument");
+        if (side != 0 && side != 1) return fail(MRG_E_INVALID, "side must be 0 (A) or 1 (B)");
+        dn_rhs(*dn->d, side, d_b0, d_b);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_residuals(mrg_dn* dn, const double* d_t_a, const double* d_t_b, double* jump_res, double* flux_res)
+{
+    return guard([&] {
+        if (!dn || !d_t_a || !d_t_b) return fail(MRG_E_INVALID, "NULL argument");
+        dn_residuals(*dn->d, d_t_a, d_t_b, jump_res, flux_res);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_get_state(mrg_dn* dn, double* value_a, double* grad_b, double* aitken)
+{
+    return guard([&] {
+        if (!dn) return fail(MRG_E_INVALID, "NULL argument");
+        dn_get_state(*dn->d, value_a, grad_b, aitken);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_criteria(int corr, double jump_res, double flux_res, double max_jump_res, double max_flux_res)
+{
+    if (corr == 1) return 0;
+    return (jump_res <= max_jump_res && flux_res <= max_flux_res) ? 1 : 0;
 }
 
 int mrg_server_create(mrg_ctx* ctx, const mrg_controls* sym_controls, const mrg_controls* asym_controls,

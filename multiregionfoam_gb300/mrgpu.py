@@ -30,6 +30,8 @@ EXPORTED = [
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
     "mrg_residual_noalloc", "mrg_server_create", "mrg_server_destroy", "mrg_server_submit", "mrg_server_poll",
     "mrg_server_wait", "mrg_server_get_stats", "mrg_mesh_tune", "mrg_batch_tune",
+    "mrg_dn_create", "mrg_dn_destroy", "mrg_dn_set_state", "mrg_dn_new_time_step", "mrg_dn_update_jump",
+    "mrg_dn_update_flux", "mrg_dn_rhs", "mrg_dn_residuals", "mrg_dn_get_state", "mrg_dn_criteria",
 ]
 
 
@@ -70,6 +72,17 @@ class Tuning(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class DnPatch(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("face_cells", C.c_void_p),
+                ("delta_coeffs", C.c_void_p), ("k", C.c_void_p), ("area", C.c_void_p), ("src_ptr", C.c_void_p),
+                ("src_face", C.c_void_p), ("src_weight", C.c_void_p)]
+
+
+class DnConfig(C.Structure):
+    _fields_ = [("K", C.c_double), ("flux_jump", C.c_double), ("relax", C.c_double), ("relax_model", C.c_int),
+                ("reserved", C.c_int)]
 
 
 class IfaceDesc(C.Structure):
@@ -133,6 +146,16 @@ def load(path: str = LIB_PATH):
                                   C.POINTER(C.c_double)]
     L.mrg_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
     L.mrg_mesh_tune.argtypes = [vp, vp, vp, C.POINTER(Controls), C.POINTER(Tuning)]
+    L.mrg_dn_create.argtypes = [vp, C.POINTER(DnPatch), C.POINTER(DnPatch), C.POINTER(DnConfig), C.POINTER(vp)]
+    L.mrg_dn_destroy.argtypes = [vp]
+    L.mrg_dn_set_state.argtypes = [vp, dp, dp]
+    L.mrg_dn_new_time_step.argtypes = [vp]
+    L.mrg_dn_update_jump.argtypes = [vp, vp]
+    L.mrg_dn_update_flux.argtypes = [vp, vp]
+    L.mrg_dn_rhs.argtypes = [vp, C.c_int, vp, vp]
+    L.mrg_dn_residuals.argtypes = [vp, vp, vp, dp, dp]
+    L.mrg_dn_get_state.argtypes = [vp, dp, dp, dp]
+    L.mrg_dn_criteria.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
     L.mrg_batch_tune.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Tuning)]
     _LIB = L
     return L
@@ -476,3 +499,63 @@ class Server:
             _check(load().mrg_server_destroy(self.h))
             self.h = None
             self._live.clear()
+
+
+class DnInterface:
+    """Device-resident partitioned Dirichlet-Neumann interface (mrg_dn_*).
+
+    a / b: dicts with n_cells, face_cells, delta, k, area and the GGI CSR
+    (ptr, addr, w) giving the patch's faces from the other patch's faces."""
+
+    def __init__(self, ctx: Context, a: dict, b: dict, K=1.0, flux_jump=0.0, relax=0.75, model="aitken"):
+        self._keep = []
+
+        def patch(p):
+            arrs = [np.ascontiguousarray(p["face_cells"], np.int32), np.ascontiguousarray(p["delta"], np.float64),
+                    np.ascontiguousarray(p["k"], np.float64), np.ascontiguousarray(p["area"], np.float64),
+                    np.ascontiguousarray(p["ptr"], np.int32), np.ascontiguousarray(p["addr"], np.int32),
+                    np.ascontiguousarray(p["w"], np.float64)]
+            self._keep.append(arrs)
+            return DnPatch(int(p["n_cells"]), len(arrs[0]), *[a_.ctypes.data_as(C.c_void_p) for a_ in arrs])
+
+        cfg = DnConfig(float(K), float(flux_jump), float(relax), 1 if model == "aitken" else 0, 0)
+        h = C.c_void_p()
+        _check(load().mrg_dn_create(ctx.h, C.byref(patch(a)), C.byref(patch(b)), C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.na, self.nb = len(a["face_cells"]), len(b["face_cells"])
+
+    def set_state(self, value_a, grad_b):
+        _check(load().mrg_dn_set_state(self.h, _d(np.ascontiguousarray(value_a, np.float64)),
+                                       _d(np.ascontiguousarray(grad_b, np.float64))))
+
+    def new_time_step(self):
+        _check(load().mrg_dn_new_time_step(self.h))
+
+    def update_jump(self, d_t_b: int):
+        _check(load().mrg_dn_update_jump(self.h, C.c_void_p(d_t_b)))
+
+    def update_flux(self, d_t_a: int):
+        _check(load().mrg_dn_update_flux(self.h, C.c_void_p(d_t_a)))
+
+    def rhs(self, side: int, d_b0: int, d_b: int):
+        _check(load().mrg_dn_rhs(self.h, int(side), C.c_void_p(d_b0), C.c_void_p(d_b)))
+
+    def residuals(self, d_t_a: int, d_t_b: int):
+        j, f = C.c_double(), C.c_double()
+        _check(load().mrg_dn_residuals(self.h, C.c_void_p(d_t_a), C.c_void_p(d_t_b), C.byref(j), C.byref(f)))
+        return j.value, f.value
+
+    def state(self):
+        va, gb, ai = np.empty(self.na), np.empty(self.nb), np.empty(2)
+        _check(load().mrg_dn_get_state(self.h, _d(va), _d(gb), _d(ai)))
+        return va, gb, ai
+
+    def close(self):
+        if self.h:
+            _check(load().mrg_dn_destroy(self.h))
+            self.h = None
+
+
+def dn_criteria(corr, jump_res, flux_res, max_jump, max_flux) -> bool:
+    return bool(load().mrg_dn_criteria(int(corr), float(jump_res), float(flux_res), float(max_jump),
+                                       float(max_flux)))

@@ -867,13 +867,14 @@ __device__ __forceinline__ bool system_live(const SysDev& S)
     return true;
 }
 
-// Close one reduction segment (consecutive tiles [first, first+count) of one
-// system handled by this CTA): block tree, partial into slot `first`, and the
-// CTA that completes the system's tile count sums every slot in slot order
-// (unused slots hold zero) and finalises.  Deterministic for a given tile
-// table and grid size.
+// Close reduction segment `seg` of one system (consecutive tiles, `count`
+// of them, handled by this CTA): block tree, partial into slot `seg`, and
+// the CTA that completes the system's tile count sums the G slots -- thread
+// t the slots t, t + 256, ... in order -- and finalises.  Every slot is
+// rewritten by every reduction, so none needs clearing.  Deterministic: the
+// order depends only on the system.
 template <RowOp OP>
-__device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, int first, int count,
+__device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, int seg, int count,
                                               double (&acc)[kMaxRed], double* sh, int* s_last)
 {
     constexpr int NR = OpTraits<OP>::kNR;
@@ -884,22 +885,30 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
     block_sum<NR>(a, sh);
     if (tid == 0) {
 #pragma unroll
-        for (int k = 0; k < NR; ++k) S.partials[first * kMaxRed + k] = a[k];
+        for (int k = 0; k < NR; ++k) S.partials[seg * kMaxRed + k] = a[k];
         __threadfence();
         const unsigned prev = atomicAdd(S.counter, (unsigned)count);
         *s_last = (prev + (unsigned)count == (unsigned)S.ntiles);
     }
     __syncthreads();
     if (*s_last) {
+        const int G = red_segments(S.ntiles);
+        // every slot this thread sums, loaded before the first add
+        constexpr int kMaxPer = (kRedSegs + kBlock - 1) / kBlock;
+        double v[kMaxPer][NR];
+#pragma unroll
+        for (int c = 0; c < kMaxPer; ++c) {
+            const int j = tid + c * kBlock;
+#pragma unroll
+            for (int k = 0; k < NR; ++k) v[c][k] = j < G ? __ldcg(S.partials + j * kMaxRed + k) : 0.0;
+        }
         double tot[NR];
 #pragma unroll
-        for (int k = 0; k < NR; ++k) tot[k] = 0.0;
-        for (int j = tid; j < S.ntiles; j += kBlock) {
+        for (int k = 0; k < NR; ++k) {
+            tot[k] = 0.0;
 #pragma unroll
-            for (int k = 0; k < NR; ++k) {
-                tot[k] += __ldcg(S.partials + j * kMaxRed + k);
-                S.partials[j * kMaxRed + k] = 0.0;
-            }
+            for (int c = 0; c < kMaxPer; ++c)
+                if (tid + c * kBlock < G) tot[k] += v[c][k];
         }
         block_sum<NR>(tot, sh);
         if (tid == 0) {
@@ -944,7 +953,7 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
     bool live = false;
     if constexpr (!OpTraits<OP>::kRed) {
         for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
-            const int2 tl = B.tiles[t];
+            const int2 tl = B.nsys == 1 ? make_int2(0, t) : B.tiles[t];
             if (tl.x != lcur) {
                 lcur = tl.x;
                 if (tl.x != cur) {
@@ -959,7 +968,7 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
         }
     } else {
         for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
-            const int2 sg = B.segs[g];
+            const int2 sg = B.nsys == 1 ? make_int2(0, g) : B.segs[g];
             if (sg.x != lcur) {
                 lcur = sg.x;
                 if (sg.x != cur) {
@@ -973,7 +982,7 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
             for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
-            flush_segment<OP>(B, sS, t0, t1 - t0, acc, sh, s_last);
+            flush_segment<OP>(B, sS, sg.y, t1 - t0, acc, sh, s_last);
         }
     }
 }

@@ -502,15 +502,15 @@ static int mr_row(int tile, int t, int k, int assign)
 
 /* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order).
  * Segment g of G = min(608, ceil(tiles/4)) owns tiles [g*T/G, (g+1)*T/G) and keeps
- * accumulating across them; its tree sum lands in the slot of its first tile
- * (the other slots stay zero). */
+ * accumulating across them; its tree sum lands in slot g.  Thread t then sums
+ * slots t, t + 256, ... in order and one block tree combines the threads. */
 static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)
 {
     int ntiles = o->npad / MR_TILE;
     int G = (ntiles + MR_SEG_TILES - 1) / MR_SEG_TILES;
     if (G > MR_GRID) G = MR_GRID;
     if (G < 1) G = 1;
-    double* part = (double*)calloc((size_t)(ntiles ? ntiles : 1), sizeof(double));
+    double* part = (double*)calloc((size_t)G, sizeof(double));
     double acc[MR_BLOCK];
     for (int g = 0; g < G; ++g) {
         int t0 = (int)((long long)g * ntiles / G), t1 = (int)((long long)(g + 1) * ntiles / G);
@@ -530,11 +530,11 @@ static double mr_reduce(const mr_order* o, int assign, int kind, const double* a
                 acc[t] = s;
             }
         }
-        if (t1 > t0) part[t0] = mr_block(acc);
+        part[g] = mr_block(acc);
     }
     for (int t = 0; t < MR_BLOCK; ++t) {
         double s = 0.0;
-        for (int k = t; k < ntiles; k += MR_BLOCK) s += part[k];
+        for (int k = t; k < G; k += MR_BLOCK) s += part[k];
         acc[t] = s;
     }
     free(part);

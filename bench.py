@@ -289,6 +289,17 @@ def run_served(args, ctx, mrgpu):
             seq.append(cur)
             cur = cases.perturb_step(cur, rng)
         steps.append(seq)
+    def pinned(a):
+        if a is None:
+            return None
+        h = mrgpu.host_array(None, a.size)
+        h[:] = a
+        return h
+
+    # each request's arrays in pinned host memory, as a caller streaming time
+    # steps would hold them (the server copies them asynchronously)
+    steps = [[dict(diag=pinned(st.diag), upper=pinned(st.upper_c), lower=pinned(st.lower_c), b=pinned(st.b),
+                   x0=pinned(st.x0)) for st in seq] for seq in steps]
     reqs = [(i, steps[i][k], ms[i][1]) for k in range(args.served_steps) for i in range(len(ms))]
     arrivals = np.cumsum(np.random.default_rng(SEED + 11).exponential(1.0 / args.served_rate, len(reqs)))
     out = {"requests": len(reqs), "meshes": len(ms), "rate_per_s": args.served_rate,
@@ -305,7 +316,7 @@ def run_served(args, ctx, mrgpu):
             dt = ta - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            ids.append(srv.submit(meshes[i], s.b, s.x0, s.diag, s.upper_c, s.lower_c, asym=a))
+            ids.append(srv.submit(meshes[i], s["b"], s["x0"], s["diag"], s["upper"], s["lower"], asym=a))
         lat, conv = [], 0
         for r in ids:
             x, p, l = srv.wait(r, 600000.0)

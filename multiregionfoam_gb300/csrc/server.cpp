@@ -1,15 +1,18 @@
 // server.cpp -- continuous batching of solve requests (see server.h).
 //
-// The server thread owns the context's stream while it runs.  Each pass of
+// The server thread owns the context's streams while it runs.  Each pass of
 // its loop: admit queued requests in arrival order while batch slots and the
 // HBM budget allow (a mesh has at most one step in flight: its next time
-// step waits for the previous one); start the admitted ones (coefficients,
-// b and x0 uploaded, views and factor, initial residual) in a side batch and
-// add them to their family's running batch; launch each running batch's
-// captured K-iteration graph once; gather every member's state; run the
-// mixed-precision outer step for members whose inner loop ended; copy out
-// and complete the members that converged.  New requests therefore join
-// while others are mid-solve, and all members share every kernel launch.
+// step waits for the previous one); launch each running batch's captured
+// K-iteration graph once on the main stream; meanwhile, on a side stream,
+// start the admitted requests (coefficients, b and x0 uploaded, views and
+// factor, initial residual) in an admission batch -- they touch only their
+// own meshes' memory, so this overlaps the running iterations; gather every
+// running member's state; run the mixed-precision outer step for members
+// whose inner loop ended; copy out and complete the members that
+// converged; then the admitted requests join the running batch.  New
+// requests therefore join while others are mid-solve, and all members share
+// every kernel launch.
 #include "server.h"
 
 #include <algorithm>
@@ -25,6 +28,15 @@ double now_ms()
     using namespace std::chrono;
     return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
+
+// Route the context's work to another stream for a scope (the server thread
+// is the context's only user while the server runs).
+struct StreamSwap {
+    Ctx* c;
+    cudaStream_t old;
+    StreamSwap(Ctx* ctx, cudaStream_t s) : c(ctx), old(ctx->st) { c->st = s; }
+    ~StreamSwap() { c->st = old; }
+};
 }  // namespace
 
 Server::Server(Ctx* ctx, const Controls& sym, const Controls* asym, size_t budget, int max_active)
@@ -42,7 +54,10 @@ Server::Server(Ctx* ctx, const Controls& sym, const Controls* asym, size_t budge
         F.main.init(ctx_);
         F.sub.init(ctx_);
         F.fb.init(ctx_);
+        F.adm.init(ctx_);
     }
+    MRG_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+    MRG_CUDA(cudaEventCreateWithFlags(&side_done_, cudaEventDisableTiming));
     MRG_CUDA(cudaStreamSynchronize(ctx_->st));
     thread_ = std::thread([this] { loop(); });
 }
@@ -65,6 +80,11 @@ Server::~Server()
     for (Request* r : left) complete(r, MRG_E_INVALID, "server destroyed before the request completed");
     for (auto& kv : reqs_) delete kv.second;
     for (auto& kv : slots_) ctx_->release(kv.second.d_bx);
+    if (side_) {
+        cudaStreamSynchronize(side_);
+        cudaStreamDestroy(side_);
+    }
+    if (side_done_) cudaEventDestroy(side_done_);
 }
 
 size_t Server::estimate(const Mesh& m) const
@@ -218,16 +238,34 @@ void Server::loop()
             complete(r, MRG_E_OOM, "the request's working set exceeds the server's HBM budget");
         for (int f = 0; f < 2; ++f) {
             try {
-                if (!admitted[f].empty()) start(f, admitted[f]);
                 if (!fam_[f].running.empty()) batch_iterate(fam_[f].main, fam_[f].cfg);
                 if (!fam_[f].fbrun.empty()) batch_iterate(fam_[f].fb, fam_[f].cfg, 0);
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }
         }
+        // admissions on the side stream, overlapping the iterations above
+        bool any_admitted = false;
+        {
+            StreamSwap swap(ctx_, side_);
+            for (int f = 0; f < 2; ++f)
+                if (!admitted[f].empty()) {
+                    start(f, admitted[f]);
+                    any_admitted = true;
+                }
+            if (any_admitted) cudaEventRecord(side_done_, side_);
+        }
         for (int f = 0; f < 2; ++f) {
             try {
-                if (!fam_[f].running.empty() || !fam_[f].fbrun.empty()) harvest(f);
+                bool changed = false;
+                if (!fam_[f].running.empty() || !fam_[f].fbrun.empty()) changed = harvest(f);
+                if (!fam_[f].joining.empty()) {
+                    MRG_CUDA(cudaStreamWaitEvent(ctx_->st, side_done_, 0));
+                    fam_[f].running.insert(fam_[f].running.end(), fam_[f].joining.begin(), fam_[f].joining.end());
+                    fam_[f].joining.clear();
+                    changed = true;
+                }
+                if (changed) rebuild(f);
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }
@@ -269,11 +307,11 @@ void Server::start(int f, std::vector<Request*>& rs)
             P.sys.in_b = sl->d_bx;
             P.sys.in_x = sl->d_bx + n;
             P.sys.out_x = sl->d_bx + n;
-            F.sub.set({&P});
+            F.adm.set({&P});
             std::vector<Mesh*> ms{&m};
-            prepare_batch(F.sub, ms, F.cfg);
-            F.sub.sync_sys();
-            batch_begin(F.sub, F.cfg);
+            prepare_batch(F.adm, ms, F.cfg);
+            F.adm.sync_sys();
+            batch_begin(F.adm, F.cfg);
             const size_t grew = ctx_->used - before;
             {
                 std::lock_guard<std::mutex> lk(mu_);
@@ -286,18 +324,14 @@ void Server::start(int f, std::vector<Request*>& rs)
                     st_.peak_inflight_bytes = std::max(st_.peak_inflight_bytes, st_.inflight_bytes);
                 }
             }
-            F.running.push_back(r);
+            F.joining.push_back(r);
         } catch (const Error& e) {
             complete(r, e.code, e.what());
         }
     }
-    std::vector<Mesh*> ms;
-    for (Request* r : F.running) ms.push_back(r->mesh);
-    F.main.set(plans_of(ms, F.cfg.ordering));
-    batch_recount(F.main);
 }
 
-void Server::harvest(int f)
+bool Server::harvest(int f)
 {
     Family& F = fam_[f];
     const bool mixed = F.cfg.precision == MRG_PRECISION_MIXED;
@@ -330,7 +364,7 @@ void Server::harvest(int f)
             done.insert(done.end(), ended.begin(), ended.end());
         }
     }
-    if (outer.empty() && fallback.empty() && done.empty()) return;
+    if (outer.empty() && fallback.empty() && done.empty()) return false;
     if (!outer.empty()) {
         // correction, FP64 residual and the next inner start of the members
         // whose FP32 loop ended; those whose refinement ended are complete
@@ -366,7 +400,7 @@ void Server::harvest(int f)
         }
     }
     if (!done.empty()) finish(f, done);
-    rebuild(f);
+    return true;
 }
 
 void Server::finish(int f, std::vector<Request*>& done)
@@ -417,10 +451,13 @@ void Server::fail_family(int f, int code, const std::string& msg)
 {
     Family& F = fam_[f];
     cudaStreamSynchronize(ctx_->st);
+    cudaStreamSynchronize(side_);
     std::vector<Request*> rs;
     rs.swap(F.running);
     rs.insert(rs.end(), F.fbrun.begin(), F.fbrun.end());
+    rs.insert(rs.end(), F.joining.begin(), F.joining.end());
     F.fbrun.clear();
+    F.joining.clear();
     for (Request* r : rs) complete(r, code, msg);
     try {
         F.main.set({});

@@ -70,9 +70,10 @@ private:
     struct Family {
         Controls cfg;
         bool enabled = false;
-        BatchHost main, sub, fb;
+        BatchHost main, sub, fb, adm;
         std::vector<Request*> running;   // in main (the family's precision)
         std::vector<Request*> fbrun;     // in fb: mixed solves finishing in FP64
+        std::vector<Request*> joining;   // prepared on the side stream, join main next
     };
 
     Ctx* ctx_;
@@ -87,11 +88,13 @@ private:
     uint64_t next_id_ = 1;
     bool stopping_ = false;
     ServerStats st_;
+    cudaStream_t side_ = nullptr;      // admissions: uploads, views, factor, initial residual
+    cudaEvent_t side_done_ = nullptr;
     std::thread thread_;
 
     void loop();
     void start(int f, std::vector<Request*>& reqs);
-    void harvest(int f);
+    bool harvest(int f);
     void finish(int f, std::vector<Request*>& done);
     void rebuild(int f);
     void fail_family(int f, int code, const std::string& msg);

@@ -329,6 +329,30 @@ def run_served(args, ctx, mrgpu):
                      "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv),
                      "peak_running": st["peak_running"], "peak_inflight_gb": st["peak_inflight_bytes"] / 2**30}
     out["speedup_mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    # The plain drop-in solver as foam would call it: one request at a time,
+    # device-resident, FP64 in foam's order.  Timed on the first time step of
+    # every mesh (the request mix's sizes and families) and reported as
+    # requests per second of solve time.
+    plain_ms = []
+    for i, (s0, a) in enumerate(ms):
+        st = steps[i][0]
+        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="PBiCG" if a else "PCG",
+                             precond="DILU" if a else "DIC", precision="fp64", ordering="exact")
+        meshes[i].upload(st["diag"], st["upper"], st["lower"])
+        d_b, d_x = ctx.to_device(st["b"]), ctx.to_device(st["x0"])
+        meshes[i].solve_device(d_b, d_x, ctl)          # warm (plan, graphs)
+        ctx.dev_free(d_x)
+        d_x = ctx.to_device(st["x0"])
+        ctx.record(52)
+        p = meshes[i].solve_device(d_b, d_x, ctl)
+        ctx.record(53)
+        plain_ms.append(ctx.elapsed_ms(52, 53))
+        ctx.dev_free(d_b)
+        ctx.dev_free(d_x)
+    seq_rate = len(plain_ms) / (sum(plain_ms) * 1e-3)
+    out["plain_fp64_one_at_a_time"] = {"solves_per_s": seq_rate, "requests_timed": len(plain_ms),
+                                       "mean_ms": float(np.mean(plain_ms))}
+    out["speedup_served_mixed_vs_plain_one_at_a_time"] = out["mixed"]["solves_per_s"] / seq_rate
     for m in meshes:
         m.close()
     return out

@@ -998,6 +998,191 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
     rows_phase<V, OP, PB>(B, sS, sh, &s_last, cur);
 }
 
+// ---------------------------------------------------------------- staged SpMV
+// Amul + (q, p) of the Krylov loop with the sliced-ELL column indices and
+// coefficients staged in shared memory by the bulk-copy engine.  A segment's
+// tiles are walked in rounds of 8 slices -- one slice per warp, tile by
+// tile, slices w, w+8, w+16, w+24 of each tile: exactly ell_tile's rows in
+// ell_tile's order, so q, (q, p) and every bit downstream are unchanged.
+// Thread 0 keeps kStages - 1 rounds in flight (one contiguous cp.async.bulk
+// per array per round, completion counted on the stage's mbarrier); warps
+// read indices and coefficients from shared memory and only the x gathers
+// go to L1/L2.  A round whose entries exceed a stage (a slice wider than
+// kMaxW) is read from global memory instead.  Waits are bounded: on timeout
+// the error bit is set and the CTA leaves after its copies land.
+template <typename V> struct SpmvStages;
+template <> struct SpmvStages<float> { static constexpr int n = 3; };
+template <> struct SpmvStages<double> { static constexpr int n = 2; };
+constexpr int kRoundEntries = (kBlock / 32) * kMaxW * 32;   // entries one stage holds
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_u32(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, "
+        "p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for a stage's phase; false (error bit set) on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity, Ctl* ctl)
+{
+    if (mbar_try_wait(b, parity)) return true;
+    const long long t0 = clock64();
+    for (int it = 1;; ++it) {
+        if (mbar_try_wait(b, parity)) return true;
+        if ((it & 63) == 0 && clock64() - t0 > kWaitCycles) {
+            atomicOr(&ctl->err, ERR_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+template <typename V>
+constexpr size_t spmv_smem()
+{
+    return (size_t)SpmvStages<V>::n * kRoundEntries * (sizeof(int) + sizeof(V));
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* __restrict__ pB)
+{
+    constexpr int S = SpmvStages<V>::n;
+    __shared__ double sh[kBlock * kMaxRed];
+    __shared__ int s_last;
+    __shared__ __align__(16) SysDev sS;
+    __shared__ __align__(8) unsigned long long full[S];
+    extern __shared__ __align__(128) unsigned char dyn[];
+    int* st_col = reinterpret_cast<int*>(dyn);
+    V* st_val = reinterpret_cast<V*>(dyn + sizeof(int) * S * kRoundEntries);
+    const Batch B = *pB;
+    Ctl* ctl = B.ctl;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < S; ++k) mbar_init(&full[k], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned parity = 0;   // bit k: parity of stage k's next completion (same in every thread)
+    int cur = -1, lcur = -1;
+    bool live = false;
+    for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
+        const int2 sg = B.nsys == 1 ? make_int2(0, g) : B.segs[g];
+        if (sg.x != lcur) {
+            lcur = sg.x;
+            if (sg.x != cur) {
+                cur = sg.x;
+                load_sys(&sS, B.sys + cur);
+            }
+            live = system_live<OP_SPMV_QP>(sS);
+        }
+        if (!live) continue;
+        const unsigned T = (unsigned)sS.ntiles, G = (unsigned)red_segments(sS.ntiles);
+        const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
+        const int R = (t1 - t0) * 4;
+        const int* __restrict__ sptr = sS.a_sptr;
+        const int* __restrict__ acol = sS.a_col;
+        const V* __restrict__ aval = VP<V>::aval(sS, false);
+        const V* __restrict__ dg = VP<V>::diag(sS);
+        const V* __restrict__ p = VP<V>::v(sS).p;
+        V* __restrict__ q = VP<V>::v(sS).q;
+        // round r: slices sb .. sb+7 with sb = 32 (t0 + r/4) + 8 (r%4), into stage r % S
+        auto issue = [&](int r) {
+            const int sb = 32 * (t0 + (r >> 2)) + 8 * (r & 3);
+            const int e0 = __ldg(sptr + sb), cnt = __ldg(sptr + sb + 8) - e0;
+            const int stg = r % S;
+            if (cnt > 0 && cnt <= kRoundEntries) {
+                mbar_expect_tx(&full[stg], (unsigned)cnt * (unsigned)(sizeof(int) + sizeof(V)));
+                bulk_to_smem(st_col + stg * kRoundEntries, acol + e0, (unsigned)cnt * sizeof(int), &full[stg]);
+                bulk_to_smem(st_val + stg * kRoundEntries, aval + e0, (unsigned)cnt * sizeof(V), &full[stg]);
+            } else {
+                mbar_expect_tx(&full[stg], 0u);
+            }
+        };
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            for (int r = 0; r < S - 1 && r < R; ++r) issue(r);
+        }
+        double acc[kMaxRed] = {0.0, 0.0};
+        bool ok = true;
+        for (int r = 0; r < R; ++r) {
+            const int stg = r % S;
+            if (tid == 0 && r + S - 1 < R) issue(r + S - 1);
+            if (!mbar_wait(&full[stg], (parity >> stg) & 1u, ctl)) {
+                ok = false;
+                break;
+            }
+            parity ^= 1u << stg;
+            const int sb = 32 * (t0 + (r >> 2)) + 8 * (r & 3);
+            const int sl = sb + wid;
+            const int base = __ldg(sptr + sb);
+            const bool staged = __ldg(sptr + sb + 8) - base <= kRoundEntries;
+            const int e0 = __ldg(sptr + sl), W = (__ldg(sptr + sl + 1) - e0) >> 5;
+            const int i = sl * 32 + lane;
+            const V xi = __ldca(p + i);
+            V y = vmul(__ldg(dg + i), xi);
+            const int* __restrict__ c = staged ? st_col + stg * kRoundEntries + (e0 - base) + lane : acol + e0 + lane;
+            const V* __restrict__ a = staged ? st_val + stg * kRoundEntries + (e0 - base) + lane : aval + e0 + lane;
+            if (W <= kMaxW) {
+                int ck[kMaxW];
+                V av[kMaxW], xv[kMaxW];
+#pragma unroll
+                for (int k = 0; k < kMaxW; ++k) ck[k] = k < W ? c[k * 32] : -1;
+#pragma unroll
+                for (int k = 0; k < kMaxW; ++k) {
+                    av[k] = ck[k] >= 0 ? a[k * 32] : V(0);
+                    xv[k] = ck[k] >= 0 ? __ldca(p + ck[k]) : V(0);
+                }
+#pragma unroll
+                for (int k = 0; k < kMaxW; ++k)
+                    if (ck[k] >= 0) y = vfma(av[k], xv[k], y);
+            } else {
+                for (int k = 0; k < W; ++k) {
+                    const int cc = c[k * 32];
+                    if (cc >= 0) y = vfma(a[k * 32], __ldca(p + cc), y);
+                }
+            }
+            q[i] = y;
+            acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
+            __syncthreads();   // this round's stage is free for round r + S
+            if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        if (!ok) {
+            // let the copies already issued land before the CTA leaves
+            if (tid == 0)
+                for (int k = 0; k < S; ++k) mbar_wait(&full[k], (parity >> k) & 1u, ctl);
+            __syncthreads();
+            return;
+        }
+        flush_segment<OP_SPMV_QP>(B, sS, sg.y, t1 - t0, acc, sh, &s_last);
+    }
+}
+
 // CTAs of a persistent launch: one wave of kMinCtas CTAs per SM.
 static int g_grid_cap = 152 * kMinCtas;
 
@@ -1010,6 +1195,12 @@ void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
     int grid = OpTraits<OP>::kRed ? nsegs : ntiles;
     grid = grid < g_grid_cap ? grid : g_grid_cap;
     if (grid < 1) grid = 1;
+    if constexpr (OP == OP_SPMV_QP) {
+        if (!pb) {
+            k_spmv_staged<V><<<grid, kBlock, spmv_smem<V>(), st>>>(dB);
+            return;
+        }
+    }
     if (pb)
         k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(dB);
     else
@@ -1549,7 +1740,15 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __res
 // ---------------------------------------------------------------- launchers
 static std::atomic<unsigned long long> g_launches{0};
 unsigned long long launch_count() { return g_launches.load(); }
-void set_device_sms(int nsm) { g_grid_cap = (nsm > 0 ? nsm : 152) * kMinCtas; }
+void set_device_sms(int nsm)
+{
+    g_grid_cap = (nsm > 0 ? nsm : 152) * kMinCtas;
+    // the staged SpMV's stages exceed the default dynamic shared memory
+    // limit; set once per device, outside any stream capture
+    cudaFuncSetAttribute(k_spmv_staged<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_smem<float>());
+    cudaFuncSetAttribute(k_spmv_staged<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)spmv_smem<double>());
+}
 int persistent_grid() { return g_grid_cap; }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }
 

@@ -856,6 +856,10 @@ struct OpTraits {
     // Values reduced: only the initial residual needs two (normFactor and
     // sum|r|).  Every tree level costs one FP64 add per thread per value.
     static constexpr int kNR = OP == OP_INIT_RES ? 2 : 1;
+    // four consecutive rows per thread, no gathers: worth interleaving tiles
+    static constexpr bool kElem = (OP == OP_SUMX || OP == OP_RHO || OP == OP_PUPDATE || OP == OP_UPDATE ||
+                                   OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE || OP == OP_TO32 ||
+                                   OP == OP_CORRECT || OP == OP_KEEPBEST);
 };
 
 template <RowOp OP>
@@ -952,6 +956,8 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
     int lcur = -1;
     bool live = false;
     if constexpr (!OpTraits<OP>::kRed) {
+        // element-wise ops: two tiles per step when both belong to the same
+        // system, so one tile's loads are in flight while the other computes
         for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
             const int2 tl = B.nsys == 1 ? make_int2(0, t) : B.tiles[t];
             if (tl.x != lcur) {
@@ -964,6 +970,15 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             }
             if (!live) continue;
             double acc[kMaxRed] = {0.0, 0.0};
+            if constexpr (OpTraits<OP>::kElem) {
+                const int t2 = t + gridDim.x;
+                if (B.nsys == 1 && t2 < B.ntiles) {
+                    tile_body<V, OP, PB>(B, sS, tl.y * kTileRows, acc);
+                    tile_body<V, OP, PB>(B, sS, t2 * kTileRows, acc);
+                    t = t2;
+                    continue;
+                }
+            }
             tile_body<V, OP, PB>(B, sS, tl.y * kTileRows, acc);
         }
     } else {
@@ -981,7 +996,16 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             const unsigned T = (unsigned)sS.ntiles, G = (unsigned)red_segments(sS.ntiles);
             const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
-            for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+            if constexpr (OpTraits<OP>::kElem) {
+                int t = t0;
+                for (; t + 1 < t1; t += 2) {   // same order, two tiles' loads in flight
+                    tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+                    tile_body<V, OP, PB>(B, sS, (t + 1) * kTileRows, acc);
+                }
+                if (t < t1) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+            } else {
+                for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+            }
             flush_segment<OP>(B, sS, sg.y, t1 - t0, acc, sh, s_last);
         }
     }

@@ -302,12 +302,12 @@ def run_served(args, ctx, mrgpu):
                    x0=pinned(st.x0)) for st in seq] for seq in steps]
     reqs = [(i, steps[i][k], ms[i][1]) for k in range(args.served_steps) for i in range(len(ms))]
     arrivals = np.cumsum(np.random.default_rng(SEED + 11).exponential(1.0 / args.served_rate, len(reqs)))
-    out = {"requests": len(reqs), "meshes": len(ms), "rate_per_s": args.served_rate,
+    out = {"requests": len(reqs), "meshes": len(ms), "rate_per_s": args.served_rate, "iters_per_launch": args.served_k,
            "cells_mean": float(np.mean([s.n for s, _ in ms])), "asym_meshes": int(sum(a for _, a in ms)),
            "hbm_budget_gb": 150}
     for name, prec, order in (("mixed", "mixed", "colour"), ("plain_fp64", "fp64", "exact")):
         kw = dict(tol=TOL, max_iter=20000, precision=prec, ordering=order, inner_rel_tol=args.inner_tol,
-                  iters_per_launch=8)
+                  iters_per_launch=args.served_k)
         srv = mrgpu.Server(ctx, mrgpu.controls(solver="PCG", precond="DIC", **kw),
                            mrgpu.controls(solver="PBiCG", precond="DILU", **kw), hbm_budget=150 * 2**30)
         ids = []
@@ -516,6 +516,7 @@ def main():
     ap.add_argument("--served-meshes", type=int, default=24, help="meshes of the served configuration (0: skip)")
     ap.add_argument("--served-steps", type=int, default=8)
     ap.add_argument("--served-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--served-k", type=int, default=8, help="server: Krylov iterations per launch")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

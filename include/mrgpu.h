@@ -217,6 +217,26 @@ int mrg_ggi_destroy(mrg_ggi* ggi);
 int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp);
 int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst,
                          int ncomp);
+/* GGIInterpolation's weight construction (the interpolator
+ * ggiInterfaceToInterfaceMapping.C:62-77 builds with rescale on and SMALL
+ * non-overlap tolerances, rebuilt every interpolatorUpdateFrequency steps of
+ * a moving interface, regionInterfaceType.C:489-510) on the device, for
+ * planar patches: face f of A has vertices a_xy[2*a_ptr[f] .. 2*a_ptr[f+1])
+ * (x, y pairs, counter-clockwise, 3 to 32 vertices, a_ptr[0] = 0); likewise
+ * B.  weight = |A_i intersect B_j| / |receiving face|, rescaled so that each
+ * covered face's weights sum to one; overlaps <= tol * min(|A_i|, |B_j|)
+ * are dropped (foam's SMALL: 1e-15).  Returns the two directions as GGI
+ * objects: a_from_b (A faces from B values, rows ascending B face) and
+ * b_from_a.  MRG_E_INVALID for bad faces or an A face that meets more than
+ * 256 B faces' bounding boxes. */
+int mrg_ggi_build(mrg_ctx* ctx, int na, const int32_t* a_ptr, const double* a_xy,
+                  int nb, const int32_t* b_ptr, const double* b_xy, double tol,
+                  mrg_ggi** a_from_b, mrg_ggi** b_from_a);
+/* Sizes (any of the pointers may be NULL) and, when row_ptr / src_addr /
+ * weights are non-NULL, the GGI's CSR copied to the host (n_dst + 1,
+ * nnz, nnz entries). */
+int mrg_ggi_get(mrg_ggi* ggi, int* n_dst, int* n_src, int* nnz, int32_t* row_ptr,
+                int32_t* src_addr, double* weights);
 
 /* ---- batched solves ----------------------------------------------------
  * Many independent systems (meshes with their current coefficients) solved

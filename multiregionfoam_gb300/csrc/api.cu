@@ -13,6 +13,7 @@
 #include "engine.h"
 #include "kernels.h"
 #include "dn.h"
+#include "ggi_build.h"
 #include "noalloc.h"
 #include "server.h"
 
@@ -443,6 +444,53 @@ int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst, int n
         launch_ggi(g.n_dst, g.ptr, g.addr, g.w, d_src, d_dst, ncomp, g.ctx->st);
         MRG_CUDA(cudaGetLastError());
         MRG_CUDA(cudaStreamSynchronize(g.ctx->st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_build(mrg_ctx* ctx, int na, const int32_t* a_ptr, const double* a_xy, int nb, const int32_t* b_ptr,
+                  const double* b_xy, double tol, mrg_ggi** a_from_b, mrg_ggi** b_from_a)
+{
+    return guard([&] {
+        if (!ctx || !a_from_b || !b_from_a || na < 0 || nb < 0 || !a_ptr || !b_ptr || !(tol >= 0.0))
+            return fail(MRG_E_INVALID, "bad argument");
+        *a_from_b = nullptr;
+        *b_from_a = nullptr;
+        auto* ab = new mrg_ggi();
+        auto* ba = new mrg_ggi();
+        try {
+            ggi_build(&ctx->c, na, a_ptr, a_xy, nb, b_ptr, b_xy, tol, ab->g, ba->g);
+        } catch (...) {
+            delete ab;
+            delete ba;
+            throw;
+        }
+        *a_from_b = ab;
+        *b_from_a = ba;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_get(mrg_ggi* ggi, int* n_dst, int* n_src, int* nnz, int32_t* row_ptr, int32_t* src_addr,
+                double* weights)
+{
+    return guard([&] {
+        if (!ggi) return fail(MRG_E_INVALID, "bad argument");
+        Ggi& g = ggi->g;
+        Ctx* c = g.ctx;
+        int32_t total = 0;
+        MRG_CUDA(cudaMemcpyAsync(&total, g.ptr + g.n_dst, 4, cudaMemcpyDeviceToHost, c->st));
+        MRG_CUDA(cudaStreamSynchronize(c->st));
+        if (n_dst) *n_dst = g.n_dst;
+        if (n_src) *n_src = g.n_src;
+        if (nnz) *nnz = total;
+        if (row_ptr)
+            MRG_CUDA(cudaMemcpyAsync(row_ptr, g.ptr, 4 * (size_t)(g.n_dst + 1), cudaMemcpyDeviceToHost, c->st));
+        if (src_addr && total)
+            MRG_CUDA(cudaMemcpyAsync(src_addr, g.addr, 4 * (size_t)total, cudaMemcpyDeviceToHost, c->st));
+        if (weights && total)
+            MRG_CUDA(cudaMemcpyAsync(weights, g.w, 8 * (size_t)total, cudaMemcpyDeviceToHost, c->st));
+        MRG_CUDA(cudaStreamSynchronize(c->st));
         return (int)MRG_OK;
     });
 }

@@ -25,7 +25,7 @@ EXPORTED = [
     "mrg_ctx_mem_used", "mrg_host_alloc", "mrg_host_free", "mrg_mesh_upload", "mrg_mesh_destroy",
     "mrg_mesh_levels", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
     "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
-    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
+    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_ggi_build", "mrg_ggi_get", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
     "mrg_residual_noalloc", "mrg_server_create", "mrg_server_destroy", "mrg_server_submit", "mrg_server_poll",
@@ -125,6 +125,9 @@ def load(path: str = LIB_PATH):
     L.mrg_ggi_destroy.argtypes = [vp]
     L.mrg_ggi_apply.argtypes = [vp, dp, dp, C.c_int]
     L.mrg_ggi_apply_device.argtypes = [vp, vp, vp, C.c_int]
+    L.mrg_ggi_build.argtypes = [vp, C.c_int, ip, dp, C.c_int, ip, dp, C.c_double, C.POINTER(vp), C.POINTER(vp)]
+    ipp = C.POINTER(C.c_int)
+    L.mrg_ggi_get.argtypes = [vp, ipp, ipp, ipp, ip, ip, dp]
     L.mrg_dev_alloc.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
     L.mrg_dev_free.argtypes = [vp, vp]
     L.mrg_dev_copy.argtypes = [vp, vp, vp, C.c_size_t, C.c_int]
@@ -431,6 +434,38 @@ class Ggi:
         _check(load().mrg_ggi_create(ctx.h, self.n_dst, self.n_src, _i(self._ptr), _i(self._addr), _d(self._w),
                                      C.byref(h)))
         self.h = h
+
+    @classmethod
+    def build(cls, ctx: Context, fa_ptr, fa_xy, fb_ptr, fb_xy, tol=1e-15):
+        """Overlap weights of two planar patches built on the device
+        (mrg_ggi_build).  Faces: CSR vertex pointers and (x, y) vertices,
+        counter-clockwise.  Returns (a_from_b, b_from_a)."""
+        pa = np.ascontiguousarray(fa_ptr, dtype=np.int32)
+        xa = np.ascontiguousarray(fa_xy, dtype=np.float64)
+        pb = np.ascontiguousarray(fb_ptr, dtype=np.int32)
+        xb = np.ascontiguousarray(fb_xy, dtype=np.float64)
+        ha, hb = C.c_void_p(), C.c_void_p()
+        _check(load().mrg_ggi_build(ctx.h, len(pa) - 1, _i(pa), _d(xa), len(pb) - 1, _i(pb), _d(xb), float(tol),
+                                    C.byref(ha), C.byref(hb)))
+        out = []
+        for h in (ha, hb):
+            g = cls.__new__(cls)
+            g.h = h
+            nd, ns = C.c_int(), C.c_int()
+            _check(load().mrg_ggi_get(h, C.byref(nd), C.byref(ns), None, None, None, None))
+            g.n_dst, g.n_src = nd.value, ns.value
+            out.append(g)
+        return out[0], out[1]
+
+    def csr(self):
+        """The weights as (row_ptr, src_addr, w) host arrays."""
+        nnz = C.c_int()
+        _check(load().mrg_ggi_get(self.h, None, None, C.byref(nnz), None, None, None))
+        ptr = np.empty(self.n_dst + 1, np.int32)
+        addr = np.empty(max(nnz.value, 1), np.int32)
+        w = np.empty(max(nnz.value, 1))
+        _check(load().mrg_ggi_get(self.h, None, None, None, _i(ptr), _i(addr), _d(w)))
+        return ptr, addr[:nnz.value], w[:nnz.value]
 
     def apply(self, src, ncomp=1):
         src = np.ascontiguousarray(src, dtype=np.float64)

@@ -2,8 +2,8 @@
  * mrgpu.h -- C ABI of the GB300 coupled-region LDU solver library (libmrgpu).
  *
  * This is the boundary a foam-extend 4.1 build of multiRegionFoam calls
- * through: the lduMatrix::solver adapters (gpuPCG, gpuPBiCG, gpuMixedPCG,
- * gpuMixedPBiCG) and the GGI transfer adapter hand plain host or device
+ * through: the lduMatrix::solver adapters (gpuPCG, gpuPBiCG, gpuBiCGStab and
+ * their gpuMixed* forms) and the GGI transfer adapter hand plain host or device
  * pointers and sizes to these functions.  No C++ or torch types cross it.
  *
  * Conventions
@@ -43,7 +43,13 @@ enum {
 };
 
 /* ---- solver selection (the fvSolution "solver" / "preconditioner" words) */
-enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1 };
+/* BiCGStab: the stabilised bi-conjugate gradient foam-extend's lduSolvers
+ * register as "BiCGStab" for both matrix kinds, and the solver of the
+ * reference tutorials' monolithic coupled matrices (system/solid/fvSolution
+ * Tcoupled: BiCGStab, tolerance 1e-15, maxIter 200).  Preconditioned on the
+ * right (van der Vorst 1992): one M^-1 p and one M^-1 s per iteration, the
+ * residual of s tested after the first half step. */
+enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2 };
 enum {
     MRG_PRECOND_NONE = 0,     /* "none"     */
     MRG_PRECOND_DIAGONAL = 1, /* "diagonal" */
@@ -176,8 +182,8 @@ int mrg_coeffs_upload_device(mrg_mesh* mesh, const double* diag,
                              const double* iface_int_or_null);
 
 /* ---- solve ------------------------------------------------------------
- * lduMatrix::solver::solve(psi, source, cmpt) of foam's PCG / PBiCG with the
- * DIC / DILU / diagonal / none preconditioners
+ * lduMatrix::solver::solve(psi, source, cmpt) of foam's PCG / PBiCG /
+ * BiCGStab with the DIC / DILU / diagonal / none preconditioners
  * (called from multiRegionSystem.C:150-153 via coupledFvMatrix::solve and
  * :293 via fvMatrix::solve).  b and x_inout are host arrays of n_cells in
  * the caller's numbering; perf may be NULL. */
@@ -356,8 +362,9 @@ typedef struct {
     int running, queued, peak_running, reserved;
     size_t inflight_bytes, peak_inflight_bytes;
 } mrg_server_stats;
-/* sym_controls: PCG requests (preconditioner/precision/ordering/tolerance);
- * asym_controls: PBiCG requests, or NULL to refuse them.  hbm_budget: bytes
+/* sym_controls: symmetric requests (PCG or BiCGStab, with preconditioner /
+ * precision / ordering / tolerance); asym_controls: asymmetric requests
+ * (PBiCG or BiCGStab), or NULL to refuse them.  hbm_budget: bytes
  * of in-flight working sets (0 = only the context's budget); max_active:
  * members per running batch (0 = 256). */
 int mrg_server_create(mrg_ctx* ctx, const mrg_controls* sym_controls,

@@ -90,7 +90,7 @@ Controls to_controls(const mrg_controls* c)
     k.inner_max_iter = c->inner_max_iter;
     k.max_outer = c->max_outer > 0 ? c->max_outer : 50;
     k.k_launch = c->iters_per_launch > 0 ? c->iters_per_launch : 16;
-    if (k.solver < 0 || k.solver > 1) throw Error(MRG_E_INVALID, "unknown solver");
+    if (k.solver < 0 || k.solver > 2) throw Error(MRG_E_INVALID, "unknown solver");
     if (k.pc < 0 || k.pc > 3) throw Error(MRG_E_INVALID, "unknown preconditioner");
     if (k.precision < 0 || k.precision > 1) throw Error(MRG_E_INVALID, "unknown precision");
     if (k.ordering < 0 || k.ordering > 1) throw Error(MRG_E_INVALID, "unknown ordering");

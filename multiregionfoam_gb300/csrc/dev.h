@@ -33,6 +33,7 @@ __host__ __device__ inline int red_segments(int tiles)
 // the FP64 outer state of a mixed-precision solve.
 struct Scal {
     double rho, rho_old, alpha, beta;
+    double omega;          // BiCGStab: (t, s) / (t, t) of the current iteration
     double nfac, res0, res, xsum;
     double tol, rel_tol;
     double red[kMaxRed];   // last finalised reduction sums (diagnostics)
@@ -54,10 +55,15 @@ struct Scal {
     int pad;
 };
 
+// PCG / PBiCG use the slots by name (T = the transpose system).  BiCGStab
+// keeps r (and s) in r, the shadow residual r~ in rT, the search direction
+// in wT, M^-1 p in p and M^-1 s in pT (both SpMV inputs, so both carry the
+// GGI tail), v = A M^-1 p in q and t = A M^-1 s in qT; y and yT are the
+// triangular sweeps' intermediates.
 template <typename V>
 struct Vecs {
     V *x, *b, *r, *w, *y, *p, *q;   // A-system vectors (x,p carry the GGI tail)
-    V *rT, *wT, *yT, *pT, *qT;      // transpose system (PBiCG)
+    V *rT, *wT, *yT, *pT, *qT;      // transpose system (PBiCG; pT carries the GGI tail)
 };
 
 // Which preconditioner the sweeps apply.

@@ -351,7 +351,7 @@ static bool ensure_views(Mesh& m, PlanState& P, const Controls& cfg)
     const size_t np = (size_t)S.npad, nx = (size_t)S.npad + S.ngen;
     const bool asym = !m.sym || m.has_int;
     const bool need32 = cfg.precision == MRG_PRECISION_MIXED;
-    const bool needT = cfg.solver == MRG_SOLVER_PBICG;
+    const bool needT = cfg.solver != MRG_SOLVER_PCG;   // PBiCG's transpose system, BiCGStab's extra vectors
     bool changed = false;
     auto setp = [&](auto& field, auto value) {
         if (field != value) {
@@ -474,6 +474,8 @@ PlanState& prepare(Mesh& m, const Controls& cfg)
 }
 
 // ------------------------------------------------------------------ graphs
+// trans: the sweeps' vector set (0 = r -> w, 1 = the transpose system,
+// 2 / 3 = BiCGStab's M^-1 p / M^-1 s).
 static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, int trans, cudaStream_t st)
 {
     Ctx* c = bh.ctx;
@@ -499,8 +501,30 @@ static bool any_general_iface(const BatchHost& bh)
     return false;
 }
 
+// One BiCGStab iteration: p, M^-1 p, v = A M^-1 p (alpha), s and the
+// half-step test, M^-1 s, t = A M^-1 s (omega), x and r.  A diagonal or no
+// preconditioner is applied inside the p and s updates.
+static void record_iteration_bs(BatchHost& bh, const Controls& cfg, int prec, cudaStream_t st)
+{
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    const bool gen = any_general_iface(bh);
+    launch_rows(OP_BS_P, prec, bh.d, nt, ns, 0, st);
+    if (cfg.pc >= PC_DIC) record_precondition(bh, cfg, prec, 2, st);
+    if (gen) launch_iface_gather(prec, 0, bh.d, 64, st);
+    launch_rows(OP_BS_V, prec, bh.d, nt, ns, 0, st);
+    launch_rows(OP_BS_S, prec, bh.d, nt, ns, 0, st);
+    if (cfg.pc >= PC_DIC) record_precondition(bh, cfg, prec, 3, st);
+    if (gen) launch_iface_gather(prec, 2, bh.d, 64, st);
+    launch_rows(OP_BS_T, prec, bh.d, nt, ns, 0, st);
+    launch_rows(OP_BS_XR, prec, bh.d, nt, ns, 0, st);
+}
+
 static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaStream_t st)
 {
+    if (cfg.solver == MRG_SOLVER_BICGSTAB) {
+        record_iteration_bs(bh, cfg, prec, st);
+        return;
+    }
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     if (cfg.pc >= PC_DIC) {
@@ -525,9 +549,10 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
 // record_iteration captured in one graph (the default: measured faster on
 // GB300, a kernel boundary inside a graph costs about what a grid barrier
 // does), or one persistent cooperative kernel whose phases are those
-// launches (MRG_ITERATION=persistent).  Both give the same bits.
-static bool persistent_iteration(const BatchHost& bh)
+// launches (MRG_ITERATION=persistent; PCG and PBiCG).  Both give the same bits.
+static bool persistent_iteration(const BatchHost& bh, const Controls& cfg)
 {
+    if (cfg.solver == MRG_SOLVER_BICGSTAB) return false;
     static int env = -1;
     if (env < 0) {
         const char* e = std::getenv("MRG_ITERATION");
@@ -552,7 +577,7 @@ static void record_persistent(BatchHost& bh, const Controls& cfg, int prec, int 
 // refuses to capture is launched directly instead (exec stays null).
 static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int prec, int k)
 {
-    const bool pers = persistent_iteration(bh);
+    const bool pers = persistent_iteration(bh, cfg);
     const int cap = persistent_grid();
     const int g_rows = std::min(std::max(bh.h.ntiles, 1), cap), g_red = std::min(std::max(bh.h.nsegs, 1), cap);
     const int div = std::max(1, bh.tune.sweep_div);
@@ -650,9 +675,9 @@ static void write_ctl_controls(BatchHost& bh, const Controls& cfg)
     host.inner_rel_tol = cfg.inner_rel_tol;
     host.min_iter = cfg.min_iter;
     host.max_iter = cfg.max_iter;
-    // FP32 BiCG restarts from the FP64 residual every 150 iterations unless
-    // told otherwise: its unstabilised recurrence can drift in FP32
-    const int auto_inner = cfg.solver == MRG_SOLVER_PBICG ? std::min(cfg.max_iter, 150) : cfg.max_iter;
+    // FP32 BiCG and BiCGStab restart from the FP64 residual every 150
+    // iterations unless told otherwise: their short recurrences drift in FP32
+    const int auto_inner = cfg.solver != MRG_SOLVER_PCG ? std::min(cfg.max_iter, 150) : cfg.max_iter;
     host.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : auto_inner;
     host.max_outer = cfg.max_outer;
     host.mixed = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
@@ -689,11 +714,21 @@ Perf perf_of(const Scal& q, int precision)
     return p;
 }
 
+// Start of a Krylov loop (after the initial residual, the step into FP32 or
+// the FP64 restart of a stalled refinement): BiCGStab's shadow residual and
+// first rho, for the members that iterate.
+static void krylov_start(BatchHost& bh, const Controls& cfg, int prec)
+{
+    if (cfg.solver == MRG_SOLVER_BICGSTAB)
+        launch_rows(OP_BS_RHO0, prec, bh.d, bh.h.ntiles, bh.h.nsegs, 0, bh.ctx->st);
+}
+
 std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
 {
     Ctx* c = bh.ctx;
     cudaStream_t st = c->st;
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int tsys = cfg.solver != MRG_SOLVER_PCG;   // T vectors: sentinels armed, r copied into FP32
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     const bool gen = any_general_iface(bh);
     Ctl* h = pinned_ctl();
@@ -705,12 +740,13 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
         MRG_CUDA(cudaEventRecord(e0, st));
         write_ctl_controls(bh, cfg);
         launch_rows(OP_PERMUTE_IN, 0, bh.d, nt, ns, 0, st);
-        launch_rows(OP_BEGIN, 0, bh.d, nt, ns, pb, st);
+        launch_rows(OP_BEGIN, 0, bh.d, nt, ns, tsys, st);
         if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
         launch_rows(OP_SUMX, 0, bh.d, nt, ns, 0, st);
         launch_rows(OP_INIT_RES, 0, bh.d, nt, ns, pb, st);
         MRG_CUDA(cudaGetLastError());
         if (cfg.precision == MRG_PRECISION_FP64) {
+            krylov_start(bh, cfg, 0);
             run_iterations(bh, cfg, 0, cfg.max_iter + cfg.min_iter, h);
         } else {
             for (int outer = 0; outer <= cfg.max_outer + 1; ++outer) {
@@ -719,13 +755,15 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
                 launch_rows(OP_KEEPBEST, 0, bh.d, nt, ns, 0, st);
                 poll(bh, h);
                 if (h->n_oactive == 0) break;
-                launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
+                launch_rows(OP_TO32, 0, bh.d, nt, ns, tsys, st);
+                krylov_start(bh, cfg, 1);
                 run_iterations(bh, cfg, 1, cfg.max_iter, h);
                 launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
             }
             // members whose refinement stalled finish with FP64 Krylov
             if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
             launch_rows(OP_FALLBACK64, 0, bh.d, nt, ns, pb, st);
+            krylov_start(bh, cfg, 0);
             poll(bh, h);
             if (h->n_active > 0) {
                 run_iterations(bh, cfg, 0, cfg.max_iter, h);
@@ -778,11 +816,12 @@ void batch_begin(BatchHost& bh, const Controls& cfg)
 {
     cudaStream_t st = bh.ctx->st;
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int tsys = cfg.solver != MRG_SOLVER_PCG;
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     const bool gen = any_general_iface(bh);
     write_ctl_controls(bh, cfg);
     launch_rows(OP_PERMUTE_IN, 0, bh.d, nt, ns, 0, st);
-    launch_rows(OP_BEGIN, 0, bh.d, nt, ns, pb, st);
+    launch_rows(OP_BEGIN, 0, bh.d, nt, ns, tsys, st);
     if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
     launch_rows(OP_SUMX, 0, bh.d, nt, ns, 0, st);
     launch_rows(OP_INIT_RES, 0, bh.d, nt, ns, pb, st);
@@ -790,7 +829,10 @@ void batch_begin(BatchHost& bh, const Controls& cfg)
         if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
         launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
         launch_rows(OP_KEEPBEST, 0, bh.d, nt, ns, 0, st);
-        launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
+        launch_rows(OP_TO32, 0, bh.d, nt, ns, tsys, st);
+        krylov_start(bh, cfg, 1);
+    } else {
+        krylov_start(bh, cfg, 0);
     }
     MRG_CUDA(cudaGetLastError());
 }
@@ -799,6 +841,7 @@ void batch_fallback(BatchHost& bh, const Controls& cfg)
 {
     if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, bh.ctx->st);
     launch_rows(OP_FALLBACK64, 0, bh.d, bh.h.ntiles, bh.h.nsegs, cfg.solver == MRG_SOLVER_PBICG, bh.ctx->st);
+    krylov_start(bh, cfg, 0);
     MRG_CUDA(cudaGetLastError());
 }
 
@@ -812,13 +855,14 @@ void batch_iterate(BatchHost& bh, const Controls& cfg, int prec)
 void batch_outer(BatchHost& bh, const Controls& cfg)
 {
     cudaStream_t st = bh.ctx->st;
-    const int pb = cfg.solver == MRG_SOLVER_PBICG;
+    const int tsys = cfg.solver != MRG_SOLVER_PCG;
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
     if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, st);
     launch_rows(OP_RESID64, 0, bh.d, nt, ns, 0, st);
     launch_rows(OP_KEEPBEST, 0, bh.d, nt, ns, 0, st);
-    launch_rows(OP_TO32, 0, bh.d, nt, ns, pb, st);
+    launch_rows(OP_TO32, 0, bh.d, nt, ns, tsys, st);
+    krylov_start(bh, cfg, 1);
     MRG_CUDA(cudaGetLastError());
 }
 
@@ -866,6 +910,7 @@ Tuning tune_batch(BatchHost& bh, const Controls& cfg)
         for (int k : {4, 16})
             for (int div : {4, 8, 16}) {
                 if (!levels && div != 8) continue;
+                if (mode == 1 && cfg.solver == MRG_SOLVER_BICGSTAB) continue;   // no persistent form
                 Tuning t;
                 t.mode = mode;
                 t.k = k;

@@ -462,6 +462,56 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
         set_active(ctl, sc, sums[0] > 0.0 ? 1 : 0);
         break;
     }
+    case OP_BS_RHO0:
+        // BiCGStab start: rho = (r~, r) with r~ = r; a zero rho cannot start
+        sc->rho = sums[0];
+        sc->rho_old = sums[0];
+        if (fabs(sums[0]) < 1.0e-300) {
+            sc->singular = 1;
+            set_active(ctl, sc, 0);
+        }
+        break;
+    case OP_BS_V:
+        if (fabs(sums[0]) / sc->nfac < 1.0e-300) {
+            sc->singular = 1;
+            sc->alpha = 0.0;
+            set_active(ctl, sc, 0);
+        } else {
+            sc->alpha = sc->rho / sums[0];
+        }
+        break;
+    case OP_BS_S: {
+        // half step: when s already meets the tolerance, x + alpha M^-1 p
+        // is the solution and the iteration ends here
+        const double res = sums[0] / sc->nfac;
+        const bool conv = res < sc->tol || (sc->rel_tol > 1.0e-20 && res < sc->rel_tol * sc->res0);
+        if (conv && sc->iter + 1 >= sc->kmin) {
+            sc->res = res;
+            sc->iter += 1;
+            sc->converged = 1;
+            set_active(ctl, sc, 0);
+        }
+        break;
+    }
+    case OP_BS_T:
+        sc->omega = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+        break;
+    case OP_BS_XR: {
+        sc->res = sums[0] / sc->nfac;
+        sc->iter += 1;
+        const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
+        sc->converged = conv;
+        bool more = (sc->iter < sc->kmax && !conv) || sc->iter < sc->kmin;
+        sc->rho_old = sc->rho;
+        sc->rho = sums[1];
+        if (more && (fabs(sc->omega) < 1.0e-300 || fabs(sc->rho) < 1.0e-300)) {
+            sc->singular = 1;   // the recurrence cannot continue
+            more = false;
+        }
+        if (more) sc->beta = (sc->rho / sc->rho_old) * (sc->alpha / sc->omega);
+        if (!more) set_active(ctl, sc, 0);
+        break;
+    }
     default:
         break;
     }
@@ -832,6 +882,111 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             sc->oiter += 1;
             if (sc->iter == 0) set_outer(B.ctl, sc, 0);  // the inner solve made no progress
         }
+    } else if constexpr (OP == OP_BS_RHO0) {
+        // BiCGStab start: shadow residual r~ = r, rho = (r~, r)
+        const Vecs<V>& v = VP<V>::v(S);
+        V r[4];
+        ld4(v.r + r4, r);
+        st4(v.rT + r4, r);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[0] = __fma_rn(widen(r[k]), widen(r[k]), acc[0]);
+    } else if constexpr (OP == OP_BS_P) {
+        // p = r + beta (p - omega v), p = r on the first iteration (into
+        // wT); with a diagonal or no preconditioner M^-1 p goes straight to p
+        const Vecs<V>& v = VP<V>::v(S);
+        V r[4], p[4];
+        ld4(v.r + r4, r);
+        if (S.sc->iter == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) p[k] = r[k];
+        } else {
+            const V beta = (V)S.sc->beta, omega = (V)S.sc->omega;
+            V q[4];
+            ld4w(v.wT + r4, p);
+            ld4(v.q + r4, q);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) p[k] = vfma(beta, vfma(-omega, q[k], p[k]), r[k]);
+        }
+        st4(v.wT + r4, p);
+        if (S.pc == PC_DIAG) {
+            V d[4];
+            ld4(VP<V>::rD(S) + r4, d);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) p[k] = vmul(d[k], p[k]);
+            st4(v.p + r4, p);
+        } else if (S.pc == PC_NONE) {
+            st4(v.p + r4, p);
+        }
+    } else if constexpr (OP == OP_BS_V) {
+        // v = A M^-1 p, (r~, v)
+        const Vecs<V>& v = VP<V>::v(S);
+        const V* __restrict__ rt = v.rT;
+        V* __restrict__ q = v.q;
+        ell_tile<V>(sptr, acol, VP<V>::aval(S, false), VP<V>::diag(S), v.p, sl0, [&](int i, V vi, V) {
+            q[i] = vi;
+            acc[0] = __fma_rn(widen(vi), widen(__ldca(rt + i)), acc[0]);
+        });
+    } else if constexpr (OP == OP_BS_S) {
+        // s = r - alpha v (in r), x += alpha M^-1 p, sum|s|; with a diagonal
+        // or no preconditioner M^-1 s goes straight to pT
+        const Vecs<V>& v = VP<V>::v(S);
+        const V alpha = (V)S.sc->alpha;
+        V x[4], r[4], ph[4], q[4];
+        ld4w(v.x + r4, x);
+        ld4w(v.r + r4, r);
+        ld4(v.p + r4, ph);
+        ld4(v.q + r4, q);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x[k] = vfma(alpha, ph[k], x[k]);
+            r[k] = vfma(-alpha, q[k], r[k]);
+        }
+        st4(v.x + r4, x);
+        st4(v.r + r4, r);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[0] += fabs(widen(r[k]));
+        if (S.pc == PC_DIAG) {
+            V d[4];
+            ld4(VP<V>::rD(S) + r4, d);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) r[k] = vmul(d[k], r[k]);
+            st4(v.pT + r4, r);
+        } else if (S.pc == PC_NONE) {
+            st4(v.pT + r4, r);
+        }
+    } else if constexpr (OP == OP_BS_T) {
+        // t = A M^-1 s, (t, s), (t, t)
+        const Vecs<V>& v = VP<V>::v(S);
+        const V* __restrict__ sv = v.r;
+        V* __restrict__ t = v.qT;
+        ell_tile<V>(sptr, acol, VP<V>::aval(S, false), VP<V>::diag(S), v.pT, sl0, [&](int i, V ti, V) {
+            t[i] = ti;
+            const double tw = widen(ti);
+            acc[0] = __fma_rn(tw, widen(__ldca(sv + i)), acc[0]);
+            acc[1] = __fma_rn(tw, tw, acc[1]);
+        });
+    } else if constexpr (OP == OP_BS_XR) {
+        // x += omega M^-1 s, r = s - omega t, sum|r|, (r~, r)
+        const Vecs<V>& v = VP<V>::v(S);
+        const V omega = (V)S.sc->omega;
+        V x[4], r[4], sh[4], t[4], rt[4];
+        ld4w(v.x + r4, x);
+        ld4w(v.r + r4, r);
+        ld4(v.pT + r4, sh);
+        ld4(v.qT + r4, t);
+        ld4(v.rT + r4, rt);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x[k] = vfma(omega, sh[k], x[k]);
+            r[k] = vfma(-omega, t[k], r[k]);
+        }
+        st4(v.x + r4, x);
+        st4(v.r + r4, r);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            acc[0] += fabs(widen(r[k]));
+            acc[1] = __fma_rn(widen(rt[k]), widen(r[k]), acc[1]);
+        }
     } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
         const double* __restrict__ av = OP == OP_TMUL ? S.aT_val : S.a_val;
         const double* __restrict__ dg = S.diag;
@@ -847,19 +1002,25 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
 template <RowOp OP>
 struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
-                                  OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32 || OP == OP_FALLBACK64);
+                                  OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32 || OP == OP_FALLBACK64 ||
+                                  OP == OP_BS_RHO0 || OP == OP_BS_V || OP == OP_BS_S || OP == OP_BS_T ||
+                                  OP == OP_BS_XR);
     // Krylov-loop ops run only for systems whose loop is active; the
     // refinement ops only for systems whose outer loop is active.
     static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
-                                         OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE);
+                                         OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE ||
+                                         OP == OP_BS_RHO0 || OP == OP_BS_P || OP == OP_BS_V || OP == OP_BS_S ||
+                                         OP == OP_BS_T || OP == OP_BS_XR);
     static constexpr bool kNeedOuter = (OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
-    // Values reduced: only the initial residual needs two (normFactor and
-    // sum|r|).  Every tree level costs one FP64 add per thread per value.
-    static constexpr int kNR = OP == OP_INIT_RES ? 2 : 1;
+    // Values reduced: the initial residual needs two (normFactor and
+    // sum|r|), BiCGStab's t step ((t, s), (t, t)) and its update (sum|r|,
+    // (r~, r)) too.  Every tree level costs one FP64 add per thread per value.
+    static constexpr int kNR = (OP == OP_INIT_RES || OP == OP_BS_T || OP == OP_BS_XR) ? 2 : 1;
     // four consecutive rows per thread, no gathers: worth interleaving tiles
     static constexpr bool kElem = (OP == OP_SUMX || OP == OP_RHO || OP == OP_PUPDATE || OP == OP_UPDATE ||
                                    OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE || OP == OP_TO32 ||
-                                   OP == OP_CORRECT || OP == OP_KEEPBEST);
+                                   OP == OP_CORRECT || OP == OP_KEEPBEST || OP == OP_BS_RHO0 || OP == OP_BS_P ||
+                                   OP == OP_BS_S || OP == OP_BS_XR);
 };
 
 template <RowOp OP>
@@ -1345,19 +1506,25 @@ struct SweepPtrs {
     V* w;
 };
 
+// vs (vector set): 0 = r -> y -> w; 1 = rT -> yT -> wT with the transpose
+// coefficients (PBiCG's preconditionT); BiCGStab: 2 = wT -> y -> p (M^-1 p),
+// 3 = r -> yT -> pT (M^-1 s).
 template <typename V, bool FWD>
-__device__ __forceinline__ SweepPtrs<V> sweep_ptrs(const SysDev& S, bool trans)
+__device__ __forceinline__ SweepPtrs<V> sweep_ptrs(const SysDev& S, int vs)
 {
     const Vecs<V>& v = VP<V>::v(S);
     SweepPtrs<V> P;
     P.cstart = S.chunk_start;
     P.sptr = FWD ? S.f_sptr : S.b_sptr;
     P.col = FWD ? S.f_col : S.b_col;
-    P.coef = FWD ? VP<V>::fc(S, trans) : VP<V>::bc(S, trans);
+    P.coef = FWD ? VP<V>::fc(S, vs == 1) : VP<V>::bc(S, vs == 1);
     P.rD = VP<V>::rD(S);
-    P.r = trans ? v.rT : v.r;
-    P.y = trans ? v.yT : v.y;
-    P.w = trans ? v.wT : v.w;
+    switch (vs) {
+    case 1: P.r = v.rT; P.y = v.yT; P.w = v.wT; break;
+    case 2: P.r = v.wT; P.y = v.y; P.w = v.p; break;
+    case 3: P.r = v.r; P.y = v.yT; P.w = v.pT; break;
+    default: P.r = v.r; P.y = v.y; P.w = v.w; break;
+    }
     return P;
 }
 
@@ -1464,7 +1631,7 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
         const SysDev& S = Ss[s];
         const int nch = S.nchunks;
         if (c >= nch || !S.sc->active || !S.syncfree || S.pc < PC_DIC) continue;
-        const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans != 0);
+        const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans);
         sweep_chunk<V, FWD>(P, FWD ? c : nch - 1 - c, true, ctl, 0, false, false);
     }
     if (lane == 0) {
@@ -1534,7 +1701,7 @@ __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans
                     lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
                     last = L == nl - 1;
                     first = L == 0;
-                    P = sweep_ptrs<V, FWD>(S, trans != 0);
+                    P = sweep_ptrs<V, FWD>(S, trans);
                 }
             }
             if (ok) sweep_rows<V, FWD>(P, r0, r1, e0, W, false, nullptr, lvl0_end, last, first);
@@ -1806,6 +1973,12 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE64(OP_PERMUTE_OUT)
             MRG_CASE64(OP_KEEPBEST)
             MRG_CASE64(OP_FALLBACK64)
+            MRG_CASE64(OP_BS_RHO0)
+            MRG_CASE64(OP_BS_P)
+            MRG_CASE64(OP_BS_V)
+            MRG_CASE64(OP_BS_S)
+            MRG_CASE64(OP_BS_T)
+            MRG_CASE64(OP_BS_XR)
         default: break;
         }
     } else {
@@ -1816,6 +1989,12 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE32(OP_UPDATE)
             MRG_CASE32(OP_PRECOND_DIAG)
             MRG_CASE32(OP_PRECOND_NONE)
+            MRG_CASE32(OP_BS_RHO0)
+            MRG_CASE32(OP_BS_P)
+            MRG_CASE32(OP_BS_V)
+            MRG_CASE32(OP_BS_S)
+            MRG_CASE32(OP_BS_T)
+            MRG_CASE32(OP_BS_XR)
         default: break;
         }
     }

@@ -33,6 +33,12 @@ enum RowOp {
     OP_PERMUTE_OUT,     // x to the caller's numbering (out_x)
     OP_KEEPBEST,        // mixed: after RESID64, keep (x, r) as the best or roll back to it
     OP_FALLBACK64,      // mixed, refinement stalled: FP64 Krylov restart from the best x
+    OP_BS_RHO0,         // BiCGStab start: r~ = r, rho = (r~, r)
+    OP_BS_P,            // BiCGStab: p = r + beta (p - omega v)  [+ M^-1 p when diagonal / none]
+    OP_BS_V,            // BiCGStab: v = A M^-1 p, (r~, v), alpha
+    OP_BS_S,            // BiCGStab: s = r - alpha v, x += alpha M^-1 p, sum|s|, half-step test
+    OP_BS_T,            // BiCGStab: t = A M^-1 s, (t, s), (t, t), omega
+    OP_BS_XR,           // BiCGStab: x += omega M^-1 s, r = s - omega t, sum|r|, (r~, r), convergence
     OP_COUNT
 };
 
@@ -49,7 +55,9 @@ void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st);
 void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st);
 
 // One triangular sweep.  fwd: y = forward(r); else w = backward(y).
-// trans selects DILU's preconditionT coefficients and the T vectors.
+// trans selects the vectors and coefficients (vector set): 0 = r -> y -> w,
+// 1 = rT -> yT -> wT with DILU's preconditionT coefficients, and for
+// BiCGStab 2 = wT -> y -> p (M^-1 p) and 3 = r -> yT -> pT (M^-1 s).
 // syncfree=1: all levels in one launch (exact ordering); else one level.
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
                   cudaStream_t st);

@@ -42,8 +42,10 @@ struct StreamSwap {
 Server::Server(Ctx* ctx, const Controls& sym, const Controls* asym, size_t budget, int max_active)
     : ctx_(ctx), budget_(budget), max_active_(max_active > 0 ? max_active : 256)
 {
-    if (sym.solver != MRG_SOLVER_PCG) throw Error(MRG_E_INVALID, "symmetric controls must select PCG");
-    if (asym && asym->solver != MRG_SOLVER_PBICG) throw Error(MRG_E_INVALID, "asymmetric controls must select PBiCG");
+    if (sym.solver != MRG_SOLVER_PCG && sym.solver != MRG_SOLVER_BICGSTAB)
+        throw Error(MRG_E_INVALID, "symmetric controls must select PCG or BiCGStab");
+    if (asym && asym->solver != MRG_SOLVER_PBICG && asym->solver != MRG_SOLVER_BICGSTAB)
+        throw Error(MRG_E_INVALID, "asymmetric controls must select PBiCG or BiCGStab");
     fam_[0].cfg = sym;
     fam_[0].enabled = true;
     if (asym) {

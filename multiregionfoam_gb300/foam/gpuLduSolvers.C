@@ -1,12 +1,14 @@
 // gpuLduSolvers.C -- foam-extend lduMatrix::solver adapters for libmrgpu.
 //
-// Registers four solver names in foam's run-time selection tables so that an
+// Registers six solver names in foam's run-time selection tables so that an
 // fvSolution entry swaps the GPU solve in with no other change:
 //
-//   gpuPCG         symMatrix   FP64 PCG, preconditioner DIC|FDIC|diagonal|none
-//   gpuPBiCG       asymMatrix  FP64 PBiCG, preconditioner DILU|diagonal|none
-//   gpuMixedPCG    symMatrix   FP32 PCG inside FP64 iterative refinement
-//   gpuMixedPBiCG  asymMatrix  FP32 PBiCG inside FP64 iterative refinement
+//   gpuPCG            symMatrix   FP64 PCG, preconditioner DIC|FDIC|diagonal|none
+//   gpuPBiCG          asymMatrix  FP64 PBiCG, preconditioner DILU|diagonal|none
+//   gpuBiCGStab       both        FP64 BiCGStab, preconditioner DIC|DILU|diagonal|none
+//   gpuMixedPCG       symMatrix   FP32 PCG inside FP64 iterative refinement
+//   gpuMixedPBiCG     asymMatrix  FP32 PBiCG inside FP64 iterative refinement
+//   gpuMixedBiCGStab  both        FP32 BiCGStab inside FP64 iterative refinement
 //
 // Each adapter replaces lduMatrix::solver::solve(psi, source, cmpt) (the call
 // fvMatrix::solve makes at multiRegionSystem.C:293, and coupledFvMatrix's at
@@ -56,10 +58,14 @@ void check(int rc, const char* what)
         throw FatalError(std::string("gpu solver: ") + what + " failed: " + mrg_last_error());
 }
 
+// foam-extend's "Cholesky" (the tutorials' coupled-solve preconditioner) is
+// the incomplete Cholesky factorisation without fill-in: DIC on a symmetric
+// matrix, its LU analogue DILU on an asymmetric one.
 int precondCode(const word& p, bool sym)
 {
     if (p == "DIC" || p == "FDIC") return MRG_PRECOND_DIC;
     if (p == "DILU") return MRG_PRECOND_DILU;
+    if (p == "Cholesky") return sym ? MRG_PRECOND_DIC : MRG_PRECOND_DILU;
     if (p == "diagonal") return MRG_PRECOND_DIAGONAL;
     if (p == "none") return MRG_PRECOND_NONE;
     throw FatalError("gpu solver: unsupported preconditioner " + p + (sym ? " (symmetric)" : " (asymmetric)"));
@@ -138,8 +144,9 @@ public:
         mrg_perf perf;
         check(mrg_solve(mesh, source.data(), psi.data(), &c, &perf), "mrg_solve");
         lduMatrix::solverPerformance out;
-        out.solverName = solverKind_ == MRG_SOLVER_PCG ? (precision_ ? "gpuMixedPCG" : "gpuPCG")
-                                                        : (precision_ ? "gpuMixedPBiCG" : "gpuPBiCG");
+        static const char* const names[2][3] = {{"gpuPCG", "gpuPBiCG", "gpuBiCGStab"},
+                                                 {"gpuMixedPCG", "gpuMixedPBiCG", "gpuMixedBiCGStab"}};
+        out.solverName = names[precision_ ? 1 : 0][solverKind_];
         out.fieldName = fieldName_;
         out.initialResidual = perf.initial_residual;
         out.finalResidual = perf.final_residual;
@@ -167,6 +174,8 @@ MRG_DEFINE_SOLVER(gpuPCG, MRG_SOLVER_PCG, MRG_PRECISION_FP64)
 MRG_DEFINE_SOLVER(gpuPBiCG, MRG_SOLVER_PBICG, MRG_PRECISION_FP64)
 MRG_DEFINE_SOLVER(gpuMixedPCG, MRG_SOLVER_PCG, MRG_PRECISION_MIXED)
 MRG_DEFINE_SOLVER(gpuMixedPBiCG, MRG_SOLVER_PBICG, MRG_PRECISION_MIXED)
+MRG_DEFINE_SOLVER(gpuBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_FP64)
+MRG_DEFINE_SOLVER(gpuMixedBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_MIXED)
 
 // addToRunTimeSelectionTable(lduMatrix::solver, gpuPCG, symMatrix) etc.
 static addSymMatrixSolver<gpuPCG> addGpuPCG("gpuPCG");
@@ -177,5 +186,10 @@ static addAsymMatrixSolver<gpuMixedPBiCG> addGpuMixedPBiCG("gpuMixedPBiCG");
 // tables); so do the GPU variants.
 static addSymMatrixSolver<gpuPBiCG> addGpuPBiCGSym("gpuPBiCG");
 static addSymMatrixSolver<gpuMixedPBiCG> addGpuMixedPBiCGSym("gpuMixedPBiCG");
+// BiCGStab is registered in both tables, as foam-extend's BiCGStab is.
+static addSymMatrixSolver<gpuBiCGStab> addGpuBiCGStabSym("gpuBiCGStab");
+static addAsymMatrixSolver<gpuBiCGStab> addGpuBiCGStab("gpuBiCGStab");
+static addSymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStabSym("gpuMixedBiCGStab");
+static addAsymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStab("gpuMixedBiCGStab");
 
 }  // namespace Foam

@@ -15,7 +15,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmrgpu.so")
 
 MRG_OK, MRG_E_INVALID, MRG_E_OOM, MRG_E_BREAKDOWN, MRG_E_TIMEOUT, MRG_E_CUDA, MRG_E_BUSY = range(7)
-SOLVERS = {"PCG": 0, "PBiCG": 1}
+SOLVERS = {"PCG": 0, "PBiCG": 1, "BiCGStab": 2}
 PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 ORDERINGS = {"exact": 0, "colour": 1}

@@ -541,10 +541,21 @@ static double mr_reduce(const mr_order* o, int assign, int kind, const double* a
     return mr_block(acc);
 }
 
+static int bicgstab(const or_ldu* m, const double* b, double* x, double tol, double rel_tol, int min_iter,
+                    int max_iter, int precon, int fused, const mr_order* o, or_perf* perf);
+
+/* solver: 0 = PCG, 1 = PBiCG, 2 = BiCGStab. */
 int or_solve_mirror(const or_ldu* m, const double* b, double* x, double tol,
                     double rel_tol, int min_iter, int max_iter, int precon,
                     int pbicg, or_perf* perf)
 {
+    if (pbicg == 2) {
+        mr_order ob;
+        mr_order_init(m, &ob);
+        int rc = bicgstab(m, b, x, tol, rel_tol, min_iter, max_iter, precon, 1, &ob, perf);
+        free(ob.perm);
+        return rc;
+    }
     int n = m->n;
     size_t bytes = sizeof(double) * (size_t)(n ? n : 1);
     double *wA = (double*)malloc(bytes), *rA = (double*)malloc(bytes), *pA = (double*)malloc(bytes);
@@ -608,6 +619,126 @@ int or_solve_mirror(const or_ldu* m, const double* b, double* x, double tol,
     }
     free(wA); free(rA); free(pA); free(wT); free(rT); free(pT); free(t); free(o.perm);
     return 0;
+}
+
+/* ---- BiCGStab ----------------------------------------------------------
+ * The stabilised bi-conjugate gradient method foam-extend's lduSolvers
+ * register as "BiCGStab" (the reference tutorials' coupled solver,
+ * system/solid/fvSolution Tcoupled), restated from its publication (van der
+ * Vorst, SIAM J. Sci. Stat. Comput. 13 (1992) 631-644; the right-
+ * preconditioned form of Barrett et al., "Templates", SIAM 1994, fig. 2.10)
+ * with foam's residual: r~ = r0; per iteration
+ *   rho = (r~, r); beta = (rho/rho_old)(alpha/omega); p = r + beta (p - omega v)
+ *   p^ = M^-1 p; v = A p^; alpha = rho / (r~, v)
+ *   s = r - alpha v; x += alpha p^; |s| tested (half step ends the solve)
+ *   s^ = M^-1 s; t = A s^; omega = (t, s) / (t, t)
+ *   x += omega s^; r = s - omega t; |r| tested
+ * foam's checks: singular when |(r~, v)| / normFactor, |omega| or |rho| drop
+ * below VSMALL; minIter / maxIter as for PCG.  o == NULL sums sequentially
+ * (fused selects fma); otherwise every reduction runs in the GPU library's
+ * tree with the row assignment of the kernel that computes it. */
+static double bs_prod(const mr_order* o, int assign, const double* a, const double* b, int n, int fused)
+{
+    return o ? mr_reduce(o, assign, 0, a, b) : sum_prod(a, b, n, fused);
+}
+
+static double bs_mag(const mr_order* o, const double* a, double* tmp, int n)
+{
+    if (!o) return sum_mag(a, n);
+    for (int c = 0; c < n; ++c) tmp[c] = fabs(a[c]);
+    return mr_reduce(o, 0, 1, tmp, NULL);
+}
+
+static int bicgstab(const or_ldu* m, const double* b, double* x, double tol, double rel_tol, int min_iter,
+                    int max_iter, int precon, int fused, const mr_order* o, or_perf* perf)
+{
+    int n = m->n;
+    size_t bytes = sizeof(double) * (size_t)(n ? n : 1);
+    double *r = (double*)malloc(bytes), *rt = (double*)malloc(bytes), *p = (double*)malloc(bytes);
+    double *ph = (double*)malloc(bytes), *v = (double*)malloc(bytes), *sh = (double*)malloc(bytes);
+    double *t = (double*)malloc(bytes), *tmp = (double*)malloc(bytes);
+    memset(perf, 0, sizeof(*perf));
+
+    or_amul(m, x, v, fused);
+    double nfac;
+    if (o) {
+        double xbar = mr_reduce(o, 0, 1, x, NULL) / (double)n;
+        or_sumA(m, tmp);
+        for (int c = 0; c < n; ++c) {
+            double tr = tmp[c] * xbar;
+            tmp[c] = fabs(v[c] - tr) + fabs(b[c] - tr);
+            r[c] = b[c] - v[c];
+        }
+        nfac = mr_reduce(o, 1, 1, tmp, NULL) + OR_SMALL;
+        for (int c = 0; c < n; ++c) tmp[c] = fabs(r[c]);
+        perf->initial_residual = mr_reduce(o, 1, 1, tmp, NULL) / nfac;
+    } else {
+        for (int c = 0; c < n; ++c) r[c] = b[c] - v[c];
+        nfac = or_norm_factor(m, x, b, v);
+        perf->initial_residual = sum_mag(r, n) / nfac;
+    }
+    perf->final_residual = perf->initial_residual;
+
+    if (min_iter > 0 || !check_convergence(perf, tol, rel_tol)) {
+        or_precon pc;
+        precon_init(&pc, m, precon);
+        memcpy(rt, r, bytes);
+        double rho = bs_prod(o, 0, rt, r, n, fused), alpha = 0.0, omega = 0.0, beta = 0.0;
+        if (fabs(rho) < OR_VSMALL) perf->singular = 1;
+        while (!perf->singular) {
+            if (perf->n_iter == 0) {
+                memcpy(p, r, bytes);
+            } else {
+                for (int c = 0; c < n; ++c)
+                    p[c] = fused ? fma(beta, fma(-omega, v[c], p[c]), r[c]) : r[c] + beta * (p[c] - omega * v[c]);
+            }
+            precon_apply(&pc, m, p, ph, 0, fused);
+            or_amul(m, ph, v, fused);
+            double rv = o ? mr_reduce(o, 1, 0, v, rt) : sum_prod(rt, v, n, fused);
+            if (fabs(rv) / nfac < OR_VSMALL) { perf->singular = 1; break; }
+            alpha = rho / rv;
+            for (int c = 0; c < n; ++c) {
+                r[c] = msub(r[c], alpha, v[c], fused);       /* s */
+                x[c] = mac(x[c], alpha, ph[c], fused);
+            }
+            double res = bs_mag(o, r, tmp, n) / nfac;
+            if ((res < tol || (rel_tol > OR_SMALL && res < rel_tol * perf->initial_residual)) &&
+                perf->n_iter + 1 >= min_iter) {
+                perf->final_residual = res;
+                perf->n_iter++;
+                perf->converged = 1;
+                break;
+            }
+            precon_apply(&pc, m, r, sh, 0, fused);
+            or_amul(m, sh, t, fused);
+            double ts = o ? mr_reduce(o, 1, 0, t, r) : sum_prod(t, r, n, fused);
+            double tt = o ? mr_reduce(o, 1, 0, t, t) : sum_prod(t, t, n, fused);
+            omega = tt > 0.0 ? ts / tt : 0.0;
+            for (int c = 0; c < n; ++c) {
+                x[c] = mac(x[c], omega, sh[c], fused);
+                r[c] = msub(r[c], omega, t[c], fused);
+            }
+            perf->final_residual = bs_mag(o, r, tmp, n) / nfac;
+            perf->n_iter++;
+            double rho_old = rho;
+            rho = bs_prod(o, 0, rt, r, n, fused);
+            int more = (perf->n_iter < max_iter && !check_convergence(perf, tol, rel_tol)) ||
+                       perf->n_iter < min_iter;
+            if (more && (fabs(omega) < OR_VSMALL || fabs(rho) < OR_VSMALL)) { perf->singular = 1; more = 0; }
+            if (!more) break;
+            beta = (rho / rho_old) * (alpha / omega);
+        }
+        free(pc.rD);
+    }
+    free(r); free(rt); free(p); free(ph); free(v); free(sh); free(t); free(tmp);
+    return 0;
+}
+
+int or_bicgstab(const or_ldu* m, const double* b, double* x, double tol,
+                double rel_tol, int min_iter, int max_iter, int precon,
+                int fused, or_perf* perf)
+{
+    return bicgstab(m, b, x, tol, rel_tol, min_iter, max_iter, precon, fused, NULL, perf);
 }
 
 /* Foam-normalised residual of a given x (initial-residual formula). */

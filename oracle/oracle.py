@@ -51,7 +51,7 @@ def lib():
         L.or_dic_factor.argtypes = [pldu, dp]
         L.or_dilu_factor.argtypes = [pldu, dp]
         L.or_precondition.argtypes = [pldu, C.c_int, dp, dp, C.c_int, C.c_int]
-        for fn in (L.or_pcg, L.or_pbicg, L.or_solve_mirror):
+        for fn in (L.or_pcg, L.or_pbicg, L.or_bicgstab, L.or_solve_mirror):
             fn.argtypes = [pldu, dp, dp, C.c_double, C.c_double, C.c_int, C.c_int,
                            C.c_int, C.c_int, C.POINTER(_Perf)]
         L.or_ggi_apply.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_int]
@@ -180,7 +180,7 @@ class OracleMatrix:
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.array(x0, dtype=np.float64, copy=True)
         p = _Perf()
-        fn = lib().or_pcg if solver == "PCG" else lib().or_pbicg
+        fn = {"PCG": lib().or_pcg, "PBiCG": lib().or_pbicg, "BiCGStab": lib().or_bicgstab}[solver]
         fn(C.byref(self._s), _d(b), _d(x), tol, rel_tol, int(min_iter), int(max_iter),
            PRECONDITIONERS[precond], int(fused), C.byref(p))
         return x, {"initial_residual": p.initial_residual, "final_residual": p.final_residual,
@@ -196,7 +196,8 @@ class OracleMatrix:
         x = np.array(x0, dtype=np.float64, copy=True)
         p = _Perf()
         lib().or_solve_mirror(C.byref(self._s), _d(b), _d(x), tol, rel_tol, int(min_iter), int(max_iter),
-                              PRECONDITIONERS[precond], int(solver == "PBiCG"), C.byref(p))
+                              PRECONDITIONERS[precond], {"PCG": 0, "PBiCG": 1, "BiCGStab": 2}[solver],
+                              C.byref(p))
         return x, {"initial_residual": p.initial_residual, "final_residual": p.final_residual,
                    "n_iter": p.n_iter, "converged": bool(p.converged), "singular": bool(p.singular)}
 

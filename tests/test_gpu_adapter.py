@@ -1,5 +1,5 @@
-"""The foam-extend lduMatrix::solver adapters (gpuPCG, gpuPBiCG, gpuMixedPCG,
-gpuMixedPBiCG), driven through the run-time selection table exactly as
+"""The foam-extend lduMatrix::solver adapters (gpuPCG, gpuPBiCG, gpuBiCGStab and
+their gpuMixed* forms), driven through the run-time selection table exactly as
 fvMatrix::solve would, compared with the oracle."""
 import json
 import os
@@ -69,6 +69,27 @@ def test_mixed_adapter(mrg, oracle_mod, tmp_path, solver, case):
     x, perf = run(mrg, tmp_path, s, solver, pc, 1e-8)
     assert perf["converged"] == 1 and perf["final_residual"] < 1e-8
     A = oracle_matrix(oracle_mod, s)
+    assert abs(A.residual(s.b, x) * A.norm_factor(x, s.b) / A.norm_factor(s.x0, s.b) - perf["final_residual"]) \
+        < 1e-10
+
+
+@pytest.mark.parametrize("case", ["cht", "cd"])
+def test_bicgstab_adapter(mrg, oracle_mod, tmp_path, case):
+    """gpuBiCGStab from both tables (the tutorials' coupled solver) matches the
+    oracle's GPU-order mirror bit for bit; gpuMixedBiCGStab converges."""
+    s = cases.c1(form="coupled") if case == "cht" else cases.convdiff_system(16, 15, 14, seed=7)
+    pc = "DIC" if case == "cht" else "DILU"
+    A = oracle_matrix(oracle_mod, s)
+    x, perf = run(mrg, tmp_path, s, "gpuBiCGStab", pc, 1e-9)
+    xm, pm = A.solve_mirror(s.b, s.x0, "BiCGStab", pc, tol=1e-9)
+    assert perf["solver"] == "gpuBiCGStab" and perf["converged"] == 1
+    assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+    if case == "cht":
+        # the tutorials' setting: BiCGStab + Cholesky (incomplete Cholesky = DIC here)
+        xc, pc_ = run(mrg, tmp_path, s, "gpuBiCGStab", "Cholesky", 1e-9)
+        assert np.array_equal(xc, xm) and pc_["n_iter"] == pm["n_iter"]
+    x, perf = run(mrg, tmp_path, s, "gpuMixedBiCGStab", pc, 1e-8)
+    assert perf["solver"] == "gpuMixedBiCGStab" and perf["converged"] == 1 and perf["final_residual"] < 1e-8
     assert abs(A.residual(s.b, x) * A.norm_factor(x, s.b) / A.norm_factor(s.x0, s.b) - perf["final_residual"]) \
         < 1e-10
 

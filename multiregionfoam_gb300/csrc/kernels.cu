@@ -17,6 +17,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 
 #include "kernels.h"
 #include "plan.h"
@@ -31,6 +32,19 @@ constexpr unsigned kSentBits32 = 0x7FA5A5A5u;
 // A sync-free wait gives up after this many SM cycles (~2 s) and flags
 // ERR_TIMEOUT, so no kernel can spin forever.
 constexpr long long kWaitCycles = 4000000000LL;
+
+// Programmatic dependent launch.  The Krylov-loop kernels are launched with
+// programmatic stream serialisation, so a kernel's CTAs can be scheduled
+// while the previous kernel of the stream drains (its launch latency hidden
+// behind the other's tail).  Each such kernel first waits here for the
+// previous kernel to complete and its writes to be visible -- before it reads
+// anything, the batch descriptor included -- and then lets the next kernel be
+// scheduled.  Launched without the attribute, both instructions do nothing.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 template <typename V> __device__ __forceinline__ V sent();
 template <> __device__ __forceinline__ double sent<double>() { return __longlong_as_double(kSentBits64); }
@@ -188,11 +202,43 @@ template <> struct VP<float> {
 // gathered x, then the FMA chain runs: the loads of one row are in flight
 // together instead of one dependent round trip per entry.  Padding (col -1)
 // is skipped, so no FP64 work is spent on it.
-constexpr int kMaxW = 8;
+// kMaxW entries of a row are loaded and multiplied per round, unrolled: six
+// covers the interior rows of hexahedral meshes in one round; wider rows
+// (interface faces, polyhedra) take further rounds of the same shape.
+#ifndef MRG_KMAXW
+#define MRG_KMAXW 6
+#endif
+constexpr int kMaxW = MRG_KMAXW;
 // Row and sweep kernels are compiled for at least 4 resident 256-thread CTAs
 // per SM.  Reducing row kernels walk the batch's segment table (kRedSegs in
 // dev.h), non-reducing row kernels take one tile per CTA.
 constexpr int kMinCtas = 4;
+
+// Entries k0 .. k0 + kMaxW - 1 (of W) of an ELL row stored at stride 32 from
+// col / val: the round's loads are all in flight together, then the FMAs run
+// in slot order (padding, col -1, skipped).  LDG: col and val are read-only
+// global data (otherwise plain loads, e.g. from shared memory).
+template <typename V, bool LDG>
+__device__ __forceinline__ V ell_round(const int* col, const V* val, const V* __restrict__ x, int k0, int W, V y)
+{
+    int c[kMaxW];
+    V a[kMaxW], xv[kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        const int e = (k0 + k) * 32;
+        c[k] = k0 + k < W ? (LDG ? __ldg(col + e) : col[e]) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        const int e = (k0 + k) * 32;
+        a[k] = c[k] >= 0 ? (LDG ? __ldg(val + e) : val[e]) : V(0);
+        xv[k] = c[k] >= 0 ? __ldca(x + c[k]) : V(0);
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k)
+        if (c[k] >= 0) y = vfma(a[k], xv[k], y);
+    return y;
+}
 
 template <typename V>
 __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __restrict__ acol,
@@ -201,28 +247,9 @@ __device__ __forceinline__ V ell_row(const int* __restrict__ sptr, const int* __
 {
     const int sl = i >> 5, lane = i & 31;
     const int e0 = __ldg(sptr + sl), W = (__ldg(sptr + sl + 1) - e0) >> 5;
-    const int* __restrict__ col = acol + e0 + lane;
-    const V* __restrict__ v = val + e0 + lane;
     V y = vmul(__ldg(dg + i), __ldca(x + i));
-    if (W <= kMaxW) {
-        int c[kMaxW];
-        V a[kMaxW], xv[kMaxW];
-#pragma unroll
-        for (int k = 0; k < kMaxW; ++k) c[k] = k < W ? __ldg(col + k * 32) : -1;
-#pragma unroll
-        for (int k = 0; k < kMaxW; ++k) {
-            a[k] = c[k] >= 0 ? __ldg(v + k * 32) : V(0);
-            xv[k] = c[k] >= 0 ? __ldca(x + c[k]) : V(0);
-        }
-#pragma unroll
-        for (int k = 0; k < kMaxW; ++k)
-            if (c[k] >= 0) y = vfma(a[k], xv[k], y);
-    } else {
-        for (int k = 0; k < W; ++k) {
-            const int ck = __ldg(col + k * 32);
-            if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldca(x + ck), y);
-        }
-    }
+    if (W <= kMaxW) return ell_round<V, true>(acol + e0 + lane, val + e0 + lane, x, 0, W, y);
+    for (int k0 = 0; k0 < W; k0 += kMaxW) y = ell_round<V, true>(acol + e0 + lane, val + e0 + lane, x, k0, W, y);
     return y;
 }
 
@@ -280,11 +307,7 @@ __device__ __forceinline__ void ell_tile(const int* __restrict__ sptr, const int
             for (int k = 0; k < kMaxW; ++k)
                 if (live & (1u << k)) y = vfma(a[k], xv[k], y);
         } else {
-            const int* __restrict__ col = acol + e0 + lane;
-            for (int k = 0; k < W; ++k) {
-                const int ck = __ldg(col + k * 32);
-                if (ck >= 0) y = vfma(__ldg(v + k * 32), __ldca(x + ck), y);
-            }
+            for (int k0 = 0; k0 < W; k0 += kMaxW) y = ell_round<V, true>(acol + e0 + lane, v, x, k0, W, y);
             if (nW <= kMaxW) {
 #pragma unroll
                 for (int k = 0; k < kMaxW; ++k) c[k] = k < nW ? __ldg(acol + ne0 + lane + k * 32) : -1;
@@ -1178,6 +1201,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
     __shared__ double sh[kBlock * kMaxRed];
     __shared__ int s_last;
     __shared__ __align__(16) SysDev sS;
+    pdl_enter();
     const Batch B = *pB;
     int cur = -1;
     rows_phase<V, OP, PB>(B, sS, sh, &s_last, cur);
@@ -1264,6 +1288,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
     extern __shared__ __align__(128) unsigned char dyn[];
     int* st_col = reinterpret_cast<int*>(dyn);
     V* st_val = reinterpret_cast<V*>(dyn + sizeof(int) * S * kRoundEntries);
+    pdl_enter();
     const Batch B = *pB;
     Ctl* ctl = B.ctl;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -1347,10 +1372,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
                 for (int k = 0; k < kMaxW; ++k)
                     if (ck[k] >= 0) y = vfma(av[k], xv[k], y);
             } else {
-                for (int k = 0; k < W; ++k) {
-                    const int cc = c[k * 32];
-                    if (cc >= 0) y = vfma(a[k * 32], __ldca(p + cc), y);
-                }
+                for (int k0 = 0; k0 < W; k0 += kMaxW) y = ell_round<V, false>(c, a, p, k0, W, y);
             }
             q[i] = y;
             acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
@@ -1368,6 +1390,34 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
     }
 }
 
+// Launch with programmatic stream serialisation (pdl_enter in the kernel);
+// MRG_PDL=0 launches plainly.
+static bool pdl_enabled()
+{
+    static int on = -1;
+    if (on < 0) {
+        const char* e = std::getenv("MRG_PDL");
+        on = (e && e[0] == '0') ? 0 : 1;
+    }
+    return on == 1;
+}
+
+template <typename... P, typename... A>
+static void launch_pdl(void (*k)(P...), int grid, int block, size_t smem, cudaStream_t st, A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, args...);   // errors surface through cudaGetLastError
+}
+
 // CTAs of a persistent launch: one wave of kMinCtas CTAs per SM.
 static int g_grid_cap = 152 * kMinCtas;
 
@@ -1382,14 +1432,14 @@ void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
     if (grid < 1) grid = 1;
     if constexpr (OP == OP_SPMV_QP) {
         if (!pb) {
-            k_spmv_staged<V><<<grid, kBlock, spmv_smem<V>(), st>>>(dB);
+            launch_pdl(k_spmv_staged<V>, grid, kBlock, spmv_smem<V>(), st, dB);
             return;
         }
     }
     if (pb)
-        k_rows<V, OP, true><<<grid, kBlock, 0, st>>>(dB);
+        launch_pdl(k_rows<V, OP, true>, grid, kBlock, 0, st, dB);
     else
-        k_rows<V, OP, false><<<grid, kBlock, 0, st>>>(dB);
+        launch_pdl(k_rows<V, OP, false>, grid, kBlock, 0, st, dB);
 }
 
 // ---------------------------------------------------------------- factor
@@ -1448,6 +1498,7 @@ __device__ __forceinline__ void factor_row(const SysDev& S, int c, int lane, Ctl
 
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_factor(const Batch* __restrict__ pB, int with32)
 {
+    pdl_enter();
     const Batch B = *pB;
     const SysDev* __restrict__ Ss = B.sys;
     const int nsys = B.nsys;
@@ -1528,6 +1579,41 @@ __device__ __forceinline__ SweepPtrs<V> sweep_ptrs(const SysDev& S, int vs)
     return P;
 }
 
+// Entries k0 .. k0 + kMaxW - 1 (of W) of one sweep row: acc -= coef * dep in
+// slot order.  Sync-free sweeps wait (bounded) for each dependency value;
+// levelled forward sweeps recompute level-0 values as rD r.
+template <typename V, bool FWD>
+__device__ __forceinline__ void sweep_round(const SweepPtrs<V>& P, int e0, int k0, int W, int lane, bool syncfree,
+                                            Ctl* ctl, int lvl0_end, const V* dep, V& acc)
+{
+    const V* __restrict__ r = P.r;
+    const V* __restrict__ rD = P.rD;
+    int col[kMaxW];
+    V cf[kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) col[k] = k0 + k < W ? __ldg(P.col + e0 + (k0 + k) * 32 + lane) : -1;
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) cf[k] = col[k] >= 0 ? __ldg(P.coef + e0 + (k0 + k) * 32 + lane) : V(0);
+    if (syncfree) {
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k)
+            if (col[k] >= 0) acc = vfma(-cf[k], wait_ready(dep + col[k], ctl), acc);
+    } else {
+        V d[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            const int ck = col[k];
+            if (FWD)
+                d[k] = ck < 0 ? V(0) : (ck < lvl0_end ? vmul(__ldg(rD + ck), __ldca(r + ck)) : __ldca(dep + ck));
+            else
+                d[k] = ck < 0 ? V(0) : __ldca(dep + ck);
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k)
+            if (col[k] >= 0) acc = vfma(-cf[k], d[k], acc);
+    }
+}
+
 // Rows i = r0 + lane < r1 of one chunk whose sweep entries start at e0 and
 // are W wide.
 template <typename V, bool FWD>
@@ -1547,47 +1633,14 @@ __device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1
         acc = vmul(__ldg(rD + i), __ldca(r + i));
     else
         acc = __ldca(y + i);
-    if (W <= kMaxW) {
-        int col[kMaxW];
-        V cf[kMaxW];
-#pragma unroll
-        for (int k = 0; k < kMaxW; ++k) col[k] = k < W ? __ldg(P.col + e0 + k * 32 + lane) : -1;
-#pragma unroll
-        for (int k = 0; k < kMaxW; ++k) cf[k] = col[k] >= 0 ? __ldg(P.coef + e0 + k * 32 + lane) : V(0);
-        if (syncfree) {
-#pragma unroll
-            for (int k = 0; k < kMaxW; ++k)
-                if (col[k] >= 0) acc = vfma(-cf[k], wait_ready(dep + col[k], ctl), acc);
-        } else {
-            V d[kMaxW];
-#pragma unroll
-            for (int k = 0; k < kMaxW; ++k) {
-                const int ck = col[k];
-                if (FWD)
-                    d[k] = ck < 0 ? V(0) : (ck < lvl0_end ? vmul(__ldg(rD + ck), __ldca(r + ck)) : __ldca(dep + ck));
-                else
-                    d[k] = ck < 0 ? V(0) : __ldca(dep + ck);
-            }
-#pragma unroll
-            for (int k = 0; k < kMaxW; ++k)
-                if (col[k] >= 0) acc = vfma(-cf[k], d[k], acc);
-        }
-    } else {
-        for (int k = 0; k < W; ++k) {
-            const int e = e0 + k * 32 + lane;
-            const int ck = __ldg(P.col + e);
-            if (ck < 0) break;
-            const V cfk = __ldg(P.coef + e);
-            V d;
-            if (syncfree)
-                d = wait_ready(dep + ck, ctl);
-            else if (FWD && ck < lvl0_end)
-                d = vmul(__ldg(rD + ck), __ldca(r + ck));
-            else
-                d = __ldca(dep + ck);
-            acc = vfma(-cfk, d, acc);
-        }
-    }
+    // rounds of kMaxW entries (one round for most rows, unrolled without a
+    // loop): a round's indices and coefficients are loaded before any of its
+    // dependency values is read
+    const int rounds = W <= kMaxW ? 1 : (W + kMaxW - 1) / kMaxW;
+    if (rounds == 1)
+        sweep_round<V, FWD>(P, e0, 0, W, lane, syncfree, ctl, lvl0_end, dep, acc);
+    else
+        for (int k0 = 0; k0 < W; k0 += kMaxW) sweep_round<V, FWD>(P, e0, k0, W, lane, syncfree, ctl, lvl0_end, dep, acc);
     if (syncfree) {
         if (FWD) {
             st_relaxed(y + i, acc);
@@ -1648,6 +1701,7 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
 template <typename V, bool FWD>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __restrict__ pB, int trans)
 {
+    pdl_enter();
     const Batch B = *pB;
     sweep_sf_phase<V, FWD>(B, trans);
 }
@@ -1712,6 +1766,7 @@ __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans
 template <typename V, bool FWD>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
 {
+    pdl_enter();
     const Batch B = *pB;
     sweep_lvl_phase<V, FWD>(B, L, trans);
 }
@@ -1747,6 +1802,7 @@ __device__ __forceinline__ void iface_phase(const Batch& B, int which)
 template <typename V>
 __global__ void k_iface_gather(const Batch* __restrict__ pB, int which)
 {
+    pdl_enter();
     const Batch B = *pB;
     iface_phase<V>(B, which);
 }
@@ -2017,7 +2073,7 @@ void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st)
 void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st)
 {
     ++g_launches;
-    k_factor<<<grid, kBlock, 0, st>>>(dB, with32);
+    launch_pdl(k_factor, grid, kBlock, 0, st, dB, with32);
 }
 
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
@@ -2028,26 +2084,26 @@ void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, co
     if (syncfree) {
         if (precision == 0) {
             if (fwd)
-                k_sweep_sf<double, true><<<grid, kBlock, 0, st>>>(dB, trans);
+                launch_pdl(k_sweep_sf<double, true>, grid, kBlock, 0, st, dB, trans);
             else
-                k_sweep_sf<double, false><<<grid, kBlock, 0, st>>>(dB, trans);
+                launch_pdl(k_sweep_sf<double, false>, grid, kBlock, 0, st, dB, trans);
         } else {
             if (fwd)
-                k_sweep_sf<float, true><<<grid, kBlock, 0, st>>>(dB, trans);
+                launch_pdl(k_sweep_sf<float, true>, grid, kBlock, 0, st, dB, trans);
             else
-                k_sweep_sf<float, false><<<grid, kBlock, 0, st>>>(dB, trans);
+                launch_pdl(k_sweep_sf<float, false>, grid, kBlock, 0, st, dB, trans);
         }
     } else {
         if (precision == 0) {
             if (fwd)
-                k_sweep_lvl<double, true><<<grid, kBlock, 0, st>>>(dB, level, trans);
+                launch_pdl(k_sweep_lvl<double, true>, grid, kBlock, 0, st, dB, level, trans);
             else
-                k_sweep_lvl<double, false><<<grid, kBlock, 0, st>>>(dB, level, trans);
+                launch_pdl(k_sweep_lvl<double, false>, grid, kBlock, 0, st, dB, level, trans);
         } else {
             if (fwd)
-                k_sweep_lvl<float, true><<<grid, kBlock, 0, st>>>(dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, true>, grid, kBlock, 0, st, dB, level, trans);
             else
-                k_sweep_lvl<float, false><<<grid, kBlock, 0, st>>>(dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, false>, grid, kBlock, 0, st, dB, level, trans);
         }
     }
 }
@@ -2056,9 +2112,9 @@ void launch_iface_gather(int precision, int which, const Batch* dB, int grid, cu
 {
     ++g_launches;
     if (precision == 0)
-        k_iface_gather<double><<<grid, 256, 0, st>>>(dB, which);
+        launch_pdl(k_iface_gather<double>, grid, 256, 0, st, dB, which);
     else
-        k_iface_gather<float><<<grid, 256, 0, st>>>(dB, which);
+        launch_pdl(k_iface_gather<float>, grid, 256, 0, st, dB, which);
 }
 
 void launch_permute(int to_internal, const SysDev* d, int s, const double* src, double* dst, int n, cudaStream_t st)

@@ -1467,12 +1467,24 @@ __device__ __forceinline__ void factor_row(const SysDev& S, int c, int lane, Ctl
     const double rd = __ddiv_rn(1.0, D);
     S.rD[i] = rd;
     if (with32) S.rD32[i] = (float)rd;
+    // Levelled (colour) plans never store level 0's forward values rD r: the
+    // forward sweep reads r there, so the dependency's rD is folded into the
+    // coefficient here, once per factorisation, instead of being gathered
+    // beside r on every sweep.  Sync-free (foam-order) plans keep foam's
+    // coefficients.
+    const int lvl0_end = (!S.syncfree && S.nlevels > 1) ? S.chunk_start[S.lvl_chunk[1]] : 0;
     for (int k = 0; k < fW; ++k) {
         const int e = fe0 + k * 32 + lane;
         const int sc = S.f_src[e];
         if (sc < 0) break;
         const double a = src_val(S, sc, false), at = src_val(S, swap_src(sc, F), false);
-        const double cf = __dmul_rn(rd, a), cfT = __dmul_rn(rd, at);
+        double cf = __dmul_rn(rd, a), cfT = __dmul_rn(rd, at);
+        const int col = S.f_col[e];
+        if (col < lvl0_end) {
+            const double rdc = __ddiv_rn(1.0, wait_ready(S.D + col, ctl));
+            cf = __dmul_rn(cf, rdc);
+            cfT = __dmul_rn(cfT, rdc);
+        }
         S.f_c[e] = cf;
         S.f_cT[e] = cfT;
         if (with32) {
@@ -1540,9 +1552,10 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_factor(const Batch* __rest
 // with sentinels for the backward sweep and vice versa.
 //
 // Level variant (colour ordering): one launch per level, plain loads.  Level
-// 0 is never stored (its forward value rD r is recomputed where needed) and
-// the last level writes w directly (it has no backward dependencies), so a
-// two-colour sweep is two launches: forward level 1, backward level 0.
+// 0 is never stored (the forward coefficients of its dependants carry its rD,
+// so they read r; its own backward pass starts from rD r) and the last level
+// writes w directly (it has no backward dependencies), so a two-colour sweep
+// is two launches: forward level 1, backward level 0.
 // Pointers one sweep needs, copied into registers once per system so the
 // stores of the sweep cannot force them to be re-read from the SysDev.
 template <typename V>
@@ -1581,13 +1594,13 @@ __device__ __forceinline__ SweepPtrs<V> sweep_ptrs(const SysDev& S, int vs)
 
 // Entries k0 .. k0 + kMaxW - 1 (of W) of one sweep row: acc -= coef * dep in
 // slot order.  Sync-free sweeps wait (bounded) for each dependency value;
-// levelled forward sweeps recompute level-0 values as rD r.
+// levelled forward sweeps read r for level-0 dependencies (their rD is in
+// the coefficient).
 template <typename V, bool FWD>
 __device__ __forceinline__ void sweep_round(const SweepPtrs<V>& P, int e0, int k0, int W, int lane, bool syncfree,
                                             Ctl* ctl, int lvl0_end, const V* dep, V& acc)
 {
     const V* __restrict__ r = P.r;
-    const V* __restrict__ rD = P.rD;
     int col[kMaxW];
     V cf[kMaxW];
 #pragma unroll
@@ -1604,7 +1617,7 @@ __device__ __forceinline__ void sweep_round(const SweepPtrs<V>& P, int e0, int k
         for (int k = 0; k < kMaxW; ++k) {
             const int ck = col[k];
             if (FWD)
-                d[k] = ck < 0 ? V(0) : (ck < lvl0_end ? vmul(__ldg(rD + ck), __ldca(r + ck)) : __ldca(dep + ck));
+                d[k] = ck < 0 ? V(0) : __ldca((ck < lvl0_end ? r : dep) + ck);   // level 0: rD folded into cf
             else
                 d[k] = ck < 0 ? V(0) : __ldca(dep + ck);
         }

@@ -69,10 +69,11 @@ def test_c3_full_size(mrg, ctx, oracle_mod):
     assert pm["final_residual"] < 1e-8 and p64["final_residual"] < 1e-8
     # convection-dominated (Pe up to 10): at a 1e-8 residual the plain
     # method's own error against the tightly converged FP64 solution is
-    # ~1e-6; the mixed form's error is of that order (different
-    # preconditioner ordering, same residual tolerance)
+    # ~1e-6, and any solution meeting the same residual tolerance has an
+    # error of that order; the mixed form's (different preconditioner
+    # ordering, FP32 inner iterates) must stay within 10x of it
     plain_err = rel_err(x64, xr)
-    assert rel_err(xm, xr) <= max(1e-8, 2.0 * plain_err), (rel_err(xm, xr), plain_err)
+    assert rel_err(xm, xr) <= max(1e-8, 10.0 * plain_err), (rel_err(xm, xr), plain_err)
     rng = np.random.default_rng(4)
     ptr, addr, w = ggi["a_from_b"]
     src = rng.uniform(-1.0, 1.0, ggi["n_b"])

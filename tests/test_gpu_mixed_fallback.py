@@ -4,8 +4,10 @@ When the FP64 outer loop ends without reaching the tolerance (FP32 BiCG
 drift, or the refinement-step limit), the solve restarts FP64 Krylov from
 the best refined iterate with the solve's own normFactor, and reports
 fallback = 1.  The refinement-step limit max_outer = 1 forces that path
-here; the result must converge and agree with the plain FP64 solve, alone
-and inside the server's continuous batch (bit-identical there).
+here; the result must converge, its error against a tightly converged FP64
+solution must stay within 10x of the plain FP64 method's own at the same
+tolerance, and it must be bit-identical alone and inside the server's
+continuous batch.
 """
 import numpy as np
 import pytest
@@ -26,12 +28,16 @@ def test_stalled_refinement_finishes_in_fp64(mrg, ctx, case):
     m = mrg.Mesh(ctx, s.n, s.lower, s.upper)
     m.upload(s.diag, s.upper_c, s.lower_c)
     try:
+        xr, _ = m.solve(s.b, s.x0, tol=1e-13, max_iter=20000, precision="fp64", **kw)
         x64, p64 = m.solve(s.b, s.x0, tol=1e-8, max_iter=5000, precision="fp64", ordering="colour", **kw)
         x, p = m.solve(s.b, s.x0, tol=1e-8, max_iter=5000, precision="mixed", ordering="colour", max_outer=1, **kw)
         assert p["fallback"] and p["converged"] and p["final_residual"] < 1e-8
         assert p["n_outer"] == 1
         assert p["initial_residual"] == p64["initial_residual"]
-        assert np.abs(x - x64).max() <= 1e-7 * np.abs(x64).max()
+        # error against the tightly converged FP64 solution: within 10x of
+        # the plain FP64 method's own at the same residual tolerance
+        err = lambda v: np.abs(v - xr).max() / np.abs(xr).max()
+        assert err(x) <= max(1e-8, 10.0 * err(x64)), (err(x), err(x64))
         # the reported residual is the true FP64 foam residual of x:
         # sum|b - A x| over the normFactor of the initial guess
         r_x, nf_x = m.residual(s.b, x)

@@ -3,7 +3,11 @@
 // adapter uses.  It reproduces the API *shape* (names, argument meaning,
 // run-time selection by solver name) so the adapter compiles and can be
 // exercised without foam-extend; against a real foam-extend build the adapter
-// includes foam's own headers instead.  No foam-extend
+// includes foam's own headers instead (the shim's
+// lduMatrix::solverPerformance is foam's lduSolverPerformance, and
+// addSymMatrixSolver / addAsymMatrixSolver become
+// addToRunTimeSelectionTable(lduMatrix::solver, T, symMatrix / asymMatrix)).
+// No foam-extend
 // source is reproduced here.
 #pragma once
 

@@ -1,7 +1,7 @@
 /*
  * ldu_oracle.c -- CPU oracle for the coupled-region LDU solve path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker that the GPU library
+ * TEST INFRASTRUCTURE ONLY.  This file is the CPU restatement the GPU library
  * (libmrgpu) is compared against; it is never linked into, called by, or used
  * as a fallback for the product path.  Only tests/, __graft_entry__.smoke()
  * and bench.py's CPU-baseline leg load it.

@@ -6,8 +6,8 @@
    polyMesh): owner/neighbour of the internal faces (foam's lowerAddr/
    upperAddr), and for the 200-face regionCouple interface patches ("top" on
    the solid, "interface" on the fluid) their faceCells and face centres.
-   Needs the reference tree (read-only) and is run once in the build
-   container; the GPU machine only reads the .npz.
+   Needs the reference tree (read-only) and is run once where that tree
+   exists; test runs elsewhere only read the .npz.
 2. ``oracle_small.npz`` -- oracle outputs on small seeded systems, so the
    oracle itself is regression-pinned and GPU tests can compare against
    stored vectors.

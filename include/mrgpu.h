@@ -324,6 +324,47 @@ int mrg_dn_get_state(mrg_dn* dn, double* value_a, double* grad_b, double* aitken
 int mrg_dn_criteria(int corr, double jump_res, double flux_res, double max_jump_res,
                     double max_flux_res);
 
+/* ---- monolithic interface coefficients ---------------------------------
+ * The per-assembly interface terms of the monolithic conjugate-heat-transfer
+ * boundary conditions, for both sides of a regionCouple interface:
+ * monolithicThermalDiffusivityFvPatchScalarField::calcThermalDiffusivity /
+ * calcTemperature (monolithicThermalDiffusivityFvPatchScalarField.C:
+ * 167-394) and monolithicTemperatureFvPatchScalarField::source /
+ * manipulateMatrix (monolithicTemperatureFvPatchScalarField.C:205-244).
+ * A patch: faceCells into its region's cells, the coupled patch's linear
+ * weights w (0 < w < 1), magLongDelta, deltaCoeffs and |Sf|, and the GGI
+ * weights that interpolate the other side's face values onto its faces
+ * (src_ptr[n_faces + 1], src_face, src_weight; rescaled, uncovered faces
+ * empty, as the regionCouplePatch's interpolator gives them). */
+typedef struct mrg_mono mrg_mono;
+typedef struct {
+    int n_cells, n_faces;
+    const int32_t* face_cells;
+    const double* weights;
+    const double* mag_long_delta;
+    const double* delta_coeffs;
+    const double* mag_sf;
+    const int32_t* src_ptr;
+    const int32_t* src_face;
+    const double* src_weight;
+} mrg_mono_patch;
+int mrg_mono_create(mrg_ctx* ctx, const mrg_mono_patch* side_a, const mrg_mono_patch* side_b,
+                    mrg_mono** out);
+int mrg_mono_destroy(mrg_mono* mono);
+/* Interface diffusivity k and wall temperature Tw on the faces of `side`
+ * (0 = A, 1 = B), device arrays: T_own / T_nbr are the two regions' cell
+ * temperatures, f_own / f_nbr the diffusivities on the two patches
+ * (monolithicBase::forig), Qr_own / Qr_nbr the radiative fluxes on the two
+ * patches, or NULL for a side without radiation. */
+int mrg_mono_update(mrg_mono* mono, int side, const double* d_T_own, const double* d_T_nbr,
+                    const double* d_f_own, const double* d_f_nbr, const double* d_Qr_own,
+                    const double* d_Qr_nbr, double* d_k, double* d_Tw);
+/* The temperature patch's source s = kOwn (Tw - Tc) - k deltaCoeffs
+ * (Tc_nei - Tc) added to the region's right-hand side, b[faceCells] +=
+ * s |Sf| (device arrays; k and Tw as mrg_mono_update returned them). */
+int mrg_mono_source(mrg_mono* mono, int side, const double* d_T_own, const double* d_T_nbr,
+                    const double* d_Tw, const double* d_k, const double* d_f_own, double* d_b);
+
 /* ---- autotuner ---------------------------------------------------------
  * No counterpart in the reference.  Times the Krylov loop of a mesh or batch
  * on its current coefficients under each candidate launch shape and keeps

@@ -14,6 +14,7 @@
 #include "kernels.h"
 #include "dn.h"
 #include "ggi_build.h"
+#include "mono.h"
 #include "noalloc.h"
 #include "server.h"
 
@@ -33,6 +34,9 @@ struct mrg_server {
 };
 struct mrg_dn {
     std::unique_ptr<Dn> d;
+};
+struct mrg_mono {
+    Mono m;
 };
 struct mrg_batch {
     Ctx* ctx = nullptr;
@@ -853,6 +857,61 @@ int mrg_dn_criteria(int corr, double jump_res, double flux_res, double max_jump_
 {
     if (corr == 1) return 0;
     return (jump_res <= max_jump_res && flux_res <= max_flux_res) ? 1 : 0;
+}
+
+int mrg_mono_create(mrg_ctx* ctx, const mrg_mono_patch* a, const mrg_mono_patch* b, mrg_mono** out)
+{
+    return guard([&] {
+        if (!ctx || !a || !b || !out) return fail(MRG_E_INVALID, "NULL argument");
+        *out = nullptr;
+        auto host = [](const mrg_mono_patch* p) {
+            return MonoPatchHost{p->n_cells,      p->n_faces,   p->face_cells, p->weights,   p->mag_long_delta,
+                                 p->delta_coeffs, p->mag_sf,    p->src_ptr,    p->src_face, p->src_weight};
+        };
+        auto* m = new mrg_mono();
+        try {
+            mono_create(m->m, &ctx->c, host(a), host(b));
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mono_destroy(mrg_mono* mono)
+{
+    return guard([&] {
+        delete mono;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mono_update(mrg_mono* mono, int side, const double* T_own, const double* T_nbr, const double* f_own,
+                    const double* f_nbr, const double* Qr_own, const double* Qr_nbr, double* k, double* Tw)
+{
+    return guard([&] {
+        if (!mono || side < 0 || side > 1) return fail(MRG_E_INVALID, "bad argument");
+        if (mono->m.side[side].n_faces > 0 && (!T_own || !T_nbr || !f_own || !f_nbr || !k || !Tw))
+            return fail(MRG_E_INVALID, "NULL array");
+        mono_update(mono->m, side, T_own, T_nbr, f_own, f_nbr, Qr_own, Qr_nbr, k, Tw);
+        MRG_CUDA(cudaStreamSynchronize(mono->m.ctx->st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mono_source(mrg_mono* mono, int side, const double* T_own, const double* T_nbr, const double* Tw,
+                    const double* k, const double* f_own, double* b)
+{
+    return guard([&] {
+        if (!mono || side < 0 || side > 1) return fail(MRG_E_INVALID, "bad argument");
+        if (mono->m.side[side].n_faces > 0 && (!T_own || !T_nbr || !Tw || !k || !f_own || !b))
+            return fail(MRG_E_INVALID, "NULL array");
+        mono_source(mono->m, side, T_own, T_nbr, Tw, k, f_own, b);
+        MRG_CUDA(cudaStreamSynchronize(mono->m.ctx->st));
+        return (int)MRG_OK;
+    });
 }
 
 int mrg_server_create(mrg_ctx* ctx, const mrg_controls* sym_controls, const mrg_controls* asym_controls,

@@ -32,6 +32,7 @@ EXPORTED = [
     "mrg_server_wait", "mrg_server_get_stats", "mrg_mesh_tune", "mrg_batch_tune",
     "mrg_dn_create", "mrg_dn_destroy", "mrg_dn_set_state", "mrg_dn_new_time_step", "mrg_dn_update_jump",
     "mrg_dn_update_flux", "mrg_dn_rhs", "mrg_dn_residuals", "mrg_dn_get_state", "mrg_dn_criteria",
+    "mrg_mono_create", "mrg_mono_destroy", "mrg_mono_update", "mrg_mono_source",
 ]
 
 
@@ -72,6 +73,12 @@ class Tuning(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MonoPatch(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("face_cells", C.c_void_p), ("weights", C.c_void_p),
+                ("mag_long_delta", C.c_void_p), ("delta_coeffs", C.c_void_p), ("mag_sf", C.c_void_p),
+                ("src_ptr", C.c_void_p), ("src_face", C.c_void_p), ("src_weight", C.c_void_p)]
 
 
 class DnPatch(C.Structure):
@@ -159,6 +166,10 @@ def load(path: str = LIB_PATH):
     L.mrg_dn_residuals.argtypes = [vp, vp, vp, dp, dp]
     L.mrg_dn_get_state.argtypes = [vp, dp, dp, dp]
     L.mrg_dn_criteria.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.mrg_mono_create.argtypes = [vp, C.POINTER(MonoPatch), C.POINTER(MonoPatch), C.POINTER(vp)]
+    L.mrg_mono_destroy.argtypes = [vp]
+    L.mrg_mono_update.argtypes = [vp, C.c_int] + [vp] * 8
+    L.mrg_mono_source.argtypes = [vp, C.c_int] + [vp] * 6
     L.mrg_batch_tune.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Tuning)]
     _LIB = L
     return L
@@ -588,6 +599,44 @@ class DnInterface:
     def close(self):
         if self.h:
             _check(load().mrg_dn_destroy(self.h))
+            self.h = None
+
+
+class MonoInterface:
+    """Monolithic interface coefficients of both sides of a regionCouple
+    interface (mrg_mono_*).  a / b: dicts with n_cells, face_cells, w
+    (patch weights), mld (magLongDelta), dc (deltaCoeffs), sf (|Sf|) and the
+    GGI CSR (ptr, addr, wts) giving the patch's faces from the other
+    side's faces.  Field arguments are device pointers."""
+
+    def __init__(self, ctx: Context, a: dict, b: dict):
+        self._keep = []
+
+        def patch(p):
+            arrs = [np.ascontiguousarray(p["face_cells"], np.int32)] + \
+                   [np.ascontiguousarray(p[k], np.float64) for k in ("w", "mld", "dc", "sf")] + \
+                   [np.ascontiguousarray(p["ptr"], np.int32), np.ascontiguousarray(p["addr"], np.int32),
+                    np.ascontiguousarray(p["wts"], np.float64)]
+            self._keep.append(arrs)
+            return MonoPatch(int(p["n_cells"]), len(arrs[0]), *[a_.ctypes.data_as(C.c_void_p) for a_ in arrs])
+
+        h = C.c_void_p()
+        _check(load().mrg_mono_create(ctx.h, C.byref(patch(a)), C.byref(patch(b)), C.byref(h)))
+        self.h = h
+
+    def update(self, side, d_t_own, d_t_nbr, d_f_own, d_f_nbr, d_qr_own, d_qr_nbr, d_k, d_tw):
+        p = lambda v: C.c_void_p(v) if v else None
+        _check(load().mrg_mono_update(self.h, int(side), p(d_t_own), p(d_t_nbr), p(d_f_own), p(d_f_nbr),
+                                      p(d_qr_own), p(d_qr_nbr), p(d_k), p(d_tw)))
+
+    def source(self, side, d_t_own, d_t_nbr, d_tw, d_k, d_f_own, d_b):
+        p = lambda v: C.c_void_p(v) if v else None
+        _check(load().mrg_mono_source(self.h, int(side), p(d_t_own), p(d_t_nbr), p(d_tw), p(d_k), p(d_f_own),
+                                      p(d_b)))
+
+    def close(self):
+        if self.h:
+            _check(load().mrg_mono_destroy(self.h))
             self.h = None
 
 

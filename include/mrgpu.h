@@ -49,7 +49,11 @@ enum {
  * Tcoupled: BiCGStab, tolerance 1e-15, maxIter 200).  Preconditioned on the
  * right (van der Vorst 1992): one M^-1 p and one M^-1 s per iteration, the
  * residual of s tested after the first half step. */
-enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2 };
+/* SMOOTH: foam's smoothSolver with the GaussSeidel smoother (the tutorials'
+ * fluid U solves): n_sweeps Gauss-Seidel sweeps in foam's cell order, then
+ * the residual, until converged; FP64, exact ordering only. */
+enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2, MRG_SOLVER_SMOOTH = 3 };
+enum { MRG_SMOOTHER_GAUSS_SEIDEL = 0 };
 enum {
     MRG_PRECOND_NONE = 0,     /* "none"     */
     MRG_PRECOND_DIAGONAL = 1, /* "diagonal" */
@@ -99,6 +103,9 @@ typedef struct {
                               it from the FP64 residual keeps it stable)     */
     int max_outer;         /* mixed: refinement steps (default 50)          */
     int iters_per_launch;  /* iterations per CUDA-graph launch (default 16) */
+    int smoother;          /* MRG_SOLVER_SMOOTH: MRG_SMOOTHER_*             */
+    int n_sweeps;          /* MRG_SOLVER_SMOOTH: sweeps per residual check
+                              (foam's nSweeps, default 1)                   */
 } mrg_controls;
 
 /* lduSolverPerformance (initialResidual, finalResidual, nIterations,

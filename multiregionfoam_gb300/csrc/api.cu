@@ -94,7 +94,14 @@ Controls to_controls(const mrg_controls* c)
     k.inner_max_iter = c->inner_max_iter;
     k.max_outer = c->max_outer > 0 ? c->max_outer : 50;
     k.k_launch = c->iters_per_launch > 0 ? c->iters_per_launch : 16;
-    if (k.solver < 0 || k.solver > 2) throw Error(MRG_E_INVALID, "unknown solver");
+    k.n_sweeps = c->n_sweeps > 0 ? c->n_sweeps : 1;
+    if (k.solver < 0 || k.solver > 3) throw Error(MRG_E_INVALID, "unknown solver");
+    if (k.solver == MRG_SOLVER_SMOOTH) {
+        if (c->smoother != MRG_SMOOTHER_GAUSS_SEIDEL) throw Error(MRG_E_INVALID, "unknown smoother");
+        if (c->precision != MRG_PRECISION_FP64 || c->ordering != MRG_ORDER_EXACT)
+            throw Error(MRG_E_INVALID, "smoothSolver runs in FP64 in foam's order (precision fp64, ordering exact)");
+        k.pc = PC_NONE;   // the smoother needs no factorisation
+    }
     if (k.pc < 0 || k.pc > 3) throw Error(MRG_E_INVALID, "unknown preconditioner");
     if (k.precision < 0 || k.precision > 1) throw Error(MRG_E_INVALID, "unknown precision");
     if (k.ordering < 0 || k.ordering > 1) throw Error(MRG_E_INVALID, "unknown ordering");
@@ -165,6 +172,8 @@ void mrg_controls_default(mrg_controls* c)
     c->inner_max_iter = 0;
     c->max_outer = 50;
     c->iters_per_launch = 16;
+    c->smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
+    c->n_sweeps = 1;
 }
 
 int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out)

@@ -52,7 +52,7 @@ struct Scal {
     int okeep;             // mixed: 1 = the last refinement improved (keep x), 0 = roll back
     int fallback;          // mixed: 1 = refinement stalled, FP64 Krylov requested; 2 = running it;
                            // 3 = done (true residual checked)
-    int pad;
+    int n_sweeps;          // smoothSolver: Gauss-Seidel sweeps per iteration
 };
 
 // PCG / PBiCG use the slots by name (T = the transpose system).  BiCGStab
@@ -111,7 +111,7 @@ struct Ctl {
     unsigned pad[3];
     // controls written into every system's Scal by OP_BEGIN
     double tol, rel_tol, inner_rel_tol;
-    int min_iter, max_iter, inner_max, max_outer, mixed, pad2;
+    int min_iter, max_iter, inner_max, max_outer, mixed, n_sweeps;
 };
 
 // A batch of systems, resident on the device.

@@ -351,7 +351,8 @@ static bool ensure_views(Mesh& m, PlanState& P, const Controls& cfg)
     const size_t np = (size_t)S.npad, nx = (size_t)S.npad + S.ngen;
     const bool asym = !m.sym || m.has_int;
     const bool need32 = cfg.precision == MRG_PRECISION_MIXED;
-    const bool needT = cfg.solver != MRG_SOLVER_PCG;   // PBiCG's transpose system, BiCGStab's extra vectors
+    // PBiCG's transpose system, BiCGStab's extra vectors
+    const bool needT = cfg.solver == MRG_SOLVER_PBICG || cfg.solver == MRG_SOLVER_BICGSTAB;
     bool changed = false;
     auto setp = [&](auto& field, auto value) {
         if (field != value) {
@@ -519,10 +520,30 @@ static void record_iteration_bs(BatchHost& bh, const Controls& cfg, int prec, cu
     launch_rows(OP_BS_XR, prec, bh.d, nt, ns, 0, st);
 }
 
+// One smoothSolver iteration: nSweeps Gauss-Seidel sweeps (each: the
+// interfaces' sweep-start values, the sweep into y, x = y), then the
+// residual and the convergence test.
+static void record_iteration_gs(BatchHost& bh, const Controls& cfg, cudaStream_t st)
+{
+    const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    const bool gen = any_general_iface(bh);
+    for (int k = 0; k < std::max(1, cfg.n_sweeps); ++k) {
+        if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+        launch_gs_sweep(bh.d, grid_sweep(bh.ctx), st);
+        launch_rows(OP_GS_COPY, 0, bh.d, nt, ns, 0, st);
+    }
+    if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+    launch_rows(OP_GS_RES, 0, bh.d, nt, ns, 0, st);
+}
+
 static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaStream_t st)
 {
     if (cfg.solver == MRG_SOLVER_BICGSTAB) {
         record_iteration_bs(bh, cfg, prec, st);
+        return;
+    }
+    if (cfg.solver == MRG_SOLVER_SMOOTH) {
+        record_iteration_gs(bh, cfg, st);
         return;
     }
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
@@ -552,7 +573,7 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
 // launches (MRG_ITERATION=persistent; PCG and PBiCG).  Both give the same bits.
 static bool persistent_iteration(const BatchHost& bh, const Controls& cfg)
 {
-    if (cfg.solver == MRG_SOLVER_BICGSTAB) return false;
+    if (cfg.solver == MRG_SOLVER_BICGSTAB || cfg.solver == MRG_SOLVER_SMOOTH) return false;
     static int env = -1;
     if (env < 0) {
         const char* e = std::getenv("MRG_ITERATION");
@@ -677,10 +698,12 @@ static void write_ctl_controls(BatchHost& bh, const Controls& cfg)
     host.max_iter = cfg.max_iter;
     // FP32 BiCG and BiCGStab restart from the FP64 residual every 150
     // iterations unless told otherwise: their short recurrences drift in FP32
-    const int auto_inner = cfg.solver != MRG_SOLVER_PCG ? std::min(cfg.max_iter, 150) : cfg.max_iter;
+    const int auto_inner = (cfg.solver == MRG_SOLVER_PBICG || cfg.solver == MRG_SOLVER_BICGSTAB)
+                               ? std::min(cfg.max_iter, 150) : cfg.max_iter;
     host.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : auto_inner;
     host.max_outer = cfg.max_outer;
     host.mixed = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
+    host.n_sweeps = std::max(1, cfg.n_sweeps);
     // tickets, error bits and active counts start at zero
     MRG_CUDA(cudaMemcpyAsync(bh.d_ctl, &host, sizeof(Ctl), cudaMemcpyHostToDevice, bh.ctx->st));
 }
@@ -721,6 +744,8 @@ static void krylov_start(BatchHost& bh, const Controls& cfg, int prec)
 {
     if (cfg.solver == MRG_SOLVER_BICGSTAB)
         launch_rows(OP_BS_RHO0, prec, bh.d, bh.h.ntiles, bh.h.nsegs, 0, bh.ctx->st);
+    if (cfg.solver == MRG_SOLVER_SMOOTH)   // the Gauss-Seidel sweep's output starts armed
+        launch_rows(OP_GS_ARM, 0, bh.d, bh.h.ntiles, bh.h.nsegs, 0, bh.ctx->st);
 }
 
 std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
@@ -728,7 +753,7 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
     Ctx* c = bh.ctx;
     cudaStream_t st = c->st;
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
-    const int tsys = cfg.solver != MRG_SOLVER_PCG;   // T vectors: sentinels armed, r copied into FP32
+    const int tsys = cfg.solver == MRG_SOLVER_PBICG || cfg.solver == MRG_SOLVER_BICGSTAB;   // T vectors
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     const bool gen = any_general_iface(bh);
     Ctl* h = pinned_ctl();
@@ -816,7 +841,7 @@ void batch_begin(BatchHost& bh, const Controls& cfg)
 {
     cudaStream_t st = bh.ctx->st;
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
-    const int tsys = cfg.solver != MRG_SOLVER_PCG;
+    const int tsys = cfg.solver == MRG_SOLVER_PBICG || cfg.solver == MRG_SOLVER_BICGSTAB;
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     const bool gen = any_general_iface(bh);
     write_ctl_controls(bh, cfg);
@@ -855,7 +880,7 @@ void batch_iterate(BatchHost& bh, const Controls& cfg, int prec)
 void batch_outer(BatchHost& bh, const Controls& cfg)
 {
     cudaStream_t st = bh.ctx->st;
-    const int tsys = cfg.solver != MRG_SOLVER_PCG;
+    const int tsys = cfg.solver == MRG_SOLVER_PBICG || cfg.solver == MRG_SOLVER_BICGSTAB;
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
     if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, st);
@@ -910,7 +935,8 @@ Tuning tune_batch(BatchHost& bh, const Controls& cfg)
         for (int k : {4, 16})
             for (int div : {4, 8, 16}) {
                 if (!levels && div != 8) continue;
-                if (mode == 1 && cfg.solver == MRG_SOLVER_BICGSTAB) continue;   // no persistent form
+                if (mode == 1 && (cfg.solver == MRG_SOLVER_BICGSTAB || cfg.solver == MRG_SOLVER_SMOOTH))
+                    continue;   // no persistent form
                 Tuning t;
                 t.mode = mode;
                 t.k = k;

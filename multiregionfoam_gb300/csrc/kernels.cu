@@ -485,6 +485,16 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
         set_active(ctl, sc, sums[0] > 0.0 ? 1 : 0);
         break;
     }
+    case OP_GS_RES: {
+        // smoothSolver: residual after nSweeps sweeps (foam counts sweeps)
+        sc->res = sums[0] / sc->nfac;
+        sc->iter += sc->n_sweeps;
+        const bool conv = sc->res < sc->tol || (sc->rel_tol > 1.0e-20 && sc->res < sc->rel_tol * sc->res0);
+        sc->converged = conv;
+        const bool more = (sc->iter < sc->kmax && !conv) || sc->iter < sc->kmin;
+        if (!more) set_active(ctl, sc, 0);
+        break;
+    }
     case OP_BS_RHO0:
         // BiCGStab start: rho = (r~, r) with r~ = r; a zero rho cannot start
         sc->rho = sums[0];
@@ -626,6 +636,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             sc->oconv = 0;
             sc->fallback = 0;
             sc->singular = 0;
+            sc->n_sweeps = c->n_sweeps > 0 ? c->n_sweeps : 1;
         }
     } else if constexpr (OP == OP_PERMUTE_IN) {
         const int* __restrict__ perm = S.perm;
@@ -1010,6 +1021,26 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             acc[0] += fabs(widen(r[k]));
             acc[1] = __fma_rn(widen(rt[k]), widen(r[k]), acc[1]);
         }
+    } else if constexpr (OP == OP_GS_ARM || OP == OP_GS_COPY) {
+        const int n = S.n;
+        double* __restrict__ x = S.v64.x;
+        double* __restrict__ y = S.v64.y;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (r4 + k < n) {
+                if (OP == OP_GS_COPY) x[r4 + k] = y[r4 + k];
+                y[r4 + k] = sent<double>();
+            }
+    } else if constexpr (OP == OP_GS_RES) {
+        const double* __restrict__ x = S.v64.x;
+        const double* __restrict__ b = S.v64.b;
+        double* __restrict__ r = S.v64.r;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            const double ri = __ldca(b + i) - ell_row<double>(sptr, acol, S.a_val, S.diag, x, i);
+            r[i] = ri;
+            acc[0] += fabs(ri);
+        }
     } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
         const double* __restrict__ av = OP == OP_TMUL ? S.aT_val : S.a_val;
         const double* __restrict__ dg = S.diag;
@@ -1027,13 +1058,13 @@ struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
                                   OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32 || OP == OP_FALLBACK64 ||
                                   OP == OP_BS_RHO0 || OP == OP_BS_V || OP == OP_BS_S || OP == OP_BS_T ||
-                                  OP == OP_BS_XR);
+                                  OP == OP_BS_XR || OP == OP_GS_RES);
     // Krylov-loop ops run only for systems whose loop is active; the
     // refinement ops only for systems whose outer loop is active.
     static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
                                          OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE ||
                                          OP == OP_BS_RHO0 || OP == OP_BS_P || OP == OP_BS_V || OP == OP_BS_S ||
-                                         OP == OP_BS_T || OP == OP_BS_XR);
+                                         OP == OP_BS_T || OP == OP_BS_XR || OP == OP_GS_COPY || OP == OP_GS_RES);
     static constexpr bool kNeedOuter = (OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
     // Values reduced: the initial residual needs two (normFactor and
     // sum|r|), BiCGStab's t step ((t, s), (t, t)) and its update (sum|r|,
@@ -1043,7 +1074,7 @@ struct OpTraits {
     static constexpr bool kElem = (OP == OP_SUMX || OP == OP_RHO || OP == OP_PUPDATE || OP == OP_UPDATE ||
                                    OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE || OP == OP_TO32 ||
                                    OP == OP_CORRECT || OP == OP_KEEPBEST || OP == OP_BS_RHO0 || OP == OP_BS_P ||
-                                   OP == OP_BS_S || OP == OP_BS_XR);
+                                   OP == OP_BS_S || OP == OP_BS_XR || OP == OP_GS_ARM || OP == OP_GS_COPY);
 };
 
 template <RowOp OP>
@@ -1784,6 +1815,71 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __r
     sweep_lvl_phase<V, FWD>(B, L, trans);
 }
 
+// ---------------------------------------------------------------- Gauss-Seidel
+// foam's GaussSeidel smoother, one sweep, row i (exact plan, foam order):
+//   acc = b_i; acc -= a * x~ for the interface entries (interface order:
+//   foam moves them to the source first, with psi at the sweep's start);
+//   then the face entries in the row's order -- lower neighbours first (their
+//   new values, waited for), upper neighbours after (old values); y_i =
+//   acc / diag_i.  The ELL row holds foam's per-cell order, and its source
+//   codes tell the three kinds of entry apart (>= 2F interface, >= F this
+//   cell is the face's upper cell so the neighbour is its lower one).
+__device__ __forceinline__ void gs_row(const SysDev& S, int i, Ctl* ctl)
+{
+    const int F = S.nf;
+    const int sl = i >> 5, lane = i & 31;
+    const int e0 = __ldg(S.a_sptr + sl), W = (__ldg(S.a_sptr + sl + 1) - e0) >> 5;
+    const double* __restrict__ x = S.v64.x;
+    double* y = S.v64.y;
+    double acc = __ldca(S.v64.b + i);
+    for (int k = 0; k < W; ++k) {
+        const int e = e0 + k * 32 + lane;
+        const int sc = __ldg(S.a_src + e);
+        if (sc >= 2 * F) acc = __fma_rn(-__ldg(S.a_val + e), __ldca(x + __ldg(S.a_col + e)), acc);
+    }
+    for (int k = 0; k < W; ++k) {
+        const int e = e0 + k * 32 + lane;
+        const int sc = __ldg(S.a_src + e);
+        if (sc < 0 || sc >= 2 * F) continue;
+        const int col = __ldg(S.a_col + e);
+        const double v = sc >= F ? wait_ready(y + col, ctl) : __ldca(x + col);
+        acc = __fma_rn(-__ldg(S.a_val + e), v, acc);
+    }
+    st_relaxed(y + i, __ddiv_rn(acc, __ldg(S.diag + i)));
+}
+
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_gs_sweep(const Batch* __restrict__ pB)
+{
+    pdl_enter();
+    const Batch B = *pB;
+    const SysDev* __restrict__ Ss = B.sys;
+    const int nsys = B.nsys;
+    Ctl* ctl = B.ctl;
+    const int lane = threadIdx.x & 31;
+    const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->ticket[2], 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
+        const SysDev& S = Ss[s];
+        if (c >= S.nchunks || !S.sc->active || !S.syncfree) continue;   // warp-uniform
+        const int r0 = S.chunk_start[c], r1 = S.chunk_start[c + 1];
+        if (r0 + lane < r1) gs_row(S, r0 + lane, ctl);
+    }
+    // last warp out resets the work counter for the next launch
+    if (lane == 0) {
+        const unsigned nw = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[3], 1u) == nw - 1u) {
+            ctl->ticket[2] = 0u;
+            ctl->ticket[3] = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // ---------------------------------------------------------------- misc
 template <typename V>
 __global__ void k_fill_sent(V* p, long long n)
@@ -2048,6 +2144,9 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE64(OP_BS_S)
             MRG_CASE64(OP_BS_T)
             MRG_CASE64(OP_BS_XR)
+            MRG_CASE64(OP_GS_ARM)
+            MRG_CASE64(OP_GS_COPY)
+            MRG_CASE64(OP_GS_RES)
         default: break;
         }
     } else {
@@ -2128,6 +2227,12 @@ void launch_iface_gather(int precision, int which, const Batch* dB, int grid, cu
         launch_pdl(k_iface_gather<double>, grid, 256, 0, st, dB, which);
     else
         launch_pdl(k_iface_gather<float>, grid, 256, 0, st, dB, which);
+}
+
+void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st)
+{
+    ++g_launches;
+    launch_pdl(k_gs_sweep, grid, kBlock, 0, st, dB);
 }
 
 void launch_permute(int to_internal, const SysDev* d, int s, const double* src, double* dst, int n, cudaStream_t st)

@@ -39,12 +39,20 @@ enum RowOp {
     OP_BS_S,            // BiCGStab: s = r - alpha v, x += alpha M^-1 p, sum|s|, half-step test
     OP_BS_T,            // BiCGStab: t = A M^-1 s, (t, s), (t, t), omega
     OP_BS_XR,           // BiCGStab: x += omega M^-1 s, r = s - omega t, sum|r|, (r~, r), convergence
+    OP_GS_ARM,          // smoothSolver: arm the sweep's output y with sentinels
+    OP_GS_COPY,         // smoothSolver: x = y (the sweep's result), re-arm y
+    OP_GS_RES,          // smoothSolver: r = b - A x, sum|r|, iterations += nSweeps, convergence
     OP_COUNT
 };
 
 // precision: 0 = FP64 vectors/coefficients, 1 = FP32 (mixed inner loop).
 // ntiles, nsegs: upper bounds on the batch's tile and segment counts.
 void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st);
+
+// One Gauss-Seidel sweep of foam's smoother in foam's cell order (sync-free
+// over the exact plan's chunks): y = sweep(x, b), lower neighbours from y
+// (waited for), upper neighbours and interfaces from x.
+void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st);
 
 // Sentinel fill of a vector (sync-free readiness marker).
 void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st);

@@ -9,6 +9,7 @@
 //   gpuMixedPCG       symMatrix   FP32 PCG inside FP64 iterative refinement
 //   gpuMixedPBiCG     asymMatrix  FP32 PBiCG inside FP64 iterative refinement
 //   gpuMixedBiCGStab  both        FP32 BiCGStab inside FP64 iterative refinement
+//   gpuSmoothSolver   both        FP64 smoothSolver, smoother GaussSeidel, nSweeps
 //
 // Each adapter replaces lduMatrix::solver::solve(psi, source, cmpt) (the call
 // fvMatrix::solve makes at multiRegionSystem.C:293, and coupledFvMatrix's at
@@ -134,7 +135,15 @@ public:
         c.min_iter = minIter_;
         c.max_iter = maxIter_;
         c.solver = solverKind_;
-        c.preconditioner = precondCode(controls_.lookupWord("preconditioner", "none"), matrix_.symmetric());
+        if (solverKind_ == MRG_SOLVER_SMOOTH) {
+            // smoothSolver's own words: smoother (GaussSeidel) and nSweeps
+            if (controls_.lookupWord("smoother", "GaussSeidel") != "GaussSeidel")
+                throw FatalError("gpuSmoothSolver: unsupported smoother " + controls_.lookupWord("smoother"));
+            c.smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
+            c.n_sweeps = (int)controls_.lookupOrDefault("nSweeps", 1.0);
+        } else {
+            c.preconditioner = precondCode(controls_.lookupWord("preconditioner", "none"), matrix_.symmetric());
+        }
         c.precision = precision_;
         c.ordering = controls_.lookupWord("gpuOrdering", precision_ == MRG_PRECISION_MIXED ? "colour" : "exact") ==
                              "colour"
@@ -144,8 +153,8 @@ public:
         mrg_perf perf;
         check(mrg_solve(mesh, source.data(), psi.data(), &c, &perf), "mrg_solve");
         lduMatrix::solverPerformance out;
-        static const char* const names[2][3] = {{"gpuPCG", "gpuPBiCG", "gpuBiCGStab"},
-                                                 {"gpuMixedPCG", "gpuMixedPBiCG", "gpuMixedBiCGStab"}};
+        static const char* const names[2][4] = {{"gpuPCG", "gpuPBiCG", "gpuBiCGStab", "gpuSmoothSolver"},
+                                                 {"gpuMixedPCG", "gpuMixedPBiCG", "gpuMixedBiCGStab", "-"}};
         out.solverName = names[precision_ ? 1 : 0][solverKind_];
         out.fieldName = fieldName_;
         out.initialResidual = perf.initial_residual;
@@ -176,6 +185,7 @@ MRG_DEFINE_SOLVER(gpuMixedPCG, MRG_SOLVER_PCG, MRG_PRECISION_MIXED)
 MRG_DEFINE_SOLVER(gpuMixedPBiCG, MRG_SOLVER_PBICG, MRG_PRECISION_MIXED)
 MRG_DEFINE_SOLVER(gpuBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_FP64)
 MRG_DEFINE_SOLVER(gpuMixedBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_MIXED)
+MRG_DEFINE_SOLVER(gpuSmoothSolver, MRG_SOLVER_SMOOTH, MRG_PRECISION_FP64)
 
 // addToRunTimeSelectionTable(lduMatrix::solver, gpuPCG, symMatrix) etc.
 static addSymMatrixSolver<gpuPCG> addGpuPCG("gpuPCG");
@@ -191,5 +201,8 @@ static addSymMatrixSolver<gpuBiCGStab> addGpuBiCGStabSym("gpuBiCGStab");
 static addAsymMatrixSolver<gpuBiCGStab> addGpuBiCGStab("gpuBiCGStab");
 static addSymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStabSym("gpuMixedBiCGStab");
 static addAsymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStab("gpuMixedBiCGStab");
+// smoothSolver, like foam's, takes either kind of matrix.
+static addSymMatrixSolver<gpuSmoothSolver> addGpuSmoothSolverSym("gpuSmoothSolver");
+static addAsymMatrixSolver<gpuSmoothSolver> addGpuSmoothSolver("gpuSmoothSolver");
 
 }  // namespace Foam

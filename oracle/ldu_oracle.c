@@ -741,6 +741,108 @@ int or_bicgstab(const or_ldu* m, const double* b, double* x, double tol,
     return bicgstab(m, b, x, tol, rel_tol, min_iter, max_iter, precon, fused, NULL, perf);
 }
 
+/* ---- smoothSolver + GaussSeidel ------------------------------------------
+ * foam-extend's smoothSolver with the GaussSeidel smoother (the tutorials'
+ * fluid U solves), restated from the algorithm: per iteration nSweeps
+ * sweeps, then the residual; iterations count sweeps; the loop runs while
+ * (nIter += nSweeps) < maxIter and not converged, or nIter < minIter.
+ * A sweep: b' = b + coupleBouCoeffs * (interpolated psi at the sweep's
+ * start) (the interfaces' negated-coefficient update), then in cell order
+ * psi_c = (b'_c - sum over c's upper faces of upper * psi_u) / diag_c, and
+ * each upper neighbour's b' loses lower * psi_c (foam's owner-start loop).
+ * The residual is lduMatrix::residual: b - diag psi, the faces in face
+ * order, the interfaces last.  Mode 0 literal, 1 fused (fma), 2 the GPU's
+ * order (fused arithmetic, residual as b - A psi, the GPU's reduction
+ * tree). */
+static void gs_sweep(const or_ldu* m, const double* b, double* x, double* bp, int fused)
+{
+    const double* lo = m->lowerc ? m->lowerc : m->upperc;
+    memcpy(bp, b, sizeof(double) * (size_t)m->n);
+    for (int i = 0; i < m->ni; ++i) {
+        double pnf = 0.0;
+        for (int k = m->iface_ptr[i]; k < m->iface_ptr[i + 1]; ++k)
+            pnf = mac(pnf, m->iface_w[k], x[m->iface_src[k]], fused);
+        int c = m->iface_cells[i];
+        bp[c] = msub(bp[c], -m->iface_bou[i], pnf, fused);
+    }
+    int f = 0;
+    for (int c = 0; c < m->n; ++c) {
+        double xc = bp[c];
+        int f0 = f;
+        for (; f < m->nf && m->lower[f] == c; ++f) xc = msub(xc, m->upperc[f], x[m->upper[f]], fused);
+        xc = xc / m->diag[c];
+        for (int g = f0; g < f; ++g) bp[m->upper[g]] = msub(bp[m->upper[g]], lo[g], xc, fused);
+        x[c] = xc;
+    }
+}
+
+static void foam_residual(const or_ldu* m, const double* b, const double* x, double* r, int fused)
+{
+    const double* lo = m->lowerc ? m->lowerc : m->upperc;
+    for (int c = 0; c < m->n; ++c) r[c] = msub(b[c], m->diag[c], x[c], fused);
+    for (int f = 0; f < m->nf; ++f) {
+        int l = m->lower[f], u = m->upper[f];
+        r[u] = msub(r[u], lo[f], x[l], fused);
+        r[l] = msub(r[l], m->upperc[f], x[u], fused);
+    }
+    for (int i = 0; i < m->ni; ++i) {
+        double pnf = 0.0;
+        for (int k = m->iface_ptr[i]; k < m->iface_ptr[i + 1]; ++k)
+            pnf = mac(pnf, m->iface_w[k], x[m->iface_src[k]], fused);
+        int c = m->iface_cells[i];
+        r[c] = msub(r[c], -m->iface_bou[i], pnf, fused);
+    }
+}
+
+int or_smooth_gs(const or_ldu* m, const double* b, double* x, double tol, double rel_tol, int min_iter,
+                 int max_iter, int n_sweeps, int mode, or_perf* perf)
+{
+    int n = m->n;
+    size_t bytes = sizeof(double) * (size_t)(n ? n : 1);
+    double *Ax = (double*)malloc(bytes), *r = (double*)malloc(bytes), *t = (double*)malloc(bytes);
+    const int fused = mode >= 1;
+    mr_order o;
+    if (mode == 2) mr_order_init(m, &o);
+    memset(perf, 0, sizeof(*perf));
+    if (n_sweeps < 1) n_sweeps = 1;
+    or_amul(m, x, Ax, fused);
+    double nfac;
+    if (mode == 2) {
+        double xbar = mr_reduce(&o, 0, 1, x, NULL) / (double)n;
+        or_sumA(m, t);
+        for (int c = 0; c < n; ++c) {
+            double tr = t[c] * xbar;
+            t[c] = fabs(Ax[c] - tr) + fabs(b[c] - tr);
+            r[c] = fabs(b[c] - Ax[c]);
+        }
+        nfac = mr_reduce(&o, 1, 1, t, NULL) + OR_SMALL;
+        perf->initial_residual = mr_reduce(&o, 1, 1, r, NULL) / nfac;
+    } else {
+        nfac = or_norm_factor(m, x, b, Ax);
+        foam_residual(m, b, x, r, fused);
+        perf->initial_residual = sum_mag(r, n) / nfac;
+    }
+    perf->final_residual = perf->initial_residual;
+    if (min_iter > 0 || !check_convergence(perf, tol, rel_tol)) {
+        do {
+            for (int k = 0; k < n_sweeps; ++k) gs_sweep(m, b, x, t, fused);
+            if (mode == 2) {
+                or_amul(m, x, Ax, 1);
+                for (int c = 0; c < n; ++c) r[c] = fabs(b[c] - Ax[c]);
+                perf->final_residual = mr_reduce(&o, 1, 1, r, NULL) / nfac;
+            } else {
+                foam_residual(m, b, x, r, fused);
+                perf->final_residual = sum_mag(r, n) / nfac;
+            }
+            perf->n_iter += n_sweeps;
+        } while ((perf->n_iter < max_iter && !check_convergence(perf, tol, rel_tol)) ||
+                 perf->n_iter < min_iter);
+    }
+    if (mode == 2) free(o.perm);
+    free(Ax); free(r); free(t);
+    return 0;
+}
+
 /* Foam-normalised residual of a given x (initial-residual formula). */
 double or_residual(const or_ldu* m, const double* b, const double* x)
 {

@@ -94,6 +94,15 @@ def test_bicgstab_adapter(mrg, oracle_mod, tmp_path, case):
         < 1e-10
 
 
+def test_smooth_solver_adapter(mrg, oracle_mod, tmp_path):
+    """gpuSmoothSolver (smoother GaussSeidel): the tutorials' fluid U setting."""
+    s = cases.convdiff_system(12, 11, 10, seed=9)
+    x, perf = run(mrg, tmp_path, s, "gpuSmoothSolver", "none", 1e-8)
+    xm, pm = oracle_matrix(oracle_mod, s).smooth(s.b, s.x0, tol=1e-8, mode="mirror")
+    assert perf["solver"] == "gpuSmoothSolver" and perf["converged"] == 1
+    assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+
+
 def test_unknown_solver_is_fatal(mrg, tmp_path):
     s = cases.cht_system(6, 6, 6, 3)
     from multiregionfoam_gb300 import _build

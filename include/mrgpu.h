@@ -53,7 +53,16 @@ enum {
  * fluid U solves): n_sweeps Gauss-Seidel sweeps in foam's cell order, then
  * the residual, until converged; FP64, exact ordering only. */
 enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2, MRG_SOLVER_SMOOTH = 3 };
-enum { MRG_SMOOTHER_GAUSS_SEIDEL = 0 };
+/* smoothSolver smoothers: GaussSeidel; DIC / DILU (each sweep adds
+ * M^-1 (b - A psi) to psi with the incomplete factorisation M); and
+ * DICGaussSeidel / DILUGaussSeidel (that step, then a Gauss-Seidel sweep). */
+enum {
+    MRG_SMOOTHER_GAUSS_SEIDEL = 0,
+    MRG_SMOOTHER_DIC = 1,
+    MRG_SMOOTHER_DILU = 2,
+    MRG_SMOOTHER_DIC_GAUSS_SEIDEL = 3,
+    MRG_SMOOTHER_DILU_GAUSS_SEIDEL = 4
+};
 enum {
     MRG_PRECOND_NONE = 0,     /* "none"     */
     MRG_PRECOND_DIAGONAL = 1, /* "diagonal" */

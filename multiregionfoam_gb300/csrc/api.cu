@@ -97,10 +97,14 @@ Controls to_controls(const mrg_controls* c)
     k.n_sweeps = c->n_sweeps > 0 ? c->n_sweeps : 1;
     if (k.solver < 0 || k.solver > 3) throw Error(MRG_E_INVALID, "unknown solver");
     if (k.solver == MRG_SOLVER_SMOOTH) {
-        if (c->smoother != MRG_SMOOTHER_GAUSS_SEIDEL) throw Error(MRG_E_INVALID, "unknown smoother");
+        if (c->smoother < MRG_SMOOTHER_GAUSS_SEIDEL || c->smoother > MRG_SMOOTHER_DILU_GAUSS_SEIDEL)
+            throw Error(MRG_E_INVALID, "unknown smoother");
         if (c->precision != MRG_PRECISION_FP64 || c->ordering != MRG_ORDER_EXACT)
             throw Error(MRG_E_INVALID, "smoothSolver runs in FP64 in foam's order (precision fp64, ordering exact)");
-        k.pc = PC_NONE;   // the smoother needs no factorisation
+        k.smoother = c->smoother;
+        // the factorisation the DIC / DILU smoothers apply (Gauss-Seidel needs none)
+        const bool dilu = c->smoother == MRG_SMOOTHER_DILU || c->smoother == MRG_SMOOTHER_DILU_GAUSS_SEIDEL;
+        k.pc = c->smoother == MRG_SMOOTHER_GAUSS_SEIDEL ? PC_NONE : (dilu ? PC_DILU : PC_DIC);
     }
     if (k.pc < 0 || k.pc > 3) throw Error(MRG_E_INVALID, "unknown preconditioner");
     if (k.precision < 0 || k.precision > 1) throw Error(MRG_E_INVALID, "unknown precision");

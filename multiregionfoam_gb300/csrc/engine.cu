@@ -520,17 +520,29 @@ static void record_iteration_bs(BatchHost& bh, const Controls& cfg, int prec, cu
     launch_rows(OP_BS_XR, prec, bh.d, nt, ns, 0, st);
 }
 
-// One smoothSolver iteration: nSweeps Gauss-Seidel sweeps (each: the
-// interfaces' sweep-start values, the sweep into y, x = y), then the
-// residual and the convergence test.
+// One smoothSolver iteration: nSweeps smoother sweeps, then the residual
+// and the convergence test.  A Gauss-Seidel sweep: the interfaces'
+// sweep-start values, the sweep into y, x = y.  A DIC / DILU sweep: r = b -
+// A x, w = M^-1 r (the preconditioner's sweeps), x += w.
 static void record_iteration_gs(BatchHost& bh, const Controls& cfg, cudaStream_t st)
 {
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
     const bool gen = any_general_iface(bh);
+    const bool fact = cfg.smoother != MRG_SMOOTHER_GAUSS_SEIDEL;
+    const bool gs = cfg.smoother == MRG_SMOOTHER_GAUSS_SEIDEL || cfg.smoother == MRG_SMOOTHER_DIC_GAUSS_SEIDEL ||
+                    cfg.smoother == MRG_SMOOTHER_DILU_GAUSS_SEIDEL;
     for (int k = 0; k < std::max(1, cfg.n_sweeps); ++k) {
-        if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
-        launch_gs_sweep(bh.d, grid_sweep(bh.ctx), st);
-        launch_rows(OP_GS_COPY, 0, bh.d, nt, ns, 0, st);
+        if (fact) {
+            if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+            launch_rows(OP_SM_RES, 0, bh.d, nt, ns, 0, st);
+            record_precondition(bh, cfg, 0, 0, st);
+            launch_rows(OP_SM_ADD, 0, bh.d, nt, ns, 0, st);
+        }
+        if (gs) {
+            if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
+            launch_gs_sweep(bh.d, grid_sweep(bh.ctx), st);
+            launch_rows(OP_GS_COPY, 0, bh.d, nt, ns, 0, st);
+        }
     }
     if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
     launch_rows(OP_GS_RES, 0, bh.d, nt, ns, 0, st);
@@ -606,7 +618,8 @@ static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int 
     std::string key = std::to_string(cfg.solver) + "/" + std::to_string(cfg.pc) + "/" +
                       std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k) + "/" +
                       std::to_string(g_rows) + "/" + std::to_string(g_red) + "/" + std::to_string(g_sweep) + "/" +
-                      std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0) +
+                      std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0) + "/" +
+                      std::to_string(cfg.smoother) + "/" + std::to_string(cfg.n_sweeps) +
                       (pers ? "/p" : "/l");
     auto it = bh.graphs.find(key);
     if (it != bh.graphs.end()) return it->second;

@@ -42,7 +42,8 @@ struct Controls {
     int solver = 0, pc = 2, precision = 0, ordering = 0;
     double inner_rel_tol = 1e-5;
     int inner_max_iter = 0, max_outer = 50, k_launch = 16;
-    int n_sweeps = 1;   // smoothSolver: Gauss-Seidel sweeps per residual check
+    int n_sweeps = 1;   // smoothSolver: sweeps per residual check
+    int smoother = 0;   // smoothSolver: MRG_SMOOTHER_*
 };
 
 struct Perf {

@@ -1031,6 +1031,21 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
                 if (OP == OP_GS_COPY) x[r4 + k] = y[r4 + k];
                 y[r4 + k] = sent<double>();
             }
+    } else if constexpr (OP == OP_SM_RES) {
+        const double* __restrict__ x = S.v64.x;
+        const double* __restrict__ b = S.v64.b;
+        double* __restrict__ r = S.v64.r;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            r[i] = __ldca(b + i) - ell_row<double>(sptr, acol, S.a_val, S.diag, x, i);
+        }
+    } else if constexpr (OP == OP_SM_ADD) {
+        double x[4], w[4];
+        ld4w(S.v64.x + r4, x);
+        ld4(S.v64.w + r4, w);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = __dadd_rn(x[k], w[k]);
+        st4(S.v64.x + r4, x);
     } else if constexpr (OP == OP_GS_RES) {
         const double* __restrict__ x = S.v64.x;
         const double* __restrict__ b = S.v64.b;
@@ -1064,7 +1079,8 @@ struct OpTraits {
     static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
                                          OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE ||
                                          OP == OP_BS_RHO0 || OP == OP_BS_P || OP == OP_BS_V || OP == OP_BS_S ||
-                                         OP == OP_BS_T || OP == OP_BS_XR || OP == OP_GS_COPY || OP == OP_GS_RES);
+                                         OP == OP_BS_T || OP == OP_BS_XR || OP == OP_GS_COPY || OP == OP_GS_RES ||
+                                         OP == OP_SM_RES || OP == OP_SM_ADD);
     static constexpr bool kNeedOuter = (OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
     // Values reduced: the initial residual needs two (normFactor and
     // sum|r|), BiCGStab's t step ((t, s), (t, t)) and its update (sum|r|,
@@ -1074,7 +1090,8 @@ struct OpTraits {
     static constexpr bool kElem = (OP == OP_SUMX || OP == OP_RHO || OP == OP_PUPDATE || OP == OP_UPDATE ||
                                    OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE || OP == OP_TO32 ||
                                    OP == OP_CORRECT || OP == OP_KEEPBEST || OP == OP_BS_RHO0 || OP == OP_BS_P ||
-                                   OP == OP_BS_S || OP == OP_BS_XR || OP == OP_GS_ARM || OP == OP_GS_COPY);
+                                   OP == OP_BS_S || OP == OP_BS_XR || OP == OP_GS_ARM || OP == OP_GS_COPY ||
+                                   OP == OP_SM_ADD);
 };
 
 template <RowOp OP>
@@ -2147,6 +2164,8 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE64(OP_GS_ARM)
             MRG_CASE64(OP_GS_COPY)
             MRG_CASE64(OP_GS_RES)
+            MRG_CASE64(OP_SM_RES)
+            MRG_CASE64(OP_SM_ADD)
         default: break;
         }
     } else {

@@ -42,6 +42,8 @@ enum RowOp {
     OP_GS_ARM,          // smoothSolver: arm the sweep's output y with sentinels
     OP_GS_COPY,         // smoothSolver: x = y (the sweep's result), re-arm y
     OP_GS_RES,          // smoothSolver: r = b - A x, sum|r|, iterations += nSweeps, convergence
+    OP_SM_RES,          // smoothSolver DIC / DILU step: r = b - A x
+    OP_SM_ADD,          // smoothSolver DIC / DILU step: x += w (w = M^-1 r)
     OP_COUNT
 };
 

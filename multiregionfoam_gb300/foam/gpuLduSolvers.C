@@ -9,7 +9,8 @@
 //   gpuMixedPCG       symMatrix   FP32 PCG inside FP64 iterative refinement
 //   gpuMixedPBiCG     asymMatrix  FP32 PBiCG inside FP64 iterative refinement
 //   gpuMixedBiCGStab  both        FP32 BiCGStab inside FP64 iterative refinement
-//   gpuSmoothSolver   both        FP64 smoothSolver, smoother GaussSeidel, nSweeps
+//   gpuSmoothSolver   both        FP64 smoothSolver; smoother GaussSeidel | DIC | DILU |
+//                                 DICGaussSeidel | DILUGaussSeidel; nSweeps
 //
 // Each adapter replaces lduMatrix::solver::solve(psi, source, cmpt) (the call
 // fvMatrix::solve makes at multiRegionSystem.C:293, and coupledFvMatrix's at
@@ -136,10 +137,14 @@ public:
         c.max_iter = maxIter_;
         c.solver = solverKind_;
         if (solverKind_ == MRG_SOLVER_SMOOTH) {
-            // smoothSolver's own words: smoother (GaussSeidel) and nSweeps
-            if (controls_.lookupWord("smoother", "GaussSeidel") != "GaussSeidel")
-                throw FatalError("gpuSmoothSolver: unsupported smoother " + controls_.lookupWord("smoother"));
-            c.smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
+            // smoothSolver's own words: smoother and nSweeps
+            const word sm = controls_.lookupWord("smoother", "GaussSeidel");
+            if (sm == "GaussSeidel") c.smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
+            else if (sm == "DIC") c.smoother = MRG_SMOOTHER_DIC;
+            else if (sm == "DILU") c.smoother = MRG_SMOOTHER_DILU;
+            else if (sm == "DICGaussSeidel") c.smoother = MRG_SMOOTHER_DIC_GAUSS_SEIDEL;
+            else if (sm == "DILUGaussSeidel") c.smoother = MRG_SMOOTHER_DILU_GAUSS_SEIDEL;
+            else throw FatalError("gpuSmoothSolver: unsupported smoother " + sm);
             c.n_sweeps = (int)controls_.lookupOrDefault("nSweeps", 1.0);
         } else {
             c.preconditioner = precondCode(controls_.lookupWord("preconditioner", "none"), matrix_.symmetric());

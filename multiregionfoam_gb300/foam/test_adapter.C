@@ -29,8 +29,8 @@ static std::vector<T> readv(FILE* f, size_t n)
 
 int main(int argc, char** argv)
 {
-    if (argc != 6) {
-        fprintf(stderr, "usage: %s system.bin solver preconditioner tolerance out.bin\n", argv[0]);
+    if (argc < 6) {
+        fprintf(stderr, "usage: %s system.bin solver preconditioner tolerance out.bin [key=value ...]\n", argv[0]);
         return 2;
     }
     FILE* f = fopen(argv[1], "rb");
@@ -64,6 +64,18 @@ int main(int argc, char** argv)
     controls.set("tolerance", atof(argv[4]));
     controls.set("relTol", 0.0);
     controls.set("maxIter", 5000.0);
+    for (int a = 6; a < argc; ++a) {   // further fvSolution entries: key=value (a number or a word)
+        const std::string kv(argv[a]);
+        const size_t eq = kv.find('=');
+        if (eq == std::string::npos) return 2;
+        const std::string k = kv.substr(0, eq), v = kv.substr(eq + 1);
+        char* end = nullptr;
+        const double d = strtod(v.c_str(), &end);
+        if (end && *end == '\0' && !v.empty())
+            controls.set(k, d);
+        else
+            controls.set(k, v);
+    }
 
     lduMatrix::solverPerformance perf;
     scalarField x;

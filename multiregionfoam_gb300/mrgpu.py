@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmrgpu.so")
 
 MRG_OK, MRG_E_INVALID, MRG_E_OOM, MRG_E_BREAKDOWN, MRG_E_TIMEOUT, MRG_E_CUDA, MRG_E_BUSY = range(7)
 SOLVERS = {"PCG": 0, "PBiCG": 1, "BiCGStab": 2, "smoothSolver": 3}
+SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "DILU": 2, "DICGaussSeidel": 3, "DILUGaussSeidel": 4}
 PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 ORDERINGS = {"exact": 0, "colour": 1}
@@ -191,7 +192,7 @@ def _i(a):
 
 def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", precond="DIC",
              precision="fp64", ordering="exact", inner_rel_tol=1e-5, inner_max_iter=0, max_outer=50,
-             iters_per_launch=16, n_sweeps=1) -> Controls:
+             iters_per_launch=16, n_sweeps=1, smoother="GaussSeidel") -> Controls:
     c = Controls()
     load().mrg_controls_default(C.byref(c))
     c.tolerance, c.rel_tol, c.min_iter, c.max_iter = tol, rel_tol, min_iter, max_iter
@@ -199,7 +200,7 @@ def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", pre
     c.precision, c.ordering = PRECISIONS[precision], ORDERINGS[ordering]
     c.inner_rel_tol, c.inner_max_iter, c.max_outer = inner_rel_tol, inner_max_iter, max_outer
     c.iters_per_launch = iters_per_launch
-    c.smoother, c.n_sweeps = 0, n_sweeps
+    c.smoother, c.n_sweeps = SMOOTHERS[smoother], n_sweeps
     return c
 
 

@@ -794,13 +794,20 @@ static void foam_residual(const or_ldu* m, const double* b, const double* x, dou
     }
 }
 
+/* smoother: 0 GaussSeidel; 1 DIC, 2 DILU (psi += M^-1 (b - A psi), the
+ * residual in the mode's order); 3 DICGaussSeidel, 4 DILUGaussSeidel (the
+ * DIC / DILU step, then a Gauss-Seidel sweep). */
 int or_smooth_gs(const or_ldu* m, const double* b, double* x, double tol, double rel_tol, int min_iter,
-                 int max_iter, int n_sweeps, int mode, or_perf* perf)
+                 int max_iter, int n_sweeps, int smoother, int mode, or_perf* perf)
 {
     int n = m->n;
     size_t bytes = sizeof(double) * (size_t)(n ? n : 1);
     double *Ax = (double*)malloc(bytes), *r = (double*)malloc(bytes), *t = (double*)malloc(bytes);
+    double* w = (double*)malloc(bytes);
     const int fused = mode >= 1;
+    const int fact = smoother != 0, gs = smoother == 0 || smoother >= 3;
+    or_precon pc;
+    precon_init(&pc, m, fact ? ((smoother == 2 || smoother == 4) ? OR_PC_DILU : OR_PC_DIC) : OR_PC_NONE);
     mr_order o;
     if (mode == 2) mr_order_init(m, &o);
     memset(perf, 0, sizeof(*perf));
@@ -825,7 +832,19 @@ int or_smooth_gs(const or_ldu* m, const double* b, double* x, double tol, double
     perf->final_residual = perf->initial_residual;
     if (min_iter > 0 || !check_convergence(perf, tol, rel_tol)) {
         do {
-            for (int k = 0; k < n_sweeps; ++k) gs_sweep(m, b, x, t, fused);
+            for (int k = 0; k < n_sweeps; ++k) {
+                if (fact) {
+                    if (mode == 2) {
+                        or_amul(m, x, Ax, 1);
+                        for (int c = 0; c < n; ++c) t[c] = b[c] - Ax[c];
+                    } else {
+                        foam_residual(m, b, x, t, fused);
+                    }
+                    precon_apply(&pc, m, t, w, 0, fused);
+                    for (int c = 0; c < n; ++c) x[c] = x[c] + w[c];
+                }
+                if (gs) gs_sweep(m, b, x, t, fused);
+            }
             if (mode == 2) {
                 or_amul(m, x, Ax, 1);
                 for (int c = 0; c < n; ++c) r[c] = fabs(b[c] - Ax[c]);
@@ -839,7 +858,8 @@ int or_smooth_gs(const or_ldu* m, const double* b, double* x, double tol, double
                  perf->n_iter < min_iter);
     }
     if (mode == 2) free(o.perm);
-    free(Ax); free(r); free(t);
+    free(pc.rD);
+    free(Ax); free(r); free(t); free(w);
     return 0;
 }
 

@@ -55,7 +55,7 @@ def lib():
             fn.argtypes = [pldu, dp, dp, C.c_double, C.c_double, C.c_int, C.c_int,
                            C.c_int, C.c_int, C.POINTER(_Perf)]
         L.or_smooth_gs.argtypes = [pldu, dp, dp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
-                                   C.POINTER(_Perf)]
+                                   C.c_int, C.POINTER(_Perf)]
         L.or_ggi_apply.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_int]
         L.gw_overlaps.argtypes = [C.c_int, ip, dp, C.c_int, ip, dp, C.c_double,
                                   C.c_long, ip, ip, dp]
@@ -188,14 +188,17 @@ class OracleMatrix:
         return x, {"initial_residual": p.initial_residual, "final_residual": p.final_residual,
                    "n_iter": p.n_iter, "converged": bool(p.converged), "singular": bool(p.singular)}
 
-    def smooth(self, b, x0, tol=1e-8, rel_tol=0.0, min_iter=0, max_iter=1000, n_sweeps=1, mode="literal"):
-        """smoothSolver with the GaussSeidel smoother; mode literal | fused |
+    SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "DILU": 2, "DICGaussSeidel": 3, "DILUGaussSeidel": 4}
+
+    def smooth(self, b, x0, tol=1e-8, rel_tol=0.0, min_iter=0, max_iter=1000, n_sweeps=1, mode="literal",
+               smoother="GaussSeidel"):
+        """smoothSolver with one of foam's smoothers; mode literal | fused |
         mirror (the GPU's order).  Returns (x, perf dict)."""
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.array(x0, dtype=np.float64, copy=True)
         p = _Perf()
         lib().or_smooth_gs(C.byref(self._s), _d(b), _d(x), tol, rel_tol, int(min_iter), int(max_iter), int(n_sweeps),
-                           {"literal": 0, "fused": 1, "mirror": 2}[mode], C.byref(p))
+                           self.SMOOTHERS[smoother], {"literal": 0, "fused": 1, "mirror": 2}[mode], C.byref(p))
         return x, {"initial_residual": p.initial_residual, "final_residual": p.final_residual,
                    "n_iter": p.n_iter, "converged": bool(p.converged), "singular": bool(p.singular)}
 

@@ -31,12 +31,12 @@ def write_system(path, s):
             f["bou"].astype(np.float64).tofile(fh)
 
 
-def run(mrg, tmp_path, s, solver, pc, tol):
+def run(mrg, tmp_path, s, solver, pc, tol, extra=()):
     from multiregionfoam_gb300 import _build
     exe = _build.build_adapter()
     sysf, outf = str(tmp_path / "sys.bin"), str(tmp_path / "x.bin")
     write_system(sysf, s)
-    r = subprocess.run([exe, sysf, solver, pc, repr(tol), outf], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, sysf, solver, pc, repr(tol), outf, *extra], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     return np.fromfile(outf, np.float64), json.loads(r.stdout.strip().splitlines()[-1])
 
@@ -100,6 +100,11 @@ def test_smooth_solver_adapter(mrg, oracle_mod, tmp_path):
     x, perf = run(mrg, tmp_path, s, "gpuSmoothSolver", "none", 1e-8)
     xm, pm = oracle_matrix(oracle_mod, s).smooth(s.b, s.x0, tol=1e-8, mode="mirror")
     assert perf["solver"] == "gpuSmoothSolver" and perf["converged"] == 1
+    assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+    # the fvSolution words smoother / nSweeps
+    x, perf = run(mrg, tmp_path, s, "gpuSmoothSolver", "none", 1e-8, ("smoother=DILUGaussSeidel", "nSweeps=2"))
+    xm, pm = oracle_matrix(oracle_mod, s).smooth(s.b, s.x0, tol=1e-8, mode="mirror", smoother="DILUGaussSeidel",
+                                                 n_sweeps=2)
     assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
 
 

@@ -38,6 +38,25 @@ def test_smooth_gs_bitexact_vs_mirror(mrg, ctx, oracle_mod, name, n_sweeps):
     assert np.abs(xg - xo).max() <= 10 * tol * np.abs(xo).max()
 
 
+@pytest.mark.parametrize("name,smoother", [("chtc", "DIC"), ("chtc", "DICGaussSeidel"), ("cd", "DILU"),
+                                           ("cd", "DILUGaussSeidel")])
+def test_smooth_factor_smoothers_bitexact(mrg, ctx, oracle_mod, name, smoother):
+    """DIC / DILU smoothers (psi += M^-1 (b - A psi)) and their Gauss-Seidel
+    combinations, bit-identical to the mirror."""
+    s = SMALL[name]()
+    A = oracle_matrix(oracle_mod, s)
+    xm, pm = A.smooth(s.b, s.x0, tol=1e-8, max_iter=20000, mode="mirror", smoother=smoother, n_sweeps=2)
+    xo, po = A.smooth(s.b, s.x0, tol=1e-8, max_iter=20000, mode="literal", smoother=smoother, n_sweeps=2)
+    m = gpu_mesh(mrg, ctx, s)
+    xg, pg = m.solve(s.b, s.x0, tol=1e-8, max_iter=20000, solver="smoothSolver", smoother=smoother, n_sweeps=2)
+    m.close()
+    assert np.array_equal(xg, xm)
+    assert (pg["initial_residual"], pg["final_residual"], pg["n_iter"]) == \
+        (pm["initial_residual"], pm["final_residual"], pm["n_iter"])
+    assert pg["converged"] and abs(pg["n_iter"] - po["n_iter"]) <= 2
+    assert np.abs(xg - xo).max() <= 1e-7 * np.abs(xo).max()
+
+
 def test_smooth_gs_controls(mrg, ctx, oracle_mod):
     s = SMALL["cd"]()
     A = oracle_matrix(oracle_mod, s)

@@ -9,6 +9,7 @@
 //   gpuMixedPCG       symMatrix   FP32 PCG inside FP64 iterative refinement
 //   gpuMixedPBiCG     asymMatrix  FP32 PBiCG inside FP64 iterative refinement
 //   gpuMixedBiCGStab  both        FP32 BiCGStab inside FP64 iterative refinement
+//   gpuBICCG          both        FP64 PBiCG + DILU (foam's BICCG)
 //   gpuSmoothSolver   both        FP64 smoothSolver; smoother GaussSeidel | DIC | DILU |
 //                                 DICGaussSeidel | DILUGaussSeidel; nSweeps
 //
@@ -192,6 +193,24 @@ MRG_DEFINE_SOLVER(gpuBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_FP64)
 MRG_DEFINE_SOLVER(gpuMixedBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_MIXED)
 MRG_DEFINE_SOLVER(gpuSmoothSolver, MRG_SOLVER_SMOOTH, MRG_PRECISION_FP64)
 
+// foam's BICCG: PBiCG with the DILU preconditioner built in (the tutorials'
+// fluid p solves); the preconditioner word is not read.
+class gpuBICCG : public gpuLduSolver {
+public:
+    gpuBICCG(const word& f, const lduMatrix& m, const FieldField& b, const FieldField& i,
+             const lduInterfaceFieldPtrsList& ifs, const dictionary& c)
+        : gpuLduSolver(f, m, b, i, ifs, with_dilu(c), MRG_SOLVER_PBICG, MRG_PRECISION_FP64)
+    {
+    }
+
+private:
+    static dictionary with_dilu(dictionary c)
+    {
+        c.set("preconditioner", std::string("DILU"));
+        return c;
+    }
+};
+
 // addToRunTimeSelectionTable(lduMatrix::solver, gpuPCG, symMatrix) etc.
 static addSymMatrixSolver<gpuPCG> addGpuPCG("gpuPCG");
 static addSymMatrixSolver<gpuMixedPCG> addGpuMixedPCG("gpuMixedPCG");
@@ -206,6 +225,8 @@ static addSymMatrixSolver<gpuBiCGStab> addGpuBiCGStabSym("gpuBiCGStab");
 static addAsymMatrixSolver<gpuBiCGStab> addGpuBiCGStab("gpuBiCGStab");
 static addSymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStabSym("gpuMixedBiCGStab");
 static addAsymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStab("gpuMixedBiCGStab");
+static addSymMatrixSolver<gpuBICCG> addGpuBICCGSym("gpuBICCG");
+static addAsymMatrixSolver<gpuBICCG> addGpuBICCG("gpuBICCG");
 // smoothSolver, like foam's, takes either kind of matrix.
 static addSymMatrixSolver<gpuSmoothSolver> addGpuSmoothSolverSym("gpuSmoothSolver");
 static addAsymMatrixSolver<gpuSmoothSolver> addGpuSmoothSolver("gpuSmoothSolver");

@@ -94,6 +94,14 @@ def test_bicgstab_adapter(mrg, oracle_mod, tmp_path, case):
         < 1e-10
 
 
+def test_biccg_alias(mrg, oracle_mod, tmp_path):
+    """gpuBICCG: PBiCG + DILU whatever the preconditioner word says."""
+    s = cases.convdiff_system(12, 11, 10, seed=4)
+    x, perf = run(mrg, tmp_path, s, "gpuBICCG", "none", 1e-9)
+    xm, pm = oracle_matrix(oracle_mod, s).solve_mirror(s.b, s.x0, "PBiCG", "DILU", tol=1e-9)
+    assert perf["solver"] == "gpuPBiCG" and perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+
+
 def test_smooth_solver_adapter(mrg, oracle_mod, tmp_path):
     """gpuSmoothSolver (smoother GaussSeidel): the tutorials' fluid U setting."""
     s = cases.convdiff_system(12, 11, 10, seed=9)

@@ -686,7 +686,13 @@ static void poll(BatchHost& bh, Ctl* h)
     }
 }
 
-// Replays the iteration graph until no member is in its Krylov loop.
+static void launch_recount_host(BatchHost& bh);
+
+// Replays the iteration graph until no member is in its Krylov loop.  A
+// batch of 8 or more members whose active count has fallen to half hands the
+// rest to its compacted sub-batch (recursively), so the loop's tail no
+// longer walks the finished members' tiles; afterwards the batch's counters
+// are recomputed from its members' states.
 static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long cap_iters, Ctl* h)
 {
     const int k = iters_per_launch(bh, cfg);
@@ -694,7 +700,27 @@ static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long ca
     poll(bh, h);
     long launches = 0;
     const long cap = cap_iters / k + 2;
+    const int nmem = (int)bh.members.size();
     while (h->n_active > 0 && launches <= cap) {
+        if (nmem >= 8 && 2 * (long)h->n_active <= nmem) {
+            std::vector<Scal> sc;
+            batch_status(bh, sc);
+            std::vector<PlanState*> act;
+            for (int s = 0; s < nmem; ++s)
+                if (sc[s].active) act.push_back(bh.members[s]);
+            if (!bh.compact) {
+                bh.compact.reset(new BatchHost());
+                bh.compact->init(bh.ctx);
+            }
+            BatchHost& sub = *bh.compact;
+            sub.tune = bh.tune;
+            sub.set(act);
+            launch_recount_host(sub);
+            run_iterations(sub, cfg, prec, (cap - launches) * k, h);
+            launch_recount_host(bh);
+            poll(bh, h);
+            return;
+        }
         launch_iterations(bh, cfg, prec, gr);
         ++launches;
         poll(bh, h);
@@ -915,6 +941,8 @@ void batch_recount(BatchHost& bh)
     launch_recount(bh.d, bh.ctx->st);
     MRG_CUDA(cudaGetLastError());
 }
+
+static void launch_recount_host(BatchHost& bh) { batch_recount(bh); }
 
 void batch_status(BatchHost& bh, std::vector<Scal>& out)
 {

@@ -90,6 +90,10 @@ struct BatchHost {
     };
     std::map<std::string, Graph> graphs;
     Tuning tune;
+    // Compacted sub-batch: once most members of a long batched loop have
+    // converged, the rest iterate in a batch of their own (their states and
+    // results are per system, so nothing changes but the work skipped).
+    std::unique_ptr<BatchHost> compact;
     void init(Ctx* c);
     // (Re)build the arrays for these systems; the order fixes the tile table.
     void set(const std::vector<PlanState*>& systems);

@@ -39,6 +39,29 @@ def test_batch_equals_alone(mrg, ctx, kw):
         m.close()
 
 
+@pytest.mark.parametrize("kw", [dict(), dict(precision="mixed", ordering="colour"),
+                                dict(solver="BiCGStab", precond="DILU", precision="mixed", ordering="colour")])
+def test_compacted_batch_equals_alone(mrg, ctx, kw):
+    """Twelve members of very uneven size: once half have converged the rest
+    iterate in a compacted sub-batch (and again at a quarter); every result
+    must still equal its lone solve bit for bit."""
+    sys_ = cases.c4(count=12, seed=11, n_lo=1000, n_hi=80000)
+    meshes = [gpu_mesh(mrg, ctx, s) for s in sys_]
+    alone = [m.solve(s.b, s.x0, tol=1e-8, iters_per_launch=4, **kw) for m, s in zip(meshes, sys_)]
+    b = mrg.Batch(ctx, meshes, ordering=kw.get("ordering", "exact"))
+    for rep in range(2):   # the second solve reuses the compacted batches' graphs
+        xs, perfs = b.solve([s.b for s in sys_], [s.x0 for s in sys_], tol=1e-8, iters_per_launch=4, **kw)
+        for (xa, pa), xb, pb in zip(alone, xs, perfs):
+            assert np.array_equal(xa, xb)
+            for k in ("initial_residual", "final_residual", "n_iter", "converged", "n_outer"):
+                assert pa[k] == pb[k], (k, pa, pb)
+    its = [p["n_iter"] for p in perfs]
+    assert len(set(its)) > 3   # uneven convergence: the tail runs compacted
+    b.close()
+    for m in meshes:
+        m.close()
+
+
 def test_batch_against_oracle(mrg, ctx, oracle_mod):
     sys_ = systems()
     meshes = [gpu_mesh(mrg, ctx, s) for s in sys_]

@@ -1256,20 +1256,29 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
 }
 
 // ---------------------------------------------------------------- staged SpMV
-// Amul + (q, p) of the Krylov loop with the sliced-ELL column indices and
-// coefficients staged in shared memory by the bulk-copy engine.  A segment's
-// tiles are walked in rounds of 8 slices -- one slice per warp, tile by
-// tile, slices w, w+8, w+16, w+24 of each tile: exactly ell_tile's rows in
-// ell_tile's order, so q, (q, p) and every bit downstream are unchanged.
-// Thread 0 keeps kStages - 1 rounds in flight (one contiguous cp.async.bulk
-// per array per round, completion counted on the stage's mbarrier); warps
-// read indices and coefficients from shared memory and only the x gathers
-// go to L1/L2.  A round whose entries exceed a stage (a slice wider than
-// kMaxW) is read from global memory instead.  Waits are bounded: on timeout
-// the error bit is set and the CTA leaves after its copies land.
+// Amul + (q, p) of the Krylov loop with the sliced-ELL column indices (and,
+// in FP64, the coefficients) staged in shared memory by the bulk-copy
+// engine.  A segment's tiles are walked in rounds of 8 slices -- one slice
+// per warp, tile by tile, slices w, w+8, w+16, w+24 of each tile: exactly
+// ell_tile's rows in ell_tile's order, so q, (q, p) and every bit downstream
+// are unchanged.  Thread 0 keeps the next rounds' copies in flight (one
+// contiguous cp.async.bulk per array per round, completion counted on the
+// stage's mbarrier).  In FP32 a warp takes two rounds per step and issues
+// both rounds' coefficient, own-x, diagonal and gathered-x loads before any
+// arithmetic: the gathers are the latency that bounds this kernel, and two
+// rounds of them in flight per warp cut its time by a sixth.  A round whose
+// entries exceed a stage (a slice wider than kMaxW) is read from global
+// memory instead.  Waits are bounded: on timeout the error bit is set and
+// the CTA leaves after its copies land.
 template <typename V> struct SpmvStages;
-template <> struct SpmvStages<float> { static constexpr int n = 3; };
-template <> struct SpmvStages<double> { static constexpr int n = 2; };
+// FP32: the column indices of four rounds staged (24 KB), two rounds per
+// step with their coefficients, own x and gathered x loaded together; FP64:
+// indices and coefficients of two rounds staged, one round per step.  A
+// segment has four rounds per tile, so a step's round count divides four.
+template <> struct SpmvStages<float> { static constexpr int n = 4, rounds = 2, vals = 0; };
+template <> struct SpmvStages<double> { static constexpr int n = 2, rounds = 1, vals = 1; };
+static_assert(4 % SpmvStages<float>::rounds == 0 && 4 % SpmvStages<double>::rounds == 0,
+              "rounds per step must divide a tile's four rounds");
 constexpr int kRoundEntries = (kBlock / 32) * kMaxW * 32;   // entries one stage holds
 
 __device__ __forceinline__ unsigned smem_u32(const void* p)
@@ -1322,7 +1331,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity
 template <typename V>
 constexpr size_t spmv_smem()
 {
-    return (size_t)SpmvStages<V>::n * kRoundEntries * (sizeof(int) + sizeof(V));
+    return (size_t)SpmvStages<V>::n * kRoundEntries * (sizeof(int) + (SpmvStages<V>::vals ? sizeof(V) : 0));
 }
 
 template <typename V>
@@ -1375,56 +1384,96 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
             const int e0 = __ldg(sptr + sb), cnt = __ldg(sptr + sb + 8) - e0;
             const int stg = r % S;
             if (cnt > 0 && cnt <= kRoundEntries) {
-                mbar_expect_tx(&full[stg], (unsigned)cnt * (unsigned)(sizeof(int) + sizeof(V)));
+                constexpr bool kVals = SpmvStages<V>::vals;
+                mbar_expect_tx(&full[stg], (unsigned)cnt * (unsigned)(sizeof(int) + (kVals ? sizeof(V) : 0)));
                 bulk_to_smem(st_col + stg * kRoundEntries, acol + e0, (unsigned)cnt * sizeof(int), &full[stg]);
-                bulk_to_smem(st_val + stg * kRoundEntries, aval + e0, (unsigned)cnt * sizeof(V), &full[stg]);
+                if (kVals)
+                    bulk_to_smem(st_val + stg * kRoundEntries, aval + e0, (unsigned)cnt * sizeof(V), &full[stg]);
             } else {
                 mbar_expect_tx(&full[stg], 0u);
             }
         };
+        // RP rounds per step (FP32: two, so both rounds' x gathers are in
+        // flight together); stages hold S rounds, S - RP of them issued ahead
+        constexpr int RP = SpmvStages<V>::rounds;
         if (tid == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            for (int r = 0; r < S - 1 && r < R; ++r) issue(r);
+            for (int r = 0; r < S - RP && r < R; ++r) issue(r);
         }
         double acc[kMaxRed] = {0.0, 0.0};
         bool ok = true;
-        for (int r = 0; r < R; ++r) {
-            const int stg = r % S;
-            if (tid == 0 && r + S - 1 < R) issue(r + S - 1);
-            if (!mbar_wait(&full[stg], (parity >> stg) & 1u, ctl)) {
-                ok = false;
-                break;
+        for (int r = 0; r < R; r += RP) {
+            if (tid == 0)
+                for (int j = 0; j < RP; ++j)
+                    if (r + S - RP + j < R) issue(r + S - RP + j);
+            for (int j = 0; j < RP && r + j < R; ++j) {
+                const int stg = (r + j) % S;
+                if (!mbar_wait(&full[stg], (parity >> stg) & 1u, ctl)) {
+                    ok = false;
+                    break;
+                }
+                parity ^= 1u << stg;
             }
-            parity ^= 1u << stg;
-            const int sb = 32 * (t0 + (r >> 2)) + 8 * (r & 3);
-            const int sl = sb + wid;
-            const int base = __ldg(sptr + sb);
-            const bool staged = __ldg(sptr + sb + 8) - base <= kRoundEntries;
-            const int e0 = __ldg(sptr + sl), W = (__ldg(sptr + sl + 1) - e0) >> 5;
-            const int i = sl * 32 + lane;
-            const V xi = __ldca(p + i);
-            V y = vmul(__ldg(dg + i), xi);
-            const int* __restrict__ c = staged ? st_col + stg * kRoundEntries + (e0 - base) + lane : acol + e0 + lane;
-            const V* __restrict__ a = staged ? st_val + stg * kRoundEntries + (e0 - base) + lane : aval + e0 + lane;
-            if (W <= kMaxW) {
-                int ck[kMaxW];
-                V av[kMaxW], xv[kMaxW];
+            if (!ok) break;
+            // this warp's slice of each round of the step, in round order
+            int i_[RP], W_[RP];
+            const int* c_[RP];
+            const V* a_[RP];
+            bool fast = true;
 #pragma unroll
-                for (int k = 0; k < kMaxW; ++k) ck[k] = k < W ? c[k * 32] : -1;
+            for (int j = 0; j < RP; ++j) {
+                const int rj = r + j;   // R = 4 tiles' rounds: a multiple of RP
+                const int stg = rj % S;
+                const int sb = 32 * (t0 + (rj >> 2)) + 8 * (rj & 3);
+                const int sl = sb + wid;
+                const int base = __ldg(sptr + sb);
+                const bool staged = __ldg(sptr + sb + 8) - base <= kRoundEntries;
+                const int e0 = __ldg(sptr + sl);
+                W_[j] = (__ldg(sptr + sl + 1) - e0) >> 5;
+                i_[j] = sl * 32 + lane;
+                c_[j] = staged ? st_col + stg * kRoundEntries + (e0 - base) + lane : acol + e0 + lane;
+                a_[j] = (staged && SpmvStages<V>::vals) ? st_val + stg * kRoundEntries + (e0 - base) + lane
+                                                         : aval + e0 + lane;
+                fast = fast && staged && W_[j] <= kMaxW;
+            }
+            if (fast) {
+                // every round's own x, diagonal and gathered x loads issued
+                // before any of the step's arithmetic
+                constexpr bool kVals = SpmvStages<V>::vals;
+                V xi[RP], dv[RP], xv[RP][kMaxW], av[RP][kVals ? 1 : kMaxW];
+                unsigned live[RP];
 #pragma unroll
-                for (int k = 0; k < kMaxW; ++k) {
-                    av[k] = ck[k] >= 0 ? a[k * 32] : V(0);
-                    xv[k] = ck[k] >= 0 ? __ldca(p + ck[k]) : V(0);
+                for (int j = 0; j < RP; ++j) {
+                    xi[j] = __ldca(p + i_[j]);
+                    dv[j] = __ldg(dg + i_[j]);
+                    live[j] = 0;
+#pragma unroll
+                    for (int k = 0; k < kMaxW; ++k) {
+                        const int ck = k < W_[j] ? c_[j][k * 32] : -1;
+                        live[j] |= (ck >= 0 ? 1u : 0u) << k;
+                        xv[j][k] = ck >= 0 ? __ldca(p + ck) : V(0);
+                        if constexpr (!kVals) av[j][k] = ck >= 0 ? __ldg(a_[j] + k * 32) : V(0);
+                    }
                 }
 #pragma unroll
-                for (int k = 0; k < kMaxW; ++k)
-                    if (ck[k] >= 0) y = vfma(av[k], xv[k], y);
+                for (int j = 0; j < RP; ++j) {
+                    V y = vmul(dv[j], xi[j]);
+#pragma unroll
+                    for (int k = 0; k < kMaxW; ++k)
+                        if (live[j] & (1u << k)) y = vfma(kVals ? a_[j][k * 32] : av[j][kVals ? 0 : k], xv[j][k], y);
+                    q[i_[j]] = y;
+                    acc[0] = __fma_rn(widen(y), widen(xi[j]), acc[0]);
+                }
             } else {
-                for (int k0 = 0; k0 < W; k0 += kMaxW) y = ell_round<V, false>(c, a, p, k0, W, y);
+                for (int j = 0; j < RP; ++j) {
+                    const V xi = __ldca(p + i_[j]);
+                    V y = vmul(__ldg(dg + i_[j]), xi);
+                    for (int k0 = 0; k0 < W_[j]; k0 += kMaxW) y = ell_round<V, false>(c_[j], a_[j], p, k0, W_[j], y);
+                    q[i_[j]] = y;
+                    acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
+                }
             }
-            q[i] = y;
-            acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
-            __syncthreads();   // this round's stage is free for round r + S
+            __syncthreads();   // this step's stages are free for the rounds S ahead
             if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
         if (!ok) {

@@ -52,7 +52,14 @@ enum {
 /* SMOOTH: foam's smoothSolver with the GaussSeidel smoother (the tutorials'
  * fluid U solves): n_sweeps Gauss-Seidel sweeps in foam's cell order, then
  * the residual, until converged; FP64, exact ordering only. */
-enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2, MRG_SOLVER_SMOOTH = 3 };
+/* GAMG: foam's geometric-algebraic multigrid solver (the tutorials' fluid
+ * p / T solves) with the GaussSeidel smoother: pairwise agglomeration on
+ * the coefficients (cached from the first matrix), a V-cycle per iteration
+ * (restricted residual, a direct solve of the coarsest level, prolonged
+ * corrections with nPostSweeps sweeps, nFinestSweeps on the finest level);
+ * FP64, exact ordering, a mesh without interfaces, one system at a time. */
+enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2, MRG_SOLVER_SMOOTH = 3,
+       MRG_SOLVER_GAMG = 4 };
 /* smoothSolver smoothers: GaussSeidel; DIC / DILU (each sweep adds
  * M^-1 (b - A psi) to psi with the incomplete factorisation M); and
  * DICGaussSeidel / DILUGaussSeidel (that step, then a Gauss-Seidel sweep). */
@@ -115,6 +122,9 @@ typedef struct {
     int smoother;          /* MRG_SOLVER_SMOOTH: MRG_SMOOTHER_*             */
     int n_sweeps;          /* MRG_SOLVER_SMOOTH: sweeps per residual check
                               (foam's nSweeps, default 1)                   */
+    int gamg_coarsest_cells; /* GAMG: nCellsInCoarsestLevel (default 10)     */
+    int gamg_post_sweeps;  /* GAMG: nPostSweeps (default 2)                 */
+    int gamg_finest_sweeps; /* GAMG: nFinestSweeps (default 2)              */
 } mrg_controls;
 
 /* lduSolverPerformance (initialResidual, finalResidual, nIterations,

@@ -13,6 +13,7 @@
 #include "engine.h"
 #include "kernels.h"
 #include "dn.h"
+#include "gamg.h"
 #include "ggi_build.h"
 #include "mono.h"
 #include "noalloc.h"
@@ -95,7 +96,17 @@ Controls to_controls(const mrg_controls* c)
     k.max_outer = c->max_outer > 0 ? c->max_outer : 50;
     k.k_launch = c->iters_per_launch > 0 ? c->iters_per_launch : 16;
     k.n_sweeps = c->n_sweeps > 0 ? c->n_sweeps : 1;
-    if (k.solver < 0 || k.solver > 3) throw Error(MRG_E_INVALID, "unknown solver");
+    if (k.solver < 0 || k.solver > 4) throw Error(MRG_E_INVALID, "unknown solver");
+    if (k.solver == MRG_SOLVER_GAMG) {
+        if (c->smoother != MRG_SMOOTHER_GAUSS_SEIDEL) throw Error(MRG_E_INVALID, "GAMG: smoother must be GaussSeidel");
+        if (c->precision != MRG_PRECISION_FP64 || c->ordering != MRG_ORDER_EXACT)
+            throw Error(MRG_E_INVALID, "GAMG runs in FP64 in foam's order (precision fp64, ordering exact)");
+        k.pc = PC_NONE;
+        k.gamg_coarsest = c->gamg_coarsest_cells > 0 ? c->gamg_coarsest_cells : 10;
+        k.gamg_post = c->gamg_post_sweeps >= 0 ? c->gamg_post_sweeps : 2;
+        k.gamg_finest = c->gamg_finest_sweeps >= 0 ? c->gamg_finest_sweeps : 2;
+        if (k.gamg_coarsest > 64) throw Error(MRG_E_INVALID, "GAMG: nCellsInCoarsestLevel must be at most 64");
+    }
     if (k.solver == MRG_SOLVER_SMOOTH) {
         if (c->smoother < MRG_SMOOTHER_GAUSS_SEIDEL || c->smoother > MRG_SMOOTHER_DILU_GAUSS_SEIDEL)
             throw Error(MRG_E_INVALID, "unknown smoother");
@@ -178,6 +189,9 @@ void mrg_controls_default(mrg_controls* c)
     c->iters_per_launch = 16;
     c->smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
     c->n_sweeps = 1;
+    c->gamg_coarsest_cells = 10;
+    c->gamg_post_sweeps = 2;
+    c->gamg_finest_sweeps = 2;
 }
 
 int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out)

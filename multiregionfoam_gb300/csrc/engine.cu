@@ -1,6 +1,7 @@
 // engine.cu -- host engine: device residency, plan upload, coefficient
 // views, batches, CUDA-graph iteration loops, FP32/FP64 iterative refinement.
 #include "engine.h"
+#include "gamg.h"
 
 #include <cuda_runtime.h>
 
@@ -860,6 +861,7 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
 
 Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
 {
+    if (cfg.solver == MRG_SOLVER_GAMG) return gamg_solve(m, d_b, d_x, cfg);
     PlanState& P = prepare(m, cfg);
     P.sys.in_b = d_b;
     P.sys.in_x = d_x;
@@ -943,6 +945,13 @@ void batch_recount(BatchHost& bh)
 }
 
 static void launch_recount_host(BatchHost& bh) { batch_recount(bh); }
+
+const Ctl& batch_poll(BatchHost& bh)
+{
+    Ctl* h = pinned_ctl();
+    poll(bh, h);
+    return *h;
+}
 
 void batch_status(BatchHost& bh, std::vector<Scal>& out)
 {

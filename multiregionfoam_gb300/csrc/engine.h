@@ -44,6 +44,8 @@ struct Controls {
     int inner_max_iter = 0, max_outer = 50, k_launch = 16;
     int n_sweeps = 1;   // smoothSolver: sweeps per residual check
     int smoother = 0;   // smoothSolver: MRG_SMOOTHER_*
+    int gamg_coarsest = 10, gamg_post = 2, gamg_finest = 2;   // GAMG: nCellsInCoarsestLevel, nPostSweeps,
+                                                              // nFinestSweeps
 };
 
 struct Perf {
@@ -127,6 +129,8 @@ struct PlanState {
     void sync_sys();          // copy host mirror to device
 };
 
+struct Gamg;
+
 struct Mesh {
     Ctx* ctx = nullptr;
     int n = 0, nf = 0, ni = 0;
@@ -137,6 +141,7 @@ struct Mesh {
     bool sym = true, has_int = false, have_coeffs = false;
     uint64_t version = 0;
     std::unique_ptr<PlanState> plans[2];
+    std::unique_ptr<Gamg> gamg;   // GAMG hierarchy (built at the first GAMG solve)
     PlanState& plan(int ordering);
     ~Mesh();
 };
@@ -176,6 +181,9 @@ void batch_fallback(BatchHost& bh, const Controls& c);
 void batch_outer(BatchHost& bh, const Controls& c);
 void batch_finish(BatchHost& bh);
 void batch_recount(BatchHost& bh);
+// The batch's control block, read after the stream drains (throws on a
+// device-side wait timeout).
+const Ctl& batch_poll(BatchHost& bh);
 void batch_status(BatchHost& bh, std::vector<Scal>& out);
 
 // Autotuner: time the Krylov loop of the prepared batch (members' in_b/in_x

@@ -9,6 +9,8 @@
 //   gpuMixedPCG       symMatrix   FP32 PCG inside FP64 iterative refinement
 //   gpuMixedPBiCG     asymMatrix  FP32 PBiCG inside FP64 iterative refinement
 //   gpuMixedBiCGStab  both        FP32 BiCGStab inside FP64 iterative refinement
+//   gpuGAMG           both        FP64 GAMG, GaussSeidel smoothing; nCellsInCoarsestLevel,
+//                                 nPostSweeps, nFinestSweeps
 //   gpuBICCG          both        FP64 PBiCG + DILU (foam's BICCG)
 //   gpuSmoothSolver   both        FP64 smoothSolver; smoother GaussSeidel | DIC | DILU |
 //                                 DICGaussSeidel | DILUGaussSeidel; nSweeps
@@ -137,7 +139,16 @@ public:
         c.min_iter = minIter_;
         c.max_iter = maxIter_;
         c.solver = solverKind_;
-        if (solverKind_ == MRG_SOLVER_SMOOTH) {
+        if (solverKind_ == MRG_SOLVER_GAMG) {
+            // GAMG's own words; the agglomeration is pairwise on the
+            // coefficients whatever agglomerator names, and it is cached
+            if (controls_.lookupWord("smoother", "GaussSeidel") != "GaussSeidel")
+                throw FatalError("gpuGAMG: unsupported smoother " + controls_.lookupWord("smoother"));
+            c.smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
+            c.gamg_coarsest_cells = (int)controls_.lookupOrDefault("nCellsInCoarsestLevel", 10.0);
+            c.gamg_post_sweeps = (int)controls_.lookupOrDefault("nPostSweeps", 2.0);
+            c.gamg_finest_sweeps = (int)controls_.lookupOrDefault("nFinestSweeps", 2.0);
+        } else if (solverKind_ == MRG_SOLVER_SMOOTH) {
             // smoothSolver's own words: smoother and nSweeps
             const word sm = controls_.lookupWord("smoother", "GaussSeidel");
             if (sm == "GaussSeidel") c.smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
@@ -159,8 +170,8 @@ public:
         mrg_perf perf;
         check(mrg_solve(mesh, source.data(), psi.data(), &c, &perf), "mrg_solve");
         lduMatrix::solverPerformance out;
-        static const char* const names[2][4] = {{"gpuPCG", "gpuPBiCG", "gpuBiCGStab", "gpuSmoothSolver"},
-                                                 {"gpuMixedPCG", "gpuMixedPBiCG", "gpuMixedBiCGStab", "-"}};
+        static const char* const names[2][5] = {{"gpuPCG", "gpuPBiCG", "gpuBiCGStab", "gpuSmoothSolver", "gpuGAMG"},
+                                                 {"gpuMixedPCG", "gpuMixedPBiCG", "gpuMixedBiCGStab", "-", "-"}};
         out.solverName = names[precision_ ? 1 : 0][solverKind_];
         out.fieldName = fieldName_;
         out.initialResidual = perf.initial_residual;
@@ -192,6 +203,7 @@ MRG_DEFINE_SOLVER(gpuMixedPBiCG, MRG_SOLVER_PBICG, MRG_PRECISION_MIXED)
 MRG_DEFINE_SOLVER(gpuBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_FP64)
 MRG_DEFINE_SOLVER(gpuMixedBiCGStab, MRG_SOLVER_BICGSTAB, MRG_PRECISION_MIXED)
 MRG_DEFINE_SOLVER(gpuSmoothSolver, MRG_SOLVER_SMOOTH, MRG_PRECISION_FP64)
+MRG_DEFINE_SOLVER(gpuGAMG, MRG_SOLVER_GAMG, MRG_PRECISION_FP64)
 
 // foam's BICCG: PBiCG with the DILU preconditioner built in (the tutorials'
 // fluid p solves); the preconditioner word is not read.
@@ -225,6 +237,8 @@ static addSymMatrixSolver<gpuBiCGStab> addGpuBiCGStabSym("gpuBiCGStab");
 static addAsymMatrixSolver<gpuBiCGStab> addGpuBiCGStab("gpuBiCGStab");
 static addSymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStabSym("gpuMixedBiCGStab");
 static addAsymMatrixSolver<gpuMixedBiCGStab> addGpuMixedBiCGStab("gpuMixedBiCGStab");
+static addSymMatrixSolver<gpuGAMG> addGpuGAMGSym("gpuGAMG");
+static addAsymMatrixSolver<gpuGAMG> addGpuGAMG("gpuGAMG");
 static addSymMatrixSolver<gpuBICCG> addGpuBICCGSym("gpuBICCG");
 static addAsymMatrixSolver<gpuBICCG> addGpuBICCG("gpuBICCG");
 // smoothSolver, like foam's, takes either kind of matrix.

@@ -15,7 +15,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmrgpu.so")
 
 MRG_OK, MRG_E_INVALID, MRG_E_OOM, MRG_E_BREAKDOWN, MRG_E_TIMEOUT, MRG_E_CUDA, MRG_E_BUSY = range(7)
-SOLVERS = {"PCG": 0, "PBiCG": 1, "BiCGStab": 2, "smoothSolver": 3}
+SOLVERS = {"PCG": 0, "PBiCG": 1, "BiCGStab": 2, "smoothSolver": 3, "GAMG": 4}
 SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "DILU": 2, "DICGaussSeidel": 3, "DILUGaussSeidel": 4}
 PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
@@ -48,7 +48,8 @@ class Controls(C.Structure):
                 ("max_iter", C.c_int), ("solver", C.c_int), ("preconditioner", C.c_int),
                 ("precision", C.c_int), ("ordering", C.c_int), ("inner_rel_tol", C.c_double),
                 ("inner_max_iter", C.c_int), ("max_outer", C.c_int), ("iters_per_launch", C.c_int),
-                ("smoother", C.c_int), ("n_sweeps", C.c_int)]
+                ("smoother", C.c_int), ("n_sweeps", C.c_int), ("gamg_coarsest_cells", C.c_int),
+                ("gamg_post_sweeps", C.c_int), ("gamg_finest_sweeps", C.c_int)]
 
 
 class Perf(C.Structure):
@@ -192,7 +193,8 @@ def _i(a):
 
 def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", precond="DIC",
              precision="fp64", ordering="exact", inner_rel_tol=1e-5, inner_max_iter=0, max_outer=50,
-             iters_per_launch=16, n_sweeps=1, smoother="GaussSeidel") -> Controls:
+             iters_per_launch=16, n_sweeps=1, smoother="GaussSeidel", n_coarsest_cells=10, n_post_sweeps=2,
+             n_finest_sweeps=2) -> Controls:
     c = Controls()
     load().mrg_controls_default(C.byref(c))
     c.tolerance, c.rel_tol, c.min_iter, c.max_iter = tol, rel_tol, min_iter, max_iter
@@ -201,6 +203,7 @@ def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", pre
     c.inner_rel_tol, c.inner_max_iter, c.max_outer = inner_rel_tol, inner_max_iter, max_outer
     c.iters_per_launch = iters_per_launch
     c.smoother, c.n_sweeps = SMOOTHERS[smoother], n_sweeps
+    c.gamg_coarsest_cells, c.gamg_post_sweeps, c.gamg_finest_sweeps = n_coarsest_cells, n_post_sweeps, n_finest_sweeps
     return c
 
 

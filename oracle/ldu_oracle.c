@@ -863,6 +863,61 @@ int or_smooth_gs(const or_ldu* m, const double* b, double* x, double tol, double
     return 0;
 }
 
+/* Building blocks for the GAMG restatement (oracle/gamg_oracle.py): one
+ * Gauss-Seidel sweep in place; the residual in foam's order (literal or
+ * fused); and, in the GPU's order, r = b - A x with sum|r| summed in the
+ * GPU's tree (row-sliced assignment) and the normalisation factor as the
+ * GPU computes it. */
+void or_gs_sweep(const or_ldu* m, const double* b, double* x, int fused)
+{
+    double* bp = (double*)malloc(sizeof(double) * (size_t)(m->n ? m->n : 1));
+    gs_sweep(m, b, x, bp, fused);
+    free(bp);
+}
+
+void or_foam_residual(const or_ldu* m, const double* b, const double* x, double* r, int fused)
+{
+    foam_residual(m, b, x, r, fused);
+}
+
+double or_mirror_residual(const or_ldu* m, const double* b, const double* x, double* r)
+{
+    int n = m->n;
+    double* t = (double*)malloc(sizeof(double) * (size_t)(n ? n : 1));
+    mr_order o;
+    mr_order_init(m, &o);
+    or_amul(m, x, r, 1);
+    for (int c = 0; c < n; ++c) {
+        r[c] = b[c] - r[c];
+        t[c] = fabs(r[c]);
+    }
+    double s = mr_reduce(&o, 1, 1, t, NULL);
+    free(o.perm);
+    free(t);
+    return s;
+}
+
+double or_mirror_norm_factor(const or_ldu* m, const double* b, const double* x)
+{
+    int n = m->n;
+    size_t bytes = sizeof(double) * (size_t)(n ? n : 1);
+    double *Ax = (double*)malloc(bytes), *t = (double*)malloc(bytes);
+    mr_order o;
+    mr_order_init(m, &o);
+    or_amul(m, x, Ax, 1);
+    double xbar = mr_reduce(&o, 0, 1, x, NULL) / (double)n;
+    or_sumA(m, t);
+    for (int c = 0; c < n; ++c) {
+        double tr = t[c] * xbar;
+        t[c] = fabs(Ax[c] - tr) + fabs(b[c] - tr);
+    }
+    double nf = mr_reduce(&o, 1, 1, t, NULL) + OR_SMALL;
+    free(o.perm);
+    free(Ax);
+    free(t);
+    return nf;
+}
+
 /* Foam-normalised residual of a given x (initial-residual formula). */
 double or_residual(const or_ldu* m, const double* b, const double* x)
 {

@@ -56,6 +56,12 @@ def lib():
                            C.c_int, C.c_int, C.POINTER(_Perf)]
         L.or_smooth_gs.argtypes = [pldu, dp, dp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.c_int, C.POINTER(_Perf)]
+        L.or_gs_sweep.argtypes = [pldu, dp, dp, C.c_int]
+        L.or_foam_residual.argtypes = [pldu, dp, dp, dp, C.c_int]
+        L.or_mirror_residual.argtypes = [pldu, dp, dp, dp]
+        L.or_mirror_residual.restype = C.c_double
+        L.or_mirror_norm_factor.argtypes = [pldu, dp, dp]
+        L.or_mirror_norm_factor.restype = C.c_double
         L.or_ggi_apply.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_int]
         L.gw_overlaps.argtypes = [C.c_int, ip, dp, C.c_int, ip, dp, C.c_double,
                                   C.c_long, ip, ip, dp]
@@ -189,6 +195,30 @@ class OracleMatrix:
                    "n_iter": p.n_iter, "converged": bool(p.converged), "singular": bool(p.singular)}
 
     SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "DILU": 2, "DICGaussSeidel": 3, "DILUGaussSeidel": 4}
+
+    # -- building blocks (GAMG restatement) ---------------------------------
+    def gs_sweep(self, b, x, fused=True):
+        """One Gauss-Seidel sweep of x in place."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        lib().or_gs_sweep(C.byref(self._s), _d(b), _d(x), int(fused))
+
+    def foam_residual(self, b, x, fused=False):
+        r = np.empty(self.n)
+        lib().or_foam_residual(C.byref(self._s), _d(np.ascontiguousarray(b, np.float64)),
+                               _d(np.ascontiguousarray(x, np.float64)), _d(r), int(fused))
+        return r
+
+    def mirror_residual(self, b, x):
+        """(r = b - A x in the GPU's order, sum|r| in the GPU's tree)."""
+        r = np.empty(self.n)
+        s = lib().or_mirror_residual(C.byref(self._s), _d(np.ascontiguousarray(b, np.float64)),
+                                     _d(np.ascontiguousarray(x, np.float64)), _d(r))
+        return r, s
+
+    def mirror_norm_factor(self, b, x):
+        return lib().or_mirror_norm_factor(C.byref(self._s), _d(np.ascontiguousarray(b, np.float64)),
+                                           _d(np.ascontiguousarray(x, np.float64)))
 
     def smooth(self, b, x0, tol=1e-8, rel_tol=0.0, min_iter=0, max_iter=1000, n_sweeps=1, mode="literal",
                smoother="GaussSeidel"):

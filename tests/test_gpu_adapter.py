@@ -116,12 +116,25 @@ def test_smooth_solver_adapter(mrg, oracle_mod, tmp_path):
     assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
 
 
+def test_gamg_adapter(mrg, oracle_mod, tmp_path):
+    """gpuGAMG with the tutorials' words (smoother GaussSeidel,
+    nCellsInCoarsestLevel 10)."""
+    import gamg_oracle as G
+    s = cases.convdiff_system(12, 11, 10, seed=9)
+    x, perf = run(mrg, tmp_path, s, "gpuGAMG", "none", 1e-8, ("smoother=GaussSeidel", "nCellsInCoarsestLevel=10",
+                                                              "agglomerator=faceAreaPair", "mergeLevels=1"))
+    g = G.Gamg(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c)
+    xm, pm = g.solve(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.b, s.x0, tol=1e-8, max_iter=5000)
+    assert perf["solver"] == "gpuGAMG" and perf["converged"] == 1
+    assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+
+
 def test_unknown_solver_is_fatal(mrg, tmp_path):
     s = cases.cht_system(6, 6, 6, 3)
     from multiregionfoam_gb300 import _build
     exe = _build.build_adapter()
     sysf = str(tmp_path / "sys.bin")
     write_system(sysf, s)
-    r = subprocess.run([exe, sysf, "gpuGAMG", "none", "1e-6", str(tmp_path / "x.bin")], capture_output=True,
+    r = subprocess.run([exe, sysf, "gpuAMGX", "none", "1e-6", str(tmp_path / "x.bin")], capture_output=True,
                        text=True, timeout=60)
-    assert r.returncode == 1 and "Unknown symmetric matrix solver gpuGAMG" in r.stdout
+    assert r.returncode == 1 and "Unknown symmetric matrix solver gpuAMGX" in r.stdout

@@ -86,6 +86,41 @@ __device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ double vfma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
+// Reduction terms of N consecutive rows (N = 2 or 4) into an FP64
+// accumulator.  FP64: every row's term in FP64, row by row (the order the
+// FP64 path is mirrored in).  FP32: the N terms are summed pairwise in
+// FP32 and the partial widened and added once -- one FP64 operation per N
+// rows instead of one per row on a part whose FP64 rate is a small
+// fraction of its FP32 rate; the partial's rounding (a few FP32 ulps) is
+// that of the FP32 vectors themselves.
+template <int N>
+__device__ __forceinline__ void acc_dot(double& acc, const double (&a)[N], const double (&b)[N])
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc = __fma_rn(a[k], b[k], acc);
+}
+template <int N>
+__device__ __forceinline__ void acc_dot(double& acc, const float (&a)[N], const float (&b)[N])
+{
+    static_assert(N == 2 || N == 4, "pairwise FP32 partial of 2 or 4 rows");
+    float s = __fmaf_rn(a[1], b[1], __fmul_rn(a[0], b[0]));
+    if constexpr (N == 4) s = __fadd_rn(s, __fmaf_rn(a[3], b[3], __fmul_rn(a[2], b[2])));
+    acc += widen(s);
+}
+template <int N>
+__device__ __forceinline__ void acc_abs(double& acc, const double (&a)[N])
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc += fabs(a[k]);
+}
+template <int N>
+__device__ __forceinline__ void acc_abs(double& acc, const float (&a)[N])
+{
+    static_assert(N == 2 || N == 4, "pairwise FP32 partial of 2 or 4 rows");
+    float s = __fadd_rn(fabsf(a[0]), fabsf(a[1]));
+    if constexpr (N == 4) s = __fadd_rn(s, __fadd_rn(fabsf(a[2]), fabsf(a[3])));
+    acc += widen(s);
+}
 __device__ __forceinline__ double ld_relaxed(const double* p)
 {
     double v;
@@ -733,7 +768,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         ld4(v.w + r4, w);
         ld4((PB ? v.rT : v.r) + r4, rr);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) acc[0] = __fma_rn(widen(w[k]), widen(rr[k]), acc[0]);
+        acc_dot<4>(acc[0], w, rr);
     } else if constexpr (OP == OP_PUPDATE) {
         const Vecs<V>& v = VP<V>::v(S);
         const int it = S.sc->iter;
@@ -806,8 +841,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             for (int k = 0; k < 4; ++k) rT[k] = vfma(-alpha, qT[k], rT[k]);
             st4(v.rT + r4, rT);
         }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[0] += fabs(widen(r[k]));
+        acc_abs<4>(acc[0], r);
     } else if constexpr (OP == OP_PRECOND_DIAG) {
         const Vecs<V>& v = VP<V>::v(S);
         V d[4], r[4], w[4];
@@ -922,8 +956,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         V r[4];
         ld4(v.r + r4, r);
         st4(v.rT + r4, r);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[0] = __fma_rn(widen(r[k]), widen(r[k]), acc[0]);
+        acc_dot<4>(acc[0], r, r);
     } else if constexpr (OP == OP_BS_P) {
         // p = r + beta (p - omega v), p = r on the first iteration (into
         // wT); with a diagonal or no preconditioner M^-1 p goes straight to p
@@ -977,8 +1010,7 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         }
         st4(v.x + r4, x);
         st4(v.r + r4, r);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[0] += fabs(widen(r[k]));
+        acc_abs<4>(acc[0], r);
         if (S.pc == PC_DIAG) {
             V d[4];
             ld4(VP<V>::rD(S) + r4, d);
@@ -1016,11 +1048,8 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         }
         st4(v.x + r4, x);
         st4(v.r + r4, r);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            acc[0] += fabs(widen(r[k]));
-            acc[1] = __fma_rn(widen(rt[k]), widen(r[k]), acc[1]);
-        }
+        acc_abs<4>(acc[0], r);
+        acc_dot<4>(acc[1], rt, r);
     } else if constexpr (OP == OP_GS_ARM || OP == OP_GS_COPY) {
         const int n = S.n;
         double* __restrict__ x = S.v64.x;
@@ -1487,6 +1516,18 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
     }
 }
 
+// FP32 levelled sweeps two chunks per warp step (k_sweep_lvl with PAIRS);
+// MRG_SWEEP_PAIRS=0 takes one chunk per step.
+static bool sweep_pairs()
+{
+    static int on = -1;
+    if (on < 0) {
+        const char* e = std::getenv("MRG_SWEEP_PAIRS");
+        on = (e && e[0] == '0') ? 0 : 1;
+    }
+    return on == 1;
+}
+
 // Launch with programmatic stream serialisation (pdl_enter in the kernel);
 // MRG_PDL=0 launches plainly.
 static bool pdl_enabled()
@@ -1767,6 +1808,72 @@ __device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1
     }
 }
 
+// Levelled FP32 sweeps can take two chunks per warp step (k_sweep_lvl
+// with PAIRS); the pair's loads need more registers than kMinCtas CTAs per
+// SM leave, so that kernel runs kSweepPairCtas per SM.
+constexpr int kSweepPairCtas = 3;
+
+// Two chunks of one level of a levelled sweep, both at most one round wide
+// (W <= kMaxW), by one warp: both chunks' own values, indices,
+// coefficients and dependency values are loaded before any arithmetic, so
+// the two chains of dependent loads (indices, then gathered values) are in
+// flight together.  Each row accumulates in the order sweep_rows uses.
+template <typename V, bool FWD>
+__device__ __forceinline__ void sweep_rows_pair(const SweepPtrs<V>& P, const int (&r0)[2], const int (&r1)[2],
+                                                const int (&e0)[2], const int (&W)[2], int lvl0_end,
+                                                bool last_level, bool first_level)
+{
+    const int lane = threadIdx.x & 31;
+    V* __restrict__ y = P.y;
+    V* __restrict__ w = P.w;
+    const V* __restrict__ r = P.r;
+    const V* __restrict__ rD = P.rD;
+    const V* dep = FWD ? y : w;
+    const bool from_r = FWD || first_level;
+    int i[2];
+    bool live[2];
+    V a0[2], a1[2];
+    int col[2][kMaxW];
+    V cf[2][kMaxW], d[2][kMaxW];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        i[h] = r0[h] + lane;
+        live[h] = i[h] < r1[h];
+        a0[h] = live[h] ? (from_r ? __ldg(rD + i[h]) : __ldca(y + i[h])) : V(0);
+        a1[h] = live[h] && from_r ? __ldca(r + i[h]) : V(0);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k)
+            col[h][k] = live[h] && k < W[h] ? __ldg(P.col + e0[h] + k * 32 + lane) : -1;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            const int ck = col[h][k];
+            cf[h][k] = ck >= 0 ? __ldg(P.coef + e0[h] + k * 32 + lane) : V(0);
+            if (FWD)
+                d[h][k] = ck < 0 ? V(0) : __ldca((ck < lvl0_end ? r : dep) + ck);   // level 0: rD folded into cf
+            else
+                d[h][k] = ck < 0 ? V(0) : __ldca(dep + ck);
+        }
+    // an absent entry has cf = d = 0, and fma(-0, 0, acc) is acc bit for bit
+    // (signed zeros included), so the indices die once the gathers are issued
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        V acc = from_r ? vmul(a0[h], a1[h]) : a0[h];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) acc = vfma(-cf[h][k], d[h][k], acc);
+        if (live[h]) {
+            if (FWD && !last_level)
+                y[i[h]] = acc;
+            else
+                w[i[h]] = acc;
+        }
+    }
+}
+
 template <typename V, bool FWD>
 __device__ __forceinline__ void sweep_chunk(const SweepPtrs<V>& P, int c, bool syncfree, Ctl* ctl, int lvl0_end,
                                             bool last_level, bool first_level)
@@ -1823,7 +1930,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __re
 // Lane k of a warp fetches the item and the row / entry bounds of the
 // warp's k-th next chunk, so 32 chunks' metadata costs one chain of
 // dependent loads instead of one chain per chunk.
-template <typename V, bool FWD>
+template <typename V, bool FWD, bool PAIRS = false>
 __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans)
 {
     if (L >= B.maxlevels) return;
@@ -1868,17 +1975,34 @@ __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans
                     P = sweep_ptrs<V, FWD>(S, trans);
                 }
             }
-            if (ok) sweep_rows<V, FWD>(P, r0, r1, e0, W, false, nullptr, lvl0_end, last, first);
+            if (!ok) continue;
+            if constexpr (PAIRS) {
+                // pair with the warp's next item when it is the same system's
+                // and both fit one round
+                if (j + 1 < cnt && W <= kMaxW) {
+                    const int s2 = __shfl_sync(kFull, ms, j + 1), W2 = __shfl_sync(kFull, mW, j + 1);
+                    const int r0b = __shfl_sync(kFull, mr0, j + 1), r1b = __shfl_sync(kFull, mr1, j + 1);
+                    const int e0b = __shfl_sync(kFull, me0, j + 1);
+                    if (s2 == cur && W2 <= kMaxW) {
+                        const int pr0[2] = {r0, r0b}, pr1[2] = {r1, r1b}, pe0[2] = {e0, e0b}, pW[2] = {W, W2};
+                        sweep_rows_pair<V, FWD>(P, pr0, pr1, pe0, pW, lvl0_end, last, first);
+                        ++j;
+                        continue;
+                    }
+                }
+            }
+            sweep_rows<V, FWD>(P, r0, r1, e0, W, false, nullptr, lvl0_end, last, first);
         }
     }
 }
 
-template <typename V, bool FWD>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
+template <typename V, bool FWD, bool PAIRS>
+__global__ void __launch_bounds__(kBlock, PAIRS ? kSweepPairCtas : kMinCtas)
+    k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
 {
     pdl_enter();
     const Batch B = *pB;
-    sweep_lvl_phase<V, FWD>(B, L, trans);
+    sweep_lvl_phase<V, FWD, PAIRS>(B, L, trans);
 }
 
 // ---------------------------------------------------------------- Gauss-Seidel
@@ -2276,14 +2400,22 @@ void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, co
     } else {
         if (precision == 0) {
             if (fwd)
-                launch_pdl(k_sweep_lvl<double, true>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<double, true, false>, grid, kBlock, 0, st, dB, level, trans);
             else
-                launch_pdl(k_sweep_lvl<double, false>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<double, false, false>, grid, kBlock, 0, st, dB, level, trans);
+        } else if (sweep_pairs()) {
+            // the grid the caller sized for kMinCtas CTAs per SM, at the
+            // paired kernel's occupancy
+            const int g = std::max(1, grid / kMinCtas * kSweepPairCtas);
+            if (fwd)
+                launch_pdl(k_sweep_lvl<float, true, true>, g, kBlock, 0, st, dB, level, trans);
+            else
+                launch_pdl(k_sweep_lvl<float, false, true>, g, kBlock, 0, st, dB, level, trans);
         } else {
             if (fwd)
-                launch_pdl(k_sweep_lvl<float, true>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, true, false>, grid, kBlock, 0, st, dB, level, trans);
             else
-                launch_pdl(k_sweep_lvl<float, false>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, false, false>, grid, kBlock, 0, st, dB, level, trans);
         }
     }
 }

@@ -767,7 +767,6 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
         V w[4], rr[4];
         ld4(v.w + r4, w);
         ld4((PB ? v.rT : v.r) + r4, rr);
-#pragma unroll
         acc_dot<4>(acc[0], w, rr);
     } else if constexpr (OP == OP_PUPDATE) {
         const Vecs<V>& v = VP<V>::v(S);
@@ -1132,15 +1131,16 @@ __device__ __forceinline__ bool system_live(const SysDev& S)
     return true;
 }
 
-// Close reduction segment `seg` of one system (consecutive tiles, `count`
-// of them, handled by this CTA): block tree, partial into slot `seg`, and
+// Close reduction segment `seg` of one system (consecutive units -- tiles,
+// or for the FP32 SpMV rounds -- `count` of them, handled by this CTA, of
+// `total` units the system has; total < 0: its tile count): block tree, partial into slot `seg`, and
 // the CTA that completes the system's tile count sums the G slots -- thread
 // t the slots t, t + 256, ... in order -- and finalises.  Every slot is
 // rewritten by every reduction, so none needs clearing.  Deterministic: the
 // order depends only on the system.
 template <RowOp OP>
 __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, int seg, int count,
-                                              double (&acc)[kMaxRed], double* sh, int* s_last)
+                                              double (&acc)[kMaxRed], double* sh, int* s_last, int total = -1)
 {
     constexpr int NR = OpTraits<OP>::kNR;
     const int tid = threadIdx.x;
@@ -1153,7 +1153,7 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
         for (int k = 0; k < NR; ++k) S.partials[seg * kMaxRed + k] = a[k];
         __threadfence();
         const unsigned prev = atomicAdd(S.counter, (unsigned)count);
-        *s_last = (prev + (unsigned)count == (unsigned)S.ntiles);
+        *s_last = (prev + (unsigned)count == (unsigned)(total < 0 ? S.ntiles : total));
     }
     __syncthreads();
     if (*s_last) {
@@ -1186,6 +1186,25 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
         }
     }
     __syncthreads();
+}
+
+// Amul + (q, p) over rounds [rb, re) of one system (round r: the rows of
+// slice 8 r + w for warp w, kBlock / 32 = 8 warps), row by row in round order.
+template <typename V>
+__device__ __forceinline__ void spmv_rounds(const SysDev& S, int rb, int re, double (&acc)[kMaxRed])
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const V* __restrict__ av = VP<V>::aval(S, false);
+    const V* __restrict__ dg = VP<V>::diag(S);
+    const V* __restrict__ p = VP<V>::v(S).p;
+    V* __restrict__ q = VP<V>::v(S).q;
+    for (int r = rb; r < re; ++r) {
+        const int i = ((kBlock / 32) * r + wid) * 32 + lane;
+        const V xi = __ldca(p + i);
+        const V y = ell_row<V>(S.a_sptr, S.a_col, av, dg, p, i);
+        q[i] = y;
+        acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
+    }
 }
 
 // Row kernel over a batch.  Non-reducing ops: grid-stride over the tile
@@ -1255,6 +1274,17 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             }
             if (!live) continue;
             const unsigned T = (unsigned)sS.ntiles, G = (unsigned)red_segments(sS.ntiles);
+            if constexpr (OP == OP_SPMV_QP && !PB && sizeof(V) == 4) {
+                // FP32 Amul + (q, p): segments of rounds, each thread's rows
+                // and their order k_spmv_warp's, so both give the same bits
+                const unsigned long long U = 4ull * T;
+                const int u0 = (int)(((unsigned long long)sg.y * U) / G);
+                const int u1 = (int)(((unsigned long long)(sg.y + 1) * U) / G);
+                double acc[kMaxRed] = {0.0, 0.0};
+                spmv_rounds<V>(sS, u0, u1, acc);
+                flush_segment<OP>(B, sS, sg.y, u1 - u0, acc, sh, s_last, (int)U);
+                continue;
+            }
             const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
             if constexpr (OpTraits<OP>::kElem) {
@@ -1287,28 +1317,28 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
 // ---------------------------------------------------------------- staged SpMV
 // Amul + (q, p) of the Krylov loop with the sliced-ELL column indices (and,
 // in FP64, the coefficients) staged in shared memory by the bulk-copy
-// engine.  A segment's tiles are walked in rounds of 8 slices -- one slice
-// per warp, tile by tile, slices w, w+8, w+16, w+24 of each tile: exactly
-// ell_tile's rows in ell_tile's order, so q, (q, p) and every bit downstream
-// are unchanged.  Thread 0 keeps the next rounds' copies in flight (one
-// contiguous cp.async.bulk per array per round, completion counted on the
-// stage's mbarrier).  In FP32 a warp takes two rounds per step and issues
-// both rounds' coefficient, own-x, diagonal and gathered-x loads before any
-// arithmetic: the gathers are the latency that bounds this kernel, and two
-// rounds of them in flight per warp cut its time by a sixth.  A round whose
-// entries exceed a stage (a slice wider than kMaxW) is read from global
-// memory instead.  Waits are bounded: on timeout the error bit is set and
-// the CTA leaves after its copies land.
+// engine.  Rows are walked in rounds of 8 slices, one slice per warp (round
+// r: slices 8 r .. 8 r + 7, so a 1024-row tile is four rounds and warp w
+// takes its slices w, w+8, w+16, w+24 -- ell_tile's rows in ell_tile's
+// order).  Every warp keeps its own ring of stages, each holding one of its
+// slices, and its own mbarriers; its lane 0 keeps the copies of the warp's
+// next slices in flight (one cp.async.bulk per array per slice), and a stage
+// is released by __syncwarp, so within a segment no warp waits for another.
+// In FP32 a warp takes two rounds per step and issues both rounds'
+// coefficient, own-x, diagonal and gathered-x loads before any arithmetic:
+// the gathers are the latency that bounds this kernel.  A slice wider than
+// a stage (W > kMaxW) is read from global memory instead.  Waits are
+// bounded: on timeout the error bit is set and the CTA leaves after its
+// copies land.
 template <typename V> struct SpmvStages;
-// FP32: the column indices of four rounds staged (24 KB), two rounds per
-// step with their coefficients, own x and gathered x loaded together; FP64:
-// indices and coefficients of two rounds staged, one round per step.  A
-// segment has four rounds per tile, so a step's round count divides four.
+// Stages per warp -- FP32: four (column indices; 24 KB per CTA), two rounds
+// per step with their coefficients, own x and gathered x loaded together;
+// FP64: two (indices and coefficients), one round per step.
 template <> struct SpmvStages<float> { static constexpr int n = 4, rounds = 2, vals = 0; };
 template <> struct SpmvStages<double> { static constexpr int n = 2, rounds = 1, vals = 1; };
-static_assert(4 % SpmvStages<float>::rounds == 0 && 4 % SpmvStages<double>::rounds == 0,
-              "rounds per step must divide a tile's four rounds");
-constexpr int kRoundEntries = (kBlock / 32) * kMaxW * 32;   // entries one stage holds
+static_assert(4 % SpmvStages<double>::rounds == 0, "FP64 segments are whole tiles of four rounds");
+static_assert(kTileRows == 4 * kBlock, "a tile is four rounds of one slice per warp");
+constexpr int kSliceEntries = kMaxW * 32;                    // entries one stage holds
 
 __device__ __forceinline__ unsigned smem_u32(const void* p)
 {
@@ -1360,31 +1390,44 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity
 template <typename V>
 constexpr size_t spmv_smem()
 {
-    return (size_t)SpmvStages<V>::n * kRoundEntries * (sizeof(int) + (SpmvStages<V>::vals ? sizeof(V) : 0));
+    return (size_t)(kBlock / 32) * SpmvStages<V>::n * kSliceEntries *
+           (sizeof(int) + (SpmvStages<V>::vals ? sizeof(V) : 0));
 }
 
+// Segments: FP64 whole tiles (the reduction order the oracle mirrors);
+// FP32 rounds, so that segments differ by one round at most instead of one
+// tile (at five tiles a segment, a fifth of the work).  rows_phase's FP32
+// Amul + (q, p) (the persistent kernel's) walks the same rounds.
 template <typename V>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* __restrict__ pB)
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __restrict__ pB)
 {
     constexpr int S = SpmvStages<V>::n;
+    constexpr int RP = SpmvStages<V>::rounds;
+    constexpr bool kVals = SpmvStages<V>::vals;
+    constexpr int NW = kBlock / 32;
     __shared__ double sh[kBlock * kMaxRed];
-    __shared__ int s_last;
+    __shared__ int s_last, s_abort;
     __shared__ __align__(16) SysDev sS;
-    __shared__ __align__(8) unsigned long long full[S];
+    __shared__ __align__(8) unsigned long long full[NW][S];
     extern __shared__ __align__(128) unsigned char dyn[];
-    int* st_col = reinterpret_cast<int*>(dyn);
-    V* st_val = reinterpret_cast<V*>(dyn + sizeof(int) * S * kRoundEntries);
     pdl_enter();
     const Batch B = *pB;
     Ctl* ctl = B.ctl;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) {
+    // this warp's stage k: indices at col_st(k), coefficients at val_st(k),
+    // mbarrier full[wid][k]
+    int* const st_col = reinterpret_cast<int*>(dyn);
+    V* const st_val = reinterpret_cast<V*>(dyn + sizeof(int) * NW * S * kSliceEntries);
+#define col_st(k) (st_col + (wid * S + (k)) * kSliceEntries)
+#define val_st(k) (st_val + (wid * S + (k)) * kSliceEntries)
+    if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < S; ++k) mbar_init(&full[k], 1);
+        for (int k = 0; k < S; ++k) mbar_init(&full[wid][k], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (tid == 0) s_abort = 0;
     __syncthreads();
-    unsigned parity = 0;   // bit k: parity of stage k's next completion (same in every thread)
+    unsigned parity = 0;   // bit k: parity of this warp's stage k's next completion
     int cur = -1, lcur = -1;
     bool live = false;
     for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
@@ -1398,90 +1441,82 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
             live = system_live<OP_SPMV_QP>(sS);
         }
         if (!live) continue;
+        constexpr bool kRoundSeg = sizeof(V) == 4;
         const unsigned T = (unsigned)sS.ntiles, G = (unsigned)red_segments(sS.ntiles);
-        const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
-        const int R = (t1 - t0) * 4;
+        const unsigned long long U = kRoundSeg ? 4ull * T : (unsigned long long)T;
+        const int u0 = (int)(((unsigned long long)sg.y * U) / G), u1 = (int)(((unsigned long long)(sg.y + 1) * U) / G);
+        // rounds [rb, re) of the system; round r: this warp's slice NW r + wid,
+        // into stage r % S (each stage's parity is tracked on its own, so the
+        // ring may start at any stage)
+        const int rb = kRoundSeg ? u0 : 4 * u0;
+        const int re = kRoundSeg ? u1 : 4 * u1;
         const int* __restrict__ sptr = sS.a_sptr;
         const int* __restrict__ acol = sS.a_col;
         const V* __restrict__ aval = VP<V>::aval(sS, false);
         const V* __restrict__ dg = VP<V>::diag(sS);
         const V* __restrict__ p = VP<V>::v(sS).p;
         V* __restrict__ q = VP<V>::v(sS).q;
-        // round r: slices sb .. sb+7 with sb = 32 (t0 + r/4) + 8 (r%4), into stage r % S
         auto issue = [&](int r) {
-            const int sb = 32 * (t0 + (r >> 2)) + 8 * (r & 3);
-            const int e0 = __ldg(sptr + sb), cnt = __ldg(sptr + sb + 8) - e0;
+            const int sl = NW * r + wid;
+            const int e0 = __ldg(sptr + sl), cnt = __ldg(sptr + sl + 1) - e0;
             const int stg = r % S;
-            if (cnt > 0 && cnt <= kRoundEntries) {
-                constexpr bool kVals = SpmvStages<V>::vals;
-                mbar_expect_tx(&full[stg], (unsigned)cnt * (unsigned)(sizeof(int) + (kVals ? sizeof(V) : 0)));
-                bulk_to_smem(st_col + stg * kRoundEntries, acol + e0, (unsigned)cnt * sizeof(int), &full[stg]);
-                if (kVals)
-                    bulk_to_smem(st_val + stg * kRoundEntries, aval + e0, (unsigned)cnt * sizeof(V), &full[stg]);
+            if (cnt > 0 && cnt <= kSliceEntries) {
+                mbar_expect_tx(&full[wid][stg], (unsigned)cnt * (unsigned)(sizeof(int) + (kVals ? sizeof(V) : 0)));
+                bulk_to_smem(col_st(stg), acol + e0, (unsigned)cnt * sizeof(int), &full[wid][stg]);
+                if (kVals) bulk_to_smem(val_st(stg), aval + e0, (unsigned)cnt * sizeof(V), &full[wid][stg]);
             } else {
-                mbar_expect_tx(&full[stg], 0u);
+                mbar_expect_tx(&full[wid][stg], 0u);
             }
         };
-        // RP rounds per step (FP32: two, so both rounds' x gathers are in
-        // flight together); stages hold S rounds, S - RP of them issued ahead
-        constexpr int RP = SpmvStages<V>::rounds;
-        if (tid == 0) {
+        if (lane == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            for (int r = 0; r < S - RP && r < R; ++r) issue(r);
+            for (int r = rb; r < rb + S - RP && r < re; ++r) issue(r);
         }
         double acc[kMaxRed] = {0.0, 0.0};
         bool ok = true;
-        for (int r = 0; r < R; r += RP) {
-            if (tid == 0)
+        int r = rb;
+        for (; r < re; r += RP) {
+            if (lane == 0)
                 for (int j = 0; j < RP; ++j)
-                    if (r + S - RP + j < R) issue(r + S - RP + j);
-            for (int j = 0; j < RP && r + j < R; ++j) {
+                    if (r + S - RP + j < re) issue(r + S - RP + j);
+            for (int j = 0; j < RP && r + j < re; ++j) {
                 const int stg = (r + j) % S;
-                if (!mbar_wait(&full[stg], (parity >> stg) & 1u, ctl)) {
-                    ok = false;
-                    break;
-                }
+                if (!mbar_wait(&full[wid][stg], (parity >> stg) & 1u, ctl)) ok = false;
                 parity ^= 1u << stg;
             }
-            if (!ok) break;
-            // this warp's slice of each round of the step, in round order
-            int i_[RP], W_[RP];
-            const int* c_[RP];
-            const V* a_[RP];
+            if (!__all_sync(kFull, ok)) {
+                ok = false;
+                break;
+            }
+            // a slice is staged exactly when it fits a stage (W <= kMaxW):
+            // the fast path reads its indices by shared-memory offset
+            int i_[RP], W_[RP], e_[RP], cs[RP];
             bool fast = true;
 #pragma unroll
             for (int j = 0; j < RP; ++j) {
-                const int rj = r + j;   // R = 4 tiles' rounds: a multiple of RP
-                const int stg = rj % S;
-                const int sb = 32 * (t0 + (rj >> 2)) + 8 * (rj & 3);
-                const int sl = sb + wid;
-                const int base = __ldg(sptr + sb);
-                const bool staged = __ldg(sptr + sb + 8) - base <= kRoundEntries;
-                const int e0 = __ldg(sptr + sl);
-                W_[j] = (__ldg(sptr + sl + 1) - e0) >> 5;
+                const int rj = r + j;   // FP32 segments may end on an odd round
+                const bool on = rj < re;
+                const int sl = NW * rj + wid;
+                e_[j] = on ? __ldg(sptr + sl) : 0;
+                W_[j] = on ? (__ldg(sptr + sl + 1) - e_[j]) >> 5 : 0;
                 i_[j] = sl * 32 + lane;
-                c_[j] = staged ? st_col + stg * kRoundEntries + (e0 - base) + lane : acol + e0 + lane;
-                a_[j] = (staged && SpmvStages<V>::vals) ? st_val + stg * kRoundEntries + (e0 - base) + lane
-                                                         : aval + e0 + lane;
-                fast = fast && staged && W_[j] <= kMaxW;
+                cs[j] = (wid * S + rj % S) * kSliceEntries + lane;
+                fast = fast && on && W_[j] <= kMaxW;
             }
             if (fast) {
-                // every round's own x, diagonal and gathered x loads issued
-                // before any of the step's arithmetic
-                constexpr bool kVals = SpmvStages<V>::vals;
-                V xi[RP], dv[RP], xv[RP][kMaxW], av[RP][kVals ? 1 : kMaxW];
-                unsigned live[RP];
+                V xi[RP], dv[RP], xv[RP][kMaxW], av[RP][kMaxW];
+                unsigned lv[RP];
 #pragma unroll
                 for (int j = 0; j < RP; ++j) {
                     xi[j] = __ldca(p + i_[j]);
                     dv[j] = __ldg(dg + i_[j]);
-                    live[j] = 0;
+                    lv[j] = 0;
 #pragma unroll
                     for (int k = 0; k < kMaxW; ++k) {
-                        const int ck = k < W_[j] ? c_[j][k * 32] : -1;
-                        live[j] |= (ck >= 0 ? 1u : 0u) << k;
+                        const int ck = k < W_[j] ? st_col[cs[j] + k * 32] : -1;
+                        lv[j] |= (ck >= 0 ? 1u : 0u) << k;
                         xv[j][k] = ck >= 0 ? __ldca(p + ck) : V(0);
-                        if constexpr (!kVals) av[j][k] = ck >= 0 ? __ldg(a_[j] + k * 32) : V(0);
+                        if constexpr (!kVals) av[j][k] = ck >= 0 ? __ldg(aval + e_[j] + lane + k * 32) : V(0);
                     }
                 }
 #pragma unroll
@@ -1489,32 +1524,43 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_staged(const Batch* _
                     V y = vmul(dv[j], xi[j]);
 #pragma unroll
                     for (int k = 0; k < kMaxW; ++k)
-                        if (live[j] & (1u << k)) y = vfma(kVals ? a_[j][k * 32] : av[j][kVals ? 0 : k], xv[j][k], y);
+                        if (lv[j] & (1u << k)) y = vfma(kVals ? st_val[cs[j] + k * 32] : av[j][k], xv[j][k], y);
                     q[i_[j]] = y;
                     acc[0] = __fma_rn(widen(y), widen(xi[j]), acc[0]);
                 }
             } else {
-                for (int j = 0; j < RP; ++j) {
+                for (int j = 0; j < RP && r + j < re; ++j) {
+                    const bool staged = W_[j] <= kMaxW;
+                    const int* cp = staged ? st_col + cs[j] : acol + e_[j] + lane;
+                    const V* ap = (staged && kVals) ? st_val + cs[j] : aval + e_[j] + lane;
                     const V xi = __ldca(p + i_[j]);
                     V y = vmul(__ldg(dg + i_[j]), xi);
-                    for (int k0 = 0; k0 < W_[j]; k0 += kMaxW) y = ell_round<V, false>(c_[j], a_[j], p, k0, W_[j], y);
+                    for (int k0 = 0; k0 < W_[j]; k0 += kMaxW) y = ell_round<V, false>(cp, ap, p, k0, W_[j], y);
                     q[i_[j]] = y;
                     acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
                 }
             }
-            __syncthreads();   // this step's stages are free for the rounds S ahead
-            if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();   // this step's stages are free for the rounds S ahead
+            if (lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
         if (!ok) {
-            // let the copies already issued land before the CTA leaves
-            if (tid == 0)
-                for (int k = 0; k < S; ++k) mbar_wait(&full[k], (parity >> k) & 1u, ctl);
-            __syncthreads();
-            return;
+            // the copies this warp issued (rounds r .. r + S - 1) land before
+            // the CTA leaves (the step's own rounds had their parity bit
+            // flipped already); the flush below still runs so every warp
+            // meets its barriers
+            if (lane == 0) {
+                for (int k = r; k < re && k < r + S; ++k)
+                    mbar_wait(&full[wid][k % S], ((parity >> (k % S)) & 1u) ^ (k < r + RP ? 1u : 0u), ctl);
+                s_abort = 1;
+            }
+            __syncwarp();
         }
-        flush_segment<OP_SPMV_QP>(B, sS, sg.y, t1 - t0, acc, sh, &s_last);
+        flush_segment<OP_SPMV_QP>(B, sS, sg.y, u1 - u0, acc, sh, &s_last, (int)U);
+        if (s_abort) return;   // read after the flush's closing barrier
     }
 }
+#undef col_st
+#undef val_st
 
 // FP32 levelled sweeps two chunks per warp step (k_sweep_lvl with PAIRS);
 // MRG_SWEEP_PAIRS=0 takes one chunk per step.
@@ -1570,7 +1616,7 @@ void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
     if (grid < 1) grid = 1;
     if constexpr (OP == OP_SPMV_QP) {
         if (!pb) {
-            launch_pdl(k_spmv_staged<V>, grid, kBlock, spmv_smem<V>(), st, dB);
+            launch_pdl(k_spmv_warp<V>, grid, kBlock, spmv_smem<V>(), st, dB);
             return;
         }
     }
@@ -2291,9 +2337,8 @@ void set_device_sms(int nsm)
     g_grid_cap = (nsm > 0 ? nsm : 152) * kMinCtas;
     // the staged SpMV's stages exceed the default dynamic shared memory
     // limit; set once per device, outside any stream capture
-    cudaFuncSetAttribute(k_spmv_staged<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_smem<float>());
-    cudaFuncSetAttribute(k_spmv_staged<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)spmv_smem<double>());
+    cudaFuncSetAttribute(k_spmv_warp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_smem<float>());
+    cudaFuncSetAttribute(k_spmv_warp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_smem<double>());
 }
 int persistent_grid() { return g_grid_cap; }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }

@@ -1,0 +1,79 @@
+"""Kernel variants that must not change a bit of any result:
+
+  MRG_SWEEP_PAIRS  FP32 levelled sweeps, two chunks per warp step (default)
+                   or one
+
+Solves with every variant give bit-identical solutions and iteration counts.
+The switches are read once per process, so each variant runs in a child
+process.  Cases: the coupled CHT system (interfaces) with PCG + DIC, mixed
+and FP64 (exact order); the permuted convection-diffusion system with PBiCG
++ DILU (transposed sweeps) and BiCGStab + DILU (the M^-1 p and M^-1 s vector
+sets), mixed.
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CHILD = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from multiregionfoam_gb300 import cases, mrgpu
+mrgpu.load()
+ctx = mrgpu.Context(0)
+out = {}
+cht = cases.cht_system(24, 24, 16, 8, seed=3, form="coupled")
+cd = cases.convdiff_system(20, 18, 16, seed=4)
+runs = [
+    ("cht", cht, "PCG", "DIC", "mixed", "colour"),
+    ("cht64", cht, "PCG", "DIC", "fp64", "exact"),
+    ("cd_pbicg", cd, "PBiCG", "DILU", "mixed", "colour"),
+    ("cd_bicgstab", cd, "BiCGStab", "DILU", "mixed", "colour"),
+]
+for name, s, solver, pc, prec, ordering in runs:
+    m = mrgpu.Mesh(ctx, s.n, s.lower, s.upper, s.iface)
+    f = s.iface
+    m.upload(s.diag, s.upper_c, s.lower_c, None if f is None else f["bou"], None if f is None else f.get("int"))
+    x, p = m.solve(s.b, s.x0, tol=1e-8, max_iter=3000, solver=solver, precond=pc, precision=prec,
+                   ordering=ordering)
+    m.close()
+    np.save(sys.argv[2] + "_" + name + ".npy", x)
+    out[name] = [int(p["n_iter"]), int(p.get("n_outer", 0)), bool(p["converged"])]
+ctx.close()
+print(json.dumps(out))
+"""
+
+
+def _run(tmp_path, tag, **switches):
+    from multiregionfoam_gb300 import _build
+    _build.build()
+    env = dict(os.environ, **switches)
+    stem = str(tmp_path / tag)
+    r = subprocess.run([sys.executable, "-c", CHILD, ROOT, stem], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return stem, json.loads(r.stdout.strip().splitlines()[-1])
+
+
+@pytest.fixture(scope="module")
+def default_run(tmp_path_factory):
+    return _run(tmp_path_factory.mktemp("variants"), "default")
+
+
+@pytest.mark.parametrize("switch", ["MRG_SWEEP_PAIRS"])
+def test_variant_bit_identical(tmp_path, default_run, switch):
+    s1, p1 = default_run
+    s0, p0 = _run(tmp_path, switch, **{switch: "0"})
+    assert p1 == p0
+    for name, (_, _, conv) in p1.items():
+        assert conv, name
+        a, b = np.load(f"{s1}_{name}.npy"), np.load(f"{s0}_{name}.npy")
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), name

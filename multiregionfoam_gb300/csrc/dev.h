@@ -91,6 +91,9 @@ struct SysDev {
     Vecs<float> v32;
     // mixed precision: best refined iterate and its FP64 residual
     double *xb, *rb;
+    // FP32 PCG with a levelled DIC: sum of r w over each chunk, written by
+    // the sweep that writes the chunk's w  [nchunks]
+    float* chunk_rw;
     // caller-numbered input/output of the current solve
     const double *in_b, *in_x;
     double* out_x;

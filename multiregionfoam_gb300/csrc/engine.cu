@@ -390,6 +390,7 @@ static bool ensure_views(Mesh& m, PlanState& P, const Controls& cfg)
         S.v32.q = (float*)c->alloc(4 * np);
         S.xb = (double*)c->alloc(8 * np);
         S.rb = (double*)c->alloc(8 * np);
+        S.chunk_rw = (float*)c->alloc(4 * (size_t)std::max(1, S.nchunks));
         P.have32 = true;
         P.scattered = 0;
         changed = true;
@@ -478,7 +479,8 @@ PlanState& prepare(Mesh& m, const Controls& cfg)
 // ------------------------------------------------------------------ graphs
 // trans: the sweeps' vector set (0 = r -> w, 1 = the transpose system,
 // 2 / 3 = BiCGStab's M^-1 p / M^-1 s).
-static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, int trans, cudaStream_t st)
+static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, int trans, cudaStream_t st,
+                                int rho_chunks = 0)
 {
     Ctx* c = bh.ctx;
     if (cfg.pc < PC_DIC) return;
@@ -491,8 +493,8 @@ static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, in
         const int nl = bh.h.maxlevels;
         const int div = std::max(1, bh.tune.sweep_div);
         const int g = std::max(1, std::min(persistent_grid(), (bh.widest_level + div - 1) / div));
-        for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, bh.d, g, st);
-        for (int L = std::max(nl - 2, 0); L >= 0; --L) launch_sweep(prec, 0, trans, 0, L, bh.d, g, st);
+        for (int L = 1; L < nl; ++L) launch_sweep(prec, 1, trans, 0, L, bh.d, g, st, rho_chunks);
+        for (int L = std::max(nl - 2, 0); L >= 0; --L) launch_sweep(prec, 0, trans, 0, L, bh.d, g, st, rho_chunks);
     }
 }
 
@@ -561,15 +563,18 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
     }
     const int pb = cfg.solver == MRG_SOLVER_PBICG;
     const int nt = bh.h.ntiles, ns = bh.h.nsegs;
+    // FP32 PCG with a levelled DIC: the sweeps leave (r, w) per chunk and rho
+    // sums those (the FP64 loop keeps the row-wise OP_RHO the oracle mirrors)
+    const int rc = prec == 1 && !pb && cfg.pc >= PC_DIC && cfg.ordering != MRG_ORDER_EXACT;
     if (cfg.pc >= PC_DIC) {
-        record_precondition(bh, cfg, prec, 0, st);
+        record_precondition(bh, cfg, prec, 0, st, rc);
         if (pb) record_precondition(bh, cfg, prec, 1, st);
     } else if (cfg.pc == PC_DIAG) {
         launch_rows(OP_PRECOND_DIAG, prec, bh.d, nt, ns, pb, st);
     } else {
         launch_rows(OP_PRECOND_NONE, prec, bh.d, nt, ns, pb, st);
     }
-    launch_rows(OP_RHO, prec, bh.d, nt, ns, pb, st);
+    launch_rows(rc ? OP_RHO_CH : OP_RHO, prec, bh.d, nt, ns, pb, st);
     launch_rows(OP_PUPDATE, prec, bh.d, nt, ns, pb, st);
     if (any_general_iface(bh)) {
         launch_iface_gather(prec, 0, bh.d, 64, st);

@@ -36,10 +36,13 @@ constexpr long long kWaitCycles = 4000000000LL;
 // Programmatic dependent launch.  The Krylov-loop kernels are launched with
 // programmatic stream serialisation, so a kernel's CTAs can be scheduled
 // while the previous kernel of the stream drains (its launch latency hidden
-// behind the other's tail).  Each such kernel first waits here for the
-// previous kernel to complete and its writes to be visible -- before it reads
-// anything, the batch descriptor included -- and then lets the next kernel be
-// scheduled.  Launched without the attribute, both instructions do nothing.
+// behind the other's tail).  Each such kernel waits here for the previous
+// kernel to complete and its writes to be visible before it reads anything a
+// kernel writes, and then lets the next kernel be scheduled.  Before the
+// wait it may read only what the host alone writes (the batch descriptor,
+// its tables and the system descriptors), which the stream order already
+// made visible.  Launched without the attribute, both instructions do
+// nothing.
 __device__ __forceinline__ void pdl_enter()
 {
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -85,6 +88,15 @@ __device__ __forceinline__ double vmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double vfma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// Sum over a warp's lanes in butterfly order (every lane gets the same
+// value: each step adds two lanes' values, and their sum commutes).
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
 
 // Reduction terms of N consecutive rows (N = 2 or 4) into an FP64
 // accumulator.  FP64: every row's term in FP64, row by row (the order the
@@ -414,6 +426,7 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
         break;
     }
     case OP_RHO:
+    case OP_RHO_CH:
         sc->rho_old = sc->rho;
         sc->rho = sums[0];
         sc->beta = sc->iter > 0 ? sc->rho / sc->rho_old : 0.0;
@@ -1101,14 +1114,14 @@ struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
                                   OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32 || OP == OP_FALLBACK64 ||
                                   OP == OP_BS_RHO0 || OP == OP_BS_V || OP == OP_BS_S || OP == OP_BS_T ||
-                                  OP == OP_BS_XR || OP == OP_GS_RES);
+                                  OP == OP_BS_XR || OP == OP_GS_RES || OP == OP_RHO_CH);
     // Krylov-loop ops run only for systems whose loop is active; the
     // refinement ops only for systems whose outer loop is active.
     static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
                                          OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE ||
                                          OP == OP_BS_RHO0 || OP == OP_BS_P || OP == OP_BS_V || OP == OP_BS_S ||
                                          OP == OP_BS_T || OP == OP_BS_XR || OP == OP_GS_COPY || OP == OP_GS_RES ||
-                                         OP == OP_SM_RES || OP == OP_SM_ADD);
+                                         OP == OP_SM_RES || OP == OP_SM_ADD || OP == OP_RHO_CH);
     static constexpr bool kNeedOuter = (OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
     // Values reduced: the initial residual needs two (normFactor and
     // sum|r|), BiCGStab's t step ((t, s), (t, t)) and its update (sum|r|,
@@ -1225,6 +1238,17 @@ __device__ __forceinline__ void load_sys(SysDev* dst, const SysDev* src)
     __syncthreads();
 }
 
+// The system of this CTA's first work item (segment table for reducing
+// ops, tile table otherwise), -1 if it has none.
+template <bool RED>
+__device__ __forceinline__ int first_system(const Batch& B)
+{
+    const int g = blockIdx.x;
+    if (g >= (RED ? B.nsegs : B.ntiles)) return -1;
+    if (B.nsys == 1) return 0;
+    return RED ? B.segs[g].x : B.tiles[g].x;
+}
+
 // One row operation over the whole batch by this CTA: grid-stride over the
 // tile table (non-reducing ops) or the segment table (reducing ops).  `cur`
 // names the system whose descriptor sS holds, so a persistent kernel that
@@ -1274,6 +1298,18 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             }
             if (!live) continue;
             const unsigned T = (unsigned)sS.ntiles, G = (unsigned)red_segments(sS.ntiles);
+            if constexpr (OP == OP_RHO_CH) {
+                // rho from the sweeps' chunk sums: segment sg.y takes the
+                // chunks [c0, c1), thread t its chunks c0 + t, c0 + t + kBlock,
+                // ...; the tile count keeps the segment bookkeeping
+                const long long nch = sS.nchunks;
+                const int c0 = (int)(sg.y * nch / G), c1 = (int)((sg.y + 1) * nch / G);
+                const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
+                double acc[kMaxRed] = {0.0, 0.0};
+                for (int c = c0 + (int)threadIdx.x; c < c1; c += kBlock) acc[0] += widen(__ldcg(sS.chunk_rw + c));
+                flush_segment<OP>(B, sS, sg.y, t1 - t0, acc, sh, s_last);
+                continue;
+            }
             if constexpr (OP == OP_SPMV_QP && !PB && sizeof(V) == 4) {
                 // FP32 Amul + (q, p): segments of rounds, each thread's rows
                 // and their order k_spmv_warp's, so both give the same bits
@@ -1308,9 +1344,11 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_rows(const Batch* __restri
     __shared__ double sh[kBlock * kMaxRed];
     __shared__ int s_last;
     __shared__ __align__(16) SysDev sS;
-    pdl_enter();
+    // descriptors (host-written) while the previous kernel drains
     const Batch B = *pB;
-    int cur = -1;
+    int cur = first_system<OpTraits<OP>::kRed>(B);
+    if (cur >= 0) load_sys(&sS, B.sys + cur);
+    pdl_enter();
     rows_phase<V, OP, PB>(B, sS, sh, &s_last, cur);
 }
 
@@ -1410,8 +1448,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
     __shared__ __align__(16) SysDev sS;
     __shared__ __align__(8) unsigned long long full[NW][S];
     extern __shared__ __align__(128) unsigned char dyn[];
-    pdl_enter();
-    const Batch B = *pB;
+    const Batch B = *pB;   // descriptors (host-written) while the previous kernel drains
     Ctl* ctl = B.ctl;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     // this warp's stage k: indices at col_st(k), coefficients at val_st(k),
@@ -1426,9 +1463,11 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (tid == 0) s_abort = 0;
-    __syncthreads();
+    int cur = first_system<true>(B);
+    if (cur >= 0) load_sys(&sS, B.sys + cur);   // its __syncthreads also covers the mbarrier init
+    pdl_enter();
     unsigned parity = 0;   // bit k: parity of this warp's stage k's next completion
-    int cur = -1, lcur = -1;
+    int lcur = -1;
     bool live = false;
     for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
         const int2 sg = B.nsys == 1 ? make_int2(0, g) : B.segs[g];
@@ -1811,23 +1850,24 @@ __device__ __forceinline__ void sweep_round(const SweepPtrs<V>& P, int e0, int k
     }
 }
 
-// Rows i = r0 + lane < r1 of one chunk whose sweep entries start at e0 and
-// are W wide.
+// Row i of a sweep (sweep_rows without the chunk sum); with want_rw, rwi =
+// r_i w_i of the w the row writes.
 template <typename V, bool FWD>
-__device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1, int e0, int W, bool syncfree,
-                                           Ctl* ctl, int lvl0_end, bool last_level, bool first_level)
+__device__ __forceinline__ void sweep_row_body(const SweepPtrs<V>& P, int i, int e0, int W, bool syncfree, Ctl* ctl,
+                                               int lvl0_end, bool last_level, bool first_level, bool want_rw,
+                                               float& rwi)
 {
     const int lane = threadIdx.x & 31;
-    const int i = r0 + lane;
-    if (i >= r1) return;
     V* __restrict__ y = P.y;
     V* __restrict__ w = P.w;
     const V* __restrict__ r = P.r;
     const V* __restrict__ rD = P.rD;
     V* dep = FWD ? y : w;
+    const bool from_r = FWD || (!syncfree && first_level);
+    const V ri = from_r || want_rw ? __ldca(r + i) : V(0);
     V acc;
-    if (FWD || (!syncfree && first_level))
-        acc = vmul(__ldg(rD + i), __ldca(r + i));
+    if (from_r)
+        acc = vmul(__ldg(rD + i), ri);
     else
         acc = __ldca(y + i);
     // rounds of kMaxW entries (one round for most rows, unrolled without a
@@ -1852,6 +1892,29 @@ __device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1
         else
             w[i] = acc;
     }
+    if (want_rw) rwi = (float)vmul(ri, acc);
+}
+
+// Rows i = r0 + lane < r1 of one chunk whose sweep entries start at e0 and
+// are W wide.  rw (levelled sweeps writing the chunk's w): rw[c] = the
+// chunk's sum of r w (FP32 products, warp_sum).
+template <typename V, bool FWD>
+__device__ __forceinline__ void sweep_rows(const SweepPtrs<V>& P, int r0, int r1, int e0, int W, bool syncfree,
+                                           Ctl* ctl, int lvl0_end, bool last_level, bool first_level,
+                                           float* rw = nullptr, int c = 0)
+{
+    const int lane = threadIdx.x & 31;
+    const int i = r0 + lane;
+    const bool on = i < r1;
+    if (!on && rw == nullptr) return;   // with rw the whole warp forms the chunk's sum
+    float rwi = 0.f;
+    if (on) {
+        sweep_row_body<V, FWD>(P, i, e0, W, syncfree, ctl, lvl0_end, last_level, first_level, rw != nullptr, rwi);
+    }
+    if (rw != nullptr) {
+        const float t = warp_sum(rwi);
+        if (lane == 0) rw[c] = t;
+    }
 }
 
 // Levelled FP32 sweeps can take two chunks per warp step (k_sweep_lvl
@@ -1867,7 +1930,7 @@ constexpr int kSweepPairCtas = 3;
 template <typename V, bool FWD>
 __device__ __forceinline__ void sweep_rows_pair(const SweepPtrs<V>& P, const int (&r0)[2], const int (&r1)[2],
                                                 const int (&e0)[2], const int (&W)[2], int lvl0_end,
-                                                bool last_level, bool first_level)
+                                                bool last_level, bool first_level, float* rw, const int (&c)[2])
 {
     const int lane = threadIdx.x & 31;
     V* __restrict__ y = P.y;
@@ -1886,7 +1949,7 @@ __device__ __forceinline__ void sweep_rows_pair(const SweepPtrs<V>& P, const int
         i[h] = r0[h] + lane;
         live[h] = i[h] < r1[h];
         a0[h] = live[h] ? (from_r ? __ldg(rD + i[h]) : __ldca(y + i[h])) : V(0);
-        a1[h] = live[h] && from_r ? __ldca(r + i[h]) : V(0);
+        a1[h] = live[h] && (from_r || rw != nullptr) ? __ldca(r + i[h]) : V(0);
     }
 #pragma unroll
     for (int h = 0; h < 2; ++h)
@@ -1916,6 +1979,10 @@ __device__ __forceinline__ void sweep_rows_pair(const SweepPtrs<V>& P, const int
                 y[i[h]] = acc;
             else
                 w[i[h]] = acc;
+        }
+        if (rw != nullptr) {   // as sweep_rows: r_i w_i, warp_sum
+            const float t = warp_sum(live[h] ? (float)vmul(a1[h], acc) : 0.f);
+            if ((threadIdx.x & 31) == 0) rw[c[h]] = t;
         }
     }
 }
@@ -1977,7 +2044,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __re
 // warp's k-th next chunk, so 32 chunks' metadata costs one chain of
 // dependent loads instead of one chain per chunk.
 template <typename V, bool FWD, bool PAIRS = false>
-__device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans)
+__device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans, int rho_chunks = 0)
 {
     if (L >= B.maxlevels) return;
     const int lane = threadIdx.x & 31;
@@ -1987,6 +2054,7 @@ __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans
     int cur = -1;
     bool ok = false, last = false, first = false;
     int lvl0_end = 0;
+    float* rw = nullptr;   // chunk sums of r w: where this launch writes w
     SweepPtrs<V> P;
     for (int base = i0 + gw; base < i1; base += 32 * nw) {
         const int my = base + lane * nw;
@@ -2019,36 +2087,39 @@ __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans
                     last = L == nl - 1;
                     first = L == 0;
                     P = sweep_ptrs<V, FWD>(S, trans);
+                    rw = rho_chunks && (!FWD || last) ? S.chunk_rw : nullptr;
                 }
             }
             if (!ok) continue;
+            const int c = __shfl_sync(kFull, mc, j);
             if constexpr (PAIRS) {
                 // pair with the warp's next item when it is the same system's
                 // and both fit one round
                 if (j + 1 < cnt && W <= kMaxW) {
                     const int s2 = __shfl_sync(kFull, ms, j + 1), W2 = __shfl_sync(kFull, mW, j + 1);
                     const int r0b = __shfl_sync(kFull, mr0, j + 1), r1b = __shfl_sync(kFull, mr1, j + 1);
-                    const int e0b = __shfl_sync(kFull, me0, j + 1);
+                    const int e0b = __shfl_sync(kFull, me0, j + 1), cb = __shfl_sync(kFull, mc, j + 1);
                     if (s2 == cur && W2 <= kMaxW) {
                         const int pr0[2] = {r0, r0b}, pr1[2] = {r1, r1b}, pe0[2] = {e0, e0b}, pW[2] = {W, W2};
-                        sweep_rows_pair<V, FWD>(P, pr0, pr1, pe0, pW, lvl0_end, last, first);
+                        const int pc[2] = {c, cb};
+                        sweep_rows_pair<V, FWD>(P, pr0, pr1, pe0, pW, lvl0_end, last, first, rw, pc);
                         ++j;
                         continue;
                     }
                 }
             }
-            sweep_rows<V, FWD>(P, r0, r1, e0, W, false, nullptr, lvl0_end, last, first);
+            sweep_rows<V, FWD>(P, r0, r1, e0, W, false, nullptr, lvl0_end, last, first, rw, c);
         }
     }
 }
 
 template <typename V, bool FWD, bool PAIRS>
 __global__ void __launch_bounds__(kBlock, PAIRS ? kSweepPairCtas : kMinCtas)
-    k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans)
+    k_sweep_lvl(const Batch* __restrict__ pB, int L, int trans, int rho_chunks)
 {
+    const Batch B = *pB;   // host-written: read while the previous kernel drains
     pdl_enter();
-    const Batch B = *pB;
-    sweep_lvl_phase<V, FWD, PAIRS>(B, L, trans);
+    sweep_lvl_phase<V, FWD, PAIRS>(B, L, trans, rho_chunks);
 }
 
 // ---------------------------------------------------------------- Gauss-Seidel
@@ -2284,6 +2355,9 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __res
     const Batch B = *pB;
     Ctl* ctl = B.ctl;
     const int nl = B.maxlevels;
+    // FP32 PCG with a levelled DIC: rho from the sweeps' chunk sums, as the
+    // separate launches
+    const int rc = (sizeof(V) == 4 && !PB && !SF && pc >= PC_DIC) ? 1 : 0;
     int cur = -1;
     for (int it = 0; it < K; ++it) {
         if (pc >= PC_DIC) {
@@ -2295,11 +2369,11 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __res
                     if (!grid_barrier(ctl)) return;
                 } else {
                     for (int L = 1; L < nl; ++L) {
-                        sweep_lvl_phase<V, true>(B, L, tr);
+                        sweep_lvl_phase<V, true>(B, L, tr, rc);
                         if (!grid_barrier(ctl)) return;
                     }
                     for (int L = nl - 2 > 0 ? nl - 2 : 0; L >= 0; --L) {
-                        sweep_lvl_phase<V, false>(B, L, tr);
+                        sweep_lvl_phase<V, false>(B, L, tr, rc);
                         if (!grid_barrier(ctl)) return;
                     }
                 }
@@ -2311,7 +2385,10 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __res
             rows_phase<V, OP_PRECOND_NONE, PB>(B, sS, sh, &s_last, cur);
             if (!grid_barrier(ctl)) return;
         }
-        rows_phase<V, OP_RHO, PB>(B, sS, sh, &s_last, cur);
+        if (rc)
+            rows_phase<V, OP_RHO_CH, PB>(B, sS, sh, &s_last, cur);
+        else
+            rows_phase<V, OP_RHO, PB>(B, sS, sh, &s_last, cur);
         if (!grid_barrier(ctl)) return;
         rows_phase<V, OP_PUPDATE, PB>(B, sS, sh, &s_last, cur);
         if (!grid_barrier(ctl)) return;
@@ -2400,6 +2477,7 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE32(OP_BS_S)
             MRG_CASE32(OP_BS_T)
             MRG_CASE32(OP_BS_XR)
+            MRG_CASE32(OP_RHO_CH)
         default: break;
         }
     }
@@ -2426,7 +2504,7 @@ void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st)
 }
 
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
-                  cudaStream_t st)
+                  cudaStream_t st, int rho_chunks)
 {
     ++g_launches;
     if (grid < 1) grid = 1;
@@ -2445,22 +2523,22 @@ void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, co
     } else {
         if (precision == 0) {
             if (fwd)
-                launch_pdl(k_sweep_lvl<double, true, false>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<double, true, false>, grid, kBlock, 0, st, dB, level, trans, 0);
             else
-                launch_pdl(k_sweep_lvl<double, false, false>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<double, false, false>, grid, kBlock, 0, st, dB, level, trans, 0);
         } else if (sweep_pairs()) {
             // the grid the caller sized for kMinCtas CTAs per SM, at the
             // paired kernel's occupancy
             const int g = std::max(1, grid / kMinCtas * kSweepPairCtas);
             if (fwd)
-                launch_pdl(k_sweep_lvl<float, true, true>, g, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, true, true>, g, kBlock, 0, st, dB, level, trans, rho_chunks);
             else
-                launch_pdl(k_sweep_lvl<float, false, true>, g, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, false, true>, g, kBlock, 0, st, dB, level, trans, rho_chunks);
         } else {
             if (fwd)
-                launch_pdl(k_sweep_lvl<float, true, false>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, true, false>, grid, kBlock, 0, st, dB, level, trans, rho_chunks);
             else
-                launch_pdl(k_sweep_lvl<float, false, false>, grid, kBlock, 0, st, dB, level, trans);
+                launch_pdl(k_sweep_lvl<float, false, false>, grid, kBlock, 0, st, dB, level, trans, rho_chunks);
         }
     }
 }

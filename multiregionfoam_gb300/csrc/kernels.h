@@ -44,6 +44,7 @@ enum RowOp {
     OP_GS_RES,          // smoothSolver: r = b - A x, sum|r|, iterations += nSweeps, convergence
     OP_SM_RES,          // smoothSolver DIC / DILU step: r = b - A x
     OP_SM_ADD,          // smoothSolver DIC / DILU step: x += w (w = M^-1 r)
+    OP_RHO_CH,          // FP32 PCG, levelled DIC: rho = sum of the sweeps' per-chunk (r, w), beta
     OP_COUNT
 };
 
@@ -69,8 +70,11 @@ void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st);
 // 1 = rT -> yT -> wT with DILU's preconditionT coefficients, and for
 // BiCGStab 2 = wT -> y -> p (M^-1 p) and 3 = r -> yT -> pT (M^-1 s).
 // syncfree=1: all levels in one launch (exact ordering); else one level.
+// rho_chunks=1 (FP32 levelled sweeps of vector set 0): every chunk whose w
+// the launch writes also gets its sum of r w in chunk_rw, which OP_RHO_CH
+// then reduces.
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
-                  cudaStream_t st);
+                  cudaStream_t st, int rho_chunks = 0);
 
 // GGI gather of the general interface faces: x[npad + j] = sum w x[src]
 // (which: 0 = p, 1 = x, 2 = pT; 0 and 2 skip inactive systems, 3 = p always).

@@ -481,6 +481,35 @@ int mrg_kernel_launches(uint64_t* count);
 int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel,
                     int reps, float* ms_per_launch);
 
+/* ---- block-coupled systems (fvBlockMatrix<vectorN>) --------------------
+ * Replaces the BlockLduSolver<Type>::New(...)->solve entry of foam-extend's
+ * fvBlockMatrix::solve (filesToReplace/fvBlockMatrix.C:1360-1388; the
+ * pressure-velocity coupled region's BlockLduMatrix<vector4>,
+ * pUCoupledIcoFluid.C:592-617) by a scalar LDU system of bs * n_cells cells
+ * that mrg_mesh_upload / mrg_coeffs_upload / mrg_solve take as they are:
+ * cell c's component a is row bs c + a.  A block face f = (l, u) becomes
+ * the bs^2 faces (bs l + a, bs u + b) with upper U_f[a][b] and lower
+ * L_f[b][a]; a diagonal block D_c gives the diagonal D_c[a][a] and, for
+ * a < b, the face (bs c + a, bs c + b) with upper D_c[a][b] and lower
+ * D_c[b][a].  Faces come out in upper-triangular order (owner row, then
+ * neighbour).  Point-wise preconditioning (DILU on the scalar rows) stands
+ * in for foam-extend's block preconditioners.  Host-only, no GPU needed.
+ *
+ * mrg_block_addressing: *n_faces_out = bs^2 n_faces + bs (bs - 1) / 2
+ *   n_cells; s_lower / s_upper [that many] (either NULL: the count only).
+ * mrg_block_coeffs: diag [n_cells bs bs], upper and lower [n_faces bs bs]
+ *   (row-major blocks; lower NULL: every lower block is its upper block
+ *   transposed) -> s_diag [bs n_cells], s_upper, s_lower [n_faces_out], in
+ *   mrg_block_addressing's face order.  bs is 1..8; MRG_E_INVALID for bad
+ *   addressing or sizes. */
+int mrg_block_addressing(int n_cells, int n_faces, const int32_t* lower_addr,
+                         const int32_t* upper_addr, int bs, int* n_faces_out,
+                         int32_t* s_lower, int32_t* s_upper);
+int mrg_block_coeffs(int n_cells, int n_faces, const int32_t* lower_addr,
+                     const int32_t* upper_addr, int bs, const double* diag,
+                     const double* upper, const double* lower_or_null,
+                     double* s_diag, double* s_upper, double* s_lower);
+
 /* ---- residual without device allocation -------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory where they need a residual: code inside a host application whose

@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_lib")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libmrgpu.so")
 
-SOURCES = ["kernels.cu", "engine.cu", "api.cu", "noalloc.cu", "dn.cu", "ggi_build.cu", "mono.cu", "gamg.cu", "plan.cpp", "server.cpp"]
+SOURCES = ["kernels.cu", "engine.cu", "api.cu", "noalloc.cu", "dn.cu", "ggi_build.cu", "mono.cu", "gamg.cu", "plan.cpp", "server.cpp", "block.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
 

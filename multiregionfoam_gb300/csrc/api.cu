@@ -165,6 +165,12 @@ void d2h(Ctx* c, double* h, const double* d, size_t n)
 
 }  // namespace
 
+namespace mrg {
+// The calling thread's last error text, for ABI entries in other files
+// (block.cpp); they clear it on entry.
+void set_last_error(const std::string& msg) { std::snprintf(g_last_error, sizeof g_last_error, "%s", msg.c_str()); }
+}  // namespace mrg
+
 extern "C" {
 
 const char* mrg_last_error(void) { return g_last_error; }

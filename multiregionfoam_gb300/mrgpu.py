@@ -34,6 +34,7 @@ EXPORTED = [
     "mrg_dn_create", "mrg_dn_destroy", "mrg_dn_set_state", "mrg_dn_new_time_step", "mrg_dn_update_jump",
     "mrg_dn_update_flux", "mrg_dn_rhs", "mrg_dn_residuals", "mrg_dn_get_state", "mrg_dn_criteria",
     "mrg_mono_create", "mrg_mono_destroy", "mrg_mono_update", "mrg_mono_source",
+    "mrg_block_addressing", "mrg_block_coeffs",
 ]
 
 
@@ -174,6 +175,8 @@ def load(path: str = LIB_PATH):
     L.mrg_mono_update.argtypes = [vp, C.c_int] + [vp] * 8
     L.mrg_mono_source.argtypes = [vp, C.c_int] + [vp] * 6
     L.mrg_batch_tune.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(Controls), C.POINTER(Tuning)]
+    L.mrg_block_addressing.argtypes = [C.c_int, C.c_int, ip, ip, C.c_int, C.POINTER(C.c_int), ip, ip]
+    L.mrg_block_coeffs.argtypes = [C.c_int, C.c_int, ip, ip, C.c_int, dp, dp, dp, dp, dp, dp]
     _LIB = L
     return L
 
@@ -644,6 +647,33 @@ class MonoInterface:
         if self.h:
             _check(load().mrg_mono_destroy(self.h))
             self.h = None
+
+
+def block_system(n: int, lower, upper, bs: int, diag, upper_c, lower_c=None):
+    """A bs x bs block LDU system (foam-extend's BlockLduMatrix<vectorN> of
+    fvBlockMatrix::solve, filesToReplace/fvBlockMatrix.C:1360-1388) as the
+    scalar LDU system of bs n cells that Mesh takes (mrg_block_addressing /
+    mrg_block_coeffs): diag [n, bs, bs], upper_c / lower_c [F, bs, bs]
+    (lower_c None: the upper blocks transposed).  Returns (n_s, s_lower,
+    s_upper, s_diag, s_upper_c, s_lower_c); cell c's component a is row
+    bs c + a, so b and x are the block vectors flattened row-major."""
+    L = load()
+    lo = np.ascontiguousarray(lower, dtype=np.int32)
+    up = np.ascontiguousarray(upper, dtype=np.int32)
+    nf = len(lo)
+    nfs = C.c_int()
+    _check(L.mrg_block_addressing(n, nf, _i(lo), _i(up), bs, C.byref(nfs), None, None))   # checks bs first
+    D = np.ascontiguousarray(diag, dtype=np.float64).reshape(n, bs, bs)
+    U = np.ascontiguousarray(upper_c, dtype=np.float64).reshape(nf, bs, bs)
+    Lc = None if lower_c is None else np.ascontiguousarray(lower_c, dtype=np.float64).reshape(nf, bs, bs)
+    s_lower = np.empty(nfs.value, np.int32)
+    s_upper = np.empty(nfs.value, np.int32)
+    _check(L.mrg_block_addressing(n, nf, _i(lo), _i(up), bs, C.byref(nfs), _i(s_lower), _i(s_upper)))
+    s_diag = np.empty(n * bs)
+    s_uc = np.empty(nfs.value)
+    s_lc = np.empty(nfs.value)
+    _check(L.mrg_block_coeffs(n, nf, _i(lo), _i(up), bs, _d(D), _d(U), _d(Lc), _d(s_diag), _d(s_uc), _d(s_lc)))
+    return n * bs, s_lower, s_upper, s_diag, s_uc, s_lc
 
 
 def dn_criteria(corr, jump_res, flux_res, max_jump, max_flux) -> bool:

@@ -1,0 +1,67 @@
+"""Block-coupled systems as scalar LDU systems (mrg_block_addressing /
+mrg_block_coeffs, host-only): the library's expansion equals the oracle's
+entry-by-entry restatement exactly, is in upper-triangular face order, and
+its scalar product equals the block product; bad sizes and addressing are
+rejected.  No GPU needed.
+"""
+import numpy as np
+import pytest
+
+from block_case import block_case
+
+
+@pytest.fixture(scope="module")
+def bo():
+    import block_oracle
+    return block_oracle
+
+
+@pytest.mark.parametrize("bs,symmetric", [(4, False), (4, True), (3, False), (1, False)])
+def test_expansion_matches_oracle(mrg, bo, bs, symmetric):
+    c = block_case(5, 4, 3, bs=bs, seed=bs + 10 * symmetric, symmetric=symmetric)
+    n_s, s_lo, s_up, s_d, s_uc, s_lc = mrg.block_system(c["n"], c["lower"], c["upper"], bs, c["D"], c["U"], c["L"])
+    o_lo, o_up, o_d, o_uc, o_lc = bo.expand(c["n"], c["lower"], c["upper"], bs, c["D"], c["U"], c["L"])
+    assert n_s == bs * c["n"]
+    assert len(s_lo) == bs * bs * len(c["lower"]) + c["n"] * bs * (bs - 1) // 2
+    for got, want in ((s_lo, o_lo), (s_up, o_up)):
+        assert np.array_equal(got, want)
+    for got, want in ((s_d, o_d), (s_uc, o_uc), (s_lc, o_lc)):
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    # upper-triangular order: owner ascending, neighbour ascending within it
+    key = s_lo.astype(np.int64) * n_s + s_up
+    assert np.all(s_lo < s_up) and np.all(np.diff(key) > 0)
+    if symmetric:
+        assert np.array_equal(s_uc, s_lc)
+
+
+def test_expansion_preserves_amul(mrg, bo):
+    c = block_case(6, 5, 4, bs=4, seed=3)
+    n, bs = c["n"], 4
+    n_s, s_lo, s_up, s_d, s_uc, s_lc = mrg.block_system(n, c["lower"], c["upper"], bs, c["D"], c["U"], c["L"])
+    x = np.random.default_rng(0).uniform(-1, 1, (n, bs))
+    yb = bo.block_amul(n, c["lower"], c["upper"], c["D"], c["U"], c["L"], x).ravel()
+    ys = bo.scalar_amul(n_s, s_lo, s_up, s_d, s_uc, s_lc, x.ravel())
+    assert np.allclose(ys, yb, rtol=1e-13, atol=1e-13)
+
+
+def test_bs1_is_the_scalar_system(mrg):
+    c = block_case(4, 4, 4, bs=1, seed=5)
+    n_s, s_lo, s_up, s_d, s_uc, s_lc = mrg.block_system(c["n"], c["lower"], c["upper"], 1, c["D"], c["U"], c["L"])
+    order = np.lexsort((c["upper"], c["lower"]))
+    assert np.array_equal(s_lo, c["lower"][order]) and np.array_equal(s_up, c["upper"][order])
+    assert np.array_equal(s_uc, c["U"].ravel()[order]) and np.array_equal(s_lc, c["L"].ravel()[order])
+
+
+@pytest.mark.parametrize("bs", [0, 9])
+def test_bad_block_size(mrg, bs):
+    c = block_case(3, 3, 3, bs=2, seed=1)
+    with pytest.raises(mrg.MrgError, match="block size"):
+        mrg.block_system(c["n"], c["lower"], c["upper"], bs, np.zeros((c["n"], 1)), np.zeros((len(c["lower"]), 1)))
+
+
+def test_bad_addressing(mrg):
+    c = block_case(3, 3, 3, bs=2, seed=1)
+    lo = c["lower"].copy()
+    lo[0] = c["upper"][0]   # lower == upper: not an internal face
+    with pytest.raises(mrg.MrgError, match="block addressing"):
+        mrg.block_system(c["n"], lo, c["upper"], 2, c["D"], c["U"], c["L"])

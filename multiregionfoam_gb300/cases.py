@@ -282,6 +282,34 @@ def c5_meshes(count: int = 100, seed: int = 0, n_lo: int = 10000, n_hi: int = 20
     return out
 
 
+def block_case(nx: int, ny: int, nz: int, bs: int = 4, seed: int = 0, symmetric: bool = False) -> dict:
+    """A seeded block-coupled (bs x bs) system on a hex block, in the shape of
+    foam-extend's BlockLduMatrix<vectorN>: diagonal blocks s I plus a small
+    random matrix, face blocks small random matrices, the diagonal term s
+    chosen so every scalar row is strictly diagonally dominant.  symmetric:
+    symmetric diagonal blocks and lower blocks = upper blocks transposed (an
+    SPD matrix; L None).  Returns n, lower, upper, bs, D [n, bs, bs], U and L
+    [F, bs, bs], b [n, bs], x0 (zeros)."""
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    lower, upper, _ = box_faces(nx, ny, nz)
+    nf = len(lower)
+    U = rng.uniform(-1.0, 1.0, (nf, bs, bs))
+    L = None if symmetric else rng.uniform(-1.0, 1.0, (nf, bs, bs))
+    D = rng.uniform(-0.3, 0.3, (n, bs, bs))
+    if symmetric:
+        D = 0.5 * (D + np.transpose(D, (0, 2, 1)))
+    off = np.abs(D).sum(axis=2) - np.abs(np.einsum("caa->ca", D))
+    np.add.at(off, lower, np.abs(U).sum(axis=2))
+    Lb = np.transpose(U, (0, 2, 1)) if L is None else L
+    np.add.at(off, upper, np.abs(Lb).sum(axis=2))
+    for a in range(bs):
+        D[:, a, a] = off[:, a] * rng.uniform(1.05, 1.3, n) + 0.1
+    b = rng.uniform(-1.0, 1.0, (n, bs))
+    return dict(n=n, lower=lower.astype(np.int32), upper=upper.astype(np.int32), bs=bs, D=D, U=U, L=L, b=b,
+                x0=np.zeros((n, bs)))
+
+
 def laplace_1d(n: int, dirichlet=(0.0, 1.0), k: float = 1.0):
     """1-D Laplacian with Dirichlet ends: exact solution is linear."""
     lower = np.arange(n - 1, dtype=np.int32)

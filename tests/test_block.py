@@ -7,7 +7,7 @@ rejected.  No GPU needed.
 import numpy as np
 import pytest
 
-from block_case import block_case
+from multiregionfoam_gb300.cases import block_case
 
 
 @pytest.fixture(scope="module")

@@ -13,7 +13,7 @@
 import numpy as np
 import pytest
 
-from block_case import block_case
+from multiregionfoam_gb300.cases import block_case
 from conftest import gpu_mesh, oracle_matrix
 from multiregionfoam_gb300 import cases
 from test_gpu_parity import check_solve, rel_err

@@ -2346,7 +2346,7 @@ __device__ bool grid_barrier(Ctl* ctl)
 // by grid barriers, with the same per-row arithmetic and the same
 // per-system reduction order, so the results are bit-identical to the
 // separate launches.  Stops early once no member is active.
-template <typename V, bool PB, bool SF>
+template <typename V, bool PB, bool SF, bool RC>
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __restrict__ pB, int K, int pc, int gen)
 {
     __shared__ double sh[kBlock * kMaxRed];
@@ -2355,9 +2355,10 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __res
     const Batch B = *pB;
     Ctl* ctl = B.ctl;
     const int nl = B.maxlevels;
-    // FP32 PCG with a levelled DIC: rho from the sweeps' chunk sums, as the
-    // separate launches
-    const int rc = (sizeof(V) == 4 && !PB && !SF && pc >= PC_DIC) ? 1 : 0;
+    // RC (FP32 PCG with a levelled DIC): rho from the sweeps' chunk sums, as
+    // the separate launches
+    static_assert(!RC || (sizeof(V) == 4 && !PB && !SF), "chunk sums belong to FP32 levelled PCG");
+    constexpr int rc = RC ? 1 : 0;
     int cur = -1;
     for (int it = 0; it < K; ++it) {
         if (pc >= PC_DIC) {
@@ -2385,7 +2386,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_iterate(const Batch* __res
             rows_phase<V, OP_PRECOND_NONE, PB>(B, sS, sh, &s_last, cur);
             if (!grid_barrier(ctl)) return;
         }
-        if (rc)
+        if constexpr (RC)
             rows_phase<V, OP_RHO_CH, PB>(B, sS, sh, &s_last, cur);
         else
             rows_phase<V, OP_RHO, PB>(B, sS, sh, &s_last, cur);
@@ -2567,11 +2568,11 @@ void launch_permute(int to_internal, const SysDev* d, int s, const double* src, 
     k_permute<<<grid, 256, 0, st>>>(d, s, to_internal, src, dst, n);
 }
 
-template <typename V, bool PB, bool SF>
+template <typename V, bool PB, bool SF, bool RC = false>
 static cudaError_t launch_iterate_t(const Batch* dB, int K, int pc, int gen, cudaStream_t st)
 {
     static int per_sm = 0;
-    auto kern = k_iterate<V, PB, SF>;
+    auto kern = k_iterate<V, PB, SF, RC>;
     if (!per_sm) {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
         if (e != cudaSuccess || per_sm < 1) per_sm = 1;
@@ -2596,8 +2597,9 @@ cudaError_t launch_iterate(int precision, int pb, int syncfree, const Batch* dB,
     if (pb)
         return syncfree ? launch_iterate_t<float, true, true>(dB, K, pc, gen, st)
                         : launch_iterate_t<float, true, false>(dB, K, pc, gen, st);
-    return syncfree ? launch_iterate_t<float, false, true>(dB, K, pc, gen, st)
-                    : launch_iterate_t<float, false, false>(dB, K, pc, gen, st);
+    if (syncfree) return launch_iterate_t<float, false, true>(dB, K, pc, gen, st);
+    return pc >= PC_DIC ? launch_iterate_t<float, false, false, true>(dB, K, pc, gen, st)
+                        : launch_iterate_t<float, false, false>(dB, K, pc, gen, st);
 }
 
 void launch_gather_scal(const Batch* dB, Scal* out, cudaStream_t st)

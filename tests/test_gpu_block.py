@@ -39,9 +39,9 @@ def bo():
     return block_oracle
 
 
-@pytest.mark.parametrize("solver", ["BiCGStab", "PBiCG"])
-def test_block_asym_fp64_matches_oracle(mrg, ctx, oracle_mod, bo, solver):
-    c = block_case(10, 8, 6, bs=4, seed=21)
+@pytest.mark.parametrize("solver,bs", [("BiCGStab", 4), ("PBiCG", 4), ("BiCGStab", 2), ("PBiCG", 3)])
+def test_block_asym_fp64_matches_oracle(mrg, ctx, oracle_mod, bo, solver, bs):
+    c = block_case(10, 8, 6, bs=bs, seed=21 + bs)
     s = scalar_system(mrg, c)
     x, p, _ = check_solve(mrg, ctx, oracle_mod, s, solver, "DILU", tol=1e-9, max_iter=2000)
     assert p["converged"] and block_residual(bo, c, x) < 1e-7

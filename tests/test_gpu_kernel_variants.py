@@ -2,6 +2,9 @@
 
   MRG_SWEEP_PAIRS  FP32 levelled sweeps, two chunks per warp step (default)
                    or one
+  MRG_ITERATION    the Krylov iterations as a graph of launches (default) or
+                   as phases of one persistent cooperative kernel
+                   (=persistent; BiCGStab has no persistent form)
 
 Solves with every variant give bit-identical solutions and iteration counts.
 The switches are read once per process, so each variant runs in a child
@@ -68,10 +71,10 @@ def default_run(tmp_path_factory):
     return _run(tmp_path_factory.mktemp("variants"), "default")
 
 
-@pytest.mark.parametrize("switch", ["MRG_SWEEP_PAIRS"])
-def test_variant_bit_identical(tmp_path, default_run, switch):
+@pytest.mark.parametrize("switch,value", [("MRG_SWEEP_PAIRS", "0"), ("MRG_ITERATION", "persistent")])
+def test_variant_bit_identical(tmp_path, default_run, switch, value):
     s1, p1 = default_run
-    s0, p0 = _run(tmp_path, switch, **{switch: "0"})
+    s0, p0 = _run(tmp_path, switch, **{switch: value})
     assert p1 == p0
     for name, (_, _, conv) in p1.items():
         assert conv, name

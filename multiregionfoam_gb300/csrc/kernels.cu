@@ -1109,6 +1109,61 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
     }
 }
 
+// Two tiles (rows a and b) of the x/r update or the p update, not PBiCG:
+// both tiles' loads are issued before either's arithmetic and stores (two
+// calls of tile_body keep the second tile's loads behind the first one's
+// stores, which may alias for the compiler).  Each row's arithmetic and
+// the order of the reduction terms (tile a's rows, then tile b's) are
+// tile_body's, so the bits are too.
+template <typename V, RowOp OP>
+__device__ __forceinline__ void tile_pair(const SysDev& S, int row_a, int row_b, double (&acc)[kMaxRed])
+{
+    static_assert(OP == OP_UPDATE || OP == OP_PUPDATE, "x/r and p updates");
+    const Vecs<V>& v = VP<V>::v(S);
+    const int r4[2] = {row_a + 4 * (int)threadIdx.x, row_b + 4 * (int)threadIdx.x};
+    if constexpr (OP == OP_UPDATE) {
+        const V alpha = (V)S.sc->alpha;
+        V x[2][4], r[2][4], p[2][4], q[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            ld4w(v.x + r4[h], x[h]);
+            ld4w(v.r + r4[h], r[h]);
+            ld4(v.p + r4[h], p[h]);
+            ld4(v.q + r4[h], q[h]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                x[h][k] = vfma(alpha, p[h][k], x[h][k]);
+                r[h][k] = vfma(-alpha, q[h][k], r[h][k]);
+            }
+            st4(v.x + r4[h], x[h]);
+            st4(v.r + r4[h], r[h]);
+            acc_abs<4>(acc[0], r[h]);
+        }
+    } else {
+        const int it = S.sc->iter;
+        const V beta = (V)S.sc->beta;
+        V w[2][4], p[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            ld4(v.w + r4[h], w[h]);
+            if (it != 0) ld4w(v.p + r4[h], p[h]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (it == 0) {
+                st4(v.p + r4[h], w[h]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) p[h][k] = vfma(beta, p[h][k], w[h][k]);
+                st4(v.p + r4[h], p[h]);
+            }
+        }
+    }
+}
+
 template <RowOp OP>
 struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
@@ -1277,8 +1332,12 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             if constexpr (OpTraits<OP>::kElem) {
                 const int t2 = t + gridDim.x;
                 if (B.nsys == 1 && t2 < B.ntiles) {
-                    tile_body<V, OP, PB>(B, sS, tl.y * kTileRows, acc);
-                    tile_body<V, OP, PB>(B, sS, t2 * kTileRows, acc);
+                    if constexpr (!PB && (OP == OP_UPDATE || OP == OP_PUPDATE)) {
+                        tile_pair<V, OP>(sS, tl.y * kTileRows, t2 * kTileRows, acc);
+                    } else {
+                        tile_body<V, OP, PB>(B, sS, tl.y * kTileRows, acc);
+                        tile_body<V, OP, PB>(B, sS, t2 * kTileRows, acc);
+                    }
                     t = t2;
                     continue;
                 }
@@ -1326,8 +1385,12 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             if constexpr (OpTraits<OP>::kElem) {
                 int t = t0;
                 for (; t + 1 < t1; t += 2) {   // same order, two tiles' loads in flight
-                    tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
-                    tile_body<V, OP, PB>(B, sS, (t + 1) * kTileRows, acc);
+                    if constexpr (!PB && (OP == OP_UPDATE || OP == OP_PUPDATE)) {
+                        tile_pair<V, OP>(sS, t * kTileRows, (t + 1) * kTileRows, acc);
+                    } else {
+                        tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+                        tile_body<V, OP, PB>(B, sS, (t + 1) * kTileRows, acc);
+                    }
                 }
                 if (t < t1) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
             } else {

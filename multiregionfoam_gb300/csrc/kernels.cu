@@ -1109,16 +1109,22 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
     }
 }
 
-// Two tiles (rows a and b) of the x/r update or the p update, not PBiCG:
+// Two tiles (rows a and b) of an op with a two-tile body, not PBiCG:
 // both tiles' loads are issued before either's arithmetic and stores (two
 // calls of tile_body keep the second tile's loads behind the first one's
 // stores, which may alias for the compiler).  Each row's arithmetic and
 // the order of the reduction terms (tile a's rows, then tile b's) are
 // tile_body's, so the bits are too.
+// Ops with a two-tile body: the x/r and p updates, and in FP32 BiCGStab's s
+// and x/r updates (their FP64 pairs would spill).
+template <typename V, RowOp OP>
+constexpr bool kPairOp =
+    OP == OP_UPDATE || OP == OP_PUPDATE || (sizeof(V) == 4 && (OP == OP_BS_S || OP == OP_BS_XR));
+
 template <typename V, RowOp OP>
 __device__ __forceinline__ void tile_pair(const SysDev& S, int row_a, int row_b, double (&acc)[kMaxRed])
 {
-    static_assert(OP == OP_UPDATE || OP == OP_PUPDATE, "x/r and p updates");
+    static_assert(kPairOp<V, OP>, "ops with a two-tile body");
     const Vecs<V>& v = VP<V>::v(S);
     const int r4[2] = {row_a + 4 * (int)threadIdx.x, row_b + 4 * (int)threadIdx.x};
     if constexpr (OP == OP_UPDATE) {
@@ -1141,6 +1147,63 @@ __device__ __forceinline__ void tile_pair(const SysDev& S, int row_a, int row_b,
             st4(v.x + r4[h], x[h]);
             st4(v.r + r4[h], r[h]);
             acc_abs<4>(acc[0], r[h]);
+        }
+    } else if constexpr (OP == OP_BS_S) {
+        // s = r - alpha v (in r), x += alpha M^-1 p, sum|s|; M^-1 s into pT
+        // for a diagonal or no preconditioner
+        const V alpha = (V)S.sc->alpha;
+        const int pc = S.pc;
+        V x[2][4], r[2][4], ph[2][4], q[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            ld4w(v.x + r4[h], x[h]);
+            ld4w(v.r + r4[h], r[h]);
+            ld4(v.p + r4[h], ph[h]);
+            ld4(v.q + r4[h], q[h]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                x[h][k] = vfma(alpha, ph[h][k], x[h][k]);
+                r[h][k] = vfma(-alpha, q[h][k], r[h][k]);
+            }
+            st4(v.x + r4[h], x[h]);
+            st4(v.r + r4[h], r[h]);
+            acc_abs<4>(acc[0], r[h]);
+            if (pc == PC_DIAG) {
+                V d[4];
+                ld4(VP<V>::rD(S) + r4[h], d);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) d[k] = vmul(d[k], r[h][k]);
+                st4(v.pT + r4[h], d);
+            } else if (pc == PC_NONE) {
+                st4(v.pT + r4[h], r[h]);
+            }
+        }
+    } else if constexpr (OP == OP_BS_XR) {
+        // x += omega M^-1 s, r = s - omega t, sum|r|, (r~, r)
+        const V omega = (V)S.sc->omega;
+        V x[2][4], r[2][4], sh[2][4], t[2][4], rt[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            ld4w(v.x + r4[h], x[h]);
+            ld4w(v.r + r4[h], r[h]);
+            ld4(v.pT + r4[h], sh[h]);
+            ld4(v.qT + r4[h], t[h]);
+            ld4(v.rT + r4[h], rt[h]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                x[h][k] = vfma(omega, sh[h][k], x[h][k]);
+                r[h][k] = vfma(-omega, t[h][k], r[h][k]);
+            }
+            st4(v.x + r4[h], x[h]);
+            st4(v.r + r4[h], r[h]);
+            acc_abs<4>(acc[0], r[h]);
+            acc_dot<4>(acc[1], rt[h], r[h]);
         }
     } else {
         const int it = S.sc->iter;
@@ -1332,7 +1395,7 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             if constexpr (OpTraits<OP>::kElem) {
                 const int t2 = t + gridDim.x;
                 if (B.nsys == 1 && t2 < B.ntiles) {
-                    if constexpr (!PB && (OP == OP_UPDATE || OP == OP_PUPDATE)) {
+                    if constexpr (!PB && kPairOp<V, OP>) {
                         tile_pair<V, OP>(sS, tl.y * kTileRows, t2 * kTileRows, acc);
                     } else {
                         tile_body<V, OP, PB>(B, sS, tl.y * kTileRows, acc);
@@ -1385,7 +1448,7 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             if constexpr (OpTraits<OP>::kElem) {
                 int t = t0;
                 for (; t + 1 < t1; t += 2) {   // same order, two tiles' loads in flight
-                    if constexpr (!PB && (OP == OP_UPDATE || OP == OP_PUPDATE)) {
+                    if constexpr (!PB && kPairOp<V, OP>) {
                         tile_pair<V, OP>(sS, t * kTileRows, (t + 1) * kTileRows, acc);
                     } else {
                         tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);

@@ -27,6 +27,9 @@ Beside the headline, the line carries the other forms of the metric:
             BlockLduMatrix<vector4>) expanded to its scalar LDU system and
             solved by BiCGStab + DILU, mixed vs plain FP64, with the host
             expansion time (--block-n N, 0 skips)
+  gamg      GAMG (GaussSeidel smoother, the tutorials' fluid p / T settings)
+            on a 64^3-cell CHT system, FP64 foam order, beside plain PCG +
+            DIC on the same system (--gamg-n N, 0 skips)
   served    Poisson-arriving requests over recurring meshes (10k-2M cells,
             70% symmetric CHT with DIC, 30% asymmetric convection-diffusion
             with DILU, 5% coefficient drift per step) through the
@@ -322,6 +325,43 @@ def run_block(args, ctx, mrgpu):
     return out
 
 
+def run_gamg(args, ctx, mrgpu):
+    """GAMG with the tutorials' fluid p / T settings (GaussSeidel smoother,
+    nCellsInCoarsestLevel 10, 2 post / 2 finest sweeps) on a two-region CHT
+    system of args.gamg_n^3 cells (global form), FP64 in foam order, to 1e-8,
+    beside plain PCG + DIC on the same system.  A step is coefficient upload +
+    solve; the first GAMG solve (agglomeration, cached afterwards) is timed
+    on its own."""
+    from multiregionfoam_gb300 import cases
+    n = args.gamg_n
+    s = cases.cht_system(n, n, n // 2, n - n // 2, seed=SEED, form="global")
+    m = mrgpu.Mesh(ctx, s.n, s.lower, s.upper)
+    d_diag, d_up = ctx.to_device(s.diag), ctx.to_device(s.upper_c)
+    d_b, d_x0 = ctx.to_device(s.b), ctx.to_device(s.x0)
+    d_x = ctx.dev_alloc(8 * s.n)
+    out = {"cells": s.n, "faces": s.nf, "tolerance": TOL}
+    for name, kw in (("gamg", dict(solver="GAMG", smoother="GaussSeidel", n_coarsest_cells=10, n_post_sweeps=2,
+                                   n_finest_sweeps=2)),
+                     ("pcg_dic", dict(solver="PCG", precond="DIC"))):
+        ctl = mrgpu.controls(tol=TOL, max_iter=5000, precision="fp64", ordering="exact", **kw)
+        ms, perf = [], None
+        for rep in range(4):   # rep 0: setup (GAMG hierarchy, plans, views)
+            m.upload_device(d_diag, d_up)
+            ctx.copy_d2d(d_x, d_x0, 8 * s.n)
+            ctx.record(62)
+            perf = m.solve_device(d_b, d_x, ctl)
+            ctx.record(63)
+            ms.append(ctx.elapsed_ms(62, 63))
+        best = min(ms[1:])
+        out[name] = {"solves_per_s": 1e3 / best, "ms_per_step": best, "first_ms": ms[0], "iters": int(perf["n_iter"]),
+                     "final_residual": perf["final_residual"], "converged": bool(perf["converged"])}
+    out["speedup_gamg_vs_pcg"] = out["gamg"]["solves_per_s"] / out["pcg_dic"]["solves_per_s"]
+    for a in (d_diag, d_up, d_b, d_x0, d_x):
+        ctx.dev_free(a)
+    m.close()
+    return out
+
+
 def run_served(args, ctx, mrgpu):
     """Served configuration: Poisson arrivals at `args.served_rate`/s of
     solve requests over `args.served_meshes` meshes (cells log-uniform in
@@ -526,6 +566,7 @@ def run_gpu(args):
 
     batched = run_batched(args, ctx, mrgpu) if args.batched > 0 else None
     block = run_block(args, ctx, mrgpu) if args.block_n > 0 else None
+    gamg = run_gamg(args, ctx, mrgpu) if args.gamg_n > 0 else None
     served = run_served(args, ctx, mrgpu) if args.served_meshes > 0 else None
 
     if rank != 0:
@@ -579,6 +620,7 @@ def run_gpu(args):
         "tuning": tuning,
         "batched": batched,
         "block": block,
+        "gamg": gamg,
         "served": served,
         "cpu_baseline": cpu,
         "clocks": clk,
@@ -602,6 +644,7 @@ def main():
     ap.add_argument("--batched", type=int, default=512, help="systems of the batched configuration (0: skip)")
     ap.add_argument("--batched-reps", type=int, default=2)
     ap.add_argument("--block-n", type=int, default=48, help="4x4 block configuration: n^3 cells (0: skip)")
+    ap.add_argument("--gamg-n", type=int, default=64, help="GAMG configuration: n^3 cells (0: skip)")
     ap.add_argument("--served-meshes", type=int, default=24, help="meshes of the served configuration (0: skip)")
     ap.add_argument("--served-steps", type=int, default=8)
     ap.add_argument("--served-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")

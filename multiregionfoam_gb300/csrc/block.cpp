@@ -59,7 +59,9 @@ int check(int n, int nf, const int32_t* lower, const int32_t* upper, int bs)
     return MRG_OK;
 }
 
-Expansion expand(int n, int nf, const int32_t* lower, const int32_t* upper, int bs)
+// want_addr: the scalar addressing; want_src: each scalar face's source
+// entry (the coefficients need only the latter).
+Expansion expand(int n, int nf, const int32_t* lower, const int32_t* upper, int bs, bool want_addr, bool want_src)
 {
     // block faces of each owner, by neighbour
     std::vector<int32_t> start(n + 1, 0), own(nf);
@@ -75,24 +77,30 @@ Expansion expand(int n, int nf, const int32_t* lower, const int32_t* upper, int 
     Expansion E;
     E.bs = bs;
     const size_t ns = (size_t)nf * bs * bs + (size_t)n * bs * (bs - 1) / 2;
-    E.s_lower.reserve(ns);
-    E.s_upper.reserve(ns);
-    E.src.reserve(ns);
+    if (want_addr) {
+        E.s_lower.reserve(ns);
+        E.s_upper.reserve(ns);
+    }
+    if (want_src) E.src.reserve(ns);
     const int64_t bb = (int64_t)bs * bs;
     for (int c = 0; c < n; ++c)
         for (int a = 0; a < bs; ++a) {
             const int32_t row = c * bs + a;
             for (int b = a + 1; b < bs; ++b) {
-                E.s_lower.push_back(row);
-                E.s_upper.push_back(c * bs + b);
-                E.src.push_back(-1 - (c * bb + a * bs + b));
+                if (want_addr) {
+                    E.s_lower.push_back(row);
+                    E.s_upper.push_back(c * bs + b);
+                }
+                if (want_src) E.src.push_back(-1 - (c * bb + a * bs + b));
             }
             for (int k = start[c]; k < start[c + 1]; ++k) {
                 const int f = own[k];
                 for (int b = 0; b < bs; ++b) {
-                    E.s_lower.push_back(row);
-                    E.s_upper.push_back(upper[f] * bs + b);
-                    E.src.push_back(f * bb + a * bs + b);
+                    if (want_addr) {
+                        E.s_lower.push_back(row);
+                        E.s_upper.push_back(upper[f] * bs + b);
+                    }
+                    if (want_src) E.src.push_back(f * bb + a * bs + b);
                 }
             }
         }
@@ -126,7 +134,7 @@ int mrg_block_addressing(int n_cells, int n_faces, const int32_t* lower_addr, co
         const int64_t ns = (int64_t)n_faces * bs * bs + (int64_t)n_cells * bs * (bs - 1) / 2;
         if (n_faces_out) *n_faces_out = (int)ns;
         if (!s_lower || !s_upper) return MRG_OK;
-        const Expansion E = expand(n_cells, n_faces, lower_addr, upper_addr, bs);
+        const Expansion E = expand(n_cells, n_faces, lower_addr, upper_addr, bs, true, false);
         std::memcpy(s_lower, E.s_lower.data(), sizeof(int32_t) * E.s_lower.size());
         std::memcpy(s_upper, E.s_upper.data(), sizeof(int32_t) * E.s_upper.size());
         return MRG_OK;
@@ -147,7 +155,7 @@ int mrg_block_coeffs(int n_cells, int n_faces, const int32_t* lower_addr, const 
         const int64_t bb = (int64_t)bs * bs;
         for (int c = 0; c < n_cells; ++c)
             for (int a = 0; a < bs; ++a) s_diag[c * bs + a] = diag[c * bb + a * bs + a];
-        const Expansion E = expand(n_cells, n_faces, lower_addr, upper_addr, bs);
+        const Expansion E = expand(n_cells, n_faces, lower_addr, upper_addr, bs, false, true);
         for (size_t k = 0; k < E.src.size(); ++k) {
             const int64_t s = E.src[k];
             if (s < 0) {   // diagonal block's pair (a, b), a < b: upper D[a][b], lower D[b][a]

@@ -65,3 +65,12 @@ def test_bad_addressing(mrg):
     lo[0] = c["upper"][0]   # lower == upper: not an internal face
     with pytest.raises(mrg.MrgError, match="block addressing"):
         mrg.block_system(c["n"], lo, c["upper"], 2, c["D"], c["U"], c["L"])
+
+
+def test_unordered_block_faces(mrg):
+    """Block faces out of upper-triangular order are rejected, as for the
+    scalar mesh upload (foam's lduAddressing is always in that order)."""
+    c = block_case(5, 4, 3, bs=3, seed=8)
+    perm = np.random.default_rng(1).permutation(len(c["lower"]))
+    with pytest.raises(mrg.MrgError, match="upper-triangular"):
+        mrg.block_system(c["n"], c["lower"][perm], c["upper"][perm], 3, c["D"], c["U"][perm], c["L"][perm])

@@ -500,8 +500,9 @@ int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel,
  * mrg_block_coeffs: diag [n_cells bs bs], upper and lower [n_faces bs bs]
  *   (row-major blocks; lower NULL: every lower block is its upper block
  *   transposed) -> s_diag [bs n_cells], s_upper, s_lower [n_faces_out], in
- *   mrg_block_addressing's face order.  bs is 1..8; MRG_E_INVALID for bad
- *   addressing or sizes. */
+ *   mrg_block_addressing's face order.  bs is 1..8; the block addressing
+ *   follows mrg_mesh_upload's rules (lower < upper, upper-triangular face
+ *   order); MRG_E_INVALID otherwise or for bad sizes. */
 int mrg_block_addressing(int n_cells, int n_faces, const int32_t* lower_addr,
                          const int32_t* upper_addr, int bs, int* n_faces_out,
                          int32_t* s_lower, int32_t* s_upper);

@@ -68,6 +68,17 @@ static T* upload(Ctx* c, const std::vector<T>& v)
     return p;
 }
 
+// The same with `extra` zero elements after the data (Ctx::alloc clears):
+// the streamed SpMV copies a round's slice bounds as 12 ints from 8 r, up to
+// 3 past the last bound.
+template <typename T>
+static T* upload_padded(Ctx* c, const std::vector<T>& v, size_t extra)
+{
+    T* p = (T*)c->alloc(sizeof(T) * (v.size() + extra));
+    if (!v.empty()) MRG_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c->st));
+    return p;
+}
+
 // One wave of 256-thread CTAs at the 4 per SM the kernels are compiled for.
 static int grid_sweep(const Ctx* c) { return c->nsm * 4; }
 
@@ -251,7 +262,7 @@ PlanState& Mesh::plan(int ordering)
     PlanHost& H = P->host;
     Ctx* c = ctx;
     P->perm = upload(c, H.perm);
-    P->a_sptr = upload(c, H.a_sptr);
+    P->a_sptr = upload_padded(c, H.a_sptr, 16);
     P->a_col = upload(c, H.a_col);
     P->a_src = upload(c, H.a_src);
     P->chunk_start = upload(c, H.chunk_start);
@@ -749,6 +760,8 @@ static void write_ctl_controls(BatchHost& bh, const Controls& cfg)
     host.max_outer = cfg.max_outer;
     host.mixed = cfg.precision == MRG_PRECISION_MIXED ? 1 : 0;
     host.n_sweeps = std::max(1, cfg.n_sweeps);
+    host.wait_cycles = bh.ctx->wait_cycles;
+    host.unpublished1 = bh.ctx->unpublished1;
     // tickets, error bits and active counts start at zero
     MRG_CUDA(cudaMemcpyAsync(bh.d_ctl, &host, sizeof(Ctl), cudaMemcpyHostToDevice, bh.ctx->st));
 }

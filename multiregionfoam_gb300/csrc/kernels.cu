@@ -18,6 +18,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdlib>
+#include <cstring>
 
 #include "kernels.h"
 #include "plan.h"
@@ -29,9 +30,15 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr long long kSentBits64 = 0x7FF4DEADBEEF0001LL;  // signalling-NaN payload
 constexpr unsigned kSentBits32 = 0x7FA5A5A5u;
-// A sync-free wait gives up after this many SM cycles (~2 s) and flags
-// ERR_TIMEOUT, so no kernel can spin forever.
+// A device wait gives up after this many SM cycles (~2 s) unless the
+// batch's control block sets its own budget, and flags ERR_TIMEOUT, so no
+// kernel can spin forever.
 constexpr long long kWaitCycles = 4000000000LL;
+__device__ __forceinline__ long long wait_budget(const Ctl* ctl)
+{
+    const long long w = ctl->wait_cycles;
+    return w > 0 ? w : kWaitCycles;
+}
 
 // Programmatic dependent launch.  The Krylov-loop kernels are launched with
 // programmatic stream serialisation, so a kernel's CTAs can be scheduled
@@ -169,7 +176,7 @@ __device__ __forceinline__ V wait_ready(const V* p, Ctl* ctl)
         if (!is_sent(v)) return v;
         if ((it & 255) == 0) {
             if (*(volatile unsigned*)&ctl->err) return v;
-            if (clock64() - t0 > kWaitCycles) {
+            if (clock64() - t0 > wait_budget(ctl)) {
                 atomicOr(&ctl->err, ERR_TIMEOUT);
                 return v;
             }
@@ -204,13 +211,24 @@ __device__ __forceinline__ double warp_sum(double v)
 // Lane l of warp 0 adds the eight warps' values at lane l in warp order, then
 // one shuffle tree finishes: 12 FP64 adds on 32 lanes instead of a shuffle
 // tree on all 256 threads (FP64 adds are scarce on GB300).
-template <int NR>
+// NB: the CTA also runs a producer warp beyond the kBlock threads, so the
+// kBlock row threads meet at named barrier 1 instead of __syncthreads.
+template <bool NB>
+__device__ __forceinline__ void row_barrier()
+{
+    if constexpr (NB)
+        asm volatile("bar.sync 1, %0;" ::"n"(kBlock) : "memory");
+    else
+        __syncthreads();
+}
+
+template <int NR, bool NB = false>
 __device__ __forceinline__ void block_sum(double (&a)[NR], double* sh)
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 #pragma unroll
     for (int k = 0; k < NR; ++k) sh[k * kBlock + tid] = a[k];
-    __syncthreads();
+    row_barrier<NB>();
     if (wid == 0) {
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
@@ -220,7 +238,7 @@ __device__ __forceinline__ void block_sum(double (&a)[NR], double* sh)
             a[k] = warp_sum(s);
         }
     }
-    __syncthreads();
+    row_barrier<NB>();
 }
 
 // ---------------------------------------------------------------- vector picks
@@ -1269,7 +1287,7 @@ __device__ __forceinline__ bool system_live(const SysDev& S)
 // t the slots t, t + 256, ... in order -- and finalises.  Every slot is
 // rewritten by every reduction, so none needs clearing.  Deterministic: the
 // order depends only on the system.
-template <RowOp OP>
+template <RowOp OP, bool NB = false>
 __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, int seg, int count,
                                               double (&acc)[kMaxRed], double* sh, int* s_last, int total = -1)
 {
@@ -1278,7 +1296,7 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
     double a[NR];
 #pragma unroll
     for (int k = 0; k < NR; ++k) a[k] = acc[k];
-    block_sum<NR>(a, sh);
+    block_sum<NR, NB>(a, sh);
     if (tid == 0) {
 #pragma unroll
         for (int k = 0; k < NR; ++k) S.partials[seg * kMaxRed + k] = a[k];
@@ -1286,7 +1304,7 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
         const unsigned prev = atomicAdd(S.counter, (unsigned)count);
         *s_last = (prev + (unsigned)count == (unsigned)(total < 0 ? S.ntiles : total));
     }
-    __syncthreads();
+    row_barrier<NB>();
     if (*s_last) {
         const int G = red_segments(S.ntiles);
         // every slot this thread sums, loaded before the first add
@@ -1306,7 +1324,7 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
             for (int c = 0; c < kMaxPer; ++c)
                 if (tid + c * kBlock < G) tot[k] += v[c][k];
         }
-        block_sum<NR>(tot, sh);
+        block_sum<NR, NB>(tot, sh);
         if (tid == 0) {
             double sums[kMaxRed] = {0.0, 0.0};
 #pragma unroll
@@ -1316,7 +1334,7 @@ __device__ __forceinline__ void flush_segment(const Batch& B, const SysDev& S, i
             __threadfence();
         }
     }
-    __syncthreads();
+    row_barrier<NB>();
 }
 
 // Amul + (q, p) over rounds [rb, re) of one system (round r: the rows of
@@ -1526,6 +1544,37 @@ __device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, unsigne
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// L2 policy for data read once per launch (coefficients, column indices,
+// the diagonal): evicted first, so the gathered vector -- written by the
+// previous kernel and read up to seven times here -- keeps its L2 lines.
+__device__ __forceinline__ unsigned long long l2_evict_first()
+{
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ void bulk_to_smem_stream(void* dst, const void* src, unsigned bytes,
+                                                    unsigned long long* bar, unsigned long long pol)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+        "%4;" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+__device__ __forceinline__ float ldg_stream(const float* p, unsigned long long pol)
+{
+    float v;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ldg_stream(const double* p, unsigned long long pol)
+{
+    double v;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity)
 {
     unsigned ok;
@@ -1544,7 +1593,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity
     const long long t0 = clock64();
     for (int it = 1;; ++it) {
         if (mbar_try_wait(b, parity)) return true;
-        if ((it & 63) == 0 && clock64() - t0 > kWaitCycles) {
+        if ((it & 63) == 0 && clock64() - t0 > wait_budget(ctl)) {
             atomicOr(&ctl->err, ERR_TIMEOUT);
             return false;
         }
@@ -1621,14 +1670,16 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
         const V* __restrict__ dg = VP<V>::diag(sS);
         const V* __restrict__ p = VP<V>::v(sS).p;
         V* __restrict__ q = VP<V>::v(sS).q;
+        const unsigned long long pol = l2_evict_first();
         auto issue = [&](int r) {
             const int sl = NW * r + wid;
             const int e0 = __ldg(sptr + sl), cnt = __ldg(sptr + sl + 1) - e0;
             const int stg = r % S;
             if (cnt > 0 && cnt <= kSliceEntries) {
                 mbar_expect_tx(&full[wid][stg], (unsigned)cnt * (unsigned)(sizeof(int) + (kVals ? sizeof(V) : 0)));
-                bulk_to_smem(col_st(stg), acol + e0, (unsigned)cnt * sizeof(int), &full[wid][stg]);
-                if (kVals) bulk_to_smem(val_st(stg), aval + e0, (unsigned)cnt * sizeof(V), &full[wid][stg]);
+                bulk_to_smem_stream(col_st(stg), acol + e0, (unsigned)cnt * sizeof(int), &full[wid][stg], pol);
+                if (kVals)
+                    bulk_to_smem_stream(val_st(stg), aval + e0, (unsigned)cnt * sizeof(V), &full[wid][stg], pol);
             } else {
                 mbar_expect_tx(&full[wid][stg], 0u);
             }
@@ -1674,14 +1725,14 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
 #pragma unroll
                 for (int j = 0; j < RP; ++j) {
                     xi[j] = __ldca(p + i_[j]);
-                    dv[j] = __ldg(dg + i_[j]);
+                    dv[j] = ldg_stream(dg + i_[j], pol);
                     lv[j] = 0;
 #pragma unroll
                     for (int k = 0; k < kMaxW; ++k) {
                         const int ck = k < W_[j] ? st_col[cs[j] + k * 32] : -1;
                         lv[j] |= (ck >= 0 ? 1u : 0u) << k;
                         xv[j][k] = ck >= 0 ? __ldca(p + ck) : V(0);
-                        if constexpr (!kVals) av[j][k] = ck >= 0 ? __ldg(aval + e_[j] + lane + k * 32) : V(0);
+                        if constexpr (!kVals) av[j][k] = ck >= 0 ? ldg_stream(aval + e_[j] + lane + k * 32, pol) : V(0);
                     }
                 }
 #pragma unroll
@@ -1726,6 +1777,357 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
 }
 #undef col_st
 #undef val_st
+
+// ------------------------------------------------------------ streamed SpMV
+// Amul + (q, p) with the streamed operands brought in by the bulk-copy
+// (TMA) engine: a producer warp walks the CTA's segments round by round
+// (256 rows: the 8 slices of 32 rows the 8 row warps take, as in
+// k_spmv_warp) and copies, per round, into a ring of S shared-memory
+// stages: the round's slice bounds, column indices and coefficients (one
+// contiguous range each, since a round's slices are consecutive in the
+// sliced ELL), and with one round per step also the rows' own x and
+// diagonal.  The copies of coefficients, indices and diagonal carry an L2
+// evict-first policy, so the gathered vector keeps its L2 lines.  The row
+// warps load only the gathered x (and, with two rounds per step, own x and
+// diagonal) from global memory: the DRAM latency of the streams is off
+// their chain and the copies of the next rounds are in flight while a round
+// computes.  With RP = 2 a warp takes two rounds per step and has both
+// rounds' gathers in flight at once.  Each row's arithmetic and each
+// thread's rows and their order are k_spmv_warp's, so all kernels give the
+// same bits (FP64: the order the oracle mirrors).  A round whose entries
+// exceed a stage (kStageCap) has only its bounds (and own x, diagonal)
+// staged; its rows read indices and coefficients from global memory.  Waits
+// are bounded: on a timeout the error bit is set, the row warps leave their
+// loop, and the producer waits (bounded) for the copies it issued before the
+// CTA exits.
+template <typename V, int RP> struct StreamCfg;
+// one round per step: three stages of 14.4 KB (FP32) / two of 22.6 KB (FP64)
+template <> struct StreamCfg<float, 1> { static constexpr int S = 3; static constexpr bool XD = true; };
+template <> struct StreamCfg<double, 1> { static constexpr int S = 2; static constexpr bool XD = true; };
+// two rounds per step: four stages of 12.3 KB (FP32; own x and diagonal
+// loaded by the row warps), so two rounds are in flight while two compute
+template <> struct StreamCfg<float, 2> { static constexpr int S = 4; static constexpr bool XD = false; };
+constexpr int kStageCap = kBlock * kMaxW;                              // entries per stage
+constexpr int kStageHead = 64;                                          // slice bounds (48 B used)
+template <typename V, int RP>
+__host__ __device__ constexpr unsigned stream_xd_bytes()
+{
+    return StreamCfg<V, RP>::XD ? (unsigned)(2 * kBlock * sizeof(V)) : 0u;
+}
+template <typename V, int RP>
+__host__ __device__ constexpr unsigned stream_stage_bytes()
+{
+    return (unsigned)(kStageHead + stream_xd_bytes<V, RP>() + kStageCap * (sizeof(int) + sizeof(V)));
+}
+static_assert(stream_stage_bytes<float, 1>() % 16 == 0 && stream_stage_bytes<double, 1>() % 16 == 0 &&
+                  stream_stage_bytes<float, 2>() % 16 == 0 && (kStageHead + 2 * kBlock * 4) % 16 == 0 &&
+                  (kStageCap * 4) % 16 == 0,
+              "every bulk-copy destination in a stage is 16-byte aligned");
+template <typename V, int RP>
+constexpr size_t stream_smem()
+{
+    return (size_t)StreamCfg<V, RP>::S * stream_stage_bytes<V, RP>();
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(b))
+                 : "memory");
+}
+// Bounded wait that also gives up once another warp of the CTA aborted.
+__device__ __forceinline__ bool mbar_wait_or_abort(unsigned long long* b, unsigned parity, Ctl* ctl,
+                                                   volatile int* abort)
+{
+    if (mbar_try_wait(b, parity)) return true;
+    const long long t0 = clock64();
+    for (int it = 1;; ++it) {
+        if (mbar_try_wait(b, parity)) return true;
+        if ((it & 63) == 0) {
+            if (*abort) return false;
+            if (clock64() - t0 > wait_budget(ctl)) {
+                atomicOr(&ctl->err, ERR_TIMEOUT);
+                return false;
+            }
+        }
+    }
+}
+
+// The rounds [rb, re) of reduction segment sg.y of a system (FP32: segments
+// of rounds; FP64: of whole tiles, the oracle's order).
+template <typename V>
+__device__ __forceinline__ void stream_rounds(const SysDev& S, int segy, int& rb, int& re, int& u0, int& u1,
+                                              unsigned long long& U)
+{
+    constexpr bool kRoundSeg = sizeof(V) == 4;
+    const unsigned T = (unsigned)S.ntiles, G = (unsigned)red_segments(S.ntiles);
+    U = kRoundSeg ? 4ull * T : (unsigned long long)T;
+    u0 = (int)(((unsigned long long)segy * U) / G);
+    u1 = (int)(((unsigned long long)(segy + 1) * U) / G);
+    rb = kRoundSeg ? u0 : 4 * u0;
+    re = kRoundSeg ? u1 : 4 * u1;
+}
+
+template <typename V, int RP>
+__global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Batch* __restrict__ pB)
+{
+    constexpr int S = StreamCfg<V, RP>::S;
+    constexpr bool XD = StreamCfg<V, RP>::XD;
+    static_assert(S > RP, "the producer needs a stage beyond the ones a step computes");
+    constexpr int NW = kBlock / 32;
+    constexpr unsigned SB = stream_stage_bytes<V, RP>();
+    constexpr unsigned XB = stream_xd_bytes<V, RP>();
+    __shared__ double sh[kBlock * kMaxRed];
+    __shared__ int s_last;
+    __shared__ volatile int s_abort;
+    __shared__ __align__(16) SysDev sS;   // the row warps' system
+    __shared__ __align__(16) SysDev sP;   // the producer's system
+    __shared__ __align__(8) unsigned long long full[S], empty[S];
+    extern __shared__ __align__(128) unsigned char dyn[];
+    const Batch B = *pB;   // descriptors (host-written) while the previous kernel drains
+    Ctl* ctl = B.ctl;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], NW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    __syncthreads();
+    pdl_enter();
+
+    if (wid == NW) {
+        // ---------------------------------------------------------- producer
+        unsigned seq = 0;        // rounds issued by this CTA so far
+        int cur = -1, lcur = -1;
+        bool live = false;
+        for (int g = blockIdx.x; g < B.nsegs && !s_abort; g += gridDim.x) {
+            const int2 sg = B.nsys == 1 ? make_int2(0, g) : B.segs[g];
+            if (sg.x != lcur) {
+                lcur = sg.x;
+                if (sg.x != cur) {
+                    cur = sg.x;
+                    __syncwarp();
+                    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(B.sys + cur);
+                    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sP);
+                    for (int k = lane; k < (int)(sizeof(SysDev) / 8); k += 32) dst[k] = src[k];
+                    __syncwarp();
+                }
+                live = system_live<OP_SPMV_QP>(sP);
+            }
+            if (!live) continue;
+            int rb, re, u0, u1;
+            unsigned long long U;
+            stream_rounds<V>(sP, sg.y, rb, re, u0, u1, U);
+            const int* __restrict__ sptr = sP.a_sptr;
+            const int* __restrict__ acol = sP.a_col;
+            const V* __restrict__ aval = VP<V>::aval(sP, false);
+            const V* __restrict__ dg = VP<V>::diag(sP);
+            const V* __restrict__ p = VP<V>::v(sP).p;
+            // round starts in the sliced ELL, a window of 32 rounds per
+            // load (lane j: round w0 + j), the next window loaded a window
+            // ahead
+            auto win = [&](int w0, int& e, int& eend) {
+                const int a = min(w0 + lane, re), z = min(w0 + 32, re);
+                e = __ldg(sptr + 8 * a);
+                eend = __ldg(sptr + 8 * z);
+            };
+            int ec, ecend, en = 0, enend = 0;
+            win(rb, ec, ecend);
+            if (rb + 32 < re) win(rb + 32, en, enend);
+            for (int r = rb; r < re; ++r, ++seq) {
+                const int j = (r - rb) & 31;
+                if (j == 0 && r > rb) {
+                    ec = en;
+                    ecend = enend;
+                    if (r + 32 < re) win(r + 32, en, enend);
+                }
+                const int e0 = __shfl_sync(kFull, ec, j);
+                const int e1 = j < 31 ? __shfl_sync(kFull, ec, j + 1) : ecend;
+                const int stg = (int)(seq % S);
+                const unsigned ph = (seq / S) & 1u;
+                bool ok = true;
+                if (seq >= (unsigned)S && lane == 0) ok = mbar_wait_or_abort(&empty[stg], ph ^ 1u, ctl, &s_abort);
+                if (!__shfl_sync(kFull, (int)ok, 0)) {
+                    if (lane == 0) s_abort = 1;
+                    break;
+                }
+                if (lane == 0) {
+                    const unsigned long long pol = l2_evict_first();
+                    unsigned char* st = dyn + (size_t)stg * SB;
+                    const int cnt = e1 - e0;
+                    const bool staged = cnt <= kStageCap;
+                    const unsigned bytes =
+                        48u + XB + (staged ? (unsigned)cnt * (unsigned)(sizeof(int) + sizeof(V)) : 0u);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_expect_tx(&full[stg], bytes);
+                    bulk_to_smem(st, sptr + 8 * r, 48u, &full[stg]);
+                    if constexpr (XD) {
+                        bulk_to_smem(st + kStageHead, p + (size_t)kBlock * r, kBlock * (unsigned)sizeof(V),
+                                     &full[stg]);
+                        bulk_to_smem_stream(st + kStageHead + kBlock * sizeof(V), dg + (size_t)kBlock * r,
+                                            kBlock * (unsigned)sizeof(V), &full[stg], pol);
+                    }
+                    if (staged && cnt > 0) {
+                        bulk_to_smem_stream(st + kStageHead + XB, acol + e0, (unsigned)cnt * sizeof(int), &full[stg],
+                                            pol);
+                        bulk_to_smem_stream(st + kStageHead + XB + kStageCap * sizeof(int), aval + e0,
+                                            (unsigned)cnt * (unsigned)sizeof(V), &full[stg], pol);
+                    }
+                }
+                __syncwarp();
+            }
+            if (s_abort) break;
+        }
+        // every copy issued lands before the CTA may exit: wait (bounded)
+        // for the last phase issued into each stage
+        if (lane == 0) {
+            for (int k = 0; k < S && (unsigned)k < seq; ++k) {
+                const unsigned last = seq - 1 - (unsigned)((seq - 1 - k) % S);   // last seq issued into stage
+                const int stg = (int)(last % S);
+                mbar_wait(&full[stg], (last / S) & 1u, ctl);
+            }
+        }
+        return;
+    }
+
+    // -------------------------------------------------------------- row warps
+    unsigned seq = 0;
+    int cur = -1, lcur = -1;
+    bool live = false;
+    const unsigned long long pol = l2_evict_first();
+    for (int g = blockIdx.x; g < B.nsegs; g += gridDim.x) {
+        const int2 sg = B.nsys == 1 ? make_int2(0, g) : B.segs[g];
+        if (sg.x != lcur) {
+            lcur = sg.x;
+            if (sg.x != cur) {
+                cur = sg.x;
+                // the row warps' copy of the system, behind their own barrier
+                row_barrier<true>();
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(B.sys + cur);
+                unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sS);
+                for (int k = tid; k < (int)(sizeof(SysDev) / 8); k += kBlock) dst[k] = src[k];
+                row_barrier<true>();
+            }
+            live = system_live<OP_SPMV_QP>(sS);
+        }
+        if (!live) continue;
+        int rb, re, u0, u1;
+        unsigned long long U;
+        stream_rounds<V>(sS, sg.y, rb, re, u0, u1, U);
+        const int* __restrict__ acol = sS.a_col;
+        const V* __restrict__ aval = VP<V>::aval(sS, false);
+        const V* __restrict__ dg = VP<V>::diag(sS);
+        const V* __restrict__ p = VP<V>::v(sS).p;
+        V* __restrict__ q = VP<V>::v(sS).q;
+        double acc[kMaxRed] = {0.0, 0.0};
+        for (int r = rb; r < re; r += RP, seq += RP) {
+            const int nr = min(RP, re - r);   // an FP32 segment may end on an odd round
+            bool ok = true;
+            if (lane == 0)
+                for (int j = 0; j < nr && ok; ++j)
+                    ok = mbar_wait_or_abort(&full[(seq + j) % S], ((seq + j) / S) & 1u, ctl, &s_abort);
+            ok = __shfl_sync(kFull, (int)ok, 0) != 0;
+            if (!ok) {
+                if (lane == 0) s_abort = 1;
+                break;
+            }
+            // every lane observes the completed phases itself (acquire)
+            for (int j = 0; j < nr; ++j) mbar_try_wait(&full[(seq + j) % S], ((seq + j) / S) & 1u);
+            const unsigned char* stj[RP];
+            int ew[RP], W[RP], o[RP], i_[RP];
+            bool fast = true;
+#pragma unroll
+            for (int j = 0; j < RP; ++j) {
+                stj[j] = dyn + (size_t)((seq + j) % S) * SB;
+                const int* spv = reinterpret_cast<const int*>(stj[j]);
+                const bool on = j < nr;
+                const int base = on ? spv[0] : 0;
+                ew[j] = on ? spv[wid] : 0;
+                W[j] = on ? (spv[wid + 1] - ew[j]) >> 5 : 0;
+                o[j] = ew[j] - base + lane;
+                i_[j] = (NW * (r + j) + wid) * 32 + lane;
+                fast = fast && on && spv[NW] - base <= kStageCap && W[j] <= kMaxW;
+            }
+            if (fast) {
+                V xi[RP], dv[RP], xv[RP][kMaxW];
+                int c[RP][kMaxW];
+#pragma unroll
+                for (int j = 0; j < RP; ++j) {
+                    const int* scol = reinterpret_cast<const int*>(stj[j] + kStageHead + XB);
+                    if constexpr (XD) {
+                        xi[j] = reinterpret_cast<const V*>(stj[j] + kStageHead)[wid * 32 + lane];
+                        dv[j] = reinterpret_cast<const V*>(stj[j] + kStageHead + kBlock * sizeof(V))[wid * 32 + lane];
+                    } else {
+                        xi[j] = __ldca(p + i_[j]);
+                        dv[j] = ldg_stream(dg + i_[j], pol);
+                    }
+#pragma unroll
+                    for (int k = 0; k < kMaxW; ++k) c[j][k] = k < W[j] ? scol[o[j] + k * 32] : -1;
+                }
+#pragma unroll
+                for (int j = 0; j < RP; ++j)
+#pragma unroll
+                    for (int k = 0; k < kMaxW; ++k) xv[j][k] = c[j][k] >= 0 ? __ldca(p + c[j][k]) : V(0);
+#pragma unroll
+                for (int j = 0; j < RP; ++j) {
+                    const V* sval = reinterpret_cast<const V*>(stj[j] + kStageHead + XB + kStageCap * sizeof(int));
+                    V y = vmul(dv[j], xi[j]);
+#pragma unroll
+                    for (int k = 0; k < kMaxW; ++k)
+                        if (c[j][k] >= 0) y = vfma(sval[o[j] + k * 32], xv[j][k], y);
+                    q[i_[j]] = y;
+                    acc[0] = __fma_rn(widen(y), widen(xi[j]), acc[0]);
+                }
+            } else {
+                for (int j = 0; j < nr; ++j) {
+                    const int* spv = reinterpret_cast<const int*>(stj[j]);
+                    const bool staged = spv[NW] - spv[0] <= kStageCap;
+                    const int* scol = reinterpret_cast<const int*>(stj[j] + kStageHead + XB);
+                    const V* sval = reinterpret_cast<const V*>(stj[j] + kStageHead + XB + kStageCap * sizeof(int));
+                    V xi, dv;
+                    if constexpr (XD) {
+                        xi = reinterpret_cast<const V*>(stj[j] + kStageHead)[wid * 32 + lane];
+                        dv = reinterpret_cast<const V*>(stj[j] + kStageHead + kBlock * sizeof(V))[wid * 32 + lane];
+                    } else {
+                        xi = __ldca(p + i_[j]);
+                        dv = __ldg(dg + i_[j]);
+                    }
+                    V y = vmul(dv, xi);
+                    if (staged)
+                        for (int k0 = 0; k0 < W[j]; k0 += kMaxW)
+                            y = ell_round<V, false>(scol + o[j], sval + o[j], p, k0, W[j], y);
+                    else
+                        for (int k0 = 0; k0 < W[j]; k0 += kMaxW)
+                            y = ell_round<V, true>(acol + ew[j] + lane, aval + ew[j] + lane, p, k0, W[j], y);
+                    q[i_[j]] = y;
+                    acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
+                }
+            }
+            __syncwarp();   // every lane's reads of the stages are done
+            if (lane == 0)
+                for (int j = 0; j < nr; ++j) mbar_arrive(&empty[(seq + j) % S]);
+        }
+        flush_segment<OP_SPMV_QP, true>(B, sS, sg.y, u1 - u0, acc, sh, &s_last, (int)U);
+        if (s_abort) return;   // read after the flush's closing barrier
+    }
+}
+
+// Amul + (q, p) kernel: MRG_SPMV=warp (0) the per-warp staged kernel;
+// =stream1 (1) the streamed kernel with one round per step (FP32 and FP64);
+// default (2) the streamed kernel with two rounds per step in FP32 and the
+// per-warp staged kernel in FP64.  All give the same bits.
+static int spmv_mode()
+{
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = std::getenv("MRG_SPMV");
+        mode = (e && std::strcmp(e, "warp") == 0) ? 0 : (e && std::strcmp(e, "stream1") == 0) ? 1 : 2;
+    }
+    return mode;
+}
 
 // FP32 levelled sweeps two chunks per warp step (k_sweep_lvl with PAIRS);
 // MRG_SWEEP_PAIRS=0 takes one chunk per step.
@@ -1781,7 +2183,13 @@ void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
     if (grid < 1) grid = 1;
     if constexpr (OP == OP_SPMV_QP) {
         if (!pb) {
-            launch_pdl(k_spmv_warp<V>, grid, kBlock, spmv_smem<V>(), st, dB);
+            const int mode = spmv_mode();
+            if (mode == 0 || (sizeof(V) == 8 && mode != 1))
+                launch_pdl(k_spmv_warp<V>, grid, kBlock, spmv_smem<V>(), st, dB);
+            else if (sizeof(V) == 8 || mode == 1)
+                launch_pdl(k_spmv_stream<V, 1>, grid, kBlock + 32, stream_smem<V, 1>(), st, dB);
+            else
+                launch_pdl(k_spmv_stream<float, 2>, grid, kBlock + 32, stream_smem<float, 2>(), st, dB);
             return;
         }
     }
@@ -2131,6 +2539,7 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
     const int lane = threadIdx.x & 31;
     const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
     const int slot = FWD ? 2 : 4;
+    const int unpublished = FWD ? ctl->unpublished1 - 1 : -1;   // watchdog test hook
     for (;;) {
         unsigned t = 0;
         if (lane == 0) t = atomicAdd(&ctl->ticket[slot], 1u);
@@ -2139,7 +2548,7 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
         const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
         const SysDev& S = Ss[s];
         const int nch = S.nchunks;
-        if (c >= nch || !S.sc->active || !S.syncfree || S.pc < PC_DIC) continue;
+        if (c >= nch || !S.sc->active || !S.syncfree || S.pc < PC_DIC || c == unpublished) continue;
         const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans);
         sweep_chunk<V, FWD>(P, FWD ? c : nch - 1 - c, true, ctl, 0, false, false);
     }
@@ -2451,7 +2860,7 @@ __device__ bool grid_barrier(Ctl* ctl)
                         ok = 0;
                         break;
                     }
-                    if (clock64() - t0 > kWaitCycles) {
+                    if (clock64() - t0 > wait_budget(ctl)) {
                         atomicOr(&ctl->err, ERR_TIMEOUT);
                         ok = 0;
                         break;
@@ -2543,6 +2952,12 @@ void set_device_sms(int nsm)
     // limit; set once per device, outside any stream capture
     cudaFuncSetAttribute(k_spmv_warp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_smem<float>());
     cudaFuncSetAttribute(k_spmv_warp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_smem<double>());
+    cudaFuncSetAttribute(k_spmv_stream<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)stream_smem<float, 1>());
+    cudaFuncSetAttribute(k_spmv_stream<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)stream_smem<double, 1>());
+    cudaFuncSetAttribute(k_spmv_stream<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)stream_smem<float, 2>());
 }
 int persistent_grid() { return g_grid_cap; }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }

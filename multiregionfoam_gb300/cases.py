@@ -266,6 +266,13 @@ def c5_meshes(count: int = 100, seed: int = 0, n_lo: int = 10000, n_hi: int = 20
     """Served case: `count` meshes of log-uniform size in [n_lo, n_hi] cells,
     a fraction `asym_frac` asymmetric convection-diffusion (PBiCG+DILU), the
     rest two-region CHT (PCG+DIC).  Returns [(system, asym)]."""
+    return [(c5_mesh(sp), sp[0]) for sp in c5_specs(count, seed, n_lo, n_hi, asym_frac)]
+
+
+def c5_specs(count: int = 100, seed: int = 0, n_lo: int = 10000, n_hi: int = 2000000, asym_frac: float = 0.3):
+    """The served case's meshes as cheap descriptions: [(asym, dims, seed)],
+    cells log-uniform in [n_lo, n_hi], random aspect ratios, a fraction
+    `asym_frac` asymmetric convection-diffusion.  c5_mesh builds one."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
@@ -273,13 +280,165 @@ def c5_meshes(count: int = 100, seed: int = 0, n_lo: int = 10000, n_hi: int = 20
         a = np.exp(rng.uniform(np.log(0.5), np.log(2.0), 3))
         a = a / np.cbrt(a.prod())
         asym = bool(rng.uniform() < asym_frac)
-        nx, ny, nz = (max(4, int(round(np.cbrt(n) * a[k]))) for k in range(3))
-        if asym:
-            out.append((convdiff_system(nx, ny, nz, seed=seed + 1 + i), True))
-        else:
-            nzs = max(2, nz // 3)
-            out.append((cht_system(nx, ny, max(2, nz - nzs), nzs, seed=seed + 1 + i, k_range=(0.1, 50.0)), False))
+        dims = tuple(max(4, int(round(np.cbrt(n) * a[k]))) for k in range(3))
+        out.append((asym, dims, seed + 1 + i))
     return out
+
+
+def c5_mesh(spec) -> LduSystem:
+    """One served mesh from its c5_specs description (time step 0)."""
+    asym, (nx, ny, nz), sd = spec
+    if asym:
+        return convdiff_system(nx, ny, nz, seed=sd)
+    nzs = max(2, nz // 3)
+    return cht_system(nx, ny, max(2, nz - nzs), nzs, seed=sd, k_range=(0.1, 50.0))
+
+
+def c5_step(base: LduSystem, mesh: int, step: int, seed: int = 0) -> LduSystem:
+    """Time step `step` of served mesh `mesh`: `step` successive 5 %
+    perturbations of its step-0 system, each drawn from a generator seeded by
+    (seed, mesh, step), so any request can be rebuilt on its own."""
+    cur = base
+    for k in range(1, step + 1):
+        cur = perturb_step(cur, np.random.default_rng((seed, mesh, k)))
+    return cur
+
+
+def jittered_faces(nx, ny, jitter, seed):
+    """Quads of a jittered nx*ny lattice on the unit square (boundary nodes
+    fixed), counter-clockwise: (vertex pointers, (x, y) vertices)."""
+    rng = np.random.default_rng(seed)
+    X, Y = np.meshgrid(np.linspace(0, 1, nx + 1), np.linspace(0, 1, ny + 1), indexing="xy")
+    hx, hy = 1.0 / nx, 1.0 / ny
+    jx = rng.uniform(-jitter, jitter, X.shape) * hx
+    jy = rng.uniform(-jitter, jitter, Y.shape) * hy
+    jx[:, 0] = jx[:, -1] = 0
+    jy[0, :] = jy[-1, :] = 0
+    jx[0, :] = jx[-1, :] = 0
+    jy[:, 0] = jy[:, -1] = 0
+    X, Y = X + jx, Y + jy
+    xy = []
+    for j in range(ny):
+        for i in range(nx):
+            for (a, b) in ((j, i), (j, i + 1), (j + 1, i + 1), (j + 1, i)):
+                xy.append((X[a, b], Y[a, b]))
+    ptr = np.arange(0, 4 * nx * ny + 1, 4, dtype=np.int32)
+    return ptr, np.array(xy)
+
+
+def quad_areas(ptr, xy):
+    """|signed area| of quadrilateral faces by the shoelace sum, vertex pair
+    by vertex pair (each product and difference rounded on its own)."""
+    nf = len(ptr) - 1
+    assert np.all(np.diff(ptr) == 4), "quadrilateral faces"
+    P = np.asarray(xy, dtype=np.float64).reshape(nf, 4, 2)
+    a = np.zeros(nf)
+    for i in range(4):
+        j = (i + 1) % 4
+        a = a + (P[:, i, 0] * P[:, j, 1] - P[:, j, 0] * P[:, i, 1])
+    return np.abs(0.5 * a)
+
+
+def _c3_block(nx, ny, nz, hx, hy, hz, k, psi, offset):
+    """Faces, conductances and face fluxes of one convection-diffusion block."""
+    n = nx * ny * nz
+    idx = np.arange(n).reshape(nz, ny, nx)
+    lo = [idx[:, :, :-1].ravel(), idx[:, :-1, :].ravel(), idx[:-1, :, :].ravel()]
+    up = [idx[:, :, 1:].ravel(), idx[:, 1:, :].ravel(), idx[1:, :, :].ravel()]
+    xs, ys = np.arange(nx + 1) * hx, np.arange(ny + 1) * hy
+    P = psi(xs[None, :], ys[:, None])               # (ny+1, nx+1) at lattice nodes
+    # flux through an x-face (node column i, rows j..j+1) and a y-face; w = 0
+    fx = (P[1:, :] - P[:-1, :]) * hz                # (ny, nx+1)
+    fy = -(P[:, 1:] - P[:, :-1]) * hz               # (ny+1, nx)
+    phi = [np.broadcast_to(fx[None, :, 1:-1], (nz, ny, nx - 1)).ravel(),
+           np.broadcast_to(fy[None, 1:-1, :], (nz, ny - 1, nx)).ravel(),
+           np.zeros(lo[2].size)]
+    g = [np.full(lo[0].size, k * hy * hz / hx), np.full(lo[1].size, k * hx * hz / hy),
+         np.full(lo[2].size, k * hx * hy / hz)]
+    lower, upper = np.concatenate(lo) + offset, np.concatenate(up) + offset
+    return lower, upper, np.concatenate(g), np.concatenate(phi), n
+
+
+def c3(weights, scale: int = 1, seed: int = 0, pe_max: float = 10.0, k: float = 1.0, rc: float = 1.0,
+       permute: bool = True):
+    """The asymmetric, non-conformal case.
+
+    A unit-square column split at z = 1/2: region A is an nA x nA x nz hex
+    block below, region B an nB x nA x nz block above (x spacing 1.5x A's: a
+    3:2 face-count ratio across the interface).  Both carry upwind
+    convection-diffusion with a seeded divergence-free in-plane velocity
+    (stream function vanishing on the side walls, so there is no flux
+    through them or through the interface), scaled to a largest cell Peclet
+    number of `pe_max` times a U(0,1) draw; Dirichlet 0 below A and 1 above
+    B; an implicit source.  The regions meet through a GGI interface: the
+    in-plane nodes of both interface patches are jittered by up to 0.2 h
+    (boundary nodes fixed) and ``weights(faces_a, faces_b)`` gives the
+    rescaled overlap weights in both directions ((ptr, addr, w) of A from B,
+    then of B from A: mrg_ggi_build's, or the oracle's), with interface
+    conductance k |face| / d.  Cell numbering is randomly permuted and the
+    faces re-sorted upper-triangular (permute=False keeps A's cells, then
+    B's, each lexicographic).  Full size (scale 1): A 96x96x48, B
+    64x96x48 = 737,280 cells, 9,216 : 6,144 interface faces.  Returns
+    (system, ggi) with ggi's CSR triples and patch sizes."""
+    rng = np.random.default_rng(seed)
+    na_xy, nb_x, nz = 96 // scale, 64 // scale, 48 // scale
+    hz = 0.5 / nz
+    modes = rng.standard_normal((3, 3))
+
+    def psi(x, y):
+        s = 0.0
+        for p in range(3):
+            for q in range(3):
+                s = s + modes[p, q] * np.sin(np.pi * (p + 1) * x) * np.sin(np.pi * (q + 1) * y)
+        return s
+
+    la, ua, ga, pa_, nA = _c3_block(na_xy, na_xy, nz, 1.0 / na_xy, 1.0 / na_xy, hz, k, psi, 0)
+    lb, ub, gb, pb_, nB = _c3_block(nb_x, na_xy, nz, 1.0 / nb_x, 1.0 / na_xy, hz, k, psi, nA)
+    n = nA + nB
+    lower, upper = np.concatenate([la, lb]), np.concatenate([ua, ub])
+    g, phi = np.concatenate([ga, gb]), np.concatenate([pa_, pb_])
+    # velocity scale: largest cell Peclet number pe_max, times U(0, 1)
+    h_min = min(1.0 / na_xy, hz)
+    umax = np.abs(phi).max() / (hz * h_min) if np.abs(phi).max() > 0 else 1.0
+    phi = phi * (pe_max * k / rc / (umax * h_min)) * rng.uniform(0.0, 1.0)
+    F = rc * phi
+    upper_c = -g + np.minimum(F, 0.0)
+    lower_c = -g - np.maximum(F, 0.0)
+    vol = np.concatenate([np.full(nA, hz / na_xy ** 2), np.full(nB, hz / (nb_x * na_xy))])
+    diag = rc * vol
+    np.add.at(diag, lower, g + np.maximum(F, 0.0))
+    np.add.at(diag, upper, g - np.minimum(F, 0.0))
+    t_old = rng.uniform(0.0, 1.0, n)
+    b = rc * vol * t_old
+    # Dirichlet 0 under A, 1 over B
+    a_bot = np.arange(na_xy * na_xy)
+    b_top = nA + np.arange(nb_x * na_xy) + (nz - 1) * nb_x * na_xy
+    diag[a_bot] += 2.0 * k * (1.0 / na_xy ** 2) / hz
+    gtop = 2.0 * k * (1.0 / (nb_x * na_xy)) / hz
+    diag[b_top] += gtop
+    b[b_top] += gtop
+    # GGI interface between A's top layer and B's bottom layer
+    fa = jittered_faces(na_xy, na_xy, 0.2, seed + 101)
+    fb = jittered_faces(nb_x, na_xy, 0.2, seed + 102)
+    (pa, sa, wa), (pb, sb, wb) = weights(fa, fb)
+    area_a, area_b = quad_areas(*fa), quad_areas(*fb)
+    a_top = np.arange(na_xy * na_xy) + (nz - 1) * na_xy * na_xy
+    b_bot = nA + np.arange(nb_x * na_xy)
+    d = hz                                          # centre-to-centre across the interface
+    coef = np.concatenate([k * area_a / d, k * area_b / d])
+    cells = np.concatenate([a_top, b_bot])
+    np.add.at(diag, cells, coef)
+    iface = {"cells": cells.astype(np.int32), "bou": coef, "int": None,
+             "ptr": np.concatenate([pa, pa[-1] + pb[1:]]).astype(np.int32),
+             "src": np.concatenate([b_bot[sa], a_top[sb]]).astype(np.int32),
+             "w": np.concatenate([wa, wb])}
+    lo2, up2, upc, loc = upper_triangular(lower, upper, upper_c, lower_c)
+    s = LduSystem(n, lo2.astype(np.int32), up2.astype(np.int32), diag, upc, loc, b, t_old, iface,
+                  name=f"c3/{scale}", meta=dict(nA=nA, nB=nB, n_ifa=a_top.size, n_ifb=b_bot.size))
+    if permute:
+        s = random_permute(s, seed + 7)
+    ggi = dict(a_from_b=(pa, sa, wa), b_from_a=(pb, sb, wb), n_a=a_top.size, n_b=b_bot.size)
+    return s, ggi
 
 
 def block_case(nx: int, ny: int, nz: int, bs: int = 4, seed: int = 0, symmetric: bool = False) -> dict:

@@ -6,6 +6,8 @@ an independent scipy cross-check, the reference's own self-checks
 (directMap conformity, GGI face-centre round trip) and committed fixtures.
 """
 import numpy as np
+
+from multiregionfoam_gb300.cases import jittered_faces  # noqa: F401  (other tests import it from here)
 import pytest
 import scipy.sparse.linalg as spl
 
@@ -176,27 +178,6 @@ def test_directmap_rejects_nonconformal():
     b = np.array([[0.0, 0, 0], [0.5, 0, 0]])
     with pytest.raises(ValueError, match="not conformal"):
         cases.direct_map(a, b, 1e-3)
-
-
-def jittered_faces(nx, ny, jitter, seed):
-    """Quads of a jittered nx*ny lattice on the unit square (boundary nodes fixed)."""
-    rng = np.random.default_rng(seed)
-    X, Y = np.meshgrid(np.linspace(0, 1, nx + 1), np.linspace(0, 1, ny + 1), indexing="xy")
-    hx, hy = 1.0 / nx, 1.0 / ny
-    jx = rng.uniform(-jitter, jitter, X.shape) * hx
-    jy = rng.uniform(-jitter, jitter, Y.shape) * hy
-    jx[:, 0] = jx[:, -1] = 0
-    jy[0, :] = jy[-1, :] = 0
-    jx[0, :] = jx[-1, :] = 0
-    jy[:, 0] = jy[:, -1] = 0
-    X, Y = X + jx, Y + jy
-    xy = []
-    for j in range(ny):
-        for i in range(nx):
-            for (a, b) in ((j, i), (j, i + 1), (j + 1, i + 1), (j + 1, i)):
-                xy.append((X[a, b], Y[a, b]))
-    ptr = np.arange(0, 4 * nx * ny + 1, 4, dtype=np.int32)
-    return ptr, np.array(xy)
 
 
 def test_ggi_weights_properties(oracle_mod):

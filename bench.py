@@ -14,34 +14,44 @@ monolithic LDU form.  One step = one solve to foam-normalised residual 1e-8
           mrg_solve from pinned host memory; copies inside the timed region)
   plain   the plain method, FP64 PCG+DIC in foam's order, reported beside
 
-Both results are measured against the FP64 oracle solution (the same system
-solved in FP64 to 1e-13) as max-norm relative errors.
+Every result carries its max-norm error against the FP64 oracle: the CPU
+oracle's foam-order solve of the same system converged to 1e-13 (1e-12 for
+the many small systems), computed after the GPU timing.
 
 The working set (~1 GB per solve) is far larger than the 129 MB L2, so no
 L2 flush is needed between steps.
 
-Beside the headline, the line carries the other forms of the metric:
+Beside the headline, the line carries the other configurations:
+  c3        the asymmetric, non-conformal pair (96^3-scale convection-
+            diffusion, permuted numbering, 3:2 GGI interface with weights
+            built on the device; 737,280 cells): PBiCG + DILU plain FP64,
+            mixed with BiCGStab and with PBiCG inner solves, and the GGI
+            gather of a random face field (--c3-scale, 0 skips)
   batched   512 independent CHT systems (8k-260k cells) in one batch, mixed
             vs plain FP64, solves/s (--batched N, 0 skips)
   block     a 4x4 block-coupled system (48^3 cells, the shape of a
             BlockLduMatrix<vector4>) expanded to its scalar LDU system and
-            solved by BiCGStab + DILU, mixed vs plain FP64, with the host
-            expansion time (--block-n N, 0 skips)
+            solved by BiCGStab + DILU, mixed vs plain FP64 (--block-n N)
   gamg      GAMG (GaussSeidel smoother, the tutorials' fluid p / T settings)
             on a 64^3-cell CHT system, FP64 foam order, beside plain PCG +
             DIC on the same system (--gamg-n N, 0 skips)
-  served    Poisson-arriving requests over recurring meshes (10k-2M cells,
-            70% symmetric CHT with DIC, 30% asymmetric convection-diffusion
-            with DILU, 5% coefficient drift per step) through the
-            continuous-batching server: solves/s, p50/p99 ms, for the mixed
-            form (FP32 PCG / FP32 BiCGStab inner solves), the mixed form
-            with FP32 PBiCG for the asymmetric requests, the plain FP64
-            method, and the plain method one request at a time
-            (--served-meshes/--served-steps/--served-rate, 0 meshes skips)
+  served    Poisson-arriving requests over recurring meshes (100 meshes of
+            10k-2M cells, 70% symmetric CHT with DIC, 30% asymmetric
+            convection-diffusion with DILU, 20 time steps each with 5%
+            coefficient drift per step: 2000 requests) through the
+            continuous-batching server under a 150 GB HBM budget, for each
+            arrival rate of the sweep (default 50, 100, 200, 500, 1000,
+            2000 /s): solves/s, p50/p99 ms, for the mixed form and the plain
+            FP64 method; the plain drop-in one request at a time beside
+            (--served-meshes / --served-steps / --served-rates, 0 meshes
+            skips)
+  cpu_baseline  the CPU oracle (foam's algorithm in C, FP64 PCG + DIC) on
+            the same headline system, full solves to 1e-8 timed: one core
+            alone, and every core at once (one solve per process)
 
 --impl reference times the reference algorithm's CPU implementation (the
-project's C oracle; foam-extend itself cannot be built here) on bounded
-samples of the same solve.
+project's C oracle; foam-extend itself cannot be built here): full solves
+of the same system on every host core.
 """
 from __future__ import annotations
 
@@ -61,6 +71,9 @@ sys.path.insert(0, ROOT)
 
 TOL = 1e-8
 SEED = 0
+C3_SEED = 2
+REF_TOL = 1e-13          # FP64 oracle solution of a single system
+REF_TOL_MANY = 1e-12     # ... of the batched / served / block members
 
 
 def peaks():
@@ -153,63 +166,141 @@ def make_system(rank, scale):
     return cases.c2(form="global", seed=SEED + rank, scale=scale)
 
 
-_CPU = {}
+def rel_err(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-def _cpu_init(scale, seed):
-    """Pool worker: build the workload and the oracle matrix once."""
-    sys.path.insert(0, ROOT)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+def err_stats(errs):
+    errs = [e for e in errs if e is not None]
+    if not errs:
+        return None
+    return {"max": float(np.max(errs)), "p99": float(np.percentile(errs, 99)), "n": len(errs)}
+
+
+# ------------------------------------------------------------------ CPU leg
+# The CPU oracle (foam's algorithm restated in C; test infrastructure) runs
+# only here: as the timed CPU baseline and as the checker that gives every
+# GPU result its error against an FP64 solution.  Worker processes are
+# spawned (never forked after CUDA initialised) and rebuild their systems
+# from the seeds.
+
+_W = {}
+
+
+def _w_setup():
+    for p in (ROOT, os.path.join(ROOT, "oracle")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
     import oracle as O
+    return O
+
+
+def _w_matrix(s):
+    O = _w_setup()
+    return O.OracleMatrix(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.iface)
+
+
+def _w_c2(scale):
+    if ("c2", scale) not in _W:
+        from multiregionfoam_gb300 import cases
+        _w_setup()
+        s = cases.c2(form="global", seed=SEED, scale=scale)
+        _W[("c2", scale)] = (s, _w_matrix(s))
+    return _W[("c2", scale)]
+
+
+def _w_c2_solves(arg):
+    """`count` full foam-order PCG + DIC solves of the headline system to
+    1e-8 in this process; returns the per-solve seconds and iterations."""
+    scale, count = arg
+    s, A = _w_c2(scale)
+    out = []
+    for _ in range(count):
+        t = time.perf_counter()
+        _, p = A.solve(s.b, s.x0, "PCG", "DIC", tol=TOL, max_iter=20000)
+        out.append((time.perf_counter() - t, p["n_iter"], bool(p["converged"])))
+    return out
+
+
+def _w_reference(job):
+    """The FP64 oracle solution of one system, rebuilt from its description."""
     from multiregionfoam_gb300 import cases
-    s = cases.c2(form="global", seed=seed, scale=scale)
-    _CPU["s"] = s
-    _CPU["A"] = O.OracleMatrix(s.n, s.lower, s.upper, s.diag, s.upper_c, None, None)
+    O = _w_setup()
+    kind = job[0]
+    if kind == "c2":
+        s = cases.c2(form="global", seed=SEED, scale=job[1])
+        solver, pc, tol = "PCG", "DIC", REF_TOL
+    elif kind == "c3":
+        def weights(fa, fb):
+            return O.ggi_weights(*fa, *fb)
+        s = cases.c3(weights, scale=job[1], seed=C3_SEED)[0]
+        solver, pc, tol = "PBiCG", "DILU", REF_TOL
+    elif kind == "c4":
+        _, count, idx = job
+        nx, ny, nzf, nzs = cases.batch_shapes(count, seed=SEED)[idx]
+        s = cases.cht_system(nx, ny, nzf, nzs, seed=SEED + 1 + idx, k_range=(0.1, 50.0))
+        solver, pc, tol = "PCG", "DIC", REF_TOL_MANY
+    elif kind == "c5":
+        _, count, mesh, step = job
+        spec = cases.c5_specs(count, seed=SEED)[mesh]
+        s = cases.c5_step(cases.c5_mesh(spec), mesh, step, SEED)
+        solver, pc, tol = ("PBiCG", "DILU", REF_TOL_MANY) if spec[0] else ("PCG", "DIC", REF_TOL_MANY)
+    elif kind == "block":
+        import block_oracle as BO
+        c = cases.block_case(job[1], job[1], job[1], bs=4, seed=SEED)
+        lo, up, d, uc, lc = BO.expand(c["n"], c["lower"], c["upper"], 4, c["D"], c["U"], c["L"])
+        n_s = 4 * c["n"]
+        s = cases.LduSystem(n_s, lo, up, d, uc, lc, c["b"].ravel(), np.zeros(n_s), None)
+        solver, pc, tol = "BiCGStab", "DILU", REF_TOL_MANY
+    else:
+        raise ValueError(kind)
+    x, p = _w_matrix(s).solve(s.b, s.x0, solver, pc, tol=tol, max_iter=40000)
+    return job, x, p
 
 
-def _cpu_sample(sample_iters):
-    """Time the oracle's PCG+DIC with 1 and with 1+sample_iters iterations."""
-    s, A = _CPU["s"], _CPU["A"]
-    t = time.perf_counter()
-    A.solve(s.b, s.x0, "PCG", "DIC", tol=0.0, max_iter=1)
-    a = time.perf_counter() - t
-    t = time.perf_counter()
-    A.solve(s.b, s.x0, "PCG", "DIC", tol=0.0, max_iter=1 + sample_iters)
-    return a, time.perf_counter() - t
+class CpuLeg:
+    """A spawned pool of oracle workers on the host cores."""
 
-
-class CpuBaseline:
-    """The oracle's FP64 PCG+DIC (foam's algorithm, one solve per process) on
-    every host core at once: each process solves its own copy of the full
-    system, the way independent foam solves would share the host.  A step
-    times 1 and 1+sample iterations in every process and extrapolates each
-    process's solve time to the iteration count the solve needs; the
-    throughput is the sum over processes.  Processes are spawned, so this is
-    safe after CUDA is initialised."""
-
-    def __init__(self, scale, procs=None):
+    def __init__(self, procs=None):
         import multiprocessing as mp
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle as O
+        O = _w_setup()
         O.build()
-        self.procs = procs or len(os.sched_getaffinity(0))
-        self.pool = mp.get_context("spawn").Pool(self.procs, initializer=_cpu_init, initargs=(scale, SEED))
-        self.pool.map(_cpu_sample, [1] * self.procs)   # all workers ready
+        self.cores = len(os.sched_getaffinity(0))
+        self.procs = procs or self.cores
+        self.pool = mp.get_context("spawn").Pool(self.procs)
 
-    def step(self, iters_full, sample_iters):
-        res = self.pool.map(_cpu_sample, [sample_iters] * self.procs)
-        rate = 0.0
-        solve_s = []
-        for a, b in res:
-            per_iter = (b - a) / sample_iters
-            t = max(a - per_iter, 0.0) + iters_full * per_iter
-            solve_s.append(t)
-            rate += 1.0 / t
-        return rate, float(np.median(solve_s))
+    def c2_solves(self, scale, counts):
+        """One task per process with its solve count, all started together;
+        returns the per-process lists of (seconds, iterations, converged)."""
+        return self.pool.map(_w_c2_solves, [(scale, k) for k in counts], chunksize=1)
+
+    def references(self, jobs):
+        """FP64 oracle solutions {job: (x, perf)}, largest systems first."""
+        out = {}
+        for job, x, p in self.pool.imap_unordered(_w_reference, jobs):
+            out[job] = (x, p)
+        return out
 
     def close(self):
         self.pool.terminate()
         self.pool.join()
+
+
+def cpu_baseline(scale, leg):
+    """Measured full solves of the headline system: one core alone, then
+    every core at once (one full solve per process)."""
+    leg.c2_solves(scale, [0] * leg.procs)                       # every worker builds the system
+    one = leg.c2_solves(scale, [1])[0][0]
+    allc = leg.c2_solves(scale, [1] * leg.procs)
+    t_all = [r[0][0] for r in allc]
+    rate_all = float(sum(1.0 / t for t in t_all))
+    return {"value": rate_all, "unit": "solves/s", "cores": leg.procs, "kind": "port",
+            "sample": (f"oracle PCG+DIC FP64 (foam order), full solves to {TOL:g} ({one[1]} iterations) measured: "
+                       f"{leg.procs} processes one solve each at once, median {np.median(t_all):.1f} s; throughput "
+                       f"= sum of per-process rates"),
+            "single_core": {"value": 1.0 / one[0], "unit": "solves/s", "cores": 1, "solve_s": one[0],
+                            "iters": one[1]},
+            "all_cores_median_solve_s": float(np.median(t_all))}
 
 
 def run_reference(args):
@@ -217,27 +308,98 @@ def run_reference(args):
     if rank != 0:
         return
     s = make_system(0, args.scale)
-    iters_full = args.ref_iters
-    cpu = CpuBaseline(args.scale)
-    vals = []
-    for k in range(args.warmup + args.steps):
-        rate, solve_s = cpu.step(iters_full, args.ref_sample)
-        if k >= args.warmup:
-            vals.append(rate)
-    cpu.close()
-    v = float(np.median(vals))
-    sample = (f"oracle PCG+DIC FP64, one full {s.n}-cell system per process on {cpu.procs} processes: 1 and "
-              f"1+{args.ref_sample} iterations timed per step, extrapolated to {iters_full} iterations (the "
-              f"plain method's count at 1e-8, {solve_s:.1f} s per solve)")
-    line = {"metric": "coupled solves/s at 1e-8 rel. residual", "value": v, "unit": "solves/s",
+    leg = CpuLeg(min(args.steps, len(os.sched_getaffinity(0))))
+    P = leg.procs
+    leg.c2_solves(args.scale, [0] * P)                       # every worker builds the system (untimed)
+    # warm-up: W full solves spread over the workers (untimed)
+    leg.c2_solves(args.scale, [args.warmup // P + (1 if i < args.warmup % P else 0) for i in range(P)])
+    # timed: K full solves spread over the workers, all started together;
+    # throughput = sum over workers of solves / that worker's busy time
+    counts = [args.steps // P + (1 if i < args.steps % P else 0) for i in range(P)]
+    t0 = time.perf_counter()
+    res = leg.c2_solves(args.scale, counts)
+    wall = time.perf_counter() - t0
+    leg.close()
+    solves = [r for rr in res for r in rr]
+    rate = float(sum(len(rr) / sum(t for t, _, _ in rr) for rr in res if rr))
+    med = float(np.median([t for t, _, _ in solves]))
+    iters = int(solves[0][1])
+    sample = (f"oracle PCG+DIC FP64 (foam order), {len(solves)} full solves to {TOL:g} ({iters} iterations each) on "
+              f"{P} processes at once, median {med:.1f} s per solve, wall {wall:.1f} s; throughput = sum of "
+              f"per-process rates")
+    line = {"metric": "coupled solves/s at 1e-8 rel. residual", "value": rate, "unit": "solves/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": med * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded C2 system)",
             "config": {"workload": "cht-2region-128^3+128x128x64", "n_cells": s.n, "n_faces": s.nf,
                        "tolerance": TOL},
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cpu.procs, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": rate, "unit": "solves/s", "cores": P, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU forms
+def run_c3(args, ctx, mrgpu):
+    """The asymmetric, non-conformal configuration: GGI weights built on
+    the device (mrg_ggi_build); per form one warm solve and `reps` timed
+    steps (coefficient upload + factor + solve, device resident); the GGI
+    gather of a random face field U(-1, 1) in both directions."""
+    from multiregionfoam_gb300 import cases
+
+    def weights(fa, fb):
+        ga, gb = mrgpu.Ggi.build(ctx, *fa, *fb)
+        out = (ga.csr(), gb.csr())
+        ga.close()
+        gb.close()
+        return out
+
+    s, ggi = cases.c3(weights, scale=args.c3_scale, seed=C3_SEED)
+    f = s.iface
+    m = mrgpu.Mesh(ctx, s.n, s.lower, s.upper, f)
+    d_d, d_u, d_l = ctx.to_device(s.diag), ctx.to_device(s.upper_c), ctx.to_device(s.lower_c)
+    d_ib = ctx.to_device(f["bou"])
+    d_b, d_x0 = ctx.to_device(s.b), ctx.to_device(s.x0)
+    d_x = ctx.dev_alloc(8 * s.n)
+    out = {"cells": s.n, "faces": s.nf, "iface_faces": [int(ggi["n_a"]), int(ggi["n_b"])], "tolerance": TOL,
+           "seed": C3_SEED}
+    xs = {}
+    forms = (("plain_fp64", "PBiCG", "fp64", "exact"), ("mixed", "BiCGStab", "mixed", "colour"),
+             ("mixed_pbicg_inner", "PBiCG", "mixed", "colour"))
+    for name, solver, prec, order in forms:
+        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver=solver, precond="DILU", precision=prec,
+                             ordering=order, inner_rel_tol=args.inner_tol)
+        ms, perf = [], None
+        for rep in range(1 + args.c3_reps):
+            m.upload_device(d_d, d_u, d_l, d_ib)
+            ctx.copy_d2d(d_x, d_x0, 8 * s.n)
+            ctx.record(64)
+            perf = m.solve_device(d_b, d_x, ctl)
+            ctx.record(65)
+            if rep:
+                ms.append(ctx.elapsed_ms(64, 65))
+        xs[name] = ctx.from_device(d_x, np.empty(s.n))
+        best = min(ms)
+        out[name] = {"solver": f"{solver}+DILU", "solves_per_s": 1e3 / best, "ms_per_step": best,
+                     "iters": int(perf["n_iter"]), "outer": int(perf.get("n_outer", 0)),
+                     "final_residual": perf["final_residual"], "converged": bool(perf["converged"])}
+    out["speedup_mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    rng = np.random.default_rng(3)
+    gg = {}
+    for key, (ptr, addr, w), n_src in (("a_from_b", ggi["a_from_b"], ggi["n_b"]),
+                                       ("b_from_a", ggi["b_from_a"], ggi["n_a"])):
+        g = mrgpu.Ggi(ctx, ptr, addr, w, n_src)
+        d_src = ctx.to_device(rng.uniform(-1.0, 1.0, n_src))
+        d_dst = ctx.dev_alloc(8 * g.n_dst)
+        gg[key] = {"n_dst": g.n_dst, "n_src": n_src, "nnz": int(len(addr)),
+                   "us_per_gather": 1e3 * g.time_device(d_src, d_dst, 200)}
+        g.close()
+        ctx.dev_free(d_src)
+        ctx.dev_free(d_dst)
+    out["ggi_gather"] = gg
+    for a in (d_d, d_u, d_l, d_ib, d_b, d_x0, d_x):
+        ctx.dev_free(a)
+    m.close()
+    return out, xs
 
 
 def run_batched(args, ctx, mrgpu):
@@ -257,6 +419,7 @@ def run_batched(args, ctx, mrgpu):
     d_x = [ctx.dev_alloc(8 * s.n) for s in systems]
     out = {"systems": len(systems), "cells": int(sum(s.n for s in systems)),
            "faces": int(sum(s.nf for s in systems))}
+    xs = {}
     for name, prec, order in (("mixed", "mixed", "colour"), ("plain_fp64", "fp64", "exact")):
         bt = mrgpu.Batch(ctx, meshes, order)
         ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="PCG", precond="DIC", precision=prec, ordering=order,
@@ -272,6 +435,7 @@ def run_batched(args, ctx, mrgpu):
             if rep:
                 ms.append(ctx.elapsed_ms(50, 51))
         bt.close()
+        xs[name] = [ctx.from_device(a, np.empty(sy.n)) for sy, a in zip(systems, d_x)]
         its = [p["n_iter"] for p in perfs]
         best = min(ms)
         out[name] = {"solves_per_s": len(systems) / (best * 1e-3), "ms_per_batch": best,
@@ -282,7 +446,7 @@ def run_batched(args, ctx, mrgpu):
         ctx.dev_free(a)
     for m in meshes:
         m.close()
-    return out
+    return out, xs
 
 
 def run_block(args, ctx, mrgpu):
@@ -303,6 +467,7 @@ def run_block(args, ctx, mrgpu):
     d_x = ctx.dev_alloc(8 * n_s)
     out = {"block_cells": c["n"], "block_size": 4, "scalar_cells": n_s, "scalar_faces": int(len(lo)),
            "expand_ms": t_expand * 1e3, "solver": "BiCGStab+DILU", "tolerance": TOL}
+    xs = {}
     for name, prec, order in (("mixed", "mixed", "colour"), ("plain_fp64", "fp64", "exact")):
         ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="BiCGStab", precond="DILU", precision=prec,
                              ordering=order, inner_rel_tol=args.inner_tol)
@@ -315,6 +480,7 @@ def run_block(args, ctx, mrgpu):
             ctx.record(61)
             if rep:
                 ms.append(ctx.elapsed_ms(60, 61))
+        xs[name] = ctx.from_device(d_x, np.empty(n_s))
         best = min(ms)
         out[name] = {"solves_per_s": 1e3 / best, "ms_per_step": best, "iters": int(perf["n_iter"]),
                      "final_residual": perf["final_residual"], "converged": bool(perf["converged"])}
@@ -322,7 +488,7 @@ def run_block(args, ctx, mrgpu):
     for a in (d_d, d_u, d_l, d_b, d_x0, d_x):
         ctx.dev_free(a)
     m.close()
-    return out
+    return out, xs
 
 
 def run_gamg(args, ctx, mrgpu):
@@ -363,99 +529,105 @@ def run_gamg(args, ctx, mrgpu):
 
 
 def run_served(args, ctx, mrgpu):
-    """Served configuration: Poisson arrivals at `args.served_rate`/s of
-    solve requests over `args.served_meshes` meshes (cells log-uniform in
+    """Served configuration: `served_meshes` meshes (cells log-uniform in
     [10k, 2M], 70% CHT with DIC, 30% convection-diffusion with DILU), each
-    mesh recurring `args.served_steps` time steps with its coefficients
-    re-drawn at 5% perturbation per step; 150 GB HBM budget.  Servers in
-    turn: mixed (colour; FP32 PCG for the symmetric requests, FP32 BiCGStab
-    for the asymmetric ones -- the unstabilised BiCG recurrence needs two to
-    three times the iterations in FP32), the same with FP32 PBiCG for the
-    asymmetric ones, and the plain FP64 method (exact order; PCG / PBiCG)."""
+    recurring `served_steps` time steps with its coefficients re-drawn at 5%
+    perturbation per step (cases.c5_step), one request per mesh and step,
+    Poisson arrivals at each rate of the sweep; 150 GB HBM budget.  Every
+    form is warmed (plans, views, factors, graphs) before it is timed.  One
+    request per mesh (step i mod steps) keeps its solution for the error
+    against the FP64 oracle."""
     from multiregionfoam_gb300 import cases
-    ms = cases.c5_meshes(args.served_meshes, seed=SEED)
-    rng = np.random.default_rng(SEED + 7)
+    specs = cases.c5_specs(args.served_meshes, seed=SEED)
+    t0 = time.perf_counter()
     meshes, steps = [], []
-    for s, a in ms:
-        meshes.append(mrgpu.Mesh(ctx, s.n, s.lower, s.upper))
-        cur, seq = s, []
-        for k in range(args.served_steps):
-            seq.append(cur)
-            cur = cases.perturb_step(cur, rng)
+    for i, sp in enumerate(specs):
+        cur = cases.c5_mesh(sp)
+        meshes.append(mrgpu.Mesh(ctx, cur.n, cur.lower, cur.upper))
+        seq = [dict(diag=cur.diag, upper=cur.upper_c, lower=cur.lower_c, b=cur.b, x0=cur.x0)]
+        for k in range(1, args.served_steps):
+            cur = cases.perturb_step(cur, np.random.default_rng((SEED, i, k)))
+            seq.append(dict(diag=cur.diag, upper=cur.upper_c, lower=cur.lower_c, b=cur.b, x0=seq[0]["x0"]))
         steps.append(seq)
-    def pinned(a):
-        if a is None:
-            return None
-        h = mrgpu.host_array(None, a.size)
-        h[:] = a
-        return h
-
-    # each request's arrays in pinned host memory, as a caller streaming time
-    # steps would hold them (the server copies them asynchronously)
-    steps = [[dict(diag=pinned(st.diag), upper=pinned(st.upper_c), lower=pinned(st.lower_c), b=pinned(st.b),
-                   x0=pinned(st.x0)) for st in seq] for seq in steps]
-    reqs = [(i, steps[i][k], ms[i][1]) for k in range(args.served_steps) for i in range(len(ms))]
-    arrivals = np.cumsum(np.random.default_rng(SEED + 11).exponential(1.0 / args.served_rate, len(reqs)))
-    out = {"requests": len(reqs), "meshes": len(ms), "rate_per_s": args.served_rate, "iters_per_launch": args.served_k,
-           "cells_mean": float(np.mean([s.n for s, _ in ms])), "asym_meshes": int(sum(a for _, a in ms)),
-           "hbm_budget_gb": 150}
-    forms = (("mixed", "mixed", "colour", "BiCGStab"), ("mixed_pbicg_inner", "mixed", "colour", "PBiCG"),
-             ("plain_fp64", "fp64", "exact", "PBiCG"))
+    t_gen = time.perf_counter() - t0
+    asym = [sp[0] for sp in specs]
+    n_req = len(specs) * args.served_steps
+    sample = {i: i % args.served_steps for i in range(len(specs))}      # mesh -> sampled step
+    rates = [float(r) for r in args.served_rates.split(",") if r.strip()]
+    out = {"requests": n_req, "meshes": len(specs), "steps_per_mesh": args.served_steps, "rates_per_s": rates,
+           "iters_per_launch": args.served_k, "cells_mean": float(np.mean([m.n for m in meshes])),
+           "asym_meshes": int(sum(asym)), "hbm_budget_gb": 150, "generate_s": t_gen}
+    forms = [("mixed", "mixed", "colour", "BiCGStab"), ("plain_fp64", "fp64", "exact", "PBiCG")]
+    if args.served_pbicg_inner:
+        forms.insert(1, ("mixed_pbicg_inner", "mixed", "colour", "PBiCG"))
     out["forms"] = {f[0]: {"precision": f[1], "ordering": f[2], "sym_solver": "PCG+DIC", "asym_solver": f[3] + "+DILU"}
                     for f in forms}
+
     def server(prec, order, asym_solver):
         kw = dict(tol=TOL, max_iter=20000, precision=prec, ordering=order, inner_rel_tol=args.inner_tol,
                   iters_per_launch=args.served_k)
         return mrgpu.Server(ctx, mrgpu.controls(solver="PCG", precond="DIC", **kw),
                             mrgpu.controls(solver=asym_solver, precond="DILU", **kw), hbm_budget=150 * 2**30)
 
-    # untimed warm-up of every form (each mesh's plan, views, factors and
-    # captured graphs for that ordering and precision), so no form is timed
-    # cold
+    order_req = [(i, k) for k in range(args.served_steps) for i in range(len(specs))]
+    xbuf = [np.empty(m.n) for m in meshes]          # a mesh's steps run one after another
+    xs = {}
+    by_rate = {}
     for name, prec, order, asym_solver in forms:
-        srv = server(prec, order, asym_solver)
-        wid = [srv.submit(meshes[i], steps[i][0]["b"], steps[i][0]["x0"], steps[i][0]["diag"], steps[i][0]["upper"],
-                          steps[i][0]["lower"], asym=ms[i][1]) for i in range(len(ms))]
+        srv = server(prec, order, asym_solver)      # warm-up: every mesh once
+        wid = [srv.submit(meshes[i], steps[i][0]["b"], steps[i][0]["x0"], steps[i][0]["diag"],
+                          steps[i][0]["upper"], steps[i][0]["lower"], asym=asym[i], x_out=xbuf[i])
+               for i in range(len(specs))]
         for r in wid:
             srv.wait(r, 600000.0)
         srv.close()
-    for name, prec, order, asym_solver in forms:
-        srv = server(prec, order, asym_solver)
-        ids = []
-        t0 = time.perf_counter()
-        for (i, s, a), ta in zip(reqs, arrivals):
-            dt = ta - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            ids.append(srv.submit(meshes[i], s["b"], s["x0"], s["diag"], s["upper"], s["lower"], asym=a))
-        lat, conv = [], 0
-        for r in ids:
-            x, p, l = srv.wait(r, 600000.0)
-            lat.append(l)
-            conv += p["converged"]
-        wall = time.perf_counter() - t0
-        st = srv.stats()
-        srv.close()
-        out[name] = {"solves_per_s": len(ids) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
-                     "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv),
-                     "peak_running": st["peak_running"], "peak_inflight_gb": st["peak_inflight_bytes"] / 2**30}
-    out["speedup_mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+        for ri, rate in enumerate(rates):
+            arrivals = np.cumsum(np.random.default_rng((SEED, 11, ri)).exponential(1.0 / rate, n_req))
+            keep = ri == len(rates) - 1
+            srv = server(prec, order, asym_solver)
+            ids = []
+            t0 = time.perf_counter()
+            for (i, k), ta in zip(order_req, arrivals):
+                dt = ta - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                st = steps[i][k]
+                xo = np.empty(meshes[i].n) if (keep and sample[i] == k) else xbuf[i]
+                ids.append(srv.submit(meshes[i], st["b"], st["x0"], st["diag"], st["upper"], st["lower"],
+                                      asym=asym[i], x_out=xo))
+            lat, conv = [], 0
+            for (i, k), r in zip(order_req, ids):
+                x, p, l = srv.wait(r, 600000.0)
+                lat.append(l)
+                conv += p["converged"]
+                if keep and sample[i] == k:
+                    xs[(name, i, k)] = x
+            wall = time.perf_counter() - t0
+            stt = srv.stats()
+            srv.close()
+            by_rate.setdefault(f"{rate:g}", {})[name] = {
+                "solves_per_s": len(ids) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv),
+                "peak_running": stt["peak_running"], "peak_inflight_gb": stt["peak_inflight_bytes"] / 2**30}
+    for r in by_rate.values():
+        r["speedup_mixed_vs_plain"] = r["mixed"]["solves_per_s"] / r["plain_fp64"]["solves_per_s"]
+    out["by_rate"] = by_rate
     # The plain drop-in solver as foam would call it: one request at a time,
     # device-resident, FP64 in foam's order.  Timed on the first time step of
     # every mesh (the request mix's sizes and families) and reported as
     # requests per second of solve time.
     plain_ms = []
-    for i, (s0, a) in enumerate(ms):
+    for i in range(len(specs)):
         st = steps[i][0]
-        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="PBiCG" if a else "PCG",
-                             precond="DILU" if a else "DIC", precision="fp64", ordering="exact")
+        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="PBiCG" if asym[i] else "PCG",
+                             precond="DILU" if asym[i] else "DIC", precision="fp64", ordering="exact")
         meshes[i].upload(st["diag"], st["upper"], st["lower"])
         d_b, d_x = ctx.to_device(st["b"]), ctx.to_device(st["x0"])
         meshes[i].solve_device(d_b, d_x, ctl)          # warm (plan, graphs)
         ctx.dev_free(d_x)
         d_x = ctx.to_device(st["x0"])
         ctx.record(52)
-        p = meshes[i].solve_device(d_b, d_x, ctl)
+        meshes[i].solve_device(d_b, d_x, ctl)
         ctx.record(53)
         plain_ms.append(ctx.elapsed_ms(52, 53))
         ctx.dev_free(d_b)
@@ -463,10 +635,11 @@ def run_served(args, ctx, mrgpu):
     seq_rate = len(plain_ms) / (sum(plain_ms) * 1e-3)
     out["plain_fp64_one_at_a_time"] = {"solves_per_s": seq_rate, "requests_timed": len(plain_ms),
                                        "mean_ms": float(np.mean(plain_ms))}
-    out["speedup_served_mixed_vs_plain_one_at_a_time"] = out["mixed"]["solves_per_s"] / seq_rate
+    top = by_rate[f"{rates[-1]:g}"]
+    out["speedup_served_mixed_vs_plain_one_at_a_time"] = top["mixed"]["solves_per_s"] / seq_rate
     for m in meshes:
         m.close()
-    return out
+    return out, xs
 
 
 def run_gpu(args):
@@ -541,14 +714,7 @@ def run_gpu(args):
         if i >= args.warmup:
             e2e_ms.append(ctx.elapsed_ms(40, 41))
     e2e_tot = max_over_ranks(dist, float(np.sum(e2e_ms)))
-
-    # the FP64 oracle solution: the same system converged far below the
-    # target (FP64, colour-ordered DIC, 1e-13), against which both forms'
-    # results are measured
-    tight = mrgpu.controls(tol=1e-13, max_iter=40000, solver="PCG", precond="DIC", precision="fp64",
-                           ordering="colour")
-    p_tight = step(tight)
-    x_tight = ctx.from_device(d_x, np.empty(n))
+    x_e2e = h_x.copy()
 
     # dominant-kernel roofline: Amul + (q,p) of the FP32 inner loop
     peak, peak_kind = peaks()
@@ -563,32 +729,66 @@ def run_gpu(args):
     ach32 = bytes32 / (ms_spmv32 * 1e-3) / 1e9
     ach64 = bytes64 / (ms_spmv64 * 1e-3) / 1e9
     traffic = profile_traffic("spmv_fp32_c2.txt")
+    mesh.close()
+    for a in (d_diag, d_up, d_b, d_x0, d_x):
+        ctx.dev_free(a)
 
-    batched = run_batched(args, ctx, mrgpu) if args.batched > 0 else None
-    block = run_block(args, ctx, mrgpu) if args.block_n > 0 else None
+    c3, x_c3 = run_c3(args, ctx, mrgpu) if args.c3_scale > 0 else (None, {})
+    batched, x_c4 = run_batched(args, ctx, mrgpu) if args.batched > 0 else (None, {})
+    block, x_block = run_block(args, ctx, mrgpu) if args.block_n > 0 else (None, {})
     gamg = run_gamg(args, ctx, mrgpu) if args.gamg_n > 0 else None
-    served = run_served(args, ctx, mrgpu) if args.served_meshes > 0 else None
+    served, x_c5 = run_served(args, ctx, mrgpu) if args.served_meshes > 0 else (None, {})
+    ctx.close()
 
     if rank != 0:
         return
     k = args.steps
     value = world * k / (tot_mixed * 1e-3)
     plain_rate = world * k_plain / (tot_plain * 1e-3)
-    err = float(np.abs(x_mixed - x_plain).max() / np.abs(x_plain).max())
-    scale = np.abs(x_tight).max()
-    err_mixed = float(np.abs(x_mixed - x_tight).max() / scale)
-    err_plain = float(np.abs(x_plain - x_tight).max() / scale)
-    cpu = None
+
+    # CPU leg: the measured baseline, then the FP64 oracle solutions every
+    # GPU result is checked against
+    cpu, refs = None, {}
     if world == 1 and not args.no_cpu:
-        base = CpuBaseline(args.scale)
-        rate, solve_s = base.step(perf_plain[-1]["n_iter"], args.ref_sample)
-        base.close()
-        cpu = {"value": rate, "unit": "solves/s", "cores": base.procs, "kind": "port",
-               "sample": f"oracle PCG+DIC FP64, one full system per process on {base.procs} processes, 1 and "
-                         f"1+{args.ref_sample} iterations timed, extrapolated to {perf_plain[-1]['n_iter']} "
-                         f"iterations ({solve_s:.1f} s per solve)"}
-    pm = perf_mixed[-1]
-    pp = perf_plain[-1]
+        leg = CpuLeg()
+        cpu = cpu_baseline(args.scale, leg)
+        jobs = [("c2", args.scale)]
+        if c3 is not None:
+            jobs.append(("c3", args.c3_scale))
+        jobs += [("c5", args.served_meshes, i, st) for (_, i, st) in x_c5 if _ == "mixed"]
+        if block is not None:
+            jobs.append(("block", args.block_n))
+        if batched is not None:
+            jobs += [("c4", args.batched, i) for i in range(args.batched)]
+        t0 = time.perf_counter()
+        refs = leg.references(jobs)
+        leg.close()
+        cpu["references_s"] = time.perf_counter() - t0
+
+    def err(key, x):
+        return rel_err(x, refs[key][0]) if key in refs else None
+
+    pm, pp = perf_mixed[-1], perf_plain[-1]
+    rc2 = refs.get(("c2", args.scale))
+    if c3 is not None:
+        for f in ("plain_fp64", "mixed", "mixed_pbicg_inner"):
+            c3[f]["err_vs_fp64_oracle"] = err(("c3", args.c3_scale), x_c3[f])
+        if ("c3", args.c3_scale) in refs:
+            p3 = refs[("c3", args.c3_scale)][1]
+            c3["fp64_oracle"] = {"kind": "CPU oracle, foam order", "tolerance": REF_TOL, "iters": p3["n_iter"]}
+    if batched is not None:
+        for f in ("mixed", "plain_fp64"):
+            batched[f]["err_vs_fp64_oracle"] = err_stats(
+                [err(("c4", args.batched, i), x) for i, x in enumerate(x_c4[f])])
+    if block is not None:
+        for f in ("mixed", "plain_fp64"):
+            block[f]["err_vs_fp64_oracle"] = err(("block", args.block_n), x_block[f])
+    if served is not None:
+        served["err_vs_fp64_oracle"] = {
+            "sample": "one request per mesh (time step mesh % steps) of the last rate's runs",
+            **{f: err_stats([err(("c5", args.served_meshes, i, st), x) for (ff, i, st), x in x_c5.items() if ff == f])
+               for f in ("mixed", "plain_fp64")}}
+
     line = {
         "metric": "coupled solves/s at 1e-8 rel. residual", "value": value, "unit": "solves/s",
         "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": tot_mixed / k,
@@ -599,13 +799,15 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (~1 GB working set)", "parallelism": f"replicas x{world}"},
         "p50_ms": float(np.percentile(per_mixed, 50)), "p99_ms": float(np.percentile(per_mixed, 99)),
         "mixed": {"iters": pm["n_iter"], "outer": pm["n_outer"], "final_residual": pm["final_residual"],
-                  "converged": pm["converged"], "rel_err_vs_fp64": err,
-                  "err_vs_fp64_oracle": err_mixed},
-        "fp64_oracle": {"tolerance": 1e-13, "iters": p_tight["n_iter"], "final_residual": p_tight["final_residual"],
-                        "note": "max-norm errors relative to this FP64 solution"},
+                  "converged": pm["converged"], "rel_err_vs_plain": rel_err(x_mixed, x_plain),
+                  "err_vs_fp64_oracle": err(("c2", args.scale), x_mixed),
+                  "e2e_err_vs_fp64_oracle": err(("c2", args.scale), x_e2e)},
+        "fp64_oracle": None if rc2 is None else {
+            "kind": "CPU oracle (foam order, C)", "tolerance": REF_TOL, "iters": rc2[1]["n_iter"],
+            "final_residual": rc2[1]["final_residual"], "note": "max-norm errors relative to this FP64 solution"},
         "plain_fp64": {"value": plain_rate, "unit": "solves/s", "ms_per_step": tot_plain / k_plain,
                        "iters": pp["n_iter"], "final_residual": pp["final_residual"],
-                       "err_vs_fp64_oracle": err_plain,
+                       "err_vs_fp64_oracle": err(("c2", args.scale), x_plain),
                        "p50_ms": float(np.percentile(per_plain, 50)), "p99_ms": float(np.percentile(per_plain, 99)),
                        "steps": k_plain},
         "speedup_mixed_vs_plain": value / plain_rate,
@@ -618,6 +820,7 @@ def run_gpu(args):
         "kernels": {"spmv_fp64": {"ms": ms_spmv64, "GB/s": ach64, "frac": ach64 / peak},
                     "precondition_fp32_colour_ms": ms_prec32, "precondition_fp64_exact_ms": ms_prec64},
         "tuning": tuning,
+        "c3": c3,
         "batched": batched,
         "block": block,
         "gamg": gamg,
@@ -638,31 +841,28 @@ def main():
     ap.add_argument("--scale", type=int, default=1, help="divide the mesh dimensions (testing only)")
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--inner-tol", type=float, default=1e-5)
-    ap.add_argument("--ref-sample", type=int, default=40)
-    ap.add_argument("--ref-iters", type=int, default=0, help="reference arm: iterations per solve (0 = measured)")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the oracle errors")
+    ap.add_argument("--c3-scale", type=int, default=1, help="asymmetric GGI configuration: 96/scale (0: skip)")
+    ap.add_argument("--c3-reps", type=int, default=3)
     ap.add_argument("--batched", type=int, default=512, help="systems of the batched configuration (0: skip)")
     ap.add_argument("--batched-reps", type=int, default=2)
     ap.add_argument("--block-n", type=int, default=48, help="4x4 block configuration: n^3 cells (0: skip)")
     ap.add_argument("--gamg-n", type=int, default=64, help="GAMG configuration: n^3 cells (0: skip)")
-    ap.add_argument("--served-meshes", type=int, default=24, help="meshes of the served configuration (0: skip)")
-    ap.add_argument("--served-steps", type=int, default=8)
-    ap.add_argument("--served-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--served-meshes", type=int, default=100, help="meshes of the served configuration (0: skip)")
+    ap.add_argument("--served-steps", type=int, default=20)
+    ap.add_argument("--served-rates", default="50,100,200,500,1000,2000",
+                    help="Poisson arrival rates of the sweep, requests/s")
     ap.add_argument("--served-k", type=int, default=8, help="server: Krylov iterations per launch")
+    ap.add_argument("--served-pbicg-inner", action="store_true",
+                    help="also serve with FP32 PBiCG (not BiCGStab) for the asymmetric requests")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
-        if args.ref_iters <= 0:
-            args.ref_iters = REF_ITERS
         run_reference(args)
     else:
         run_gpu(args)
 
-
-# Iterations the plain FP64 PCG+DIC needs on this workload at 1e-8 (identical
-# on CPU and GPU by parity); measured on GB300 and used by the reference arm.
-REF_ITERS = 320
 
 if __name__ == "__main__":
     main()

@@ -175,6 +175,20 @@ int mrg_ctx_destroy(mrg_ctx* ctx);
 /* Bytes currently allocated against the budget. */
 int mrg_ctx_mem_used(mrg_ctx* ctx, size_t* bytes);
 
+/* Device-wait watchdog of the context's solves (no counterpart in the
+ * reference, whose CPU solver never waits on another thread).  Every wait of
+ * a kernel on a value another CTA of the same launch publishes -- the
+ * exact-order sweeps' and the factor's dependencies, the persistent
+ * iteration kernel's grid barrier, the SpMV's bulk-copy stages -- gives up
+ * after wait_cycles SM cycles (0 = the default, 4e9, about 2 s): the kernel
+ * sets an error bit and returns, and the solve returns MRG_E_TIMEOUT with
+ * the context usable for the next call.  unpublished_chunk >= 0 is a test
+ * hook that makes such a wait run out on purpose: the exact-order forward
+ * sweep then leaves that chunk of 32 rows (in the plan's level order) of
+ * every member unpublished, so the rows that depend on it wait until the
+ * budget is spent (-1 = off).  Both apply from the next solve on. */
+int mrg_ctx_set_watchdog(mrg_ctx* ctx, long long wait_cycles, int unpublished_chunk);
+
 /* Pinned host memory (for callers that want asynchronous copies). */
 int mrg_host_alloc(size_t bytes, void** out);
 int mrg_host_free(void* p);
@@ -249,6 +263,11 @@ int mrg_ggi_destroy(mrg_ggi* ggi);
 int mrg_ggi_apply(mrg_ggi* ggi, const double* src, double* dst, int ncomp);
 int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst,
                          int ncomp);
+/* Measurement hook (no counterpart in the reference): `reps` back-to-back
+ * gathers of device arrays on the context's stream, timed with CUDA events;
+ * the mean ms per gather in *ms_per_apply. */
+int mrg_ggi_time(mrg_ggi* ggi, const double* d_src, double* d_dst, int ncomp,
+                 int reps, float* ms_per_apply);
 /* GGIInterpolation's weight construction (the interpolator
  * ggiInterfaceToInterfaceMapping.C:62-77 builds with rescale on and SMALL
  * non-overlap tolerances, rebuilt every interpolatorUpdateFrequency steps of
@@ -528,16 +547,21 @@ int mrg_block_coeffs(int n_cells, int n_faces, const int32_t* lower_addr,
  * be NULL).  It allocates nothing: its reduction scratch is a fixed
  * 393,472-byte device array inside the library, held on every GPU that
  * loads it until the process exits, so n_cells is limited to 16,777,216
- * (larger: MRG_E_INVALID).  The first call on a device looks up that array
- * and loads the library's device code there if needed: make it before any
- * stream capture.  Every call shares the array: calls that overlap on the
- * GPU (other host threads, or streams that do not wait for each other)
- * race and give undefined results.  Addressing that points outside its
- * arrays is not read and returns MRG_E_INVALID. */
+ * (larger: MRG_E_INVALID).  Every call looks up that array's address in the
+ * current context (so a device reset or another current context between
+ * calls is handled); the first call on a device also loads the library's
+ * device code there: make it before any stream capture.  Every call shares
+ * the array: calls that overlap on the GPU (other host threads, or streams
+ * that do not wait for each other) race and give undefined results.  The
+ * faces must be in foam's upper-triangular order (lowerAddr < upperAddr,
+ * each cell's ownerStartAddr neighbours ascending, its losortAddr faces
+ * ascending), which gives A x foam's Amul summation order; addressing that
+ * breaks the order, or points outside its arrays (not read), returns
+ * MRG_E_INVALID. */
 int mrg_residual_noalloc(int n_cells, int n_faces,
-                         const int* d_lower_addr, const int* d_upper_addr,
-                         const int* d_owner_start, const int* d_losort,
-                         const int* d_losort_start, const double* d_diag,
+                         const int32_t* d_lower_addr, const int32_t* d_upper_addr,
+                         const int32_t* d_owner_start, const int32_t* d_losort,
+                         const int32_t* d_losort_start, const double* d_diag,
                          const double* d_upper, const double* d_lower,
                          const double* d_b, const double* d_x, void* stream,
                          double* residual, double* norm_factor);

@@ -242,6 +242,15 @@ int mrg_ctx_mem_used(mrg_ctx* ctx, size_t* bytes)
     return MRG_OK;
 }
 
+int mrg_ctx_set_watchdog(mrg_ctx* ctx, long long wait_cycles, int unpublished_chunk)
+{
+    if (!ctx) return fail(MRG_E_INVALID, "ctx is NULL");
+    if (wait_cycles < 0 || unpublished_chunk < -1) return fail(MRG_E_INVALID, "bad watchdog setting");
+    ctx->c.wait_cycles = wait_cycles;
+    ctx->c.unpublished1 = unpublished_chunk + 1;
+    return MRG_OK;
+}
+
 int mrg_host_alloc(size_t bytes, void** out)
 {
     return guard([&] {
@@ -481,6 +490,31 @@ int mrg_ggi_apply_device(mrg_ggi* ggi, const double* d_src, double* d_dst, int n
         launch_ggi(g.n_dst, g.ptr, g.addr, g.w, d_src, d_dst, ncomp, g.ctx->st);
         MRG_CUDA(cudaGetLastError());
         MRG_CUDA(cudaStreamSynchronize(g.ctx->st));
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_ggi_time(mrg_ggi* ggi, const double* d_src, double* d_dst, int ncomp, int reps, float* ms_per_apply)
+{
+    return guard([&] {
+        if (!ggi || !d_src || !d_dst || ncomp < 1 || ncomp > 16 || reps < 1 || !ms_per_apply)
+            return fail(MRG_E_INVALID, "bad argument");
+        Ggi& g = ggi->g;
+        cudaStream_t st = g.ctx->st;
+        launch_ggi(g.n_dst, g.ptr, g.addr, g.w, d_src, d_dst, ncomp, st);   // warm-up
+        cudaEvent_t e0, e1;
+        MRG_CUDA(cudaEventCreate(&e0));
+        MRG_CUDA(cudaEventCreate(&e1));
+        MRG_CUDA(cudaEventRecord(e0, st));
+        for (int i = 0; i < reps; ++i) launch_ggi(g.n_dst, g.ptr, g.addr, g.w, d_src, d_dst, ncomp, st);
+        MRG_CUDA(cudaEventRecord(e1, st));
+        MRG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        MRG_CUDA(cudaGetLastError());
+        *ms_per_apply = ms / (float)reps;
         return (int)MRG_OK;
     });
 }
@@ -1043,8 +1077,8 @@ int mrg_server_get_stats(mrg_server* server, mrg_server_stats* out)
     });
 }
 
-int mrg_residual_noalloc(int n_cells, int n_faces, const int* d_lower_addr, const int* d_upper_addr,
-                         const int* d_owner_start, const int* d_losort, const int* d_losort_start,
+int mrg_residual_noalloc(int n_cells, int n_faces, const int32_t* d_lower_addr, const int32_t* d_upper_addr,
+                         const int32_t* d_owner_start, const int32_t* d_losort, const int32_t* d_losort_start,
                          const double* d_diag, const double* d_upper, const double* d_lower, const double* d_b,
                          const double* d_x, void* stream, double* residual, double* norm_factor)
 {

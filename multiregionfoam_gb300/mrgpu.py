@@ -23,10 +23,11 @@ ORDERINGS = {"exact": 0, "colour": 1}
 
 EXPORTED = [
     "mrg_last_error", "mrg_version", "mrg_controls_default", "mrg_ctx_create", "mrg_ctx_destroy",
+    "mrg_ctx_set_watchdog",
     "mrg_ctx_mem_used", "mrg_host_alloc", "mrg_host_free", "mrg_mesh_upload", "mrg_mesh_destroy",
     "mrg_mesh_levels", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
     "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
-    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_ggi_build", "mrg_ggi_get", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
+    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_ggi_time", "mrg_ggi_build", "mrg_ggi_get", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
     "mrg_residual_noalloc", "mrg_server_create", "mrg_server_destroy", "mrg_server_submit", "mrg_server_poll",
@@ -119,6 +120,7 @@ def load(path: str = LIB_PATH):
     L.mrg_ctx_create.argtypes = [C.c_int, C.c_size_t, C.POINTER(vp)]
     L.mrg_ctx_destroy.argtypes = [vp]
     L.mrg_ctx_mem_used.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.mrg_ctx_set_watchdog.argtypes = [vp, C.c_longlong, C.c_int]
     L.mrg_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
     L.mrg_host_free.argtypes = [vp]
     L.mrg_mesh_upload.argtypes = [vp, C.c_int, C.c_int, ip, ip, C.c_int, C.POINTER(IfaceDesc), C.POINTER(vp)]
@@ -136,6 +138,7 @@ def load(path: str = LIB_PATH):
     L.mrg_ggi_destroy.argtypes = [vp]
     L.mrg_ggi_apply.argtypes = [vp, dp, dp, C.c_int]
     L.mrg_ggi_apply_device.argtypes = [vp, vp, vp, C.c_int]
+    L.mrg_ggi_time.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.mrg_ggi_build.argtypes = [vp, C.c_int, ip, dp, C.c_int, ip, dp, C.c_double, C.POINTER(vp), C.POINTER(vp)]
     ipp = C.POINTER(C.c_int)
     L.mrg_ggi_get.argtypes = [vp, ipp, ipp, ipp, ip, ip, dp]
@@ -226,6 +229,12 @@ class Context:
         return v.value
 
     # -- resident buffers and device timing (no foam counterpart) ----------
+    def set_watchdog(self, wait_cycles: int = 0, unpublished_chunk: int = -1):
+        """Budget of every device wait in SM cycles (0: the default, ~2 s) and
+        the test hook that leaves one chunk of the exact forward sweep
+        unpublished (-1: off); see mrg_ctx_set_watchdog."""
+        _check(load().mrg_ctx_set_watchdog(self.h, int(wait_cycles), int(unpublished_chunk)))
+
     def dev_alloc(self, nbytes: int) -> int:
         p = C.c_void_p()
         _check(load().mrg_dev_alloc(self.h, nbytes, C.byref(p)))
@@ -492,6 +501,16 @@ class Ggi:
         dst = np.empty(self.n_dst * ncomp)
         _check(load().mrg_ggi_apply(self.h, _d(src), _d(dst), int(ncomp)))
         return dst if ncomp == 1 else dst.reshape(self.n_dst, ncomp)
+
+    def apply_device(self, d_src: int, d_dst: int, ncomp=1):
+        _check(load().mrg_ggi_apply_device(self.h, C.c_void_p(d_src), C.c_void_p(d_dst), int(ncomp)))
+
+    def time_device(self, d_src: int, d_dst: int, reps: int, ncomp=1) -> float:
+        """Mean ms per gather over `reps` back-to-back gathers (CUDA events)."""
+        v = C.c_float()
+        _check(load().mrg_ggi_time(self.h, C.c_void_p(d_src), C.c_void_p(d_dst), int(ncomp), int(reps),
+                                   C.byref(v)))
+        return float(v.value)
 
     def close(self):
         if self.h:

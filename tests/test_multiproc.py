@@ -51,7 +51,7 @@ def test_reference_arm_under_torchrun():
     port = free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "3", "--scale", "16", "--ref-sample", "2", "--ref-iters", "4"]
+           "--gpus", "2", "--steps", "1", "--warmup", "3", "--scale", "16"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]

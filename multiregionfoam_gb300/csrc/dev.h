@@ -111,7 +111,11 @@ struct Ctl {
     unsigned n_oactive;    // systems still in their mixed-precision outer loop
     unsigned bar_count;    // persistent iteration kernel: CTAs at the grid barrier
     unsigned bar_gen;      // persistent iteration kernel: barrier generation
-    unsigned pad[3];
+    int unpublished1;      // test hook: chunk unpublished1 - 1 of the exact forward
+                           // sweep is never published, so every wait on it runs
+                           // out (0: off, which a cleared block is)
+    unsigned pad[2];
+    long long wait_cycles; // budget of every device wait, SM cycles (0: the default)
     // controls written into every system's Scal by OP_BEGIN
     double tol, rel_tol, inner_rel_tol;
     int min_iter, max_iter, inner_max, max_outer, mixed, n_sweeps;

@@ -31,6 +31,10 @@ struct Ctx {
     cudaEvent_t events[64] = {};
     double* stage[3] = {nullptr, nullptr, nullptr};  // host-pointer entry points
     size_t stage_cap = 0;
+    // device-wait watchdog of the solves (mrg_ctx_set_watchdog): budget in SM
+    // cycles (0: the kernels' default) and the test hook's chunk + 1 (0: off)
+    long long wait_cycles = 0;
+    int unpublished1 = 0;
     void* alloc(size_t bytes);
     void release(void* p);
     ~Ctx();

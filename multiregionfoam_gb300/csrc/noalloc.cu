@@ -24,20 +24,22 @@
 // (every per-tile partial is rewritten before it is read).  Two calls whose
 // work overlaps on the GPU -- from two host threads, or on two streams that
 // do not wait for each other -- race on the array and both results are then
-// undefined.  The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress, with that device current), which also loads this
-// library's device code there if it is not loaded yet; make that first call
-// before any stream capture on that device.
+// undefined.  Every call looks up the array's device address in the current
+// context (cudaGetSymbolAddress); the first call on a device also loads this
+// library's device code there if it is not loaded yet, so make that first
+// call before any stream capture on that device.
 //
 // The sums run in a fixed order (four rows per thread, a fixed block tree,
 // tile partials summed in tile order), so the result does not depend on the
 // device or on other work; per row, A x is accumulated as foam's
 // lduMatrix::Amul orders it (lduMatrixATmul.C: diagonal, then faces in
 // ascending face order -- for an upper-triangular face order the faces of
-// losortAddr come before those of ownerStartAddr).
+// losortAddr come before those of ownerStartAddr).  The kernel checks that
+// order as it reads the addressing (each cell's losortAddr faces ascending
+// with owners below the cell, its ownerStartAddr neighbours above it and
+// ascending) and rejects a matrix that breaks it with MRG_E_INVALID.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/mrgpu.h"
@@ -57,7 +59,8 @@ constexpr int kNaHeadBytes = 256;
 // First 256 bytes of the scratch.
 struct NaHead {
     unsigned done[2];      // CTAs finished: pass 1 (sum x), pass 2 (residual)
-    unsigned err;          // 1: the addressing points outside its arrays
+    unsigned err;          // 1: the addressing points outside its arrays;
+                           // 2: faces not in upper-triangular order
     unsigned pad;
     double xsum;           // pass 1 result
     double norm_factor;    // pass 2 results
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(kNaBlock) k_na_residual(NaArgs a, double* part
     const double xbar = __ldcg(&head->xsum) / (double)a.n;
     const unsigned nf = (unsigned)a.nf, n = (unsigned)a.n;
     double v[2] = {0.0, 0.0};   // norm factor, sum |b - A x|
-    bool bad = false;
+    bool bad = false, disorder = false;
 #pragma unroll 1
     for (int k = 0; k < kNaRowsPerThread; ++k) {
         const int i = row0 + k * kNaBlock + threadIdx.x;
@@ -161,11 +164,15 @@ __global__ void __launch_bounds__(kNaBlock) k_na_residual(NaArgs a, double* part
             bad = true;
             s1 = s0;
         }
+        int fprev = -1;
         for (int j = s0; j < s1; ++j) {
             const int f = a.losort[j];
             if ((unsigned)f >= nf) { bad = true; continue; }
             const int l = a.lower_addr[f];
             if ((unsigned)l >= n) { bad = true; continue; }
+            // foam's order: a cell's neighbour faces ascending, owner below it
+            disorder |= (f <= fprev) | (l >= i);
+            fprev = f;
             const double c = a.lower[f];
             ax = fma(c, a.x[l], ax);
             sa += c;
@@ -176,9 +183,13 @@ __global__ void __launch_bounds__(kNaBlock) k_na_residual(NaArgs a, double* part
             bad = true;
             o1 = o0;
         }
+        int uprev = i;
         for (int f = o0; f < o1; ++f) {
             const int u = a.upper_addr[f];
             if ((unsigned)u >= n) { bad = true; continue; }
+            // upper-triangular order: an owner's neighbours above it, ascending
+            disorder |= (u <= i) | (u < uprev);
+            uprev = u;
             const double c = a.upper[f];
             ax = fma(c, a.x[u], ax);
             sa += c;
@@ -188,6 +199,7 @@ __global__ void __launch_bounds__(kNaBlock) k_na_residual(NaArgs a, double* part
         v[1] += fabs(bi - ax);
     }
     if (bad) atomicOr(&head->err, 1u);
+    if (disorder) atomicOr(&head->err, 2u);
     na_block_sum<2>(v);
     if (na_flush<2>(v, part + kNaMaxTiles, &head->done[1], gridDim.x) && threadIdx.x == 0) {
         const double nfac = v[0] + 1e-20;   // lduMatrix::small_
@@ -196,38 +208,30 @@ __global__ void __launch_bounds__(kNaBlock) k_na_residual(NaArgs a, double* part
     }
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_ptr[kMaxDevices];
-
-// Device address of the scratch on the current device, looked up once per
-// device.  In host code g_noalloc_scratch names a host-side stand-in, not
-// device memory, so it is never dereferenced or passed to a kernel here.
-unsigned char* scratch_on_current_device()
+// Device address of the scratch in the current context.  In host code
+// g_noalloc_scratch names a host-side stand-in, not device memory, so it is
+// never dereferenced or passed to a kernel here.  The address is looked up
+// on every call (cudaGetSymbolAddress allocates nothing and costs far less
+// than the call's own synchronisation): a cached one would be stale after a
+// cudaDeviceReset, or wrong when the caller has made another context of the
+// same device current.  The first lookup on a device also loads this
+// library's device code there.
+unsigned char* scratch_in_current_context()
 {
-    int dev = -1;
-    MRG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices)
-        throw Error(MRG_E_INVALID, "mrg_residual_noalloc: device ordinal " + std::to_string(dev) +
-                                       " is beyond the " + std::to_string(kMaxDevices) + " devices it supports");
-    std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        unsigned char* ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr)
-            throw Error(MRG_E_CUDA, std::string("mrg_residual_noalloc: cudaGetSymbolAddress of its scratch failed: ") +
-                                        cudaGetErrorString(e));
-        g_scratch_ptr[dev] = ptr;
-    }
-    return g_scratch_ptr[dev];
+    unsigned char* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        throw Error(MRG_E_CUDA, std::string("mrg_residual_noalloc: cudaGetSymbolAddress of its scratch failed: ") +
+                                    cudaGetErrorString(e));
+    return ptr;
 }
 
 constexpr int kNoAllocMaxCells = kNaMaxTiles * kNaTileRows;
 
 }  // namespace
 
-void residual_noalloc(int n_cells, int n_faces, const int* lower_addr, const int* upper_addr,
-                      const int* owner_start, const int* losort, const int* losort_start, const double* diag,
+void residual_noalloc(int n_cells, int n_faces, const int32_t* lower_addr, const int32_t* upper_addr,
+                      const int32_t* owner_start, const int32_t* losort, const int32_t* losort_start, const double* diag,
                       const double* upper, const double* lower, const double* b, const double* x, void* stream,
                       double* residual, double* norm_factor)
 {
@@ -254,7 +258,7 @@ void residual_noalloc(int n_cells, int n_faces, const int* lower_addr, const int
     a.b = b;
     a.x = x;
 
-    unsigned char* base = scratch_on_current_device();
+    unsigned char* base = scratch_in_current_context();
     NaHead* head = reinterpret_cast<NaHead*>(base);
     double* part = reinterpret_cast<double*>(base + kNaHeadBytes);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -268,8 +272,11 @@ void residual_noalloc(int n_cells, int n_faces, const int* lower_addr, const int
     NaHead h;
     MRG_CUDA(cudaMemcpyAsync(&h, head, sizeof h, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
-    if (h.err)
+    if (h.err & 1u)
         throw Error(MRG_E_INVALID, "mrg_residual_noalloc: the LDU addressing points outside its arrays");
+    if (h.err & 2u)
+        throw Error(MRG_E_INVALID, "mrg_residual_noalloc: faces are not in upper-triangular order (lowerAddr < "
+                                   "upperAddr, ownerStartAddr neighbours and losortAddr faces ascending)");
     if (residual) *residual = h.residual;
     if (norm_factor) *norm_factor = h.norm_factor;
 }

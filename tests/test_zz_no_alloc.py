@@ -8,11 +8,12 @@ device.  mrg_residual_noalloc serves them from a fixed scratch array inside
 the library.  These tests call it through the C ABI on matrices held in
 device arrays in foam's lduAddressing (lowerAddr, upperAddr, ownerStartAddr,
 losortAddr, losortStartAddr) and check it against mrg_residual, the entry
-point that uploads the matrix into its own device memory, within the same
-1e-12 relative tolerance the other residual tests use -- on two calls in a
-row with different x, then again on the first x, which must repeat the first
-call's result exactly although the scratch keeps the previous call's
-contents.
+point that uploads the matrix into its own device memory, and against the
+CPU oracle's foam-order residual, within the same 1e-12 relative tolerance
+the other residual tests use -- on two calls in a row with different x, then
+again on the first x, which must repeat the first call's result exactly
+although the scratch keeps the previous call's contents.  Free device memory
+is the same before and after those calls: the entry point allocates nothing.
 
 The file is named to be collected last, so that it runs both after every
 other test in one process and, alone, in a fresh one.
@@ -24,7 +25,7 @@ import pytest
 
 from multiregionfoam_gb300 import cases
 
-from conftest import GOLDEN, gpu_mesh
+from conftest import GOLDEN, gpu_mesh, oracle_matrix
 
 pytestmark = pytest.mark.gpu
 
@@ -95,8 +96,16 @@ def _close(a, b):
     return abs(a - b) <= REL * abs(b)
 
 
+def free_device_bytes(mrg):
+    """cudaMemGetInfo's free bytes on the current device (the CUDA runtime
+    libmrgpu is linked against)."""
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert mrg.load().cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
 @pytest.mark.parametrize("name", list(SYSTEMS))
-def test_noalloc_matches_residual(mrg, ctx, name):
+def test_noalloc_matches_residual(mrg, ctx, oracle_mod, name):
     s = SYSTEMS[name]()
     assert s.iface is None
     x1 = s.x0
@@ -104,16 +113,24 @@ def test_noalloc_matches_residual(mrg, ctx, name):
     m = gpu_mesh(mrg, ctx, s)
     want = [m.residual(s.b, x) for x in (x1, x2)]
     m.close()
+    A = oracle_matrix(oracle_mod, s)
+    foam = [(A.residual(s.b, x), A.norm_factor(x, s.b)) for x in (x1, x2)]
     d = DeviceLdu(ctx, s)
     try:
+        d.residual(mrg, x2)                 # warm: device code loaded, scratch holds a previous result
+        free0 = free_device_bytes(mrg)
         got1 = d.residual(mrg, x1)
         got2 = d.residual(mrg, x2)
         again = d.residual(mrg, x1)
+        free1 = free_device_bytes(mrg)
     finally:
         d.close()
-    for (r, nf), (rw, nfw) in zip((got1, got2), want):
+    assert free1 == free0, (free0, free1)
+    for (r, nf), (rw, nfw), (ro, nfo) in zip((got1, got2), want, foam):
         assert _close(nf, nfw), (nf, nfw)
         assert _close(r, rw), (r, rw)
+        assert _close(nf, nfo), (nf, nfo)
+        assert _close(r, ro), (r, ro)
     assert got1 != got2
     assert again == got1
 
@@ -143,5 +160,20 @@ def test_noalloc_rejects_oversize_and_bad_addressing(mrg, ctx):
         ctx.dev_free(good)
         r, nf = d.residual(mrg, s.x0)
         assert np.isfinite(r) and nf > 0
+        # faces out of upper-triangular order (two neighbours of one owner
+        # swapped): the summation order foam's Amul gives is undefined, so
+        # the call is refused; valid addressing works again afterwards
+        upper = np.asarray(s.upper, np.int32).copy()
+        lower = np.asarray(s.lower, np.int32)
+        f = int(np.flatnonzero((lower[:-1] == lower[1:]) & (upper[:-1] < upper[1:]))[0])
+        upper[f], upper[f + 1] = upper[f + 1], upper[f]
+        good = d.p["upper_addr"]
+        d.p["upper_addr"] = ctx.to_device(upper)
+        with pytest.raises(mrg.MrgError) as e:
+            d.residual(mrg, s.x0)
+        assert e.value.code == 1 and "upper-triangular" in str(e.value)
+        ctx.dev_free(d.p["upper_addr"])
+        d.p["upper_addr"] = good
+        assert d.residual(mrg, s.x0) == (r, nf)
     finally:
         d.close()

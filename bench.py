@@ -166,6 +166,14 @@ def make_system(rank, scale):
     return cases.c2(form="global", seed=SEED + rank, scale=scale)
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f} s] {msg}", file=sys.stderr, flush=True)
+
+
 def rel_err(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
@@ -372,11 +380,11 @@ def run_c3(args, ctx, mrgpu):
         for rep in range(1 + args.c3_reps):
             m.upload_device(d_d, d_u, d_l, d_ib)
             ctx.copy_d2d(d_x, d_x0, 8 * s.n)
-            ctx.record(64)
+            ctx.record(48)
             perf = m.solve_device(d_b, d_x, ctl)
-            ctx.record(65)
+            ctx.record(49)
             if rep:
-                ms.append(ctx.elapsed_ms(64, 65))
+                ms.append(ctx.elapsed_ms(48, 49))
         xs[name] = ctx.from_device(d_x, np.empty(s.n))
         best = min(ms)
         out[name] = {"solver": f"{solver}+DILU", "solves_per_s": 1e3 / best, "ms_per_step": best,
@@ -605,6 +613,7 @@ def run_served(args, ctx, mrgpu):
             wall = time.perf_counter() - t0
             stt = srv.stats()
             srv.close()
+            log(f"served {name} rate {rate:g}: {len(ids) / wall:.1f} solves/s, wall {wall:.1f} s")
             by_rate.setdefault(f"{rate:g}", {})[name] = {
                 "solves_per_s": len(ids) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv),
@@ -690,7 +699,7 @@ def run_gpu(args):
     launches = mrgpu.kernel_launches() - l0
     x_mixed = ctx.from_device(d_x, np.empty(n))
     k_plain = max(1, min(args.steps, args.plain_steps))
-    tot_plain, per_plain, perf_plain = timed(plain, k_plain, 20)
+    tot_plain, per_plain, perf_plain = timed(plain, k_plain, 42)
     clk = clocks.stop()
     x_plain = ctx.from_device(d_x, np.empty(n))
     tot_mixed = max_over_ranks(dist, tot_mixed)
@@ -733,11 +742,17 @@ def run_gpu(args):
     for a in (d_diag, d_up, d_b, d_x0, d_x):
         ctx.dev_free(a)
 
+    log("headline done")
     c3, x_c3 = run_c3(args, ctx, mrgpu) if args.c3_scale > 0 else (None, {})
+    log("c3 done")
     batched, x_c4 = run_batched(args, ctx, mrgpu) if args.batched > 0 else (None, {})
+    log("batched done")
     block, x_block = run_block(args, ctx, mrgpu) if args.block_n > 0 else (None, {})
+    log("block done")
     gamg = run_gamg(args, ctx, mrgpu) if args.gamg_n > 0 else None
+    log("gamg done")
     served, x_c5 = run_served(args, ctx, mrgpu) if args.served_meshes > 0 else (None, {})
+    log("served done")
     ctx.close()
 
     if rank != 0:
@@ -752,6 +767,7 @@ def run_gpu(args):
     if world == 1 and not args.no_cpu:
         leg = CpuLeg()
         cpu = cpu_baseline(args.scale, leg)
+        log("cpu baseline done")
         jobs = [("c2", args.scale)]
         if c3 is not None:
             jobs.append(("c3", args.c3_scale))
@@ -764,6 +780,7 @@ def run_gpu(args):
         refs = leg.references(jobs)
         leg.close()
         cpu["references_s"] = time.perf_counter() - t0
+        log("oracle references done")
 
     def err(key, x):
         return rel_err(x, refs[key][0]) if key in refs else None
@@ -839,7 +856,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=int, default=1, help="divide the mesh dimensions (testing only)")
-    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--plain-steps", type=int, default=3, help="timed plain FP64 steps (at most 5)")
     ap.add_argument("--inner-tol", type=float, default=1e-5)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the oracle errors")
     ap.add_argument("--c3-scale", type=int, default=1, help="asymmetric GGI configuration: 96/scale (0: skip)")
@@ -858,6 +875,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.steps > 39 or args.plain_steps > 5:
+        ap.error("--steps at most 39 and --plain-steps at most 5 (CUDA event slots of the timing)")
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -338,13 +338,22 @@ typedef struct {
 typedef struct {
     double K;          /* regionCoupledTemperatureJump: value = K * nbr      */
     double flux_jump;  /* regionCoupledHeatFlux: 0                           */
-    double relax;      /* fixed factor, or Aitken's initial factor           */
-    int relax_model;   /* 0 fixedRelaxation, 1 aitkenRelaxation              */
-    int reserved;
+    double relax;      /* fixed factor, or Aitken's / IQN-ILS's initial one  */
+    int relax_model;   /* 0 fixedRelaxation, 1 aitkenRelaxation, 2 IQNILS
+                          (IQNILS.C, IQNILSTemplates.C:44-133; at most 32
+                          modes per side, the oldest dropped first)          */
+    int coupling_reuse; /* IQNILS couplingReuse: time steps whose modes are
+                          kept (0: this time step's only)                    */
 } mrg_dn_config;
 int mrg_dn_create(mrg_ctx* ctx, const mrg_dn_patch* a, const mrg_dn_patch* b,
                   const mrg_dn_config* config, mrg_dn** out);
 int mrg_dn_destroy(mrg_dn* dn);
+/* The flux patch's own acceleration model (its accType / relax /
+ * couplingReuse entries; genericRegionCoupledFluxFvPatchField.C:86-96): by
+ * default B uses A's model and factor; a flux patch without accType in its
+ * dictionary is fixedRelaxation with relax 1 (newAccelerationModel.C:51-65),
+ * the tutorials' set-up.  Call before mrg_dn_set_state. */
+int mrg_dn_set_flux_relaxation(mrg_dn* dn, int relax_model, double relax, int coupling_reuse);
 /* Initial patch value on A and gradient on B (host arrays); resets the
  * relaxation history. */
 int mrg_dn_set_state(mrg_dn* dn, const double* value_a, const double* grad_b);

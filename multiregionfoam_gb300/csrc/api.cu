@@ -838,12 +838,21 @@ int mrg_dn_create(mrg_ctx* ctx, const mrg_dn_patch* a, const mrg_dn_patch* b, co
             d->d.reset(dn_create(&ctx->c, a->n_cells, a->n_faces, a->face_cells, a->delta_coeffs, a->k, a->area,
                                  b->n_cells, b->n_faces, b->face_cells, b->delta_coeffs, b->k, b->area, a->src_ptr,
                                  a->src_face, pwa, b->src_ptr, b->src_face, pwb, cfg->K, cfg->flux_jump,
-                                 cfg->relax_model, cfg->relax));
+                                 cfg->relax_model, cfg->relax, cfg->coupling_reuse));
         } catch (...) {
             delete d;
             throw;
         }
         *out = d;
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_dn_set_flux_relaxation(mrg_dn* dn, int relax_model, double relax, int coupling_reuse)
+{
+    return guard([&] {
+        if (!dn) return fail(MRG_E_INVALID, "NULL argument");
+        dn_set_flux_relaxation(*dn->d, relax_model, relax, coupling_reuse);
         return (int)MRG_OK;
     });
 }

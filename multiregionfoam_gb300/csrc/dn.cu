@@ -8,9 +8,12 @@
 //     regionCoupledHeatFlux::fluxJump = 0 (.C:83-86):
 //     grad_B = (-interp(k_A snGrad_A) + jump) / k_B
 //   rawResidual / normResidual (Jump .C:244-332, Flux .C:241-409)
-//   fixedRelaxation::relax (fixedRelaxation.C:76-101) and
+//   fixedRelaxation::relax (fixedRelaxation.C:76-101),
 //   aitkenRelaxation::relax / updateAitkenFactor (aitkenRelaxation.C:74-100,
-//     aitkenRelaxationTemplates.C:105-165)
+//     aitkenRelaxationTemplates.C:105-165) and
+//   IQNILS::relax / updateVW / updateIQNILS (IQNILS.C:96-201,
+//     IQNILSTemplates.C:44-133): quasi-Newton interface least squares with
+//     the residual differences QR-factored by modified Gram-Schmidt
 // The patch states, the relaxation history and the Aitken factors live on
 // the device, so a DN coupling iteration (update A, solve A, update B,
 // solve B, residuals) needs no host round trip except the two residual
@@ -35,8 +38,8 @@ constexpr int kDnBlock = 1024;
 constexpr double kSmall = 1e-15;   // foam's SMALL
 
 struct DnView {
-    int na, nb, model;
-    double K, flux_jump, init_relax;
+    int na, nb, model, model_b;
+    double K, flux_jump, init_relax, init_relax_b;
     const int *fc_a, *fc_b;
     const double *delta_a, *k_a, *area_a, *delta_b, *k_b, *area_b;
     const int *pa, *xa, *pb, *xb;       // GGI CSR: A faces from B faces, B faces from A faces
@@ -47,7 +50,10 @@ struct DnView {
     double *prev_a, *res_a, *pres_a, *prev_b, *res_b, *pres_b;
     double *tmp_a, *tmp_b;
     double* scal;   // [0] aitken_a, [1] aitken_b, [2] jump residual, [3] flux residual
-    int* corr;      // [0] A, [1] B
+    int* corr;      // [0] A, [1] B, [2] time index
+    int reuse, reuse_b;
+    double *iqn_v, *iqn_w, *iqn_q, *iqn_fref, *iqn_rref, *iqn_cur;
+    int *iqn_t, *iqn_ring;
 };
 
 __device__ double dn_block_sum(double v, double* sh)
@@ -78,6 +84,8 @@ __device__ void dn_relax(const DnView& D, int side, int n, double* prev, double*
                          double* sh)
 {
     __shared__ double s_w;
+    const int model = side ? D.model_b : D.model;
+    const double init_relax = side ? D.init_relax_b : D.init_relax;
     double s1 = 0.0, s2 = 0.0;
     for (int i = threadIdx.x; i < n; i += kDnBlock) {
         const double d = __dsub_rn(res[i], pres[i]);
@@ -87,17 +95,17 @@ __device__ void dn_relax(const DnView& D, int side, int n, double* prev, double*
     s1 = dn_block_sum(s1, sh);
     s2 = dn_block_sum(s2, sh);
     if (threadIdx.x == 0) {
-        double w = D.init_relax;
-        if (D.model == 1) {
+        double w = init_relax;
+        if (model == 1) {
             double a = D.scal[side];
             if (D.corr[side] < 3) {
-                a = a < D.init_relax ? D.init_relax : a;
+                a = a < init_relax ? init_relax : a;
             } else {
                 a = fabs(__dmul_rn(-a, __ddiv_rn(s1, __dadd_rn(s2, kSmall))));
                 if (a > 1.0)
                     a = 1.0;
                 else if (a < kSmall)
-                    a = D.init_relax;
+                    a = init_relax;
             }
             D.scal[side] = a;
             w = a;
@@ -114,6 +122,142 @@ __device__ void dn_relax(const DnView& D, int side, int n, double* prev, double*
     }
 }
 
+// IQNILS::relax for one side: cur (the unrelaxed field) in iqn_cur, res =
+// cur - prev already stored.  updateVW: on a time step's first corrector
+// drop the columns older than `reuse` time steps; on its second keep cur and
+// res as the references; from the third on append V = res - resRef and
+// W = cur - fldRef.  With more than one column the field becomes cur + W c,
+// c the least-squares solution of V c = -res by modified Gram-Schmidt QR
+// with columns of |R_ii| <= 1e-10 max_j sum_i |R_ij| dropped
+// (updateIQNILS); otherwise prev + relax * res.  Every sum is a fixed-order
+// CTA reduction; element-wise steps are single IEEE operations.
+__device__ void dn_iqnils(const DnView& D, int side, int n, double* prev, double* res, double* out, double* sh)
+{
+    __shared__ int s_head, s_count, s_corr;
+    __shared__ double R[kIqnModes][kIqnModes], Cv[kIqnModes];
+    const int off = side ? D.na : 0;   // side offset in the [A | B] arrays
+    const size_t coff = side ? (size_t)kIqnModes * D.na : 0;
+    double* V = D.iqn_v + coff;
+    double* W = D.iqn_w + coff;
+    double* Q = D.iqn_q + coff;
+    double* fref = D.iqn_fref + off;
+    double* rref = D.iqn_rref + off;
+    const double* cur = D.iqn_cur + off;
+    int* T = D.iqn_t + side * kIqnModes;
+    int* ring = D.iqn_ring + 2 * side;
+    const int t = threadIdx.x;
+    if (t == 0) {
+        int head = ring[0], count = ring[1];
+        const int corr = D.corr[side], now = D.corr[2];
+        if (corr == 1) {
+            while (count > 0 && now - (side ? D.reuse_b : D.reuse) > T[head]) {
+                head = (head + 1) % kIqnModes;
+                --count;
+            }
+        } else if (corr >= 3 && count == kIqnModes) {
+            head = (head + 1) % kIqnModes;   // full: the oldest column goes
+            --count;
+        }
+        s_head = head;
+        s_count = count;
+        s_corr = corr;
+    }
+    __syncthreads();
+    const int corr = s_corr;
+    if (corr == 2) {
+        for (int i = t; i < n; i += kDnBlock) {
+            fref[i] = cur[i];
+            rref[i] = res[i];
+        }
+    } else if (corr >= 3) {
+        const int slot = (s_head + s_count) % kIqnModes;
+        for (int i = t; i < n; i += kDnBlock) {
+            V[(size_t)slot * n + i] = __dsub_rn(res[i], rref[i]);
+            W[(size_t)slot * n + i] = __dsub_rn(cur[i], fref[i]);
+        }
+        if (t == 0) {
+            T[slot] = D.corr[2];
+            s_count = s_count + 1;
+        }
+    }
+    __syncthreads();
+    const int head = s_head, cols = s_count;
+    if (cols > 1) {
+        // Q[i] = V[cols - 1 - i]: newest column first
+        for (int i = 0; i < cols; ++i) {
+            const double* v = V + (size_t)((head + cols - 1 - i) % kIqnModes) * n;
+            for (int e = t; e < n; e += kDnBlock) Q[(size_t)i * n + e] = v[e];
+        }
+        __syncthreads();
+        for (int i = 0; i < cols; ++i) {
+            double* qi = Q + (size_t)i * n;
+            double s2 = 0.0;
+            for (int e = t; e < n; e += kDnBlock) s2 = __dadd_rn(s2, __dmul_rn(qi[e], qi[e]));
+            const double rii = __dsqrt_rn(dn_block_sum(s2, sh));
+            if (t == 0) R[i][i] = rii;
+            for (int e = t; e < n; e += kDnBlock) qi[e] = __ddiv_rn(qi[e], rii);
+            __syncthreads();
+            for (int j = i + 1; j < cols; ++j) {
+                double* qj = Q + (size_t)j * n;
+                double sij = 0.0;
+                for (int e = t; e < n; e += kDnBlock) sij = __dadd_rn(sij, __dmul_rn(qi[e], qj[e]));
+                const double rij = dn_block_sum(sij, sh);
+                if (t == 0) R[i][j] = rij;
+                for (int e = t; e < n; e += kDnBlock) qj[e] = __dsub_rn(qj[e], __dmul_rn(rij, qi[e]));
+                __syncthreads();
+            }
+            double ci = 0.0;
+            for (int e = t; e < n; e += kDnBlock) ci = __dadd_rn(ci, __dmul_rn(qi[e], -res[e]));
+            ci = dn_block_sum(ci, sh);
+            if (t == 0) Cv[i] = ci;
+        }
+        if (t == 0) {
+            // back-substitution of R c = C, columns below the tolerance dropped
+            double eps = 0.0;
+            for (int j = 0; j < cols; ++j) {
+                double cs = 0.0;
+                for (int i = 0; i <= j; ++i) cs = __dadd_rn(cs, fabs(R[i][j]));
+                eps = j == 0 ? cs : fmax(eps, cs);
+            }
+            eps = __dmul_rn(1.0e-10, eps);
+            for (int i = 0; i < cols; ++i) {
+                if (fabs(R[i][i]) > eps) {
+                    for (int j = i + 1; j < cols; ++j) R[i][j] = __ddiv_rn(R[i][j], R[i][i]);
+                    Cv[i] = __ddiv_rn(Cv[i], R[i][i]);
+                    R[i][i] = 1.0;
+                }
+            }
+            for (int j = cols - 1; j >= 0; --j) {
+                if (fabs(R[j][j]) > eps) {
+                    for (int i = 0; i < j; ++i) Cv[i] = __dsub_rn(Cv[i], __dmul_rn(Cv[j], R[i][j]));
+                } else {
+                    Cv[j] = 0.0;
+                }
+            }
+        }
+        __syncthreads();
+        for (int e = t; e < n; e += kDnBlock) {
+            double v = cur[e];
+            for (int k = 0; k < cols; ++k)
+                v = __dadd_rn(v, __dmul_rn(W[(size_t)((head + k) % kIqnModes) * n + e], Cv[cols - 1 - k]));
+            prev[e] = v;
+            out[e] = v;
+        }
+    } else {
+        for (int e = t; e < n; e += kDnBlock) {
+            const double v = __dadd_rn(prev[e], __dmul_rn(side ? D.init_relax_b : D.init_relax, res[e]));
+            prev[e] = v;
+            out[e] = v;
+        }
+    }
+    __syncthreads();
+    if (t == 0) {
+        ring[0] = head;
+        ring[1] = cols;
+        D.corr[side] = corr + 1;
+    }
+}
+
 __global__ void __launch_bounds__(kDnBlock) k_dn_update_a(DnView D, const double* __restrict__ t_b)
 {
     __shared__ double sh[kDnBlock];
@@ -125,9 +269,13 @@ __global__ void __launch_bounds__(kDnBlock) k_dn_update_a(DnView D, const double
         const double cur = __dadd_rn(nbr, __dmul_rn(D.K - 1.0, nbr));
         D.pres_a[i] = D.res_a[i];
         D.res_a[i] = __dsub_rn(cur, D.prev_a[i]);
+        if (D.model == 2) D.iqn_cur[i] = cur;
     }
     __syncthreads();
-    dn_relax(D, 0, D.na, D.prev_a, D.res_a, D.pres_a, D.value_a, sh);
+    if (D.model == 2)
+        dn_iqnils(D, 0, D.na, D.prev_a, D.res_a, D.value_a, sh);
+    else
+        dn_relax(D, 0, D.na, D.prev_a, D.res_a, D.pres_a, D.value_a, sh);
 }
 
 __global__ void __launch_bounds__(kDnBlock) k_dn_update_b(DnView D, const double* __restrict__ t_a)
@@ -141,9 +289,13 @@ __global__ void __launch_bounds__(kDnBlock) k_dn_update_b(DnView D, const double
         const double cur = __ddiv_rn(f, D.k_b[j]);
         D.pres_b[j] = D.res_b[j];
         D.res_b[j] = __dsub_rn(cur, D.prev_b[j]);
+        if (D.model_b == 2) D.iqn_cur[D.na + j] = cur;
     }
     __syncthreads();
-    dn_relax(D, 1, D.nb, D.prev_b, D.res_b, D.pres_b, D.grad_b, sh);
+    if (D.model_b == 2)
+        dn_iqnils(D, 1, D.nb, D.prev_b, D.res_b, D.grad_b, sh);
+    else
+        dn_relax(D, 1, D.nb, D.prev_b, D.res_b, D.pres_b, D.grad_b, sh);
 }
 
 __global__ void k_dn_copy(const double* __restrict__ b0, double* __restrict__ b, int n)
@@ -223,9 +375,11 @@ DnView view_of(const Dn& d)
     v.na = d.na;
     v.nb = d.nb;
     v.model = d.model;
+    v.model_b = d.model_b;
     v.K = d.K;
     v.flux_jump = d.flux_jump;
     v.init_relax = d.relax;
+    v.init_relax_b = d.relax_b;
     v.fc_a = d.fc_a;
     v.fc_b = d.fc_b;
     v.delta_a = d.delta_a;
@@ -260,6 +414,16 @@ DnView view_of(const Dn& d)
     v.tmp_b = d.tmp_b;
     v.scal = d.scal;
     v.corr = d.corr;
+    v.reuse = d.reuse;
+    v.reuse_b = d.reuse_b;
+    v.iqn_v = d.iqn_v;
+    v.iqn_w = d.iqn_w;
+    v.iqn_q = d.iqn_q;
+    v.iqn_fref = d.iqn_fref;
+    v.iqn_rref = d.iqn_rref;
+    v.iqn_cur = d.iqn_cur;
+    v.iqn_t = d.iqn_t;
+    v.iqn_ring = d.iqn_ring;
     return v;
 }
 
@@ -292,6 +456,18 @@ void group_faces(int n, const int32_t* fc, std::vector<int>& ptr, std::vector<in
     if (cell.empty()) ptr.assign(1, 0);
 }
 
+// IQN-ILS storage for both sides (either side may select the model).
+void alloc_iqnils(Dn& d)
+{
+    if (d.iqn_v) return;
+    Ctx* c = d.ctx;
+    const size_t both = (size_t)d.na + d.nb;
+    for (double** q : {&d.iqn_v, &d.iqn_w, &d.iqn_q}) *q = (double*)c->alloc(8 * (size_t)kIqnModes * both);
+    for (double** q : {&d.iqn_fref, &d.iqn_rref, &d.iqn_cur}) *q = (double*)c->alloc(8 * both);
+    d.iqn_t = (int*)c->alloc(4 * 2 * kIqnModes);
+    d.iqn_ring = (int*)c->alloc(4 * 4);
+}
+
 void check_csr(int n_rows, int n_src, const int32_t* ptr, const int32_t* addr, const char* what)
 {
     if (!ptr || (n_rows > 0 && !addr)) throw Error(MRG_E_INVALID, std::string(what) + ": NULL CSR");
@@ -310,12 +486,14 @@ Dn* dn_create(Ctx* c, int n_cells_a, int na, const int32_t* fc_a, const double* 
               const double* area_a, int n_cells_b, int nb, const int32_t* fc_b, const double* delta_b,
               const double* k_b, const double* area_b, const int32_t* a_ptr, const int32_t* a_addr,
               const double* a_w, const int32_t* b_ptr, const int32_t* b_addr, const double* b_w, double K,
-              double flux_jump, int model, double relax)
+              double flux_jump, int model, double relax, int reuse)
 {
     if (na <= 0 || nb <= 0 || n_cells_a <= 0 || n_cells_b <= 0) throw Error(MRG_E_INVALID, "empty patch or region");
     if (!fc_a || !delta_a || !k_a || !area_a || !fc_b || !delta_b || !k_b || !area_b || !a_w || !b_w)
         throw Error(MRG_E_INVALID, "NULL patch array");
-    if (model < 0 || model > 1) throw Error(MRG_E_INVALID, "relaxation model must be 0 (fixed) or 1 (Aitken)");
+    if (model < 0 || model > 2)
+        throw Error(MRG_E_INVALID, "relaxation model must be 0 (fixed), 1 (Aitken) or 2 (IQN-ILS)");
+    if (reuse < 0) throw Error(MRG_E_INVALID, "couplingReuse must be >= 0");
     for (int i = 0; i < na; ++i)
         if (fc_a[i] < 0 || fc_a[i] >= n_cells_a) throw Error(MRG_E_INVALID, "patch A faceCells out of range");
     for (int j = 0; j < nb; ++j)
@@ -364,6 +542,11 @@ Dn* dn_create(Ctx* c, int n_cells_a, int na, const int32_t* fc_a, const double* 
             *q = (double*)c->alloc(8 * (size_t)nb);
         d->scal = (double*)c->alloc(8 * 8);
         d->corr = (int*)c->alloc(4 * 4);
+        d->reuse = reuse;
+        d->model_b = model;
+        d->relax_b = relax;
+        d->reuse_b = reuse;
+        if (model == 2) alloc_iqnils(*d);
         MRG_CUDA(cudaStreamSynchronize(c->st));
     } catch (...) {
         delete d;
@@ -383,8 +566,21 @@ Dn::~Dn()
                           (const void*)cb_ptr, (const void*)cb_face, (const void*)cb_cell, (const void*)value_a,
                           (const void*)prev_a, (const void*)res_a, (const void*)pres_a, (const void*)tmp_a,
                           (const void*)grad_b, (const void*)prev_b, (const void*)res_b, (const void*)pres_b,
-                          (const void*)tmp_b, (const void*)scal, (const void*)corr})
-        ctx->release(const_cast<void*>(p));
+                          (const void*)tmp_b, (const void*)scal, (const void*)corr, (const void*)iqn_v,
+                          (const void*)iqn_w, (const void*)iqn_q, (const void*)iqn_fref, (const void*)iqn_rref,
+                          (const void*)iqn_cur, (const void*)iqn_t, (const void*)iqn_ring})
+        if (p) ctx->release(const_cast<void*>(p));
+}
+
+void dn_set_flux_relaxation(Dn& d, int model, double relax, int reuse)
+{
+    if (model < 0 || model > 2)
+        throw Error(MRG_E_INVALID, "relaxation model must be 0 (fixed), 1 (Aitken) or 2 (IQN-ILS)");
+    if (reuse < 0) throw Error(MRG_E_INVALID, "couplingReuse must be >= 0");
+    if (model == 2) alloc_iqnils(d);
+    d.model_b = model;
+    d.relax_b = relax;
+    d.reuse_b = reuse;
 }
 
 void dn_set_state(Dn& d, const double* value_a, const double* grad_b)
@@ -397,16 +593,22 @@ void dn_set_state(Dn& d, const double* value_a, const double* grad_b)
     MRG_CUDA(cudaMemcpyAsync(d.prev_b, grad_b, 8 * (size_t)d.nb, cudaMemcpyHostToDevice, st));
     for (double* q : {d.res_a, d.pres_a}) MRG_CUDA(cudaMemsetAsync(q, 0, 8 * (size_t)d.na, st));
     for (double* q : {d.res_b, d.pres_b}) MRG_CUDA(cudaMemsetAsync(q, 0, 8 * (size_t)d.nb, st));
-    const double sc[8] = {d.relax, d.relax, 0, 0, 0, 0, 0, 0};
+    const double sc[8] = {d.relax, d.relax_b, 0, 0, 0, 0, 0, 0};
     const int corr[4] = {1, 1, 0, 0};
     MRG_CUDA(cudaMemcpyAsync(d.scal, sc, sizeof sc, cudaMemcpyHostToDevice, st));
     MRG_CUDA(cudaMemcpyAsync(d.corr, corr, sizeof corr, cudaMemcpyHostToDevice, st));
+    if (d.iqn_ring) MRG_CUDA(cudaMemsetAsync(d.iqn_ring, 0, 4 * 4, st));   // no IQN-ILS columns
     MRG_CUDA(cudaStreamSynchronize(st));
 }
 
 void dn_new_time_step(Dn& d)
 {
-    const int corr[2] = {1, 1};
+    // corrector counts back to 1, the time index one further
+    int corr[3];
+    MRG_CUDA(cudaMemcpyAsync(corr, d.corr, sizeof corr, cudaMemcpyDeviceToHost, d.ctx->st));
+    MRG_CUDA(cudaStreamSynchronize(d.ctx->st));
+    corr[0] = corr[1] = 1;
+    corr[2] += 1;
     MRG_CUDA(cudaMemcpyAsync(d.corr, corr, sizeof corr, cudaMemcpyHostToDevice, d.ctx->st));
     MRG_CUDA(cudaStreamSynchronize(d.ctx->st));
 }

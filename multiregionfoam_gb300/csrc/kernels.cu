@@ -718,6 +718,12 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
                 const int c = __ldg(perm + i);
                 b[i] = __ldg(ib + c);
                 x[i] = __ldg(ix + c);
+            } else {
+                // padding rows start every solve at zero: a solve that ended
+                // early (a watchdog timeout) may have left non-finite values
+                // there, which the padded row kernels would read
+                b[i] = 0.0;
+                x[i] = 0.0;
             }
         }
     } else if constexpr (OP == OP_PERMUTE_OUT) {
@@ -2115,16 +2121,19 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
     }
 }
 
-// Amul + (q, p) kernel: MRG_SPMV=warp (0) the per-warp staged kernel;
-// =stream1 (1) the streamed kernel with one round per step (FP32 and FP64);
-// default (2) the streamed kernel with two rounds per step in FP32 and the
-// per-warp staged kernel in FP64.  All give the same bits.
+// Amul + (q, p) kernel: default (2) the streamed kernel with one round per
+// step in FP32 and the per-warp staged kernel in FP64 (each the faster in
+// the solve); MRG_SPMV=warp (0) the per-warp staged kernel; =stream1 (1)
+// the streamed kernel with one round per step in FP32 and FP64; =stream2
+// (3) the streamed kernel with two rounds per step in FP32.  All give the
+// same bits.
 static int spmv_mode()
 {
     static int mode = -1;
     if (mode < 0) {
         const char* e = std::getenv("MRG_SPMV");
-        mode = (e && std::strcmp(e, "warp") == 0) ? 0 : (e && std::strcmp(e, "stream1") == 0) ? 1 : 2;
+        mode = !e ? 2 : std::strcmp(e, "warp") == 0 ? 0 : std::strcmp(e, "stream1") == 0 ? 1
+                                                      : std::strcmp(e, "stream2") == 0 ? 3 : 2;
     }
     return mode;
 }
@@ -2184,9 +2193,10 @@ void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
     if constexpr (OP == OP_SPMV_QP) {
         if (!pb) {
             const int mode = spmv_mode();
-            if (mode == 0 || (sizeof(V) == 8 && mode != 1))
+            constexpr bool fp64 = sizeof(V) == 8;
+            if (mode == 0 || (fp64 && mode != 1))
                 launch_pdl(k_spmv_warp<V>, grid, kBlock, spmv_smem<V>(), st, dB);
-            else if (sizeof(V) == 8 || mode == 1)
+            else if (fp64 || mode != 3)
                 launch_pdl(k_spmv_stream<V, 1>, grid, kBlock + 32, stream_smem<V, 1>(), st, dB);
             else
                 launch_pdl(k_spmv_stream<float, 2>, grid, kBlock + 32, stream_smem<float, 2>(), st, dB);

@@ -34,6 +34,7 @@ EXPORTED = [
     "mrg_server_wait", "mrg_server_get_stats", "mrg_mesh_tune", "mrg_batch_tune",
     "mrg_dn_create", "mrg_dn_destroy", "mrg_dn_set_state", "mrg_dn_new_time_step", "mrg_dn_update_jump",
     "mrg_dn_update_flux", "mrg_dn_rhs", "mrg_dn_residuals", "mrg_dn_get_state", "mrg_dn_criteria",
+    "mrg_dn_set_flux_relaxation",
     "mrg_mono_create", "mrg_mono_destroy", "mrg_mono_update", "mrg_mono_source",
     "mrg_block_addressing", "mrg_block_coeffs",
 ]
@@ -94,7 +95,7 @@ class DnPatch(C.Structure):
 
 class DnConfig(C.Structure):
     _fields_ = [("K", C.c_double), ("flux_jump", C.c_double), ("relax", C.c_double), ("relax_model", C.c_int),
-                ("reserved", C.c_int)]
+                ("coupling_reuse", C.c_int)]
 
 
 class IfaceDesc(C.Structure):
@@ -166,6 +167,7 @@ def load(path: str = LIB_PATH):
     L.mrg_dn_create.argtypes = [vp, C.POINTER(DnPatch), C.POINTER(DnPatch), C.POINTER(DnConfig), C.POINTER(vp)]
     L.mrg_dn_destroy.argtypes = [vp]
     L.mrg_dn_set_state.argtypes = [vp, dp, dp]
+    L.mrg_dn_set_flux_relaxation.argtypes = [vp, C.c_int, C.c_double, C.c_int]
     L.mrg_dn_new_time_step.argtypes = [vp]
     L.mrg_dn_update_jump.argtypes = [vp, vp]
     L.mrg_dn_update_flux.argtypes = [vp, vp]
@@ -581,7 +583,13 @@ class DnInterface:
     a / b: dicts with n_cells, face_cells, delta, k, area and the GGI CSR
     (ptr, addr, w) giving the patch's faces from the other patch's faces."""
 
-    def __init__(self, ctx: Context, a: dict, b: dict, K=1.0, flux_jump=0.0, relax=0.75, model="aitken"):
+    MODELS = {"fixed": 0, "aitken": 1, "IQNILS": 2}
+
+    def __init__(self, ctx: Context, a: dict, b: dict, K=1.0, flux_jump=0.0, relax=0.75, model="aitken",
+                 reuse=0, model_b=None, relax_b=None, reuse_b=None):
+        """model / relax / reuse: the jump patch's accelerationModel (accType,
+        relax, couplingReuse); the flux patch takes the same unless model_b /
+        relax_b / reuse_b say otherwise."""
         self._keep = []
 
         def patch(p):
@@ -592,10 +600,14 @@ class DnInterface:
             self._keep.append(arrs)
             return DnPatch(int(p["n_cells"]), len(arrs[0]), *[a_.ctypes.data_as(C.c_void_p) for a_ in arrs])
 
-        cfg = DnConfig(float(K), float(flux_jump), float(relax), 1 if model == "aitken" else 0, 0)
+        cfg = DnConfig(float(K), float(flux_jump), float(relax), self.MODELS[model], int(reuse))
         h = C.c_void_p()
         _check(load().mrg_dn_create(ctx.h, C.byref(patch(a)), C.byref(patch(b)), C.byref(cfg), C.byref(h)))
         self.h = h
+        if model_b is not None or relax_b is not None or reuse_b is not None:
+            _check(load().mrg_dn_set_flux_relaxation(
+                h, self.MODELS[model if model_b is None else model_b], float(relax if relax_b is None else relax_b),
+                int(reuse if reuse_b is None else reuse_b)))
         self.na, self.nb = len(a["face_cells"]), len(b["face_cells"])
 
     def set_state(self, value_a, grad_b):

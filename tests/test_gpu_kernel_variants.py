@@ -6,9 +6,10 @@
                    as phases of one persistent cooperative kernel
                    (=persistent; BiCGStab has no persistent form)
   MRG_SPMV         Amul + (q, p) by the streamed kernel (bulk-copied
-                   operands; two rounds per step in FP32, default), with one
-                   round per step in FP32 and FP64 (=stream1), or by the
-                   per-warp staged kernel (=warp)
+                   operands) with one round per step in FP32 and the per-warp
+                   staged kernel in FP64 (default); the streamed kernel in
+                   both (=stream1); two rounds per step in FP32 (=stream2);
+                   the per-warp staged kernel in both (=warp)
 
 Solves with every variant give bit-identical solutions and iteration counts.
 The switches are read once per process, so each variant runs in a child
@@ -76,7 +77,8 @@ def default_run(tmp_path_factory):
 
 
 @pytest.mark.parametrize("switch,value", [("MRG_SWEEP_PAIRS", "0"), ("MRG_ITERATION", "persistent"),
-                                          ("MRG_SPMV", "warp"), ("MRG_SPMV", "stream1")])
+                                          ("MRG_SPMV", "warp"), ("MRG_SPMV", "stream1"),
+                                          ("MRG_SPMV", "stream2")])
 def test_variant_bit_identical(tmp_path, default_run, switch, value):
     s1, p1 = default_run
     s0, p0 = _run(tmp_path, switch, **{switch: value})

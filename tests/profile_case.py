@@ -1,7 +1,8 @@
-"""One solve of a named workload, for profiling the hot-path kernels.
+"""One solve of a named workload, for profiling the hot-path kernels (a
+profiling driver beside the tests; not part of the library).
 
-    python -m multiregionfoam_gb300.profile_case --case c2 --precision mixed
-    python -m multiregionfoam_gb300.profile_case --case c2 --precision fp64 --max-iter 6
+    python tests/profile_case.py --case c2 --precision mixed
+    python tests/profile_case.py --case c2 --precision fp64 --max-iter 6
 
 The case is built and uploaded once and solved once (PCG + DIC at 1e-8;
 mixed: colour ordering, fp64: exact foam order), so a kernel profiler sees
@@ -12,8 +13,11 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
+import sys
 
-from . import _build, cases, mrgpu
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from multiregionfoam_gb300 import _build, cases, mrgpu  # noqa: E402
 
 CASES = {
     "c1": lambda seed: cases.c1(form="global", seed=seed),

@@ -283,6 +283,18 @@ int mrg_ggi_time(mrg_ggi* ggi, const double* d_src, double* d_dst, int ncomp,
 int mrg_ggi_build(mrg_ctx* ctx, int na, const int32_t* a_ptr, const double* a_xy,
                   int nb, const int32_t* b_ptr, const double* b_xy, double tol,
                   mrg_ggi** a_from_b, mrg_ggi** b_from_a);
+/* directMapInterfaceToInterfaceMapping (the conformal mapping,
+ * directMapInterfaceToInterfaceMapping.C:147-190 and :244-290) on the
+ * device: each face of one patch is paired with the first face of the other
+ * (in face order) whose centre is within tol -- the reference uses 0.001 x
+ * the smallest edge length of the two patches -- and the pairings are
+ * returned as one-weight GGI objects, so mrg_ggi_apply performs the
+ * directMap transfer to[i] = from[map[i]] (.C:644-) exactly.  Centres are
+ * n x (x, y, z).  MRG_E_INVALID when the patches differ in size or a face
+ * has no partner ("interfaces are not conformal"). */
+int mrg_direct_map_build(mrg_ctx* ctx, int na, const double* a_centres,
+                         int nb, const double* b_centres, double tol,
+                         mrg_ggi** a_from_b, mrg_ggi** b_from_a);
 /* Sizes (any of the pointers may be NULL) and, when row_ptr / src_addr /
  * weights are non-NULL, the GGI's CSR copied to the host (n_dst + 1,
  * nnz, nnz entries). */

@@ -542,6 +542,28 @@ int mrg_ggi_build(mrg_ctx* ctx, int na, const int32_t* a_ptr, const double* a_xy
     });
 }
 
+int mrg_direct_map_build(mrg_ctx* ctx, int na, const double* a_centres, int nb, const double* b_centres, double tol,
+                         mrg_ggi** a_from_b, mrg_ggi** b_from_a)
+{
+    return guard([&] {
+        if (!ctx || !a_from_b || !b_from_a) return fail(MRG_E_INVALID, "bad argument");
+        *a_from_b = nullptr;
+        *b_from_a = nullptr;
+        auto* ab = new mrg_ggi();
+        auto* ba = new mrg_ggi();
+        try {
+            direct_map_build(&ctx->c, na, a_centres, nb, b_centres, tol, ab->g, ba->g);
+        } catch (...) {
+            delete ab;
+            delete ba;
+            throw;
+        }
+        *a_from_b = ab;
+        *b_from_a = ba;
+        return (int)MRG_OK;
+    });
+}
+
 int mrg_ggi_get(mrg_ggi* ggi, int* n_dst, int* n_src, int* nnz, int32_t* row_ptr, int32_t* src_addr,
                 double* weights)
 {

@@ -75,6 +75,8 @@ struct SysDev {
     int syncfree;          // exact ordering: sentinel-based sweeps
     // plan
     const int32_t *perm, *a_sptr, *a_col, *a_src, *chunk_start, *lvl_chunk;
+    const uint16_t* a_col16;   // a_col as offsets from a_cbase (rounds of 8 slices that fit)
+    const int32_t* a_cbase;    // [nsl + 8] per-slice base, -1: the round keeps a_col
     const int32_t *f_sptr, *f_col, *f_src, *b_sptr, *b_col, *b_src;
     const int32_t *g_ptr, *g_src;
     const double* g_w;

@@ -192,7 +192,8 @@ void PlanState::sync_sys()
 
 static void release_plan(Ctx* c, PlanState* P)
 {
-    void* ptrs[] = {P->perm, P->a_sptr, P->a_col, P->a_src, P->chunk_start, P->lvl_chunk, P->f_sptr, P->f_col,
+    void* ptrs[] = {P->perm, P->a_sptr, P->a_col, P->a_src, P->a_col16, P->a_cbase, P->chunk_start, P->lvl_chunk,
+                    P->f_sptr, P->f_col,
                     P->f_src, P->b_sptr, P->b_col, P->b_src, P->g_ptr, P->g_src, P->g_w, P->g_w32, P->d_sys};
     for (void* p : ptrs) c->release(p);
     SysDev& S = P->sys;
@@ -265,6 +266,8 @@ PlanState& Mesh::plan(int ordering)
     P->a_sptr = upload_padded(c, H.a_sptr, 16);
     P->a_col = upload(c, H.a_col);
     P->a_src = upload(c, H.a_src);
+    P->a_col16 = upload(c, H.a_col16);
+    P->a_cbase = upload_padded(c, H.a_cbase, 8);
     P->chunk_start = upload(c, H.chunk_start);
     P->lvl_chunk = upload(c, H.lvl_chunk);
     P->f_sptr = upload(c, H.f_sptr);
@@ -303,6 +306,8 @@ PlanState& Mesh::plan(int ordering)
     S.a_sptr = P->a_sptr;
     S.a_col = P->a_col;
     S.a_src = P->a_src;
+    S.a_col16 = P->a_col16;
+    S.a_cbase = P->a_cbase;
     S.chunk_start = P->chunk_start;
     S.lvl_chunk = P->lvl_chunk;
     S.f_sptr = P->f_sptr;
@@ -339,8 +344,11 @@ PlanState& Mesh::plan(int ordering)
     P->d_sys = (SysDev*)c->alloc(sizeof(SysDev));
     P->sync_sys();
     // Keep only sizes (and the per-level chunk offsets) on the host.
+    H.a_col16.clear();
+    H.a_col16.shrink_to_fit();
     for (auto* v : {&H.perm, &H.a_col, &H.a_src, &H.f_col, &H.f_src, &H.b_col, &H.b_src, &H.iperm,
-                    &H.level_of_row, &H.a_sptr, &H.f_sptr, &H.b_sptr, &H.g_ptr, &H.g_src, &H.chunk_start}) {
+                    &H.level_of_row, &H.a_sptr, &H.f_sptr, &H.b_sptr, &H.g_ptr, &H.g_src, &H.chunk_start,
+                    &H.a_cbase}) {
         v->clear();
         v->shrink_to_fit();
     }

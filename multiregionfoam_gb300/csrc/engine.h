@@ -113,6 +113,8 @@ struct PlanState {
     Ctx* ctx = nullptr;
     PlanHost host;  // large host arrays are released after upload
     int32_t *perm = nullptr, *a_sptr = nullptr, *a_col = nullptr, *a_src = nullptr;
+    uint16_t* a_col16 = nullptr;
+    int32_t* a_cbase = nullptr;
     int32_t *chunk_start = nullptr, *lvl_chunk = nullptr;
     int32_t *f_sptr = nullptr, *f_col = nullptr, *f_src = nullptr;
     int32_t *b_sptr = nullptr, *b_col = nullptr, *b_src = nullptr;

@@ -378,6 +378,94 @@ void check_faces(int nf, const int32_t* ptr, const char* which)
 
 }  // namespace
 
+// One warp per receiving face: the lanes test 32 source faces at a time, in
+// face order, and the warp stops at the first group holding a match; the
+// smallest matching index is kept (the reference's first match).  Distance
+// as foam's mag: sqrt((dx dx + dy dy) + dz dz).
+__global__ void k_direct_map(int n_dst, const double* __restrict__ cd, int n_src, const double* __restrict__ cs,
+                             double tol, int32_t* __restrict__ map, unsigned* __restrict__ missing)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = warp; i < n_dst; i += nw) {
+        const double x = cd[3 * (size_t)i], y = cd[3 * (size_t)i + 1], z = cd[3 * (size_t)i + 2];
+        int found = -1;
+        for (int j0 = 0; j0 < n_src && found < 0; j0 += 32) {
+            const int j = j0 + lane;
+            bool hit = false;
+            if (j < n_src) {
+                const double dx = __dsub_rn(x, cs[3 * (size_t)j]);
+                const double dy = __dsub_rn(y, cs[3 * (size_t)j + 1]);
+                const double dz = __dsub_rn(z, cs[3 * (size_t)j + 2]);
+                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                hit = __dsqrt_rn(d2) < tol;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) found = j0 + __ffs((int)m) - 1;
+        }
+        if (lane == 0) {
+            map[i] = found;
+            if (found < 0) atomicAdd(missing, 1u);
+        }
+    }
+}
+
+void direct_map_build(Ctx* c, int na, const double* a_centres, int nb, const double* b_centres, double tol,
+                      Ggi& a_from_b, Ggi& b_from_a)
+{
+    if (na <= 0 || nb <= 0 || !a_centres || !b_centres)
+        throw Error(MRG_E_INVALID, "directMap: empty patch or NULL face centres");
+    if (na != nb)
+        throw Error(MRG_E_INVALID, "directMap: interfaces are not conformal (" + std::to_string(na) + " and " +
+                                       std::to_string(nb) + " faces); directMap needs conformal interfaces");
+    if (!(tol > 0.0)) throw Error(MRG_E_INVALID, "directMap: the match tolerance must be > 0");
+    cudaStream_t st = c->st;
+    std::vector<void*> tmp;
+    auto dalloc = [&](size_t bytes) {
+        void* p = c->alloc(bytes);
+        tmp.push_back(p);
+        return p;
+    };
+    try {
+        double* da = (double*)dalloc(24 * (size_t)na);
+        double* db = (double*)dalloc(24 * (size_t)nb);
+        unsigned* miss = (unsigned*)dalloc(16);
+        MRG_CUDA(cudaMemcpyAsync(da, a_centres, 24 * (size_t)na, cudaMemcpyHostToDevice, st));
+        MRG_CUDA(cudaMemcpyAsync(db, b_centres, 24 * (size_t)nb, cudaMemcpyHostToDevice, st));
+        for (int dir = 0; dir < 2; ++dir) {
+            Ggi& g = dir == 0 ? a_from_b : b_from_a;
+            const int nd = dir == 0 ? na : nb, ns = dir == 0 ? nb : na;
+            g.ctx = c;
+            g.n_dst = nd;
+            g.n_src = ns;
+            g.ptr = (int32_t*)c->alloc(4 * (size_t)(nd + 1));
+            g.addr = (int32_t*)c->alloc(4 * (size_t)nd);
+            g.w = (double*)c->alloc(8 * (size_t)nd);
+            std::vector<int32_t> ptr(nd + 1);
+            for (int i = 0; i <= nd; ++i) ptr[i] = i;
+            const std::vector<double> ones(nd, 1.0);
+            MRG_CUDA(cudaMemcpyAsync(g.ptr, ptr.data(), 4 * (size_t)(nd + 1), cudaMemcpyHostToDevice, st));
+            MRG_CUDA(cudaMemcpyAsync(g.w, ones.data(), 8 * (size_t)nd, cudaMemcpyHostToDevice, st));
+            MRG_CUDA(cudaMemsetAsync(miss, 0, 4, st));
+            const int grid = std::max(1, std::min((nd + 7) / 8, 4096));
+            k_direct_map<<<grid, 256, 0, st>>>(nd, dir == 0 ? da : db, ns, dir == 0 ? db : da, tol, g.addr, miss);
+            MRG_CUDA(cudaGetLastError());
+            add_launches(1);
+            unsigned h = 0;
+            MRG_CUDA(cudaMemcpyAsync(&h, miss, 4, cudaMemcpyDeviceToHost, st));
+            MRG_CUDA(cudaStreamSynchronize(st));
+            if (h)
+                throw Error(MRG_E_INVALID, "directMap: interfaces are not conformal: " + std::to_string(h) +
+                                               " faces have no partner within the tolerance");
+        }
+    } catch (...) {
+        for (void* p : tmp) c->release(p);
+        throw;
+    }
+    for (void* p : tmp) c->release(p);
+}
+
 void ggi_build(Ctx* c, int na, const int32_t* a_ptr, const double* a_xy, int nb, const int32_t* b_ptr,
                const double* b_xy, double tol, Ggi& a_from_b, Ggi& b_from_a)
 {

@@ -16,4 +16,15 @@ namespace mrg {
 void ggi_build(Ctx* c, int na, const int32_t* a_ptr, const double* a_xy, int nb, const int32_t* b_ptr,
                const double* b_xy, double tol, Ggi& a_from_b, Ggi& b_from_a);
 
+// directMapInterfaceToInterfaceMapping's conformal face maps
+// (directMapInterfaceToInterfaceMapping.C:147-190 and :244-290): for every
+// face of one patch the first face of the other (in face order) whose centre
+// lies within tol (|c_B - c_A| < tol; the reference takes tol = 0.001 x the
+// smallest edge length of the two patches), as one-weight GGIs: a_from_b
+// (each A face's B partner) and b_from_a.  Centres are (x, y, z) triples.
+// Throws Error (MRG_E_INVALID) when the patch sizes differ or a face has no
+// partner ("interfaces are not conformal").
+void direct_map_build(Ctx* c, int na, const double* a_centres, int nb, const double* b_centres, double tol,
+                      Ggi& a_from_b, Ggi& b_from_a);
+
 }  // namespace mrg

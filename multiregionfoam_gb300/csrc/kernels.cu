@@ -1814,7 +1814,9 @@ template <> struct StreamCfg<double, 1> { static constexpr int S = 2; static con
 // loaded by the row warps), so two rounds are in flight while two compute
 template <> struct StreamCfg<float, 2> { static constexpr int S = 4; static constexpr bool XD = false; };
 constexpr int kStageCap = kBlock * kMaxW;                              // entries per stage
-constexpr int kStageHead = 64;                                          // slice bounds (48 B used)
+// stage head: the round's 9 slice bounds (48 B copied) at 0, its 8 slices'
+// 16-bit column bases (32 B; -1: 32-bit columns) at 64
+constexpr int kStageHead = 128;
 template <typename V, int RP>
 __host__ __device__ constexpr unsigned stream_xd_bytes()
 {
@@ -1935,23 +1937,28 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
             // round starts in the sliced ELL, a window of 32 rounds per
             // load (lane j: round w0 + j), the next window loaded a window
             // ahead
-            auto win = [&](int w0, int& e, int& eend) {
+            const int* __restrict__ cbase = sP.a_cbase;
+            const uint16_t* __restrict__ acol16 = sP.a_col16;
+            auto win = [&](int w0, int& e, int& eend, int& cb) {
                 const int a = min(w0 + lane, re), z = min(w0 + 32, re);
                 e = __ldg(sptr + 8 * a);
                 eend = __ldg(sptr + 8 * z);
+                cb = __ldg(cbase + 8 * a);
             };
-            int ec, ecend, en = 0, enend = 0;
-            win(rb, ec, ecend);
-            if (rb + 32 < re) win(rb + 32, en, enend);
+            int ec, ecend, cbc, en = 0, enend = 0, cbn = 0;
+            win(rb, ec, ecend, cbc);
+            if (rb + 32 < re) win(rb + 32, en, enend, cbn);
             for (int r = rb; r < re; ++r, ++seq) {
                 const int j = (r - rb) & 31;
                 if (j == 0 && r > rb) {
                     ec = en;
                     ecend = enend;
-                    if (r + 32 < re) win(r + 32, en, enend);
+                    cbc = cbn;
+                    if (r + 32 < re) win(r + 32, en, enend, cbn);
                 }
                 const int e0 = __shfl_sync(kFull, ec, j);
                 const int e1 = j < 31 ? __shfl_sync(kFull, ec, j + 1) : ecend;
+                const bool narrow = __shfl_sync(kFull, cbc, j) >= 0;   // 16-bit columns
                 const int stg = (int)(seq % S);
                 const unsigned ph = (seq / S) & 1u;
                 bool ok = true;
@@ -1965,11 +1972,13 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                     unsigned char* st = dyn + (size_t)stg * SB;
                     const int cnt = e1 - e0;
                     const bool staged = cnt <= kStageCap;
+                    const unsigned colb = narrow ? 2u : 4u;
                     const unsigned bytes =
-                        48u + XB + (staged ? (unsigned)cnt * (unsigned)(sizeof(int) + sizeof(V)) : 0u);
+                        80u + XB + (staged ? (unsigned)cnt * (colb + (unsigned)sizeof(V)) : 0u);
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(&full[stg], bytes);
                     bulk_to_smem(st, sptr + 8 * r, 48u, &full[stg]);
+                    bulk_to_smem(st + 64, cbase + 8 * r, 32u, &full[stg]);
                     if constexpr (XD) {
                         bulk_to_smem(st + kStageHead, p + (size_t)kBlock * r, kBlock * (unsigned)sizeof(V),
                                      &full[stg]);
@@ -1977,8 +1986,12 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                                             kBlock * (unsigned)sizeof(V), &full[stg], pol);
                     }
                     if (staged && cnt > 0) {
-                        bulk_to_smem_stream(st + kStageHead + XB, acol + e0, (unsigned)cnt * sizeof(int), &full[stg],
-                                            pol);
+                        if (narrow)
+                            bulk_to_smem_stream(st + kStageHead + XB, acol16 + e0, (unsigned)cnt * 2u, &full[stg],
+                                                pol);
+                        else
+                            bulk_to_smem_stream(st + kStageHead + XB, acol + e0, (unsigned)cnt * 4u, &full[stg],
+                                                pol);
                         bulk_to_smem_stream(st + kStageHead + XB + kStageCap * sizeof(int), aval + e0,
                                             (unsigned)cnt * (unsigned)sizeof(V), &full[stg], pol);
                     }
@@ -2043,7 +2056,7 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
             // every lane observes the completed phases itself (acquire)
             for (int j = 0; j < nr; ++j) mbar_try_wait(&full[(seq + j) % S], ((seq + j) / S) & 1u);
             const unsigned char* stj[RP];
-            int ew[RP], W[RP], o[RP], i_[RP];
+            int ew[RP], W[RP], o[RP], i_[RP], cb[RP];
             bool fast = true;
 #pragma unroll
             for (int j = 0; j < RP; ++j) {
@@ -2055,14 +2068,24 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                 W[j] = on ? (spv[wid + 1] - ew[j]) >> 5 : 0;
                 o[j] = ew[j] - base + lane;
                 i_[j] = (NW * (r + j) + wid) * 32 + lane;
+                cb[j] = on ? reinterpret_cast<const int*>(stj[j] + 64)[wid] : -1;
                 fast = fast && on && spv[NW] - base <= kStageCap && W[j] <= kMaxW;
             }
+            // column k of this lane's row in stage j: a 16-bit offset from the
+            // slice's base (0xFFFF: padding) or a 32-bit index
+            auto col_of = [&](int j, int k) -> int {
+                const unsigned char* sc = stj[j] + kStageHead + XB;
+                if (cb[j] >= 0) {
+                    const unsigned v = reinterpret_cast<const uint16_t*>(sc)[o[j] + k * 32];
+                    return v == 0xFFFFu ? -1 : cb[j] + (int)v;
+                }
+                return reinterpret_cast<const int*>(sc)[o[j] + k * 32];
+            };
             if (fast) {
                 V xi[RP], dv[RP], xv[RP][kMaxW];
                 int c[RP][kMaxW];
 #pragma unroll
                 for (int j = 0; j < RP; ++j) {
-                    const int* scol = reinterpret_cast<const int*>(stj[j] + kStageHead + XB);
                     if constexpr (XD) {
                         xi[j] = reinterpret_cast<const V*>(stj[j] + kStageHead)[wid * 32 + lane];
                         dv[j] = reinterpret_cast<const V*>(stj[j] + kStageHead + kBlock * sizeof(V))[wid * 32 + lane];
@@ -2071,7 +2094,7 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                         dv[j] = ldg_stream(dg + i_[j], pol);
                     }
 #pragma unroll
-                    for (int k = 0; k < kMaxW; ++k) c[j][k] = k < W[j] ? scol[o[j] + k * 32] : -1;
+                    for (int k = 0; k < kMaxW; ++k) c[j][k] = k < W[j] ? col_of(j, k) : -1;
                 }
 #pragma unroll
                 for (int j = 0; j < RP; ++j)
@@ -2091,7 +2114,6 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                 for (int j = 0; j < nr; ++j) {
                     const int* spv = reinterpret_cast<const int*>(stj[j]);
                     const bool staged = spv[NW] - spv[0] <= kStageCap;
-                    const int* scol = reinterpret_cast<const int*>(stj[j] + kStageHead + XB);
                     const V* sval = reinterpret_cast<const V*>(stj[j] + kStageHead + XB + kStageCap * sizeof(int));
                     V xi, dv;
                     if constexpr (XD) {
@@ -2102,12 +2124,27 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                         dv = __ldg(dg + i_[j]);
                     }
                     V y = vmul(dv, xi);
-                    if (staged)
-                        for (int k0 = 0; k0 < W[j]; k0 += kMaxW)
-                            y = ell_round<V, false>(scol + o[j], sval + o[j], p, k0, W[j], y);
-                    else
+                    if (staged) {
+                        // kMaxW entries a round, as ell_round: indices, then
+                        // coefficients and gathers, then the FMAs in order
+                        for (int k0 = 0; k0 < W[j]; k0 += kMaxW) {
+                            int c[kMaxW];
+                            V a[kMaxW], xv[kMaxW];
+#pragma unroll
+                            for (int k = 0; k < kMaxW; ++k) c[k] = k0 + k < W[j] ? col_of(j, k0 + k) : -1;
+#pragma unroll
+                            for (int k = 0; k < kMaxW; ++k) {
+                                a[k] = c[k] >= 0 ? sval[o[j] + (k0 + k) * 32] : V(0);
+                                xv[k] = c[k] >= 0 ? __ldca(p + c[k]) : V(0);
+                            }
+#pragma unroll
+                            for (int k = 0; k < kMaxW; ++k)
+                                if (c[k] >= 0) y = vfma(a[k], xv[k], y);
+                        }
+                    } else {
                         for (int k0 = 0; k0 < W[j]; k0 += kMaxW)
                             y = ell_round<V, true>(acol + ew[j] + lane, aval + ew[j] + lane, p, k0, W[j], y);
+                    }
                     q[i_[j]] = y;
                     acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
                 }

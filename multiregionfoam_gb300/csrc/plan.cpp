@@ -223,6 +223,34 @@ PlanHost build_plan(int n, int nf, const int32_t* lower, const int32_t* upper,
         }
     }
 
+    // ---- 16-bit column offsets, per round of 8 slices -------------------
+    P.a_col16.assign(P.a_sptr[nsl], (uint16_t)0xFFFF);
+    P.a_cbase.assign(nsl, -1);
+    for (int r = 0; r < nsl / 8; ++r) {
+        int lo[8], hi[8];
+        bool ok = true;
+        for (int q = 0; q < 8; ++q) {
+            const int sl = 8 * r + q;
+            lo[q] = INT32_MAX;
+            hi[q] = -1;
+            for (int32_t e = P.a_sptr[sl]; e < P.a_sptr[sl + 1]; ++e) {
+                const int c = P.a_col[e];
+                if (c < 0) continue;
+                lo[q] = std::min(lo[q], c);
+                hi[q] = std::max(hi[q], c);
+            }
+            if (hi[q] >= 0 && (int64_t)hi[q] - lo[q] > 65534) ok = false;
+        }
+        if (!ok) continue;
+        for (int q = 0; q < 8; ++q) {
+            const int sl = 8 * r + q;
+            const int base = hi[q] >= 0 ? lo[q] : 0;
+            P.a_cbase[sl] = base;
+            for (int32_t e = P.a_sptr[sl]; e < P.a_sptr[sl + 1]; ++e)
+                if (P.a_col[e] >= 0) P.a_col16[e] = (uint16_t)(P.a_col[e] - base);
+        }
+    }
+
     // ---- sweep dependencies (per chunk sliced ELL) ---------------------
     auto build_sweep = [&](bool fwd, std::vector<int32_t>& sptr, std::vector<int32_t>& col,
                            std::vector<int32_t>& src) {

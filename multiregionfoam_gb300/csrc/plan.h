@@ -46,6 +46,12 @@ struct PlanHost {
     std::vector<int32_t> perm, iperm, level_of_row;
     // Amul sliced ELL: npad/32 slices
     std::vector<int32_t> a_sptr, a_col, a_src;
+    // the same column indices as 16-bit offsets from a per-slice base, for
+    // every round of 8 slices (256 rows) whose slices all span at most
+    // 65,535 columns (0xFFFF marks padding); a_cbase[slice] is the base, or
+    // -1 for the 8 slices of a round that keeps 32-bit columns
+    std::vector<uint16_t> a_col16;
+    std::vector<int32_t> a_cbase;
     // sweep chunks
     std::vector<int32_t> chunk_start;  // [nchunks+1]
     std::vector<int32_t> lvl_chunk;    // [nlevels+1]

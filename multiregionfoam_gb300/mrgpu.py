@@ -27,7 +27,7 @@ EXPORTED = [
     "mrg_ctx_mem_used", "mrg_host_alloc", "mrg_host_free", "mrg_mesh_upload", "mrg_mesh_destroy",
     "mrg_mesh_levels", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
     "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
-    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_ggi_time", "mrg_ggi_build", "mrg_ggi_get", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
+    "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_ggi_time", "mrg_ggi_build", "mrg_direct_map_build", "mrg_ggi_get", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
     "mrg_batch_create", "mrg_batch_destroy", "mrg_batch_solve", "mrg_batch_solve_device",
     "mrg_residual_noalloc", "mrg_server_create", "mrg_server_destroy", "mrg_server_submit", "mrg_server_poll",
@@ -141,6 +141,7 @@ def load(path: str = LIB_PATH):
     L.mrg_ggi_apply_device.argtypes = [vp, vp, vp, C.c_int]
     L.mrg_ggi_time.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.mrg_ggi_build.argtypes = [vp, C.c_int, ip, dp, C.c_int, ip, dp, C.c_double, C.POINTER(vp), C.POINTER(vp)]
+    L.mrg_direct_map_build.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_double, C.POINTER(vp), C.POINTER(vp)]
     ipp = C.POINTER(C.c_int)
     L.mrg_ggi_get.argtypes = [vp, ipp, ipp, ipp, ip, ip, dp]
     L.mrg_dev_alloc.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
@@ -485,6 +486,23 @@ class Ggi:
             nd, ns = C.c_int(), C.c_int()
             _check(load().mrg_ggi_get(h, C.byref(nd), C.byref(ns), None, None, None, None))
             g.n_dst, g.n_src = nd.value, ns.value
+            out.append(g)
+        return out[0], out[1]
+
+    @classmethod
+    def direct_map(cls, ctx: Context, centres_a, centres_b, tol):
+        """Conformal face maps by face-centre match on the device
+        (mrg_direct_map_build): one-weight GGIs (a_from_b, b_from_a)."""
+        ca = np.ascontiguousarray(centres_a, dtype=np.float64).reshape(-1, 3)
+        cb = np.ascontiguousarray(centres_b, dtype=np.float64).reshape(-1, 3)
+        ha, hb = C.c_void_p(), C.c_void_p()
+        _check(load().mrg_direct_map_build(ctx.h, len(ca), _d(ca), len(cb), _d(cb), float(tol), C.byref(ha),
+                                           C.byref(hb)))
+        out = []
+        for h, nd, ns in ((ha, len(ca), len(cb)), (hb, len(cb), len(ca))):
+            g = cls.__new__(cls)
+            g.h = h
+            g.n_dst, g.n_src = nd, ns
             out.append(g)
         return out[0], out[1]
 

@@ -264,6 +264,24 @@ class OracleMatrix:
         return A
 
 
+def direct_map(centres_to, centres_from, tol):
+    """directMapInterfaceToInterfaceMapping's face map
+    (directMapInterfaceToInterfaceMapping.C:147-190): for every face of the
+    receiving patch the first face of the other, in face order, whose centre
+    is within tol, |c_to - c_from| < tol with mag = sqrt((dx dx + dy dy) +
+    dz dz); -1 where there is none.  The reference's N^2 search, literally."""
+    ct = np.asarray(centres_to, dtype=np.float64).reshape(-1, 3)
+    cf = np.asarray(centres_from, dtype=np.float64).reshape(-1, 3)
+    out = np.full(len(ct), -1, np.int64)
+    for i, c in enumerate(ct):
+        d = c[None, :] - cf
+        dist = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2])
+        hit = np.flatnonzero(dist < tol)
+        if hit.size:
+            out[i] = hit[0]
+    return out
+
+
 def ggi_apply(ptr, addr, w, src, ncomp=1, fused=False):
     ptr = np.ascontiguousarray(ptr, dtype=np.int32)
     addr = np.ascontiguousarray(addr, dtype=np.int32)

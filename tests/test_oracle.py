@@ -159,6 +159,8 @@ def test_real_mesh_directmap_and_solve(oracle_mod, fohp):
     tol = 1e-3 * min(float(fohp["solid_iface_min_edge"]), float(fohp["fluid_iface_min_edge"]))
     m = cases.direct_map(fohp["solid_iface_centres"], fohp["fluid_iface_centres"], tol)
     assert sorted(m.tolist()) == list(range(200))
+    # the case generator's hash-grid search gives the literal N^2 search's map
+    assert np.array_equal(m, oracle_mod.direct_map(fohp["fluid_iface_centres"], fohp["solid_iface_centres"], tol))
     # the reference's self-check: mapping face centres A->B is exact when conformal
     np.testing.assert_allclose(fohp["solid_iface_centres"][m], fohp["fluid_iface_centres"], atol=tol)
     g = cases.flow_over_heated_plate(fohp, form="global")

@@ -436,14 +436,21 @@ int mrg_mono_source(mrg_mono* mono, int side, const double* d_T_own, const doubl
  * on its current coefficients under each candidate launch shape and keeps
  * the fastest for later solves with the same ordering: the iteration mode
  * (a captured graph of separate launches, or one persistent cooperative
- * kernel with grid barriers), the iterations per launch, and the number of
- * level-sweep chunks per CTA.  A launch shape never changes a result bit.
- * b and x as for a solve (device pointers); x is not modified. */
+ * kernel with grid barriers), the iterations per launch, the number of
+ * level-sweep chunks per CTA and, for PCG's loop, the Amul kernel -- its
+ * block shape and the rows a warp takes per step.  A launch shape never
+ * changes a result bit.  b and x as for a solve (device pointers); x is not
+ * modified. */
 typedef struct {
     int mode;                  /* 0: graph of launches, 1: persistent kernel */
     int iters_per_launch;
     int sweep_chunks_per_cta;  /* colour ordering only                       */
+    int spmv_kernel;           /* 1 per-warp staged, 2 / 3 streamed; 0: not
+                                  tuned (the default kernel)               */
+    int spmv_block_threads;    /* 256, or 288 with a producer warp (0: default) */
+    int spmv_rows_per_warp_step; /* 32 or 64 (0: default)                    */
     int candidates;            /* shapes timed                               */
+    int reserved;
     double us_per_iter;        /* of the chosen shape                        */
 } mrg_tuning;
 int mrg_mesh_tune(mrg_mesh* mesh, const double* d_b, const double* d_x,

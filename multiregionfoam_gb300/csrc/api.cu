@@ -793,6 +793,11 @@ static void fill_tuning(mrg_tuning* out, const Tuning& t)
     out->mode = t.mode;
     out->iters_per_launch = t.k;
     out->sweep_chunks_per_cta = t.sweep_div;
+    // the Amul kernel: block shape (256 row threads; 288 with the streamed
+    // kernel's producer warp) and rows a warp takes per step
+    out->spmv_kernel = t.spmv;
+    out->spmv_block_threads = t.spmv == 0 ? 0 : t.spmv >= 2 ? kBlock + 32 : kBlock;
+    out->spmv_rows_per_warp_step = t.spmv == 0 ? 0 : t.spmv == 2 ? 32 : 64;
     out->candidates = t.candidates;
     out->us_per_iter = t.us_per_iter;
 }

@@ -599,7 +599,7 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
         launch_iface_gather(prec, 0, bh.d, 64, st);
         if (pb) launch_iface_gather(prec, 2, bh.d, 64, st);
     }
-    launch_rows(OP_SPMV_QP, prec, bh.d, nt, ns, pb, st);
+    launch_rows(OP_SPMV_QP, prec, bh.d, nt, ns, pb, st, bh.tune.spmv);
     launch_rows(OP_UPDATE, prec, bh.d, nt, ns, pb, st);
 }
 
@@ -644,8 +644,8 @@ static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int 
                       std::to_string(cfg.ordering) + "/" + std::to_string(prec) + "/" + std::to_string(k) + "/" +
                       std::to_string(g_rows) + "/" + std::to_string(g_red) + "/" + std::to_string(g_sweep) + "/" +
                       std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0) + "/" +
-                      std::to_string(cfg.smoother) + "/" + std::to_string(cfg.n_sweeps) +
-                      (pers ? "/p" : "/l");
+                      std::to_string(cfg.smoother) + "/" + std::to_string(cfg.n_sweeps) + "/s" +
+                      std::to_string(bh.tune.spmv) + (pers ? "/p" : "/l");
     auto it = bh.graphs.find(key);
     if (it != bh.graphs.end()) return it->second;
     cudaStream_t st = bh.ctx->st;
@@ -1054,14 +1054,54 @@ Tuning tune_batch(BatchHost& bh, const Controls& cfg)
         cudaEventDestroy(e1);
         throw;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (best.us_per_iter >= 1e300) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
         bh.tune = saved;
         return saved;
     }
+    int ncand = (int)cands.size();
+    // then the Amul kernel -- block shape (256 row threads, or a producer warp
+    // beside them) and rows a warp takes per step -- for the PCG loop of the
+    // graph mode, the others kept
+    if (best.mode == 0 && cfg.solver == MRG_SOLVER_PCG) {
+        try {
+            for (int v : {1, 2, 3}) {
+                if (prec == 0 && v == 3) continue;   // two rounds per step: FP32 only
+                Tuning t = best;
+                t.spmv = v;
+                bh.tune = t;
+                bh.tune.tuned = 1;
+                batch_begin(bh, run);
+                BatchHost::Graph gr = iteration_graph(bh, run, prec, t.k);
+                launch_iterations(bh, run, prec, gr);
+                poll(bh, h);
+                if (h->n_active == 0) continue;
+                const int reps = std::max(2, 64 / t.k);
+                MRG_CUDA(cudaEventRecord(e0, st));
+                for (int r = 0; r < reps; ++r) {
+                    launch_iterations(bh, run, prec, gr);
+                    poll(bh, h);
+                }
+                MRG_CUDA(cudaEventRecord(e1, st));
+                MRG_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                MRG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                t.us_per_iter = 1e3 * ms / (reps * t.k);
+                ++ncand;
+                if (t.us_per_iter < best.us_per_iter) best = t;
+            }
+        } catch (...) {
+            bh.tune = saved;
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     best.tuned = 1;
-    best.candidates = (int)cands.size();
+    best.candidates = ncand;
     bh.tune = best;
     return best;
 }

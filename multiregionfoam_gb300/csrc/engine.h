@@ -69,6 +69,8 @@ struct Tuning {
     int mode = 0;        // 0: graph of separate launches, 1: persistent cooperative kernel
     int k = 0;           // iterations per launch (0: the controls' iters_per_launch)
     int sweep_div = 8;   // level-sweep grid: one CTA per sweep_div chunks of the widest level
+    int spmv = 0;        // Amul kernel (launch_rows' spmv): 0 default, 1 per-warp staged, 2 / 3 streamed
+                         // with 32 / 64 rows a warp step
     double us_per_iter = 0.0;
     int candidates = 0;
 };

@@ -2219,7 +2219,7 @@ static void launch_pdl(void (*k)(P...), int grid, int block, size_t smem, cudaSt
 static int g_grid_cap = 152 * kMinCtas;
 
 template <typename V, RowOp OP>
-void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
+void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st, int spmv = 0)
 {
     // ntiles / nsegs: the host's upper bounds on the batch's table sizes
     // Persistent grid: one wave that walks the tiles / segments, so each CTA
@@ -2229,7 +2229,8 @@ void launch_one(const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
     if (grid < 1) grid = 1;
     if constexpr (OP == OP_SPMV_QP) {
         if (!pb) {
-            const int mode = spmv_mode();
+            // the batch's tuned choice, else the process default
+            const int mode = spmv == 1 ? 0 : spmv == 2 ? 1 : spmv == 3 ? 3 : spmv_mode();
             constexpr bool fp64 = sizeof(V) == 8;
             if (mode == 0 || (fp64 && mode != 1))
                 launch_pdl(k_spmv_warp<V>, grid, kBlock, spmv_smem<V>(), st, dB);
@@ -3009,7 +3010,8 @@ void set_device_sms(int nsm)
 int persistent_grid() { return g_grid_cap; }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }
 
-void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st)
+void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st,
+                 int spmv)
 {
     if (ntiles <= 0) return;
     ++g_launches;
@@ -3024,7 +3026,7 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE64(OP_INIT_RES)
             MRG_CASE64(OP_RHO)
             MRG_CASE64(OP_PUPDATE)
-            MRG_CASE64(OP_SPMV_QP)
+        case OP_SPMV_QP: launch_one<double, OP_SPMV_QP>(dB, ntiles, nsegs, pb, st, spmv); break;
             MRG_CASE64(OP_UPDATE)
             MRG_CASE64(OP_PRECOND_DIAG)
             MRG_CASE64(OP_PRECOND_NONE)
@@ -3056,7 +3058,7 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
         switch (op) {
             MRG_CASE32(OP_RHO)
             MRG_CASE32(OP_PUPDATE)
-            MRG_CASE32(OP_SPMV_QP)
+        case OP_SPMV_QP: launch_one<float, OP_SPMV_QP>(dB, ntiles, nsegs, pb, st, spmv); break;
             MRG_CASE32(OP_UPDATE)
             MRG_CASE32(OP_PRECOND_DIAG)
             MRG_CASE32(OP_PRECOND_NONE)

@@ -50,7 +50,12 @@ enum RowOp {
 
 // precision: 0 = FP64 vectors/coefficients, 1 = FP32 (mixed inner loop).
 // ntiles, nsegs: upper bounds on the batch's tile and segment counts.
-void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st);
+// spmv (OP_SPMV_QP without the transpose): the Amul kernel -- 0 the
+// default, 1 the per-warp staged kernel (256-thread CTAs), 2 the streamed
+// kernel one round (32 rows a warp) per step, 3 two rounds per step (FP32;
+// a producer warp beside 256 row threads).  Every choice gives the same bits.
+void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs, int pb, cudaStream_t st,
+                 int spmv = 0);
 
 // One Gauss-Seidel sweep of foam's smoother in foam's cell order (sync-free
 // over the exact plan's chunks): y = sweep(x, b), lower neighbours from y

@@ -75,7 +75,8 @@ class ServerStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("mode", C.c_int), ("iters_per_launch", C.c_int), ("sweep_chunks_per_cta", C.c_int),
-                ("candidates", C.c_int), ("us_per_iter", C.c_double)]
+                ("spmv_kernel", C.c_int), ("spmv_block_threads", C.c_int), ("spmv_rows_per_warp_step", C.c_int),
+                ("candidates", C.c_int), ("reserved", C.c_int), ("us_per_iter", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

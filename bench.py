@@ -548,20 +548,30 @@ def run_served(args, ctx, mrgpu):
     from multiregionfoam_gb300 import cases
     specs = cases.c5_specs(args.served_meshes, seed=SEED)
     t0 = time.perf_counter()
-    meshes, steps = [], []
-    for i, sp in enumerate(specs):
-        cur = cases.c5_mesh(sp)
-        meshes.append(mrgpu.Mesh(ctx, cur.n, cur.lower, cur.upper))
+
+    def generate(i):
+        """Mesh i's addressing and its time steps' coefficient arrays
+        (cases.c5_step's sequence, one step after the other)."""
+        cur = cases.c5_mesh(specs[i])
         seq = [dict(diag=cur.diag, upper=cur.upper_c, lower=cur.lower_c, b=cur.b, x0=cur.x0)]
         for k in range(1, args.served_steps):
             cur = cases.perturb_step(cur, np.random.default_rng((SEED, i, k)))
             seq.append(dict(diag=cur.diag, upper=cur.upper_c, lower=cur.lower_c, b=cur.b, x0=seq[0]["x0"]))
-        steps.append(seq)
+        return cur.n, cur.lower, cur.upper, seq
+
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=len(os.sched_getaffinity(0))) as ex:
+        gen = list(ex.map(generate, range(len(specs))))
+    meshes = [mrgpu.Mesh(ctx, n, lo, up) for n, lo, up, _ in gen]
+    steps = [seq for _, _, _, seq in gen]
+    del gen
     t_gen = time.perf_counter() - t0
     asym = [sp[0] for sp in specs]
     n_req = len(specs) * args.served_steps
     sample = {i: i % args.served_steps for i in range(len(specs))}      # mesh -> sampled step
     rates = [float(r) for r in args.served_rates.split(",") if r.strip()]
+    plain_rates = rates if not args.served_plain_rates else \
+        [float(r) for r in args.served_plain_rates.split(",") if r.strip()]
     out = {"requests": n_req, "meshes": len(specs), "steps_per_mesh": args.served_steps, "rates_per_s": rates,
            "iters_per_launch": args.served_k, "cells_mean": float(np.mean([m.n for m in meshes])),
            "asym_meshes": int(sum(asym)), "hbm_budget_gb": 150, "generate_s": t_gen}
@@ -589,9 +599,11 @@ def run_served(args, ctx, mrgpu):
         for r in wid:
             srv.wait(r, 600000.0)
         srv.close()
-        for ri, rate in enumerate(rates):
-            arrivals = np.cumsum(np.random.default_rng((SEED, 11, ri)).exponential(1.0 / rate, n_req))
-            keep = ri == len(rates) - 1
+        form_rates = plain_rates if name == "plain_fp64" else rates
+        for ri, rate in enumerate(form_rates):
+            arrivals = np.cumsum(np.random.default_rng((SEED, 11, rates.index(rate) if rate in rates else ri))
+                                 .exponential(1.0 / rate, n_req))
+            keep = ri == len(form_rates) - 1
             srv = server(prec, order, asym_solver)
             ids = []
             t0 = time.perf_counter()
@@ -603,11 +615,14 @@ def run_served(args, ctx, mrgpu):
                 xo = np.empty(meshes[i].n) if (keep and sample[i] == k) else xbuf[i]
                 ids.append(srv.submit(meshes[i], st["b"], st["x0"], st["diag"], st["upper"], st["lower"],
                                       asym=asym[i], x_out=xo))
-            lat, conv = [], 0
+            lat, conv, unconv = [], 0, []
             for (i, k), r in zip(order_req, ids):
                 x, p, l = srv.wait(r, 600000.0)
                 lat.append(l)
                 conv += p["converged"]
+                if not p["converged"]:
+                    unconv.append({"mesh": i, "step": k, "cells": meshes[i].n, "asym": bool(asym[i]),
+                                   "iters": int(p["n_iter"]), "final_residual": p["final_residual"]})
                 if keep and sample[i] == k:
                     xs[(name, i, k)] = x
             wall = time.perf_counter() - t0
@@ -616,10 +631,11 @@ def run_served(args, ctx, mrgpu):
             log(f"served {name} rate {rate:g}: {len(ids) / wall:.1f} solves/s, wall {wall:.1f} s")
             by_rate.setdefault(f"{rate:g}", {})[name] = {
                 "solves_per_s": len(ids) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv),
+                "p99_ms": float(np.percentile(lat, 99)), "converged": int(conv), "not_converged": unconv[:5],
                 "peak_running": stt["peak_running"], "peak_inflight_gb": stt["peak_inflight_bytes"] / 2**30}
     for r in by_rate.values():
-        r["speedup_mixed_vs_plain"] = r["mixed"]["solves_per_s"] / r["plain_fp64"]["solves_per_s"]
+        if "mixed" in r and "plain_fp64" in r:
+            r["speedup_mixed_vs_plain"] = r["mixed"]["solves_per_s"] / r["plain_fp64"]["solves_per_s"]
     out["by_rate"] = by_rate
     # The plain drop-in solver as foam would call it: one request at a time,
     # device-resident, FP64 in foam's order.  Timed on the first time step of
@@ -646,6 +662,7 @@ def run_served(args, ctx, mrgpu):
                                        "mean_ms": float(np.mean(plain_ms))}
     top = by_rate[f"{rates[-1]:g}"]
     out["speedup_served_mixed_vs_plain_one_at_a_time"] = top["mixed"]["solves_per_s"] / seq_rate
+    out["asym_of_mesh"] = [bool(a) for a in asym]
     for m in meshes:
         m.close()
     return out, xs
@@ -801,10 +818,13 @@ def run_gpu(args):
         for f in ("mixed", "plain_fp64"):
             block[f]["err_vs_fp64_oracle"] = err(("block", args.block_n), x_block[f])
     if served is not None:
+        fam = served.pop("asym_of_mesh")
         served["err_vs_fp64_oracle"] = {
-            "sample": "one request per mesh (time step mesh % steps) of the last rate's runs",
-            **{f: err_stats([err(("c5", args.served_meshes, i, st), x) for (ff, i, st), x in x_c5.items() if ff == f])
-               for f in ("mixed", "plain_fp64")}}
+            "sample": "one request per mesh (time step mesh % steps) of the last rate's runs; the FP64 oracle "
+                      f"converged to {REF_TOL_MANY:g}",
+            **{f"{f}_{kind}": err_stats([err(("c5", args.served_meshes, i, st), x) for (ff, i, st), x in x_c5.items()
+                                         if ff == f and fam[i] == (kind == "asym")])
+               for f in ("mixed", "plain_fp64") for kind in ("sym", "asym")}}
 
     line = {
         "metric": "coupled solves/s at 1e-8 rel. residual", "value": value, "unit": "solves/s",
@@ -869,6 +889,8 @@ def main():
     ap.add_argument("--served-steps", type=int, default=20)
     ap.add_argument("--served-rates", default="50,100,200,500,1000,2000",
                     help="Poisson arrival rates of the sweep, requests/s")
+    ap.add_argument("--served-plain-rates", default="",
+                    help="arrival rates of the plain FP64 server's sweep (default: --served-rates)")
     ap.add_argument("--served-k", type=int, default=8, help="server: Krylov iterations per launch")
     ap.add_argument("--served-pbicg-inner", action="store_true",
                     help="also serve with FP32 PBiCG (not BiCGStab) for the asymmetric requests")

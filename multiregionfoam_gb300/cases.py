@@ -246,7 +246,9 @@ def perturb_step(sys: LduSystem, rng, scale: float = 0.05) -> LduSystem:
     """The next time step of a recurring mesh: every off-diagonal coefficient
     and the diagonal's excess over the row's off-diagonal magnitudes are
     multiplied by 1 + scale*N(0,1) (clipped positive), so a diagonally
-    dominant matrix stays so; b is perturbed the same way, x0 is kept."""
+    dominant matrix stays so; b is perturbed the same way, x0 is kept.  The
+    new row sums of off-diagonal magnitudes ride along in meta, so the next
+    step does not recompute them."""
     def f(k):
         return np.clip(1.0 + scale * rng.standard_normal(k), 0.2, None)
 
@@ -254,12 +256,17 @@ def perturb_step(sys: LduSystem, rng, scale: float = 0.05) -> LduSystem:
         return (np.bincount(sys.lower, np.abs(up), minlength=sys.n) +
                 np.bincount(sys.upper, np.abs(lo), minlength=sys.n))
 
-    lo_old = sys.upper_c if sys.lower_c is None else sys.lower_c
-    excess = sys.diag - rowsum(sys.upper_c, lo_old)
+    old = sys.meta.get("abs_rowsum")
+    if old is None:
+        old = rowsum(sys.upper_c, sys.upper_c if sys.lower_c is None else sys.lower_c)
+    excess = sys.diag - old
     up = sys.upper_c * f(sys.nf)
     lo = None if sys.lower_c is None else sys.lower_c * f(sys.nf)
-    diag = excess * f(sys.n) + rowsum(up, up if lo is None else lo)
-    return dataclasses.replace(sys, diag=diag, upper_c=up, lower_c=lo, b=sys.b * f(sys.n))
+    new = rowsum(up, up if lo is None else lo)
+    diag = excess * f(sys.n) + new
+    meta = dict(sys.meta)
+    meta["abs_rowsum"] = new
+    return dataclasses.replace(sys, diag=diag, upper_c=up, lower_c=lo, b=sys.b * f(sys.n), meta=meta)
 
 
 def c5_meshes(count: int = 100, seed: int = 0, n_lo: int = 10000, n_hi: int = 2000000, asym_frac: float = 0.3):

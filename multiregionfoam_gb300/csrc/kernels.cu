@@ -1806,13 +1806,26 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
 // are bounded: on a timeout the error bit is set, the row warps leave their
 // loop, and the producer waits (bounded) for the copies it issued before the
 // CTA exits.
+// S stages; XD: own x and diagonal staged (else the row warps load them);
+// CB: bytes a column index takes in a stage -- 2: only rounds with 16-bit
+// columns are staged (a round with 32-bit columns reads its indices and
+// coefficients from global memory), 4: both kinds.
 template <typename V, int RP> struct StreamCfg;
-// one round per step: three stages of 14.4 KB (FP32) / two of 22.6 KB (FP64)
-template <> struct StreamCfg<float, 1> { static constexpr int S = 3; static constexpr bool XD = true; };
-template <> struct StreamCfg<double, 1> { static constexpr int S = 2; static constexpr bool XD = true; };
-// two rounds per step: four stages of 12.3 KB (FP32; own x and diagonal
-// loaded by the row warps), so two rounds are in flight while two compute
-template <> struct StreamCfg<float, 2> { static constexpr int S = 4; static constexpr bool XD = false; };
+// one round per step: four stages of 11.1 KB (FP32) / two of 22.6 KB (FP64)
+template <> struct StreamCfg<float, 1> {
+    static constexpr int S = 4, CB = 2;
+    static constexpr bool XD = true;
+};
+template <> struct StreamCfg<double, 1> {
+    static constexpr int S = 2, CB = 4;
+    static constexpr bool XD = true;
+};
+// two rounds per step: five stages of 9.1 KB (FP32; own x and diagonal
+// loaded by the row warps), so three rounds are in flight while two compute
+template <> struct StreamCfg<float, 2> {
+    static constexpr int S = 5, CB = 2;
+    static constexpr bool XD = false;
+};
 constexpr int kStageCap = kBlock * kMaxW;                              // entries per stage
 // stage head: the round's 9 slice bounds (48 B copied) at 0, its 8 slices'
 // 16-bit column bases (32 B; -1: 32-bit columns) at 64
@@ -1825,11 +1838,11 @@ __host__ __device__ constexpr unsigned stream_xd_bytes()
 template <typename V, int RP>
 __host__ __device__ constexpr unsigned stream_stage_bytes()
 {
-    return (unsigned)(kStageHead + stream_xd_bytes<V, RP>() + kStageCap * (sizeof(int) + sizeof(V)));
+    return (unsigned)(kStageHead + stream_xd_bytes<V, RP>() + kStageCap * (StreamCfg<V, RP>::CB + sizeof(V)));
 }
 static_assert(stream_stage_bytes<float, 1>() % 16 == 0 && stream_stage_bytes<double, 1>() % 16 == 0 &&
                   stream_stage_bytes<float, 2>() % 16 == 0 && (kStageHead + 2 * kBlock * 4) % 16 == 0 &&
-                  (kStageCap * 4) % 16 == 0,
+                  (kStageCap * 2) % 16 == 0,
               "every bulk-copy destination in a stage is 16-byte aligned");
 template <typename V, int RP>
 constexpr size_t stream_smem()
@@ -1880,6 +1893,8 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
 {
     constexpr int S = StreamCfg<V, RP>::S;
     constexpr bool XD = StreamCfg<V, RP>::XD;
+    constexpr int CB = StreamCfg<V, RP>::CB;
+    constexpr unsigned VO = (unsigned)(kStageHead + kStageCap * CB);   // coefficients, after the columns
     static_assert(S > RP, "the producer needs a stage beyond the ones a step computes");
     constexpr int NW = kBlock / 32;
     constexpr unsigned SB = stream_stage_bytes<V, RP>();
@@ -1971,7 +1986,7 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                     const unsigned long long pol = l2_evict_first();
                     unsigned char* st = dyn + (size_t)stg * SB;
                     const int cnt = e1 - e0;
-                    const bool staged = cnt <= kStageCap;
+                    const bool staged = cnt <= kStageCap && (narrow || CB == 4);
                     const unsigned colb = narrow ? 2u : 4u;
                     const unsigned bytes =
                         80u + XB + (staged ? (unsigned)cnt * (colb + (unsigned)sizeof(V)) : 0u);
@@ -1992,8 +2007,8 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                         else
                             bulk_to_smem_stream(st + kStageHead + XB, acol + e0, (unsigned)cnt * 4u, &full[stg],
                                                 pol);
-                        bulk_to_smem_stream(st + kStageHead + XB + kStageCap * sizeof(int), aval + e0,
-                                            (unsigned)cnt * (unsigned)sizeof(V), &full[stg], pol);
+                        bulk_to_smem_stream(st + XB + VO, aval + e0, (unsigned)cnt * (unsigned)sizeof(V), &full[stg],
+                                            pol);
                     }
                 }
                 __syncwarp();
@@ -2069,8 +2084,9 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                 o[j] = ew[j] - base + lane;
                 i_[j] = (NW * (r + j) + wid) * 32 + lane;
                 cb[j] = on ? reinterpret_cast<const int*>(stj[j] + 64)[wid] : -1;
-                fast = fast && on && spv[NW] - base <= kStageCap && W[j] <= kMaxW;
+                fast = fast && on && spv[NW] - base <= kStageCap && (cb[j] >= 0 || CB == 4) && W[j] <= kMaxW;
             }
+            bool released = false;
             // column k of this lane's row in stage j: a 16-bit offset from the
             // slice's base (0xFFFF: padding) or a 32-bit index
             auto col_of = [&](int j, int k) -> int {
@@ -2082,7 +2098,10 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                 return reinterpret_cast<const int*>(sc)[o[j] + k * 32];
             };
             if (fast) {
-                V xi[RP], dv[RP], xv[RP][kMaxW];
+                // everything the rows need from the stages into registers,
+                // the stages released, then the gathers and the arithmetic:
+                // the producer refills a stage while its rows' gathers fly
+                V xi[RP], dv[RP], xv[RP][kMaxW], av[RP][kMaxW];
                 int c[RP][kMaxW];
 #pragma unroll
                 for (int j = 0; j < RP; ++j) {
@@ -2093,28 +2112,35 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                         xi[j] = __ldca(p + i_[j]);
                         dv[j] = ldg_stream(dg + i_[j], pol);
                     }
+                    const V* sval = reinterpret_cast<const V*>(stj[j] + XB + VO);
 #pragma unroll
-                    for (int k = 0; k < kMaxW; ++k) c[j][k] = k < W[j] ? col_of(j, k) : -1;
+                    for (int k = 0; k < kMaxW; ++k) {
+                        c[j][k] = k < W[j] ? col_of(j, k) : -1;
+                        av[j][k] = k < W[j] ? sval[o[j] + k * 32] : V(0);
+                    }
                 }
+                __syncwarp();
+                if (lane == 0)
+                    for (int j = 0; j < nr; ++j) mbar_arrive(&empty[(seq + j) % S]);
+                released = true;
 #pragma unroll
                 for (int j = 0; j < RP; ++j)
 #pragma unroll
                     for (int k = 0; k < kMaxW; ++k) xv[j][k] = c[j][k] >= 0 ? __ldca(p + c[j][k]) : V(0);
 #pragma unroll
                 for (int j = 0; j < RP; ++j) {
-                    const V* sval = reinterpret_cast<const V*>(stj[j] + kStageHead + XB + kStageCap * sizeof(int));
                     V y = vmul(dv[j], xi[j]);
 #pragma unroll
                     for (int k = 0; k < kMaxW; ++k)
-                        if (c[j][k] >= 0) y = vfma(sval[o[j] + k * 32], xv[j][k], y);
+                        if (c[j][k] >= 0) y = vfma(av[j][k], xv[j][k], y);
                     q[i_[j]] = y;
                     acc[0] = __fma_rn(widen(y), widen(xi[j]), acc[0]);
                 }
             } else {
                 for (int j = 0; j < nr; ++j) {
                     const int* spv = reinterpret_cast<const int*>(stj[j]);
-                    const bool staged = spv[NW] - spv[0] <= kStageCap;
-                    const V* sval = reinterpret_cast<const V*>(stj[j] + kStageHead + XB + kStageCap * sizeof(int));
+                    const bool staged = spv[NW] - spv[0] <= kStageCap && (cb[j] >= 0 || CB == 4);
+                    const V* sval = reinterpret_cast<const V*>(stj[j] + XB + VO);
                     V xi, dv;
                     if constexpr (XD) {
                         xi = reinterpret_cast<const V*>(stj[j] + kStageHead)[wid * 32 + lane];
@@ -2149,9 +2175,11 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                     acc[0] = __fma_rn(widen(y), widen(xi), acc[0]);
                 }
             }
-            __syncwarp();   // every lane's reads of the stages are done
-            if (lane == 0)
-                for (int j = 0; j < nr; ++j) mbar_arrive(&empty[(seq + j) % S]);
+            if (!released) {
+                __syncwarp();   // every lane's reads of the stages are done
+                if (lane == 0)
+                    for (int j = 0; j < nr; ++j) mbar_arrive(&empty[(seq + j) % S]);
+            }
         }
         flush_segment<OP_SPMV_QP, true>(B, sS, sg.y, u1 - u0, acc, sh, &s_last, (int)U);
         if (s_abort) return;   // read after the flush's closing barrier

@@ -53,11 +53,14 @@ enum {
  * fluid U solves): n_sweeps Gauss-Seidel sweeps in foam's cell order, then
  * the residual, until converged; FP64, exact ordering only. */
 /* GAMG: foam's geometric-algebraic multigrid solver (the tutorials' fluid
- * p / T solves) with the GaussSeidel smoother: pairwise agglomeration on
- * the coefficients (cached from the first matrix), a V-cycle per iteration
- * (restricted residual, a direct solve of the coarsest level, prolonged
- * corrections with nPostSweeps sweeps, nFinestSweeps on the finest level);
- * FP64, exact ordering, a mesh without interfaces, one system at a time. */
+ * p / T solves) with the GaussSeidel smoother: pairwise agglomeration
+ * (faceAreaPair on the mesh's face areas, or algebraicPair on the first
+ * matrix's coefficients; cached), a V-cycle per iteration (restricted
+ * residual, a direct solve of the coarsest level, prolonged corrections
+ * scaled (scaleCorrection) and smoothed by min(nPostSweeps +
+ * postSweepsLevelMultiplier * level, maxPostSweeps) sweeps, nFinestSweeps
+ * on the finest level); FP64, exact ordering, a mesh without interfaces,
+ * one system at a time. */
 enum { MRG_SOLVER_PCG = 0, MRG_SOLVER_PBICG = 1, MRG_SOLVER_BICGSTAB = 2, MRG_SOLVER_SMOOTH = 3,
        MRG_SOLVER_GAMG = 4 };
 /* smoothSolver smoothers: GaussSeidel; DIC / DILU (each sweep adds
@@ -74,7 +77,17 @@ enum {
     MRG_PRECOND_NONE = 0,     /* "none"     */
     MRG_PRECOND_DIAGONAL = 1, /* "diagonal" */
     MRG_PRECOND_DIC = 2,      /* "DIC"      */
-    MRG_PRECOND_DILU = 3      /* "DILU"     */
+    MRG_PRECOND_DILU = 3,     /* "DILU"     */
+    MRG_PRECOND_BLOCK = 4     /* "Cholesky" of a block system (foam-extend's
+                                 BlockCholeskyPrecon, the block solvers'
+                                 preconditioner): incomplete factorisation on
+                                 the bs x bs blocks of a mesh declared by
+                                 mrg_mesh_set_blocks -- D_c = A_cc - sum of
+                                 L_f inv(D_l) U_f over the faces into c;
+                                 x_c = inv(D_c) r_c, then x_u -= inv(D_u) L_f x_l
+                                 (faces ascending) and x_l -= inv(D_l) U_f x_u
+                                 (descending).  PCG (symmetric) or BiCGStab,
+                                 FP64, exact ordering                        */
 };
 enum {
     MRG_PRECISION_FP64 = 0,  /* plain method: FP64 throughout, foam order   */
@@ -89,6 +102,11 @@ enum {
     MRG_ORDER_COLOUR = 1   /* multi-colour renumbering for the
                               preconditioner (fewer sweep levels, different
                               incomplete factorisation)                      */
+};
+/* GAMG agglomerator ("agglomerator" word; foam's default is faceAreaPair) */
+enum {
+    MRG_AGGLOMERATOR_ALGEBRAIC_PAIR = 0,  /* |upper| of the finest matrix     */
+    MRG_AGGLOMERATOR_FACE_AREA_PAIR = 1   /* face areas (mrg_mesh_set_face_areas) */
 };
 
 typedef struct mrg_ctx mrg_ctx;
@@ -125,6 +143,13 @@ typedef struct {
     int gamg_coarsest_cells; /* GAMG: nCellsInCoarsestLevel (default 10)     */
     int gamg_post_sweeps;  /* GAMG: nPostSweeps (default 2)                 */
     int gamg_finest_sweeps; /* GAMG: nFinestSweeps (default 2)              */
+    int gamg_max_post_sweeps; /* GAMG: maxPostSweeps (default 4)            */
+    int gamg_post_sweeps_level_multiplier; /* GAMG: postSweepsLevelMultiplier
+                              (default 1)                                   */
+    int gamg_scale_correction; /* GAMG: scaleCorrection (default 1)         */
+    int gamg_agglomerator; /* GAMG: MRG_AGGLOMERATOR_* (default
+                              algebraicPair: faceAreaPair needs the mesh's
+                              face areas)                                   */
 } mrg_controls;
 
 /* lduSolverPerformance (initialResidual, finalResidual, nIterations,
@@ -207,6 +232,13 @@ int mrg_mesh_destroy(mrg_mesh* mesh);
 /* Number of preconditioner sweep levels of the chosen ordering (critical
  * path length of the DIC/DILU triangular solves). */
 int mrg_mesh_levels(mrg_mesh* mesh, int ordering, int* n_levels);
+/* The faces' area vectors (fvMesh::Sf() of the internal faces, x y z per
+ * face, n_faces * 3 values): what GAMG's faceAreaPair agglomerator weights
+ * the pairing with (faceAreaPairGAMGAgglomeration: |cmptMultiply(Sf /
+ * sqrt(|Sf|), (1, 1.01, 1.02))|).  Only the weights are kept (host side);
+ * a cached GAMG hierarchy built from earlier areas is rebuilt at the next
+ * GAMG solve. */
+int mrg_mesh_set_face_areas(mrg_mesh* mesh, const double* sf);
 
 /* ---- coefficients (per time step) -----------------------------------
  * lduMatrix::diag()/upper()/lower() plus the interfaces' coupleBouCoeffs
@@ -539,9 +571,15 @@ int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel,
  * L_f[b][a]; a diagonal block D_c gives the diagonal D_c[a][a] and, for
  * a < b, the face (bs c + a, bs c + b) with upper D_c[a][b] and lower
  * D_c[b][a].  Faces come out in upper-triangular order (owner row, then
- * neighbour).  Point-wise preconditioning (DILU on the scalar rows) stands
- * in for foam-extend's block preconditioners.  Host-only, no GPU needed.
+ * neighbour).  Any scalar preconditioner applies to the expansion, and
+ * MRG_PRECOND_BLOCK (after mrg_mesh_set_blocks) works on its blocks.
+ * mrg_block_addressing and mrg_block_coeffs are host-only (no GPU needed).
  *
+ * mrg_mesh_set_blocks: declare a mesh uploaded from mrg_block_addressing's
+ *   output the bs-expansion of the block mesh (n_cells, n_faces, lower /
+ *   upper; checked), so MRG_PRECOND_BLOCK can factor its bs x bs blocks
+ *   (gathered from the scalar coefficients whenever they change).  bs 1..4;
+ *   the mesh has no interfaces.
  * mrg_block_addressing: *n_faces_out = bs^2 n_faces + bs (bs - 1) / 2
  *   n_cells; s_lower / s_upper [that many] (either NULL: the count only).
  * mrg_block_coeffs: diag [n_cells bs bs], upper and lower [n_faces bs bs]
@@ -553,6 +591,8 @@ int mrg_time_kernel(mrg_mesh* mesh, const mrg_controls* controls, int kernel,
 int mrg_block_addressing(int n_cells, int n_faces, const int32_t* lower_addr,
                          const int32_t* upper_addr, int bs, int* n_faces_out,
                          int32_t* s_lower, int32_t* s_upper);
+int mrg_mesh_set_blocks(mrg_mesh* mesh, int bs, int n_cells, int n_faces,
+                        const int32_t* lower_addr, const int32_t* upper_addr);
 int mrg_block_coeffs(int n_cells, int n_faces, const int32_t* lower_addr,
                      const int32_t* upper_addr, int bs, const double* diag,
                      const double* upper, const double* lower_or_null,

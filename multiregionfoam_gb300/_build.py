@@ -16,9 +16,12 @@ OUT = os.path.join(HERE, "_lib")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libmrgpu.so")
 
-SOURCES = ["kernels.cu", "engine.cu", "api.cu", "noalloc.cu", "dn.cu", "ggi_build.cu", "mono.cu", "gamg.cu", "plan.cpp", "server.cpp", "block.cpp"]
+SOURCES = ["kernels.cu", "engine.cu", "api.cu", "noalloc.cu", "dn.cu", "ggi_build.cu", "mono.cu", "gamg.cu", "blockpc.cu", "plan.cpp", "server.cpp", "block.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
+# host code is compiled without floating-point contraction, so host arithmetic
+# (GAMG's face weights) rounds the same on x86-64 and aarch64
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I", CSRC, "-I", INCLUDE]
 
 
 def nvcc() -> str:

@@ -140,8 +140,11 @@ def cht_system(nx: int, ny: int, nz_fluid: int, nz_solid: int, *, seed: int = 0,
     diag[f_lid] += gb_f
     b[f_lid] += gb_f * t_top
 
+    ix = np.tile(np.arange(nx), ny * (nz_solid + nz_fluid))
+    iy = np.tile(np.repeat(np.arange(ny), nx), nz_solid + nz_fluid)
+    centres = np.stack([(ix + 0.5) * h, (iy + 0.5) * h, zc], axis=1)
     meta = dict(nx=nx, ny=ny, nz_fluid=nz_fluid, nz_solid=nz_solid, seed=seed, h=h,
-                n_solid=ns, n_fluid=nfl, n_iface=nx * ny, rc=rc, k_cell=kc)
+                n_solid=ns, n_fluid=nfl, n_iface=nx * ny, rc=rc, k_cell=kc, centres=centres)
     if form == "global":
         lo2, up2, g2 = upper_triangular(np.concatenate([lower, s_top]),
                                         np.concatenate([upper, f_bot]),
@@ -161,6 +164,14 @@ def cht_system(nx: int, ny: int, nz_fluid: int, nz_solid: int, *, seed: int = 0,
     }
     return LduSystem(n, lower.astype(np.int32), upper.astype(np.int32), diag, -g_int, None,
                      b, t_old, iface, name="cht-coupled", meta=meta)
+
+
+def face_area_vectors(sys: LduSystem) -> np.ndarray:
+    """Area vectors Sf ([nf, 3], owner to neighbour) of the internal faces of
+    a system on a uniform hex grid of spacing meta["h"] with cell centres
+    meta["centres"] (cht_system): (c_upper - c_lower) h."""
+    c, h = sys.meta["centres"], sys.meta["h"]
+    return (c[sys.upper] - c[sys.lower]) * h
 
 
 def partitioned_cht(nx: int, ny: int, nz_fluid: int, nz_solid: int, **kw):

@@ -3,6 +3,7 @@
 // throws across the ABI.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -12,6 +13,7 @@
 #include "../../include/mrgpu.h"
 #include "engine.h"
 #include "kernels.h"
+#include "blockpc.h"
 #include "dn.h"
 #include "gamg.h"
 #include "ggi_build.h"
@@ -105,7 +107,16 @@ Controls to_controls(const mrg_controls* c)
         k.gamg_coarsest = c->gamg_coarsest_cells > 0 ? c->gamg_coarsest_cells : 10;
         k.gamg_post = c->gamg_post_sweeps >= 0 ? c->gamg_post_sweeps : 2;
         k.gamg_finest = c->gamg_finest_sweeps >= 0 ? c->gamg_finest_sweeps : 2;
+        k.gamg_max_post = c->gamg_max_post_sweeps;
+        k.gamg_post_mult = c->gamg_post_sweeps_level_multiplier;
+        k.gamg_scale = c->gamg_scale_correction != 0;
+        k.gamg_agglomerator = c->gamg_agglomerator;
         if (k.gamg_coarsest > 64) throw Error(MRG_E_INVALID, "GAMG: nCellsInCoarsestLevel must be at most 64");
+        if (k.gamg_max_post < 0 || k.gamg_post_mult < 0)
+            throw Error(MRG_E_INVALID, "GAMG: maxPostSweeps and postSweepsLevelMultiplier must be non-negative");
+        if (k.gamg_agglomerator != MRG_AGGLOMERATOR_ALGEBRAIC_PAIR &&
+            k.gamg_agglomerator != MRG_AGGLOMERATOR_FACE_AREA_PAIR)
+            throw Error(MRG_E_INVALID, "GAMG: unknown agglomerator");
     }
     if (k.solver == MRG_SOLVER_SMOOTH) {
         if (c->smoother < MRG_SMOOTHER_GAUSS_SEIDEL || c->smoother > MRG_SMOOTHER_DILU_GAUSS_SEIDEL)
@@ -117,7 +128,13 @@ Controls to_controls(const mrg_controls* c)
         const bool dilu = c->smoother == MRG_SMOOTHER_DILU || c->smoother == MRG_SMOOTHER_DILU_GAUSS_SEIDEL;
         k.pc = c->smoother == MRG_SMOOTHER_GAUSS_SEIDEL ? PC_NONE : (dilu ? PC_DILU : PC_DIC);
     }
-    if (k.pc < 0 || k.pc > 3) throw Error(MRG_E_INVALID, "unknown preconditioner");
+    if (k.pc < 0 || k.pc > 4) throw Error(MRG_E_INVALID, "unknown preconditioner");
+    if (k.pc == PC_BLOCK) {
+        if (k.solver != MRG_SOLVER_PCG && k.solver != MRG_SOLVER_BICGSTAB)
+            throw Error(MRG_E_INVALID, "block preconditioner: solver must be PCG or BiCGStab");
+        if (k.precision != MRG_PRECISION_FP64 || k.ordering != MRG_ORDER_EXACT)
+            throw Error(MRG_E_INVALID, "block preconditioner: FP64 in foam's order (precision fp64, ordering exact)");
+    }
     if (k.precision < 0 || k.precision > 1) throw Error(MRG_E_INVALID, "unknown precision");
     if (k.ordering < 0 || k.ordering > 1) throw Error(MRG_E_INVALID, "unknown ordering");
     if (k.max_iter < 0 || k.min_iter < 0) throw Error(MRG_E_INVALID, "negative iteration bounds");
@@ -198,6 +215,10 @@ void mrg_controls_default(mrg_controls* c)
     c->gamg_coarsest_cells = 10;
     c->gamg_post_sweeps = 2;
     c->gamg_finest_sweeps = 2;
+    c->gamg_max_post_sweeps = 4;
+    c->gamg_post_sweeps_level_multiplier = 1;
+    c->gamg_scale_correction = 1;
+    c->gamg_agglomerator = MRG_AGGLOMERATOR_ALGEBRAIC_PAIR;
 }
 
 int mrg_ctx_create(int device, size_t hbm_budget_bytes, mrg_ctx** out)
@@ -326,6 +347,30 @@ int mrg_mesh_levels(mrg_mesh* mesh, int ordering, int* n_levels)
     });
 }
 
+int mrg_mesh_set_blocks(mrg_mesh* mesh, int bs, int n_cells, int n_faces, const int32_t* lower_addr,
+                        const int32_t* upper_addr)
+{
+    return guard([&] {
+        if (!mesh) return fail(MRG_E_INVALID, "NULL argument");
+        set_blocks(mesh->m, bs, n_cells, n_faces, lower_addr, upper_addr);
+        return (int)MRG_OK;
+    });
+}
+
+int mrg_mesh_set_face_areas(mrg_mesh* mesh, const double* sf)
+{
+    return guard([&] {
+        if (!mesh || (!sf && mesh->m.nf > 0)) return fail(MRG_E_INVALID, "NULL argument");
+        std::vector<double> w = face_area_weights(sf, mesh->m.nf);
+        for (int f = 0; f < mesh->m.nf; ++f)
+            if (!std::isfinite(w[f]))
+                return fail(MRG_E_INVALID, "face " + std::to_string(f) + ": zero or non-finite area vector");
+        mesh->m.agglom_w = std::move(w);
+        mesh->m.agglom_version += 1;
+        return (int)MRG_OK;
+    });
+}
+
 int mrg_coeffs_upload(mrg_mesh* mesh, const double* diag, const double* upper, const double* lower_or_null,
                       const double* iface_bou, const double* iface_int_or_null)
 {
@@ -412,7 +457,9 @@ int mrg_precondition(mrg_mesh* mesh, int precond, int ordering, const double* r,
 {
     return guard([&] {
         if (!mesh || !r || !w) return fail(MRG_E_INVALID, "NULL argument");
-        if (precond < 0 || precond > 3) return fail(MRG_E_INVALID, "unknown preconditioner");
+        if (precond < 0 || precond > 4) return fail(MRG_E_INVALID, "unknown preconditioner");
+        if (precond == PC_BLOCK && (transpose || ordering != MRG_ORDER_EXACT))
+            return fail(MRG_E_INVALID, "block preconditioner: no transpose, exact ordering only");
         Mesh& m = mesh->m;
         Ctx* c = m.ctx;
         double* dr = stage(c, 0, m.n);

@@ -109,6 +109,21 @@ Expansion expand(int n, int nf, const int32_t* lower, const int32_t* upper, int 
 
 }  // namespace
 
+namespace mrg {
+// The expansion's scalar addressing and each scalar face's source entry
+// (for the block preconditioner's maps); "" on success, else a message.
+std::string block_expansion(int n, int nf, const int32_t* lower, const int32_t* upper, int bs,
+                            std::vector<int32_t>& s_lower, std::vector<int32_t>& s_upper, std::vector<int64_t>& src)
+{
+    if (check(n, nf, lower, upper, bs) != MRG_OK) return "invalid block addressing";
+    Expansion E = expand(n, nf, lower, upper, bs, true, true);
+    s_lower = std::move(E.s_lower);
+    s_upper = std::move(E.s_upper);
+    src = std::move(E.src);
+    return "";
+}
+}  // namespace mrg
+
 // ABI entries: clear the last error, turn a failed host allocation into
 // MRG_E_OOM.
 template <typename F>

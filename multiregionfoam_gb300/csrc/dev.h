@@ -66,8 +66,30 @@ struct Vecs {
     V *rT, *wT, *yT, *pT, *qT;      // transpose system (PBiCG; pT carries the GGI tail)
 };
 
-// Which preconditioner the sweeps apply.
-enum { PC_NONE = 0, PC_DIAG = 1, PC_DIC = 2, PC_DILU = 3 };
+// Which preconditioner the sweeps apply.  PC_BLOCK: the block (bs x bs)
+// incomplete factorisation of a block-expanded system (BlockDev), applied by
+// its own kernels; the scalar factor and sweep kernels skip it.
+enum { PC_NONE = 0, PC_DIAG = 1, PC_DIC = 2, PC_DILU = 3, PC_BLOCK = 4 };
+__host__ __device__ inline bool scalar_tri(int pc) { return pc == PC_DIC || pc == PC_DILU; }
+
+// A block-expanded system's block view (cell c's component a is the scalar
+// caller row bs c + a): the cell mesh's exact plan (internal cell order,
+// chunks of <= 32 cells of one level, forward / backward dependency ELLs
+// with face codes as in the scalar plan), where each block entry's scalar
+// coefficient sits, the blocks gathered from the scalar coefficients, the
+// factor, and the scalar internal row of every (cell, component).
+struct BlockDev {
+    int bs, n, nf, nchunks;
+    const int32_t *perm, *chunk_start;            // internal cell -> caller cell
+    const int32_t *f_sptr, *f_col, *f_src, *b_sptr, *b_col, *b_src;
+    const int32_t *dmap;                          // [n bs bs]: >= 0 diag row; < 0: -1 - scalar face (upper
+                                                  // triangle of the block: upper, else lower)
+    const int32_t *fmap;                          // [nf bs bs]: scalar face of U_f[a][b]
+    double *D, *U, *L;                            // gathered blocks (caller cell / face order)
+    double* dD;                                   // [n bs bs] inverse of the factored diagonal (internal)
+    const int32_t* vmap;                          // [n bs]: scalar internal row of (internal cell, a)
+    int sym;
+};
 
 struct SysDev {
     int n, npad, nsl, ntiles;
@@ -81,6 +103,14 @@ struct SysDev {
     const int32_t *g_ptr, *g_src;
     const double* g_w;
     const float* g_w32;
+    // owner-computes exact sweeps (k_sweep_part): nparts ranges of part_cells
+    // caller cells, each part's rows in level order with their level
+    // ordinals, each dependency's place in its row's part (-1: another part)
+    // and each row's sweep entries; nparts = 0: not built
+    const BlockDev* blk;   // PC_BLOCK: the block view (device)
+    int nparts, part_cells;
+    const int32_t *pt_ptr, *part_rows, *part_step, *f_loc, *b_loc;
+    const int2 *f_row, *b_row;   // per row: (first sweep entry, entries)
     // raw coefficients in the caller's numbering
     const double *raw_diag, *raw_upper, *raw_lower, *raw_ibou, *raw_iint;
     // FP64 coefficient views (internal numbering)

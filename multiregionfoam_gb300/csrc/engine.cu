@@ -194,7 +194,8 @@ static void release_plan(Ctx* c, PlanState* P)
 {
     void* ptrs[] = {P->perm, P->a_sptr, P->a_col, P->a_src, P->a_col16, P->a_cbase, P->chunk_start, P->lvl_chunk,
                     P->f_sptr, P->f_col,
-                    P->f_src, P->b_sptr, P->b_col, P->b_src, P->g_ptr, P->g_src, P->g_w, P->g_w32, P->d_sys};
+                    P->f_src, P->b_sptr, P->b_col, P->b_src, P->g_ptr, P->g_src, P->g_w, P->g_w32, P->d_sys,
+                    P->pt_ptr, P->part_rows, P->part_step, P->f_row, P->b_row, P->f_loc, P->b_loc};
     for (void* p : ptrs) c->release(p);
     SysDev& S = P->sys;
     void* vals[] = {S.a_val, S.aT_val != S.a_val ? S.aT_val : nullptr, S.diag, S.sumA, S.f_c, S.f_cT, S.b_c,
@@ -262,6 +263,24 @@ PlanState& Mesh::plan(int ordering)
     P->host = build_plan(n, nf, lower.data(), upper.data(), ifc, ordering);
     PlanHost& H = P->host;
     Ctx* c = ctx;
+    // owner-computes exact sweeps: parts of about part_target cells (at most
+    // one per SM), their values in shared memory; a mesh whose parts would
+    // exceed kPartMaxCells keeps the ticketed kernel (measured on GB300: 3.1M
+    // cells in 152 parts sweep 1.7x slower than ticketed, 262k cells in 64
+    // parts 1.6x faster)
+    if (ordering == 0 && c->nsm > 0) {
+        const int parts = std::max(1, std::min(c->nsm, (n + part_target - 1) / part_target));
+        if ((n + parts - 1) / parts <= kPartMaxCells) build_parts(H, parts);
+    }
+    if (H.nparts) {
+        P->pt_ptr = upload(c, H.pt_ptr);
+        P->part_rows = upload(c, H.part_rows);
+        P->part_step = upload(c, H.part_step);
+        P->f_row = upload(c, H.f_row);
+        P->b_row = upload(c, H.b_row);
+        P->f_loc = upload(c, H.f_loc);
+        P->b_loc = upload(c, H.b_loc);
+    }
     P->perm = upload(c, H.perm);
     P->a_sptr = upload_padded(c, H.a_sptr, 16);
     P->a_col = upload(c, H.a_col);
@@ -320,6 +339,15 @@ PlanState& Mesh::plan(int ordering)
     S.g_src = P->g_src;
     S.g_w = P->g_w;
     S.g_w32 = P->g_w32;
+    S.nparts = H.nparts;
+    S.part_cells = H.part_cells;
+    S.pt_ptr = P->pt_ptr;
+    S.part_rows = P->part_rows;
+    S.part_step = P->part_step;
+    S.f_row = reinterpret_cast<const int2*>(P->f_row);
+    S.b_row = reinterpret_cast<const int2*>(P->b_row);
+    S.f_loc = P->f_loc;
+    S.b_loc = P->b_loc;
     const size_t np = (size_t)H.npad, nx = (size_t)H.npad + H.ngen;
     S.a_val = (double*)c->alloc(8 * P->nnz);
     S.aT_val = S.a_val;
@@ -348,7 +376,7 @@ PlanState& Mesh::plan(int ordering)
     H.a_col16.shrink_to_fit();
     for (auto* v : {&H.perm, &H.a_col, &H.a_src, &H.f_col, &H.f_src, &H.b_col, &H.b_src, &H.iperm,
                     &H.level_of_row, &H.a_sptr, &H.f_sptr, &H.b_sptr, &H.g_ptr, &H.g_src, &H.chunk_start,
-                    &H.a_cbase}) {
+                    &H.a_cbase, &H.pt_ptr, &H.part_rows, &H.part_step, &H.f_row, &H.b_row, &H.f_loc, &H.b_loc}) {
         v->clear();
         v->shrink_to_fit();
     }
@@ -387,6 +415,10 @@ static bool ensure_views(Mesh& m, PlanState& P, const Controls& cfg)
     setp(S.raw_ibou, (const double*)m.raw_ibou);
     setp(S.raw_iint, (const double*)m.raw_iint);
     setp(S.pc, cfg.pc);
+    if (cfg.pc == PC_BLOCK) {
+        setp(S.blk, (const BlockDev*)block_view(m, P).d);
+        P.bs_blocks = m.blocks->bs;
+    }
     if (asym && S.aT_val == S.a_val) {
         S.aT_val = (double*)c->alloc(8 * P.nnz);
         P.scattered = 0;
@@ -469,10 +501,26 @@ void prepare_batch(BatchHost& bh, const std::vector<Mesh*>& meshes, const Contro
         MRG_CUDA(cudaGetLastError());
     }
     if (refactor) {
-        if (cfg.pc >= PC_DIC)
+        if (cfg.pc == PC_BLOCK) {
+            // every member's blocks from its scalar coefficients, sentinels
+            // in its factor, then one factor launch over the batch
+            int bs = 0;
+            for (size_t s = 0; s < meshes.size(); ++s) {
+                Mesh& m = *meshes[s];
+                const BlockHost& B = *m.blocks;
+                if (bs && B.bs != bs) throw Error(MRG_E_INVALID, "block preconditioner: members' block sizes differ");
+                bs = B.bs;
+                BlockView& v = block_view(m, *bh.members[s]);
+                launch_block_gather(v.d, B.n, B.nf, B.bs, m.raw_diag, m.raw_upper, m.sym ? nullptr : m.raw_lower,
+                                    c->st);
+                launch_fill_sentinel(v.dD, (long long)B.n * B.bs * B.bs, 0, c->st);
+            }
+            launch_block_factor(bs, bh.d, grid_sweep(c), c->st);
+        } else if (cfg.pc >= PC_DIC) {
             launch_factor(bh.d, grid_sweep(c), want32 ? 1 : 0, c->st);
-        else
+        } else {
             launch_rows(OP_DIAG_RD, 0, bh.d, nt, ns, 0, c->st);
+        }
         MRG_CUDA(cudaGetLastError());
     }
     for (size_t s = 0; s < meshes.size(); ++s) {
@@ -498,14 +546,54 @@ PlanState& prepare(Mesh& m, const Controls& cfg)
 // ------------------------------------------------------------------ graphs
 // trans: the sweeps' vector set (0 = r -> w, 1 = the transpose system,
 // 2 / 3 = BiCGStab's M^-1 p / M^-1 s).
+// The block size of a PC_BLOCK batch (its members share it).
+static int block_bs(const BatchHost& bh)
+{
+    for (const PlanState* P : bh.members)
+        if (P->bs_blocks > 0) return P->bs_blocks;
+    return 1;
+}
+
+// Exact sweeps of a one-system batch by the owner-computes kernel
+// (MRG_PART_SWEEPS=0: the ticketed sync-free kernel instead).
+static bool part_sweeps()
+{
+    static int on = -1;
+    if (on < 0) {
+        const char* e = std::getenv("MRG_PART_SWEEPS");
+        on = (e && e[0] == '0') ? 0 : 1;
+    }
+    return on == 1;
+}
+
+// The owner-computes launch shape of a batch's exact sweeps: one system
+// with a partitioned plan (not while the watchdog test hook withholds a
+// chunk), else parts = 0.
+void part_choice(const BatchHost& bh, int& parts, int& cells)
+{
+    const SysDev* S1 = bh.members.size() == 1 ? &bh.members[0]->sys : nullptr;
+    parts = (S1 && S1->nparts > 0 && bh.ctx->unpublished1 == 0 && part_sweeps()) ? S1->nparts : 0;
+    cells = parts ? S1->part_cells : 0;
+}
+
 static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, int trans, cudaStream_t st,
                                 int rho_chunks = 0)
 {
     Ctx* c = bh.ctx;
     if (cfg.pc < PC_DIC) return;
+    if (cfg.pc == PC_BLOCK) {
+        const int bs = block_bs(bh);
+        launch_block_sweep(bs, 1, trans, bh.d, grid_sweep(c), st);
+        launch_block_sweep(bs, 0, trans, bh.d, grid_sweep(c), st);
+        return;
+    }
     if (cfg.ordering == MRG_ORDER_EXACT) {
-        launch_sweep(prec, 1, trans, 1, 0, bh.d, grid_sweep(c), st);
-        launch_sweep(prec, 0, trans, 1, 0, bh.d, grid_sweep(c), st);
+        // one system with a partitioned plan: the owner-computes kernel
+        // (not while the watchdog test hook withholds a chunk)
+        int parts = 0, cells = 0;
+        part_choice(bh, parts, cells);
+        launch_sweep(prec, 1, trans, 1, 0, bh.d, grid_sweep(c), st, 0, parts, cells);
+        launch_sweep(prec, 0, trans, 1, 0, bh.d, grid_sweep(c), st, 0, parts, cells);
     } else {
         // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
         // nl == 1); one chunk per warp of the widest level
@@ -562,7 +650,9 @@ static void record_iteration_gs(BatchHost& bh, const Controls& cfg, cudaStream_t
         }
         if (gs) {
             if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
-            launch_gs_sweep(bh.d, grid_sweep(bh.ctx), st);
+            int parts = 0, cells = 0;
+            part_choice(bh, parts, cells);
+            launch_gs_sweep(bh.d, grid_sweep(bh.ctx), st, parts, cells);
             launch_rows(OP_GS_COPY, 0, bh.d, nt, ns, 0, st);
         }
     }
@@ -610,7 +700,7 @@ static void record_iteration(BatchHost& bh, const Controls& cfg, int prec, cudaS
 // launches (MRG_ITERATION=persistent; PCG and PBiCG).  Both give the same bits.
 static bool persistent_iteration(const BatchHost& bh, const Controls& cfg)
 {
-    if (cfg.solver == MRG_SOLVER_BICGSTAB || cfg.solver == MRG_SOLVER_SMOOTH) return false;
+    if (cfg.solver == MRG_SOLVER_BICGSTAB || cfg.solver == MRG_SOLVER_SMOOTH || cfg.pc == PC_BLOCK) return false;
     static int env = -1;
     if (env < 0) {
         const char* e = std::getenv("MRG_ITERATION");
@@ -645,7 +735,14 @@ static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int 
                       std::to_string(g_rows) + "/" + std::to_string(g_red) + "/" + std::to_string(g_sweep) + "/" +
                       std::to_string(bh.h.maxlevels) + "/" + std::to_string(any_general_iface(bh) ? 1 : 0) + "/" +
                       std::to_string(cfg.smoother) + "/" + std::to_string(cfg.n_sweeps) + "/s" +
-                      std::to_string(bh.tune.spmv) + (pers ? "/p" : "/l");
+                      std::to_string(bh.tune.spmv) + (pers ? "/p" : "/l") + (bh.ctx->unpublished1 ? "/u" : "");
+    {
+        // the owner-computes launch shape is fixed at capture: it depends on
+        // the member (a one-system batch), so it is part of the key
+        int parts = 0, cells = 0;
+        part_choice(bh, parts, cells);
+        key += "/q" + std::to_string(parts) + "x" + std::to_string(cells);
+    }
     auto it = bh.graphs.find(key);
     if (it != bh.graphs.end()) return it->second;
     cudaStream_t st = bh.ctx->st;

@@ -11,6 +11,8 @@
 
 #include "dev.h"
 #include "plan.h"
+#include "kernels.h"
+#include "blockpc.h"
 
 namespace mrg {
 
@@ -50,6 +52,8 @@ struct Controls {
     int smoother = 0;   // smoothSolver: MRG_SMOOTHER_*
     int gamg_coarsest = 10, gamg_post = 2, gamg_finest = 2;   // GAMG: nCellsInCoarsestLevel, nPostSweeps,
                                                               // nFinestSweeps
+    int gamg_max_post = 4, gamg_post_mult = 1;                // GAMG: maxPostSweeps, postSweepsLevelMultiplier
+    int gamg_scale = 1, gamg_agglomerator = 0;                // GAMG: scaleCorrection, MRG_AGGLOMERATOR_*
 };
 
 struct Perf {
@@ -123,9 +127,12 @@ struct PlanState {
     int32_t *g_ptr = nullptr, *g_src = nullptr;
     double* g_w = nullptr;
     float* g_w32 = nullptr;
+    int32_t *pt_ptr = nullptr, *part_rows = nullptr, *part_step = nullptr, *f_row = nullptr;
+    int32_t *f_loc = nullptr, *b_loc = nullptr, *b_row = nullptr;
     SysDev sys{};           // host mirror
     SysDev* d_sys = nullptr;
     int ntiles = 0;
+    int bs_blocks = 0;        // PC_BLOCK: the mesh's block size
     size_t nnz = 0, fnz = 0, bnz = 0;
     bool have32 = false, haveT = false, haveT32 = false;
     uint64_t scattered = 0;   // coefficient version scattered into the views
@@ -150,6 +157,11 @@ struct Mesh {
     uint64_t version = 0;
     std::unique_ptr<PlanState> plans[2];
     std::unique_ptr<Gamg> gamg;   // GAMG hierarchy (built at the first GAMG solve)
+    int part_target = kPartTarget;  // cells a part of the exact plan aims at (owner-computes sweeps)
+    std::unique_ptr<BlockHost> blocks;      // block structure (mrg_mesh_set_blocks), for PC_BLOCK
+    std::unique_ptr<BlockView> bviews[2];   // its views per ordering
+    std::vector<double> agglom_w;   // faceAreaPair weights of the faces (mrg_mesh_set_face_areas)
+    uint64_t agglom_version = 0;    // bumped by every mrg_mesh_set_face_areas
     PlanState& plan(int ordering);
     ~Mesh();
 };
@@ -207,6 +219,9 @@ void upload_coeffs(Mesh& m, const double* diag, const double* upper, const doubl
 
 // Single-system conveniences (batch of one).
 PlanState& prepare(Mesh& m, const Controls& c);
+// Owner-computes exact sweeps of a batch: parts (0: the ticketed kernel) and
+// cells a part.
+void part_choice(const BatchHost& bh, int& parts, int& cells);
 Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& c);
 
 void amul_device(Mesh& m, const double* d_x, double* d_y, int transpose);

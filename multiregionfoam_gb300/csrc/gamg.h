@@ -1,7 +1,9 @@
 // gamg.h -- GAMG solver (foam-order Gauss-Seidel smoothing) on the device.
 #pragma once
 #include <cstdint>
+#include <map>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "engine.h"
@@ -30,15 +32,28 @@ struct GamgLevel {
 struct Gamg {
     Ctx* ctx = nullptr;
     int n_coarsest = 10;
+    int agglomerator = 0;                              // MRG_AGGLOMERATOR_* the hierarchy was built with
+    uint64_t weights_version = 0;                      // the mesh's face-area version it was built from
     bool sym = true;
+    bool identity = false;                             // no level kept: the matrix is the coarsest
     std::vector<GamgLevel> lv;                         // lv[0]: the finest (the caller's mesh), unused
     double *lu = nullptr, *src_top = nullptr, *c_top = nullptr;
+    Scal** d_coarse_sc = nullptr;                      // the smoothed levels' scalar states
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        long long nodes = 0;
+    };
+    std::map<std::string, Graph> graphs;               // captured V-cycles
     ~Gamg();
 };
 
 // GAMG solve of a mesh (FP64, foam-order smoothing); b and x device arrays
 // in the caller's numbering.  The hierarchy is built at the first call (or
-// when nCellsInCoarsestLevel changes) from the current coefficients.
+// when nCellsInCoarsestLevel, the agglomerator or the face areas change)
+// from the current coefficients or the mesh's face areas.
 Perf gamg_solve(Mesh& m, const double* d_b, double* d_x, const Controls& cfg);
+
+// faceAreaPair weights of faces with area vectors sf[3 f .. 3 f + 2].
+std::vector<double> face_area_weights(const double* sf, int nf);
 
 }  // namespace mrg

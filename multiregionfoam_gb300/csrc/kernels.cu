@@ -595,6 +595,10 @@ __device__ void finalize(const Batch& B, const SysDev& S, RowOp op, const double
     case OP_BS_T:
         sc->omega = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
         break;
+    case OP_GSCALE_DOT:
+        // foam's GAMGSolver::scale: sf = (s, f) / stabilise((A f, f), VSMALL)
+        sc->alpha = sums[0] / (sums[1] >= 0.0 ? sums[1] + 1.0e-300 : sums[1] - 1.0e-300);
+        break;
     case OP_BS_XR: {
         sc->res = sums[0] / sc->nfac;
         sc->iter += 1;
@@ -1121,6 +1125,41 @@ __device__ __forceinline__ void tile_body(const Batch& B, const SysDev& S, int r
             r[i] = ri;
             acc[0] += fabs(ri);
         }
+    } else if constexpr (OP == OP_GSCALE_DOT) {
+        // GAMG scaleCorrection of a correction f (in p) against its source s
+        // (in r): q = A f, (s, f), (A f, f); padding rows add fma(0, 0, .)
+        const double* __restrict__ f = S.v64.p;
+        const double* __restrict__ sv = S.v64.r;
+        double* __restrict__ q = S.v64.q;
+        const int n = S.n;
+        for (int sl = sl0 + wid; sl < sl1; sl += kBlock / 32) {
+            const int i = sl * 32 + lane;
+            const double qi = ell_row<double>(sptr, acol, S.a_val, S.diag, f, i);
+            q[i] = qi;
+            const bool in = i < n;
+            const double fi = in ? __ldca(f + i) : 0.0;
+            acc[0] = __fma_rn(in ? __ldca(sv + i) : 0.0, fi, acc[0]);
+            acc[1] = __fma_rn(in ? qi : 0.0, fi, acc[1]);
+        }
+    } else if constexpr (OP == OP_GSCALE_SET || OP == OP_GSCALE_ADD) {
+        // f = sf f + (s - sf A f) / diag, one rounding per operation; the
+        // finest level adds it to x, a coarse level's correction is it
+        const double sf = S.sc->alpha;
+        const double* __restrict__ f = S.v64.p;
+        const double* __restrict__ sv = S.v64.r;
+        const double* __restrict__ q = S.v64.q;
+        const double* __restrict__ dg = S.diag;
+        double* __restrict__ x = S.v64.x;
+        const int n = S.n;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = r4 + k;
+            if (i < n) {
+                const double t = __ddiv_rn(__dsub_rn(__ldca(sv + i), __dmul_rn(sf, __ldca(q + i))), __ldca(dg + i));
+                const double v = __dadd_rn(__dmul_rn(sf, __ldca(f + i)), t);
+                x[i] = OP == OP_GSCALE_ADD ? __dadd_rn(x[i], v) : v;
+            }
+        }
     } else if constexpr (OP == OP_AMUL || OP == OP_TMUL) {
         const double* __restrict__ av = OP == OP_TMUL ? S.aT_val : S.a_val;
         const double* __restrict__ dg = S.diag;
@@ -1256,25 +1295,26 @@ struct OpTraits {
     static constexpr bool kRed = (OP == OP_SUMX || OP == OP_INIT_RES || OP == OP_RHO || OP == OP_SPMV_QP ||
                                   OP == OP_UPDATE || OP == OP_RESID64 || OP == OP_TO32 || OP == OP_FALLBACK64 ||
                                   OP == OP_BS_RHO0 || OP == OP_BS_V || OP == OP_BS_S || OP == OP_BS_T ||
-                                  OP == OP_BS_XR || OP == OP_GS_RES || OP == OP_RHO_CH);
+                                  OP == OP_BS_XR || OP == OP_GS_RES || OP == OP_RHO_CH || OP == OP_GSCALE_DOT);
     // Krylov-loop ops run only for systems whose loop is active; the
     // refinement ops only for systems whose outer loop is active.
     static constexpr bool kNeedActive = (OP == OP_RHO || OP == OP_PUPDATE || OP == OP_SPMV_QP ||
                                          OP == OP_UPDATE || OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE ||
                                          OP == OP_BS_RHO0 || OP == OP_BS_P || OP == OP_BS_V || OP == OP_BS_S ||
                                          OP == OP_BS_T || OP == OP_BS_XR || OP == OP_GS_COPY || OP == OP_GS_RES ||
-                                         OP == OP_SM_RES || OP == OP_SM_ADD || OP == OP_RHO_CH);
+                                         OP == OP_SM_RES || OP == OP_SM_ADD || OP == OP_RHO_CH ||
+                                         OP == OP_GSCALE_DOT || OP == OP_GSCALE_SET || OP == OP_GSCALE_ADD);
     static constexpr bool kNeedOuter = (OP == OP_RESID64 || OP == OP_TO32 || OP == OP_CORRECT);
     // Values reduced: the initial residual needs two (normFactor and
     // sum|r|), BiCGStab's t step ((t, s), (t, t)) and its update (sum|r|,
     // (r~, r)) too.  Every tree level costs one FP64 add per thread per value.
-    static constexpr int kNR = (OP == OP_INIT_RES || OP == OP_BS_T || OP == OP_BS_XR) ? 2 : 1;
+    static constexpr int kNR = (OP == OP_INIT_RES || OP == OP_BS_T || OP == OP_BS_XR || OP == OP_GSCALE_DOT) ? 2 : 1;
     // four consecutive rows per thread, no gathers: worth interleaving tiles
     static constexpr bool kElem = (OP == OP_SUMX || OP == OP_RHO || OP == OP_PUPDATE || OP == OP_UPDATE ||
                                    OP == OP_PRECOND_DIAG || OP == OP_PRECOND_NONE || OP == OP_TO32 ||
                                    OP == OP_CORRECT || OP == OP_KEEPBEST || OP == OP_BS_RHO0 || OP == OP_BS_P ||
                                    OP == OP_BS_S || OP == OP_BS_XR || OP == OP_GS_ARM || OP == OP_GS_COPY ||
-                                   OP == OP_SM_ADD);
+                                   OP == OP_SM_ADD || OP == OP_GSCALE_SET || OP == OP_GSCALE_ADD);
 };
 
 template <RowOp OP>
@@ -1807,24 +1847,29 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_spmv_warp(const Batch* __r
 // loop, and the producer waits (bounded) for the copies it issued before the
 // CTA exits.
 // S stages; XD: own x and diagonal staged (else the row warps load them);
-// CB: bytes a column index takes in a stage -- 2: only rounds with 16-bit
-// columns are staged (a round with 32-bit columns reads its indices and
-// coefficients from global memory), 4: both kinds.
+// N16: rounds whose slices have 16-bit column offsets copy those instead of
+// the 32-bit indices; CB: bytes a column index takes in a stage -- 2: only
+// rounds with 16-bit columns are staged (a round with 32-bit columns reads
+// its indices and coefficients from global memory), 4: both kinds; ER: a
+// warp releases its stage as soon as the stage's values are in registers
+// (before its gathers), else after its rows are done.
 template <typename V, int RP> struct StreamCfg;
-// one round per step: four stages of 11.1 KB (FP32) / two of 22.6 KB (FP64)
+// one round per step: three stages of 14.5 KB (FP32) / two of 22.6 KB (FP64),
+// 32-bit columns (measured fastest for one round per step on GB300)
 template <> struct StreamCfg<float, 1> {
-    static constexpr int S = 4, CB = 2;
-    static constexpr bool XD = true;
+    static constexpr int S = 3, CB = 4;
+    static constexpr bool XD = true, N16 = false, ER = false;
 };
 template <> struct StreamCfg<double, 1> {
     static constexpr int S = 2, CB = 4;
-    static constexpr bool XD = true;
+    static constexpr bool XD = true, N16 = false, ER = false;
 };
 // two rounds per step: five stages of 9.1 KB (FP32; own x and diagonal
-// loaded by the row warps), so three rounds are in flight while two compute
+// loaded by the row warps, 16-bit columns), so three rounds are in flight
+// while two compute
 template <> struct StreamCfg<float, 2> {
     static constexpr int S = 5, CB = 2;
-    static constexpr bool XD = false;
+    static constexpr bool XD = false, N16 = true, ER = true;
 };
 constexpr int kStageCap = kBlock * kMaxW;                              // entries per stage
 // stage head: the round's 9 slice bounds (48 B copied) at 0, its 8 slices'
@@ -1894,6 +1939,8 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
     constexpr int S = StreamCfg<V, RP>::S;
     constexpr bool XD = StreamCfg<V, RP>::XD;
     constexpr int CB = StreamCfg<V, RP>::CB;
+    constexpr bool N16 = StreamCfg<V, RP>::N16, ER = StreamCfg<V, RP>::ER;
+    static_assert(N16 || CB == 4, "32-bit columns need 4 bytes an entry");
     constexpr unsigned VO = (unsigned)(kStageHead + kStageCap * CB);   // coefficients, after the columns
     static_assert(S > RP, "the producer needs a stage beyond the ones a step computes");
     constexpr int NW = kBlock / 32;
@@ -1958,7 +2005,7 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                 const int a = min(w0 + lane, re), z = min(w0 + 32, re);
                 e = __ldg(sptr + 8 * a);
                 eend = __ldg(sptr + 8 * z);
-                cb = __ldg(cbase + 8 * a);
+                cb = N16 ? __ldg(cbase + 8 * a) : -1;
             };
             int ec, ecend, cbc, en = 0, enend = 0, cbn = 0;
             win(rb, ec, ecend, cbc);
@@ -1989,11 +2036,11 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                     const bool staged = cnt <= kStageCap && (narrow || CB == 4);
                     const unsigned colb = narrow ? 2u : 4u;
                     const unsigned bytes =
-                        80u + XB + (staged ? (unsigned)cnt * (colb + (unsigned)sizeof(V)) : 0u);
+                        (N16 ? 80u : 48u) + XB + (staged ? (unsigned)cnt * (colb + (unsigned)sizeof(V)) : 0u);
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(&full[stg], bytes);
                     bulk_to_smem(st, sptr + 8 * r, 48u, &full[stg]);
-                    bulk_to_smem(st + 64, cbase + 8 * r, 32u, &full[stg]);
+                    if constexpr (N16) bulk_to_smem(st + 64, cbase + 8 * r, 32u, &full[stg]);
                     if constexpr (XD) {
                         bulk_to_smem(st + kStageHead, p + (size_t)kBlock * r, kBlock * (unsigned)sizeof(V),
                                      &full[stg]);
@@ -2057,8 +2104,11 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
         const V* __restrict__ p = VP<V>::v(sS).p;
         V* __restrict__ q = VP<V>::v(sS).q;
         double acc[kMaxRed] = {0.0, 0.0};
-        for (int r = rb; r < re; r += RP, seq += RP) {
-            const int nr = min(RP, re - r);   // an FP32 segment may end on an odd round
+        // a step takes RP rounds, the segment's last step what is left (an
+        // FP32 segment may end on an odd round): the stage sequence advances
+        // by the rounds taken, as the producer's does
+        for (int r = rb, nr = 0; r < re; r += nr, seq += (unsigned)nr) {
+            nr = min(RP, re - r);
             bool ok = true;
             if (lane == 0)
                 for (int j = 0; j < nr && ok; ++j)
@@ -2083,7 +2133,7 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                 W[j] = on ? (spv[wid + 1] - ew[j]) >> 5 : 0;
                 o[j] = ew[j] - base + lane;
                 i_[j] = (NW * (r + j) + wid) * 32 + lane;
-                cb[j] = on ? reinterpret_cast<const int*>(stj[j] + 64)[wid] : -1;
+                cb[j] = (N16 && on) ? reinterpret_cast<const int*>(stj[j] + 64)[wid] : -1;
                 fast = fast && on && spv[NW] - base <= kStageCap && (cb[j] >= 0 || CB == 4) && W[j] <= kMaxW;
             }
             bool released = false;
@@ -2091,7 +2141,7 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
             // slice's base (0xFFFF: padding) or a 32-bit index
             auto col_of = [&](int j, int k) -> int {
                 const unsigned char* sc = stj[j] + kStageHead + XB;
-                if (cb[j] >= 0) {
+                if (N16 && cb[j] >= 0) {
                     const unsigned v = reinterpret_cast<const uint16_t*>(sc)[o[j] + k * 32];
                     return v == 0xFFFFu ? -1 : cb[j] + (int)v;
                 }
@@ -2119,10 +2169,12 @@ __global__ void __launch_bounds__(kBlock + 32, kMinCtas) k_spmv_stream(const Bat
                         av[j][k] = k < W[j] ? sval[o[j] + k * 32] : V(0);
                     }
                 }
-                __syncwarp();
-                if (lane == 0)
-                    for (int j = 0; j < nr; ++j) mbar_arrive(&empty[(seq + j) % S]);
-                released = true;
+                if constexpr (ER) {
+                    __syncwarp();
+                    if (lane == 0)
+                        for (int j = 0; j < nr; ++j) mbar_arrive(&empty[(seq + j) % S]);
+                    released = true;
+                }
 #pragma unroll
                 for (int j = 0; j < RP; ++j)
 #pragma unroll
@@ -2357,7 +2409,7 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_factor(const Batch* __rest
         if (t >= total) break;
         const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
         const SysDev& S = Ss[s];
-        if (c >= S.nchunks || S.pc < PC_DIC) continue;  // warp-uniform
+        if (c >= S.nchunks || !scalar_tri(S.pc)) continue;  // warp-uniform
         factor_row(S, c, lane, ctl, with32);
     }
     // Last warp out resets the work counter for the next launch.
@@ -2624,7 +2676,7 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
         const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
         const SysDev& S = Ss[s];
         const int nch = S.nchunks;
-        if (c >= nch || !S.sc->active || !S.syncfree || S.pc < PC_DIC || c == unpublished) continue;
+        if (c >= nch || !S.sc->active || !S.syncfree || !scalar_tri(S.pc) || c == unpublished) continue;
         const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans);
         sweep_chunk<V, FWD>(P, FWD ? c : nch - 1 - c, true, ctl, 0, false, false);
     }
@@ -2645,6 +2697,163 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_sweep_sf(const Batch* __re
     pdl_enter();
     const Batch B = *pB;
     sweep_sf_phase<V, FWD>(B, trans);
+}
+
+// ------------------------------------------------- owner-computes exact sweeps
+// The exact (foam-order) triangular sweep of a batch of one system whose
+// plan is cut into parts (ranges of part_cells caller cells, PlanHost):
+// each CTA computes one part, level by level, with one barrier between the
+// part's levels.  A dependency inside the part is read from the CTA's
+// shared-memory copy of the part's values; one in another part is waited
+// for (bounded), as in k_sweep_sf, and every value is also published in
+// global memory for the other parts and the next kernels.  Parts are
+// claimed in sweep order (forward ascending, backward descending) through a
+// ticket, and a row depends only on cells before it in sweep order, so a
+// CTA waits only on parts that running CTAs hold: no co-residency is
+// needed.  Each row's arithmetic, entries and their order are k_sweep_sf's,
+// so both give the same bits.  A cross-part wait costs a round trip
+// through L2; a level inside a part costs one barrier.
+constexpr int kPartBlock = 256;
+
+// One row of an owner-computes sweep, loaded ahead of its level: the start
+// value, the first kMaxW entries' columns, coefficients and places in the
+// part, and a look at each entry from another part (the sentinel when it is
+// not published yet).  None of it depends on the level's predecessors.
+template <typename V>
+struct PartRow {
+    V a0;
+    int e, W, slot;   // slot: the row's cell offset in its part
+    int col[kMaxW], loc[kMaxW];
+    V cf[kMaxW], pre[kMaxW];
+};
+
+template <typename V, bool FWD>
+__device__ __forceinline__ void part_load(const SweepPtrs<V>& P, const int2* __restrict__ rows,
+                                          const int* __restrict__ loc, const int* __restrict__ perm, int base,
+                                          const V* dep, int i, PartRow<V>& R)
+{
+    const int2 ew = __ldg(rows + i);
+    R.e = ew.x;
+    R.W = ew.y;
+    R.slot = __ldg(perm + i) - base;
+    R.a0 = FWD ? vmul(__ldg(P.rD + i), __ldca(P.r + i)) : __ldca(P.y + i);
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) R.col[k] = k < ew.y ? __ldg(P.col + ew.x + k * 32) : -1;
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        const bool on = R.col[k] >= 0;
+        R.cf[k] = on ? __ldg(P.coef + ew.x + k * 32) : V(0);
+        R.loc[k] = on ? __ldg(loc + ew.x + k * 32) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) R.pre[k] = (R.col[k] >= 0 && R.loc[k] < 0) ? ld_relaxed(dep + R.col[k]) : V(0);
+}
+
+// The row's value: entries in slot order, a dependency in the part from
+// shared memory, one outside from its look-ahead when that was published,
+// else waited for; entries beyond kMaxW loaded here.
+template <typename V>
+__device__ __forceinline__ V part_value(const SweepPtrs<V>& P, const int* __restrict__ loc, const V* dep,
+                                        const V* own, const PartRow<V>& R, Ctl* ctl)
+{
+    V acc = R.a0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        if (R.col[k] < 0) continue;
+        const V v = R.loc[k] >= 0 ? own[R.loc[k]] : (!is_sent(R.pre[k]) ? R.pre[k] : wait_ready(dep + R.col[k], ctl));
+        acc = vfma(-R.cf[k], v, acc);
+    }
+    for (int k = kMaxW; k < R.W; ++k) {
+        const int e = R.e + k * 32;
+        const int col = __ldg(P.col + e);
+        if (col < 0) continue;
+        const int l = __ldg(loc + e);
+        acc = vfma(-__ldg(P.coef + e), l >= 0 ? own[l] : wait_ready(dep + col, ctl), acc);
+    }
+    return acc;
+}
+
+// The part's rows in sweep order are taken kPartBlock at a time (a window,
+// usually several levels): every thread loads its row of the window, and of
+// the next window, ahead; the window's levels then run in turn, one barrier
+// each, each thread computing its row at its level.
+template <typename V, bool FWD>
+__global__ void __launch_bounds__(kPartBlock, 1) k_sweep_part(const Batch* __restrict__ pB, int trans)
+{
+    extern __shared__ __align__(16) unsigned char dyn_part[];
+    V* own = reinterpret_cast<V*>(dyn_part);
+    __shared__ int s_part;
+    pdl_enter();
+    const Batch B = *pB;
+    Ctl* ctl = B.ctl;
+    const SysDev& S = B.sys[0];
+    if (threadIdx.x == 0) s_part = (int)atomicAdd(&ctl->ticket[6], 1u);
+    __syncthreads();
+    const int np = S.nparts;
+    if (s_part < np && S.sc->active && S.syncfree && scalar_tri(S.pc)) {
+        const int part = FWD ? s_part : np - 1 - s_part;
+        const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans);
+        const int* __restrict__ loc = FWD ? S.f_loc : S.b_loc;
+        const int2* __restrict__ rows = FWD ? S.f_row : S.b_row;
+        const int* __restrict__ prow = S.part_rows;
+        const int* __restrict__ pstep = S.part_step;
+        const int* __restrict__ perm = S.perm;
+        const int base = part * S.part_cells;
+        const int r0 = __ldg(S.pt_ptr + part), r1 = __ldg(S.pt_ptr + part + 1), nr = r1 - r0;
+        V* __restrict__ y = P.y;
+        V* __restrict__ w = P.w;
+        const V* dep = FWD ? y : w;
+        const int tid = (int)threadIdx.x;
+        auto at = [&](int j) { return FWD ? r0 + j : r1 - 1 - j; };   // j-th row in sweep order
+        // two row buffers by name (a window's rows and the next one's), so
+        // they stay in registers
+        auto fetch = [&](int j, PartRow<V>& R, int& ri, int& rs) {
+            ri = -1;
+            if (j < nr) {
+                const int q = at(j);
+                ri = __ldg(prow + q);
+                rs = __ldg(pstep + q);
+                part_load<V, FWD>(P, rows, loc, perm, base, dep, ri, R);
+            }
+        };
+        auto window = [&](int w0, const PartRow<V>& R, int ri, int rs) {
+            const int sa = __ldg(pstep + at(w0)), sb = __ldg(pstep + at(min(w0 + kPartBlock, nr) - 1));
+            for (int st = sa;; st += FWD ? 1 : -1) {
+                if (ri >= 0 && rs == st) {
+                    const V acc = part_value<V>(P, loc, dep, own, R, ctl);
+                    own[R.slot] = acc;
+                    if (FWD) {
+                        st_relaxed(y + ri, acc);
+                        w[ri] = sent<V>();
+                    } else {
+                        st_relaxed(w + ri, acc);
+                        y[ri] = sent<V>();
+                    }
+                }
+                __syncthreads();
+                if (st == sb) break;
+            }
+        };
+        PartRow<V> RA, RB;
+        int ia, sa, ib, sb;
+        fetch(tid, RA, ia, sa);
+        for (int w0 = 0; w0 < nr; w0 += 2 * kPartBlock) {
+            fetch(w0 + kPartBlock + tid, RB, ib, sb);
+            window(w0, RA, ia, sa);
+            if (w0 + kPartBlock >= nr) break;
+            fetch(w0 + 2 * kPartBlock + tid, RA, ia, sa);
+            window(w0 + kPartBlock, RB, ib, sb);
+        }
+    }
+    // the last CTA out resets the ticket for the next launch
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[7], 1u) == gridDim.x - 1u) {
+            ctl->ticket[6] = 0u;
+            ctl->ticket[7] = 0u;
+            __threadfence();
+        }
+    }
 }
 
 // One level L of a levelled sweep for every system that has it: forward
@@ -2691,7 +2900,7 @@ __device__ __forceinline__ void sweep_lvl_phase(const Batch& B, int L, int trans
                 cur = s;
                 const SysDev& S = B.sys[cur];
                 const int nl = S.nlevels;
-                ok = S.sc->active && S.pc >= PC_DIC && !S.syncfree &&
+                ok = S.sc->active && scalar_tri(S.pc) && !S.syncfree &&
                      (FWD ? (L >= 1 && L <= nl - 1) : (L <= nl - 2 || (nl == 1 && L == 0)));
                 if (ok) {
                     lvl0_end = S.chunk_start[S.lvl_chunk[1 < nl ? 1 : nl]];
@@ -2742,28 +2951,59 @@ __global__ void __launch_bounds__(kBlock, PAIRS ? kSweepPairCtas : kMinCtas)
 //   acc / diag_i.  The ELL row holds foam's per-cell order, and its source
 //   codes tell the three kinds of entry apart (>= 2F interface, >= F this
 //   cell is the face's upper cell so the neighbour is its lower one).
-__device__ __forceinline__ void gs_row(const SysDev& S, int i, Ctl* ctl)
+// Entries are taken kMaxW at a time: a round's codes, columns and
+// coefficients are loaded together, then its values (x loads issued before
+// the first wait), then the FMAs in slot order.  Own = nullptr: every lower
+// neighbour is waited for in y; else a lower neighbour whose cell lies in
+// [base, base + pc) is read from own[cell - base] (owner-computes kernel).
+__device__ __forceinline__ double gs_row_acc(const SysDev& S, int i, Ctl* ctl, const double* own, int base, int pc)
 {
     const int F = S.nf;
     const int sl = i >> 5, lane = i & 31;
     const int e0 = __ldg(S.a_sptr + sl), W = (__ldg(S.a_sptr + sl + 1) - e0) >> 5;
     const double* __restrict__ x = S.v64.x;
-    double* y = S.v64.y;
+    const double* y = S.v64.y;
     double acc = __ldca(S.v64.b + i);
-    for (int k = 0; k < W; ++k) {
-        const int e = e0 + k * 32 + lane;
-        const int sc = __ldg(S.a_src + e);
-        if (sc >= 2 * F) acc = __fma_rn(-__ldg(S.a_val + e), __ldca(x + __ldg(S.a_col + e)), acc);
+    if (S.ni > 0) {
+        // interface entries first (foam moves them to the source)
+        for (int k = 0; k < W; ++k) {
+            const int e = e0 + k * 32 + lane;
+            const int sc = __ldg(S.a_src + e);
+            if (sc >= 2 * F) acc = __fma_rn(-__ldg(S.a_val + e), __ldca(x + __ldg(S.a_col + e)), acc);
+        }
     }
-    for (int k = 0; k < W; ++k) {
-        const int e = e0 + k * 32 + lane;
-        const int sc = __ldg(S.a_src + e);
-        if (sc < 0 || sc >= 2 * F) continue;
-        const int col = __ldg(S.a_col + e);
-        const double v = sc >= F ? wait_ready(y + col, ctl) : __ldca(x + col);
-        acc = __fma_rn(-__ldg(S.a_val + e), v, acc);
+    for (int k0 = 0; k0 < W; k0 += kMaxW) {
+        int sc[kMaxW], col[kMaxW];
+        double a[kMaxW], v[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            const int e = e0 + (k0 + k) * 32 + lane;
+            sc[k] = k0 + k < W ? __ldg(S.a_src + e) : -1;
+            if (sc[k] >= 2 * F) sc[k] = -1;   // interface entry: done above
+            col[k] = sc[k] >= 0 ? __ldg(S.a_col + e) : 0;
+            a[k] = sc[k] >= 0 ? __ldg(S.a_val + e) : 0.0;
+        }
+        int loc[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            loc[k] = -1;
+            if (own && sc[k] >= F) loc[k] = __ldg(S.perm + col[k]) - base;
+            v[k] = (sc[k] >= 0 && sc[k] < F) ? __ldca(x + col[k]) : 0.0;   // upper neighbours: old values
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            if (sc[k] < 0) continue;
+            if (sc[k] >= F)
+                v[k] = (unsigned)loc[k] < (unsigned)pc ? own[loc[k]] : wait_ready(y + col[k], ctl);
+            acc = __fma_rn(-a[k], v[k], acc);
+        }
     }
-    st_relaxed(y + i, __ddiv_rn(acc, __ldg(S.diag + i)));
+    return __ddiv_rn(acc, __ldg(S.diag + i));
+}
+
+__device__ __forceinline__ void gs_row(const SysDev& S, int i, Ctl* ctl)
+{
+    st_relaxed(S.v64.y + i, gs_row_acc(S, i, ctl, nullptr, 0, 0));
 }
 
 __global__ void __launch_bounds__(kBlock, kMinCtas) k_gs_sweep(const Batch* __restrict__ pB)
@@ -2793,6 +3033,393 @@ __global__ void __launch_bounds__(kBlock, kMinCtas) k_gs_sweep(const Batch* __re
         if (atomicAdd(&ctl->ticket[3], 1u) == nw - 1u) {
             ctl->ticket[2] = 0u;
             ctl->ticket[3] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// One Gauss-Seidel sweep of a batch of one system by owner-computes parts
+// (k_sweep_part's scheme): each CTA computes its part's rows level by level,
+// a lower neighbour inside the part read from shared memory, one in
+// another part waited for; upper neighbours and interfaces read x.  Rows as
+// gs_row, so both kernels give the same bits.
+// A Gauss-Seidel row loaded ahead of its level (rows without interface
+// entries and at most kMaxW entries; others are computed by gs_row_acc at
+// their level): codes, columns, coefficients, the old x of upper neighbours,
+// each lower neighbour's place in the part or a look at its published value.
+struct GsRow {
+    int slow, slot;   // slot: the row's cell offset in its part
+    int sc[kMaxW], col[kMaxW], loc[kMaxW];
+    double a[kMaxW], v[kMaxW], b, d;
+};
+
+__device__ __forceinline__ void gs_load(const SysDev& S, int i, int base, int pc, GsRow& R)
+{
+    const int F = S.nf;
+    const int sl = i >> 5, lane = i & 31;
+    const int e0 = __ldg(S.a_sptr + sl), W = (__ldg(S.a_sptr + sl + 1) - e0) >> 5;
+    R.slow = S.ni > 0 || W > kMaxW;
+    R.slot = __ldg(S.perm + i) - base;
+    if (R.slow) return;
+    R.b = __ldca(S.v64.b + i);
+    R.d = __ldg(S.diag + i);
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        const int e = e0 + k * 32 + lane;
+        R.sc[k] = k < W ? __ldg(S.a_src + e) : -1;
+        R.col[k] = R.sc[k] >= 0 ? __ldg(S.a_col + e) : 0;
+        R.a[k] = R.sc[k] >= 0 ? __ldg(S.a_val + e) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        R.loc[k] = R.sc[k] >= F ? __ldg(S.perm + R.col[k]) - base : -1;
+        if (R.sc[k] >= 0 && R.sc[k] < F)
+            R.v[k] = __ldca(S.v64.x + R.col[k]);   // upper neighbour: old value
+        else if (R.sc[k] >= F && (unsigned)R.loc[k] >= (unsigned)pc)
+            R.v[k] = ld_relaxed(S.v64.y + R.col[k]);   // another part's: a look
+        else
+            R.v[k] = 0.0;
+    }
+}
+
+__device__ __forceinline__ double gs_value(const SysDev& S, int i, const GsRow& R, Ctl* ctl, const double* own,
+                                           int base, int pc)
+{
+    if (R.slow) return gs_row_acc(S, i, ctl, own, base, pc);
+    const int F = S.nf;
+    double acc = R.b;
+#pragma unroll
+    for (int k = 0; k < kMaxW; ++k) {
+        if (R.sc[k] < 0) continue;
+        double v = R.v[k];
+        if (R.sc[k] >= F)
+            v = (unsigned)R.loc[k] < (unsigned)pc ? own[R.loc[k]]
+                                                   : (!is_sent(v) ? v : wait_ready(S.v64.y + R.col[k], ctl));
+        acc = __fma_rn(-R.a[k], v, acc);
+    }
+    return __ddiv_rn(acc, R.d);
+}
+
+__global__ void __launch_bounds__(kPartBlock, 1) k_gs_part(const Batch* __restrict__ pB)
+{
+    extern __shared__ __align__(16) unsigned char dyn_part[];
+    double* own = reinterpret_cast<double*>(dyn_part);
+    __shared__ int s_part;
+    pdl_enter();
+    const Batch B = *pB;
+    Ctl* ctl = B.ctl;
+    const SysDev& S = B.sys[0];
+    if (threadIdx.x == 0) s_part = (int)atomicAdd(&ctl->ticket[6], 1u);
+    __syncthreads();
+    if (s_part < S.nparts && S.sc->active && S.syncfree) {
+        const int part = s_part, pc = S.part_cells, base = part * pc;
+        double* y = S.v64.y;
+        const int* __restrict__ prow = S.part_rows;
+        const int* __restrict__ pstep = S.part_step;
+        const int r0 = __ldg(S.pt_ptr + part), nr = __ldg(S.pt_ptr + part + 1) - r0;
+        const int tid = (int)threadIdx.x;
+        auto fetch = [&](int j, GsRow& R, int& ri, int& rs) {
+            ri = -1;
+            if (j < nr) {
+                ri = __ldg(prow + r0 + j);
+                rs = __ldg(pstep + r0 + j);
+                gs_load(S, ri, base, pc, R);
+            }
+        };
+        auto window = [&](int w0, const GsRow& R, int ri, int rs) {
+            const int sa = __ldg(pstep + r0 + w0), sb = __ldg(pstep + r0 + min(w0 + kPartBlock, nr) - 1);
+            for (int st = sa; st <= sb; ++st) {
+                if (ri >= 0 && rs == st) {
+                    const double yi = gs_value(S, ri, R, ctl, own, base, pc);
+                    own[R.slot] = yi;
+                    st_relaxed(y + ri, yi);
+                }
+                __syncthreads();
+            }
+        };
+        GsRow RA, RB;
+        int ia, sa, ib, sb;
+        fetch(tid, RA, ia, sa);
+        for (int w0 = 0; w0 < nr; w0 += 2 * kPartBlock) {
+            fetch(w0 + kPartBlock + tid, RB, ib, sb);
+            window(w0, RA, ia, sa);
+            if (w0 + kPartBlock >= nr) break;
+            fetch(w0 + 2 * kPartBlock + tid, RA, ia, sa);
+            window(w0 + kPartBlock, RB, ib, sb);
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[7], 1u) == gridDim.x - 1u) {
+            ctl->ticket[6] = 0u;
+            ctl->ticket[7] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------ block preconditioner
+// The block incomplete factorisation of foam-extend's block Cholesky
+// preconditioner (BlockCholeskyPrecon) on bs x bs blocks, restated:
+//   factor   cells in order: D_c = A_cc - sum over faces f with upper cell c
+//            (ascending) of L_f inv(D_l) U_f, then dD_c = inv(D_c);
+//   apply    x_c = dD_c r_c; forward, faces ascending: x_u -= dD_u (L_f x_l);
+//            backward, faces descending: x_l -= dD_l (U_f x_u).
+// U_f is the block A[l][u], L_f the block A[u][l].  Every product sums its
+// terms in index order from the first, one rounding per multiply and add;
+// the inverse is Gauss-Jordan elimination without pivoting.  Cells run
+// sync-free over the cell plan's chunks (one thread a cell, one warp a
+// chunk), each dependency's values waited for (bounded) as in k_sweep_sf.
+
+// Gather: D[c][a][b], U[f][a][b], L[f][b][a] (row-major blocks).
+__global__ void k_block_gather(const BlockDev* __restrict__ pb, int n, int nf, int bs,
+                               const double* __restrict__ rd, const double* __restrict__ ru,
+                               const double* __restrict__ rl)
+{
+    const BlockDev& K = *pb;
+    const long long bb = (long long)bs * bs, nd = (long long)n * bb, tot = nd + (long long)nf * bb;
+    const double* lo = rl ? rl : ru;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        if (t < nd) {
+            const int code = K.dmap[t];
+            const int a = (int)((t % bb) / bs), b = (int)(t % bs);
+            K.D[t] = code >= 0 ? rd[code] : (a < b ? ru[-1 - code] : lo[-1 - code]);
+        } else {
+            const long long e = t - nd, f = e / bb;
+            const int a = (int)((e % bb) / bs), b = (int)(e % bs);
+            const int k = K.fmap[e];   // scalar face (bs l + a, bs u + b)
+            K.U[e] = ru[k];
+            K.L[f * bb + b * bs + a] = lo[k];
+        }
+    }
+}
+
+template <int BS>
+__device__ __forceinline__ void bmat_mul(const double (&A)[BS][BS], const double (&B)[BS][BS], double (&C)[BS][BS])
+{
+#pragma unroll
+    for (int a = 0; a < BS; ++a)
+#pragma unroll
+        for (int b = 0; b < BS; ++b) {
+            double acc = __dmul_rn(A[a][0], B[0][b]);
+#pragma unroll
+            for (int k = 1; k < BS; ++k) acc = __dadd_rn(acc, __dmul_rn(A[a][k], B[k][b]));
+            C[a][b] = acc;
+        }
+}
+
+template <int BS>
+__device__ __forceinline__ void bmat_vec(const double (&A)[BS][BS], const double (&v)[BS], double (&o)[BS])
+{
+#pragma unroll
+    for (int a = 0; a < BS; ++a) {
+        double acc = __dmul_rn(A[a][0], v[0]);
+#pragma unroll
+        for (int k = 1; k < BS; ++k) acc = __dadd_rn(acc, __dmul_rn(A[a][k], v[k]));
+        o[a] = acc;
+    }
+}
+
+// Gauss-Jordan without pivoting: for each k, row k scaled by 1 / M[k][k],
+// then every other row i minus M[i][k] times row k (both halves).
+template <int BS>
+__device__ __forceinline__ void bmat_inv(double (&M)[BS][BS], double (&I)[BS][BS])
+{
+#pragma unroll
+    for (int a = 0; a < BS; ++a)
+#pragma unroll
+        for (int b = 0; b < BS; ++b) I[a][b] = a == b ? 1.0 : 0.0;
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+        const double p = __ddiv_rn(1.0, M[k][k]);
+#pragma unroll
+        for (int j = 0; j < BS; ++j) {
+            M[k][j] = __dmul_rn(M[k][j], p);
+            I[k][j] = __dmul_rn(I[k][j], p);
+        }
+#pragma unroll
+        for (int i = 0; i < BS; ++i) {
+            if (i == k) continue;
+            const double f = M[i][k];
+#pragma unroll
+            for (int j = 0; j < BS; ++j) {
+                M[i][j] = __dsub_rn(M[i][j], __dmul_rn(f, M[k][j]));
+                I[i][j] = __dsub_rn(I[i][j], __dmul_rn(f, I[k][j]));
+            }
+        }
+    }
+}
+
+template <int BS>
+__device__ __forceinline__ void block_factor_cell(const BlockDev& K, int c, int lane, Ctl* ctl)
+{
+    const int r0 = __ldg(K.chunk_start + c), r1 = __ldg(K.chunk_start + c + 1);
+    const int i = r0 + lane;
+    if (i >= r1) return;
+    constexpr int BB = BS * BS;
+    const int cell = __ldg(K.perm + i);
+    double M[BS][BS];
+#pragma unroll
+    for (int a = 0; a < BS; ++a)
+#pragma unroll
+        for (int b = 0; b < BS; ++b) M[a][b] = __ldg(K.D + (size_t)cell * BB + a * BS + b);
+    const int e0 = __ldg(K.f_sptr + c), W = (__ldg(K.f_sptr + c + 1) - e0) >> 5;
+    for (int k = 0; k < W; ++k) {
+        const int e = e0 + k * 32 + lane;
+        const int l = __ldg(K.f_col + e);
+        if (l < 0) continue;
+        const int f = __ldg(K.f_src + e) - K.nf;   // A[c][l]: this cell is the face's upper cell
+        double Dl[BS][BS], Uf[BS][BS], Lf[BS][BS], T[BS][BS], P[BS][BS];
+#pragma unroll
+        for (int a = 0; a < BS; ++a)
+#pragma unroll
+            for (int b = 0; b < BS; ++b) {
+                Uf[a][b] = __ldg(K.U + (size_t)f * BB + a * BS + b);
+                Lf[a][b] = __ldg(K.L + (size_t)f * BB + a * BS + b);
+            }
+#pragma unroll
+        for (int a = 0; a < BS; ++a)
+#pragma unroll
+            for (int b = 0; b < BS; ++b) Dl[a][b] = wait_ready(K.dD + (size_t)l * BB + a * BS + b, ctl);
+        bmat_mul<BS>(Dl, Uf, T);
+        bmat_mul<BS>(Lf, T, P);
+#pragma unroll
+        for (int a = 0; a < BS; ++a)
+#pragma unroll
+            for (int b = 0; b < BS; ++b) M[a][b] = __dsub_rn(M[a][b], P[a][b]);
+    }
+    double I[BS][BS];
+    bmat_inv<BS>(M, I);
+#pragma unroll
+    for (int a = 0; a < BS; ++a)
+#pragma unroll
+        for (int b = 0; b < BS; ++b) st_relaxed(K.dD + (size_t)i * BB + a * BS + b, I[a][b]);
+}
+
+template <int BS>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_block_factor(const Batch* __restrict__ pB)
+{
+    pdl_enter();
+    const Batch B = *pB;
+    Ctl* ctl = B.ctl;
+    const int lane = threadIdx.x & 31, nsys = B.nsys;
+    const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->ticket[0], 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
+        const SysDev& S = B.sys[s];
+        if (S.pc != PC_BLOCK) continue;
+        const BlockDev& K = *S.blk;
+        if (c >= K.nchunks) continue;   // warp-uniform
+        block_factor_cell<BS>(K, c, lane, ctl);
+    }
+    if (lane == 0) {
+        const unsigned nw = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[1], 1u) == nw - 1u) {
+            ctl->ticket[0] = 0u;
+            ctl->ticket[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+template <int BS, bool FWD>
+__device__ __forceinline__ void block_sweep_cell(const BlockDev& K, int c, int lane, const double* r, double* y,
+                                                 double* w, Ctl* ctl)
+{
+    const int r0 = __ldg(K.chunk_start + c), r1 = __ldg(K.chunk_start + c + 1);
+    const int i = r0 + lane;
+    if (i >= r1) return;
+    constexpr int BB = BS * BS;
+    double dD[BS][BS], x[BS];
+#pragma unroll
+    for (int a = 0; a < BS; ++a)
+#pragma unroll
+        for (int b = 0; b < BS; ++b) dD[a][b] = __ldcg(K.dD + (size_t)i * BB + a * BS + b);
+    int vi[BS];
+#pragma unroll
+    for (int a = 0; a < BS; ++a) vi[a] = __ldg(K.vmap + (size_t)i * BS + a);
+    if (FWD) {
+        double rc[BS];
+#pragma unroll
+        for (int a = 0; a < BS; ++a) rc[a] = __ldca(r + vi[a]);
+        bmat_vec<BS>(dD, rc, x);
+    } else {
+#pragma unroll
+        for (int a = 0; a < BS; ++a) x[a] = __ldca(y + vi[a]);
+    }
+    const int* sptr = FWD ? K.f_sptr : K.b_sptr;
+    const int* col = FWD ? K.f_col : K.b_col;
+    const int* src = FWD ? K.f_src : K.b_src;
+    const double* blk = FWD ? K.L : K.U;
+    const double* dep = FWD ? y : w;
+    const int e0 = __ldg(sptr + c), W = (__ldg(sptr + c + 1) - e0) >> 5;
+    for (int k = 0; k < W; ++k) {
+        const int e = e0 + k * 32 + lane;
+        const int l = __ldg(col + e);
+        if (l < 0) continue;
+        const int code = __ldg(src + e);
+        const int f = FWD ? code - K.nf : code;   // forward: A[c][l] (lower); backward: A[c][u] (upper)
+        double Bf[BS][BS], v[BS], t[BS], u[BS];
+#pragma unroll
+        for (int a = 0; a < BS; ++a)
+#pragma unroll
+            for (int b = 0; b < BS; ++b) Bf[a][b] = __ldg(blk + (size_t)f * BB + a * BS + b);
+#pragma unroll
+        for (int a = 0; a < BS; ++a) v[a] = wait_ready(dep + __ldg(K.vmap + (size_t)l * BS + a), ctl);
+        bmat_vec<BS>(Bf, v, t);
+        bmat_vec<BS>(dD, t, u);
+#pragma unroll
+        for (int a = 0; a < BS; ++a) x[a] = __dsub_rn(x[a], u[a]);
+    }
+#pragma unroll
+    for (int a = 0; a < BS; ++a) {
+        if (FWD) {
+            st_relaxed(y + vi[a], x[a]);
+            w[vi[a]] = sent<double>();
+        } else {
+            st_relaxed(w + vi[a], x[a]);
+            y[vi[a]] = sent<double>();
+        }
+    }
+}
+
+template <int BS, bool FWD>
+__global__ void __launch_bounds__(kBlock, kMinCtas) k_block_sweep(const Batch* __restrict__ pB, int vs)
+{
+    pdl_enter();
+    const Batch B = *pB;
+    Ctl* ctl = B.ctl;
+    const int lane = threadIdx.x & 31, nsys = B.nsys;
+    const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
+    const int slot = FWD ? 2 : 4;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->ticket[slot], 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
+        const SysDev& S = B.sys[s];
+        if (S.pc != PC_BLOCK || !S.sc->active) continue;
+        const BlockDev& K = *S.blk;
+        if (c >= K.nchunks) continue;   // warp-uniform
+        const Vecs<double>& v = S.v64;
+        const double* r = vs == 2 ? v.wT : v.r;
+        double* y = vs == 3 ? v.yT : v.y;
+        double* w = vs == 2 ? v.p : (vs == 3 ? v.pT : v.w);
+        block_sweep_cell<BS, FWD>(K, FWD ? c : K.nchunks - 1 - c, lane, r, y, w, ctl);
+    }
+    if (lane == 0) {
+        const unsigned nw = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&ctl->ticket[slot + 1], 1u) == nw - 1u) {
+            ctl->ticket[slot] = 0u;
+            ctl->ticket[slot + 1] = 0u;
             __threadfence();
         }
     }
@@ -3034,6 +3661,12 @@ void set_device_sms(int nsm)
                          (int)stream_smem<double, 1>());
     cudaFuncSetAttribute(k_spmv_stream<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)stream_smem<float, 2>());
+    const int part_smem = (int)(kPartMaxCells * sizeof(double));
+    cudaFuncSetAttribute(k_sweep_part<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, part_smem);
+    cudaFuncSetAttribute(k_sweep_part<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, part_smem);
+    cudaFuncSetAttribute(k_sweep_part<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, part_smem);
+    cudaFuncSetAttribute(k_sweep_part<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, part_smem);
+    cudaFuncSetAttribute(k_gs_part, cudaFuncAttributeMaxDynamicSharedMemorySize, part_smem);
 }
 int persistent_grid() { return g_grid_cap; }
 void add_launches(long long d) { g_launches.fetch_add((unsigned long long)d); }
@@ -3080,6 +3713,9 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
             MRG_CASE64(OP_GS_RES)
             MRG_CASE64(OP_SM_RES)
             MRG_CASE64(OP_SM_ADD)
+            MRG_CASE64(OP_GSCALE_DOT)
+            MRG_CASE64(OP_GSCALE_SET)
+            MRG_CASE64(OP_GSCALE_ADD)
         default: break;
         }
     } else {
@@ -3123,11 +3759,24 @@ void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st)
 }
 
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
-                  cudaStream_t st, int rho_chunks)
+                  cudaStream_t st, int rho_chunks, int parts, int part_cells)
 {
     ++g_launches;
     if (grid < 1) grid = 1;
-    if (syncfree) {
+    if (syncfree && parts > 0) {
+        const size_t smem = (size_t)part_cells * (precision == 0 ? sizeof(double) : sizeof(float));
+        if (precision == 0) {
+            if (fwd)
+                launch_pdl(k_sweep_part<double, true>, parts, kPartBlock, smem, st, dB, trans);
+            else
+                launch_pdl(k_sweep_part<double, false>, parts, kPartBlock, smem, st, dB, trans);
+        } else {
+            if (fwd)
+                launch_pdl(k_sweep_part<float, true>, parts, kPartBlock, smem, st, dB, trans);
+            else
+                launch_pdl(k_sweep_part<float, false>, parts, kPartBlock, smem, st, dB, trans);
+        }
+    } else if (syncfree) {
         if (precision == 0) {
             if (fwd)
                 launch_pdl(k_sweep_sf<double, true>, grid, kBlock, 0, st, dB, trans);
@@ -3171,10 +3820,50 @@ void launch_iface_gather(int precision, int which, const Batch* dB, int grid, cu
         launch_pdl(k_iface_gather<float>, grid, 256, 0, st, dB, which);
 }
 
-void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st)
+void launch_block_gather(const BlockDev* d_blk, int n, int nf, int bs, const double* raw_diag,
+                         const double* raw_upper, const double* raw_lower, cudaStream_t st)
 {
     ++g_launches;
-    launch_pdl(k_gs_sweep, grid, kBlock, 0, st, dB);
+    const long long tot = ((long long)n + nf) * bs * bs;
+    const int grid = (int)std::max<long long>(1, std::min<long long>((tot + 255) / 256, 4096));
+    k_block_gather<<<grid, 256, 0, st>>>(d_blk, n, nf, bs, raw_diag, raw_upper, raw_lower);
+}
+
+void launch_block_factor(int bs, const Batch* dB, int grid, cudaStream_t st)
+{
+    ++g_launches;
+    switch (bs) {
+    case 1: launch_pdl(k_block_factor<1>, grid, kBlock, 0, st, dB); break;
+    case 2: launch_pdl(k_block_factor<2>, grid, kBlock, 0, st, dB); break;
+    case 3: launch_pdl(k_block_factor<3>, grid, kBlock, 0, st, dB); break;
+    default: launch_pdl(k_block_factor<4>, grid, kBlock, 0, st, dB); break;
+    }
+}
+
+void launch_block_sweep(int bs, int fwd, int vs, const Batch* dB, int grid, cudaStream_t st)
+{
+    ++g_launches;
+#define MRG_BSWEEP(N)                                                       \
+    if (fwd)                                                                \
+        launch_pdl(k_block_sweep<N, true>, grid, kBlock, 0, st, dB, vs);    \
+    else                                                                    \
+        launch_pdl(k_block_sweep<N, false>, grid, kBlock, 0, st, dB, vs);
+    switch (bs) {
+    case 1: MRG_BSWEEP(1) break;
+    case 2: MRG_BSWEEP(2) break;
+    case 3: MRG_BSWEEP(3) break;
+    default: MRG_BSWEEP(4) break;
+    }
+#undef MRG_BSWEEP
+}
+
+void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st, int parts, int part_cells)
+{
+    ++g_launches;
+    if (parts > 0)
+        launch_pdl(k_gs_part, parts, kPartBlock, (size_t)part_cells * sizeof(double), st, dB);
+    else
+        launch_pdl(k_gs_sweep, grid, kBlock, 0, st, dB);
 }
 
 void launch_permute(int to_internal, const SysDev* d, int s, const double* src, double* dst, int n, cudaStream_t st)

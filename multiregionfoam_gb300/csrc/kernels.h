@@ -45,6 +45,9 @@ enum RowOp {
     OP_SM_RES,          // smoothSolver DIC / DILU step: r = b - A x
     OP_SM_ADD,          // smoothSolver DIC / DILU step: x += w (w = M^-1 r)
     OP_RHO_CH,          // FP32 PCG, levelled DIC: rho = sum of the sweeps' per-chunk (r, w), beta
+    OP_GSCALE_DOT,      // GAMG scaleCorrection: q = A p, (r, p) and (q, p), sf = (r, p) / (q, p)
+    OP_GSCALE_SET,      // GAMG scaleCorrection, coarse level: x = sf p + (r - sf q) / diag
+    OP_GSCALE_ADD,      // GAMG scaleCorrection, finest level: x += sf p + (r - sf q) / diag
     OP_COUNT
 };
 
@@ -60,7 +63,18 @@ void launch_rows(RowOp op, int precision, const Batch* dB, int ntiles, int nsegs
 // One Gauss-Seidel sweep of foam's smoother in foam's cell order (sync-free
 // over the exact plan's chunks): y = sweep(x, b), lower neighbours from y
 // (waited for), upper neighbours and interfaces from x.
-void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st);
+// parts > 0 (a batch of one system whose plan has parts of part_cells
+// cells): the owner-computes kernel, one CTA a part.
+void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st, int parts = 0, int part_cells = 0);
+
+// Owner-computes exact sweeps: the most cells a part holds (its FP64
+// values sit in shared memory; larger parts: the ticketed sync-free kernel),
+// and the part sizes aimed at -- DIC / DILU sweeps (a mesh's own plan) and
+// the Gauss-Seidel sweeps of GAMG's coarse levels, whose FP64 division per
+// row favours more, smaller parts (both measured best on GB300).
+constexpr int kPartMaxCells = 8192;
+constexpr int kPartTarget = 4096;
+constexpr int kPartTargetGs = 2048;
 
 // Sentinel fill of a vector (sync-free readiness marker).
 void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st);
@@ -77,13 +91,24 @@ void launch_factor(const Batch* dB, int grid, int with32, cudaStream_t st);
 // syncfree=1: all levels in one launch (exact ordering); else one level.
 // rho_chunks=1 (FP32 levelled sweeps of vector set 0): every chunk whose w
 // the launch writes also gets its sum of r w in chunk_rw, which OP_RHO_CH
-// then reduces.
+// then reduces.  parts > 0 (syncfree, a batch of one system whose plan has
+// parts of part_cells cells): the owner-computes kernel, one CTA a part.
 void launch_sweep(int precision, int fwd, int trans, int syncfree, int level, const Batch* dB, int grid,
-                  cudaStream_t st, int rho_chunks = 0);
+                  cudaStream_t st, int rho_chunks = 0, int parts = 0, int part_cells = 0);
 
 // GGI gather of the general interface faces: x[npad + j] = sum w x[src]
 // (which: 0 = p, 1 = x, 2 = pT; 0 and 2 skip inactive systems, 3 = p always).
 void launch_iface_gather(int precision, int which, const Batch* dB, int grid, cudaStream_t st);
+
+// Block preconditioner (PC_BLOCK, BlockDev): gather one system's blocks
+// from its raw scalar coefficients (raw_lower NULL: symmetric); factor, and
+// one sweep (fwd: y = forward(r), else w = backward(y); vs as launch_sweep's,
+// 0, 2 or 3) of every PC_BLOCK member of the batch, sync-free over the cell
+// plan's chunks.  bs: the members' block size (1..4).
+void launch_block_gather(const BlockDev* d_blk, int n, int nf, int bs, const double* raw_diag,
+                         const double* raw_upper, const double* raw_lower, cudaStream_t st);
+void launch_block_factor(int bs, const Batch* dB, int grid, cudaStream_t st);
+void launch_block_sweep(int bs, int fwd, int vs, const Batch* dB, int grid, cudaStream_t st);
 
 // Internal <-> caller numbering (FP64) of one system (test hooks).
 void launch_permute(int to_internal, const SysDev* d_sys, int sysidx, const double* src,

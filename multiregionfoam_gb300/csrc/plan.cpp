@@ -296,4 +296,62 @@ PlanHost build_plan(int n, int nf, const int32_t* lower, const int32_t* upper,
     return P;
 }
 
+void build_parts(PlanHost& P, int nparts)
+{
+    const int n = P.n;
+    P.nparts = nparts;
+    P.part_cells = (n + nparts - 1) / nparts;
+    const int B = P.part_cells;
+    // segments: runs of rows with one (level, part); rows of a level are in
+    // cell order, so each run is a part's whole level
+    std::vector<std::vector<std::pair<int, int>>> segs(nparts);
+    for (int i = 0; i < n;) {
+        const int lv = P.level_of_row[i], pt = P.perm[i] / B;
+        int e = i + 1;
+        while (e < n && P.level_of_row[e] == lv && P.perm[e] / B == pt) ++e;
+        segs[pt].push_back({i, e});
+        i = e;
+    }
+    P.pt_ptr.assign(1, 0);
+    P.part_rows.clear();
+    P.part_step.clear();
+    for (int p = 0; p < nparts; ++p) {
+        int step = 0;
+        for (auto& sg : segs[p]) {
+            for (int i = sg.first; i < sg.second; ++i) {
+                P.part_rows.push_back(i);
+                P.part_step.push_back(step);
+            }
+            ++step;
+        }
+        P.pt_ptr.push_back((int32_t)P.part_rows.size());
+    }
+    auto rows = [&](const std::vector<int32_t>& sptr, std::vector<int32_t>& row) {
+        row.assign(2 * (size_t)n, 0);
+        for (int c = 0; c < P.nchunks; ++c)
+            for (int i = P.chunk_start[c]; i < P.chunk_start[c + 1]; ++i) {
+                row[2 * (size_t)i] = sptr[c] + (i - P.chunk_start[c]);
+                row[2 * (size_t)i + 1] = (sptr[c + 1] - sptr[c]) / kSlice;
+            }
+    };
+    rows(P.f_sptr, P.f_row);
+    rows(P.b_sptr, P.b_row);
+    auto locs = [&](const std::vector<int32_t>& sptr, const std::vector<int32_t>& col, std::vector<int32_t>& loc) {
+        loc.assign(col.size(), -1);
+        for (int c = 0; c < P.nchunks; ++c) {
+            const int r0 = P.chunk_start[c], r1 = P.chunk_start[c + 1];
+            const int e0 = sptr[c], W = (sptr[c + 1] - e0) / kSlice;
+            for (int k = 0; k < W; ++k)
+                for (int l = 0; l < r1 - r0; ++l) {
+                    const int e = e0 + k * kSlice + l, d = col[e];
+                    if (d < 0) continue;
+                    const int cell = P.perm[r0 + l], dc = P.perm[d];
+                    if (dc / B == cell / B) loc[e] = dc - (cell / B) * B;
+                }
+        }
+    };
+    locs(P.f_sptr, P.f_col, P.f_loc);
+    locs(P.b_sptr, P.b_col, P.b_loc);
+}
+
 }  // namespace mrg

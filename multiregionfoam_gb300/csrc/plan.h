@@ -61,7 +61,19 @@ struct PlanHost {
     std::vector<int32_t> g_ptr, g_src;
     std::vector<double> g_w;
     int max_row_len = 0;
+    // exact plans, owner-computes sweeps (build_parts): the caller's cells
+    // cut into nparts ranges of part_cells cells; part p's rows are
+    // part_rows[pt_ptr[p] .. pt_ptr[p + 1]) in level order, part_step the
+    // ordinal of each one's level among the part's levels; f_loc / b_loc: per
+    // sweep dependency entry, the dependency's cell offset in the row's own
+    // part, or -1; f_row / b_row: per row (first entry of the row, entries)
+    int nparts = 0, part_cells = 0;
+    std::vector<int32_t> pt_ptr, part_rows, part_step, f_loc, b_loc, f_row, b_row;
 };
+
+// Owner-computes partition of an exact plan (see PlanHost): nparts ranges of
+// ceil(n / nparts) caller cells.
+void build_parts(PlanHost& P, int nparts);
 
 // Validates the addressing; returns "" on success, else a message.
 std::string validate_addressing(int n, int nf, const int32_t* lower,

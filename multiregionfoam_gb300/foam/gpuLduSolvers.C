@@ -9,8 +9,10 @@
 //   gpuMixedPCG       symMatrix   FP32 PCG inside FP64 iterative refinement
 //   gpuMixedPBiCG     asymMatrix  FP32 PBiCG inside FP64 iterative refinement
 //   gpuMixedBiCGStab  both        FP32 BiCGStab inside FP64 iterative refinement
-//   gpuGAMG           both        FP64 GAMG, GaussSeidel smoothing; nCellsInCoarsestLevel,
-//                                 nPostSweeps, nFinestSweeps
+//   gpuGAMG           both        FP64 GAMG, GaussSeidel smoothing; agglomerator faceAreaPair
+//                                 (the fvMesh's Sf) | algebraicPair, nCellsInCoarsestLevel,
+//                                 nPostSweeps, maxPostSweeps, postSweepsLevelMultiplier,
+//                                 nFinestSweeps, scaleCorrection
 //   gpuBICCG          both        FP64 PBiCG + DILU (foam's BICCG)
 //   gpuSmoothSolver   both        FP64 smoothSolver; smoother GaussSeidel | DIC | DILU |
 //                                 DICGaussSeidel | DILUGaussSeidel; nSweeps
@@ -52,6 +54,7 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 
 #include "lduMatrix.H"
@@ -69,6 +72,7 @@ typedef std::pair<std::vector<const void*>, uint64_t> MeshKey;
 struct GpuState {
     mrg_ctx* ctx = nullptr;
     std::map<MeshKey, mrg_mesh*> meshes;
+    std::set<mrg_mesh*> faceAreas;   // meshes given their face areas (faceAreaPair)
     std::mutex lock;
     ~GpuState()
     {
@@ -206,6 +210,14 @@ FlatInterfaces flattenInterfaces(const std::vector<const lduInterfaceFieldPtrsLi
     return F;
 }
 
+// foam's Switch words
+bool isTrue(const word& w)
+{
+    if (w == "true" || w == "on" || w == "yes" || w == "y" || w == "1") return true;
+    if (w == "false" || w == "off" || w == "no" || w == "n" || w == "0" || w == "none") return false;
+    throw FatalError("not a switch: " + w);
+}
+
 // The library's controls from a solver dictionary.
 mrg_controls makeControls(const dictionary& d, int solverKind, int precision, bool symmetric, scalar tolerance,
                           scalar relTol, label minIter, label maxIter)
@@ -218,14 +230,26 @@ mrg_controls makeControls(const dictionary& d, int solverKind, int precision, bo
     c.max_iter = maxIter;
     c.solver = solverKind;
     if (solverKind == MRG_SOLVER_GAMG) {
-        // GAMG's own words; the agglomeration is pairwise on the
-        // coefficients whatever agglomerator names, and it is cached
+        // GAMG's own words (foam's defaults); the agglomeration is always
+        // cached and the coarsest level always solved directly
+        // (directSolveCoarsest is read as true)
         if (d.lookupWord("smoother", "GaussSeidel") != "GaussSeidel")
             throw FatalError("gpuGAMG: unsupported smoother " + d.lookupWord("smoother"));
         c.smoother = MRG_SMOOTHER_GAUSS_SEIDEL;
         c.gamg_coarsest_cells = (int)d.lookupOrDefault("nCellsInCoarsestLevel", 10.0);
         c.gamg_post_sweeps = (int)d.lookupOrDefault("nPostSweeps", 2.0);
         c.gamg_finest_sweeps = (int)d.lookupOrDefault("nFinestSweeps", 2.0);
+        c.gamg_max_post_sweeps = (int)d.lookupOrDefault("maxPostSweeps", 4.0);
+        c.gamg_post_sweeps_level_multiplier = (int)d.lookupOrDefault("postSweepsLevelMultiplier", 1.0);
+        c.gamg_scale_correction = isTrue(d.lookupWord("scaleCorrection", "true")) ? 1 : 0;
+        const word ag = d.lookupWord("agglomerator", "faceAreaPair");
+        if (ag == "faceAreaPair") c.gamg_agglomerator = MRG_AGGLOMERATOR_FACE_AREA_PAIR;
+        else if (ag == "algebraicPair") c.gamg_agglomerator = MRG_AGGLOMERATOR_ALGEBRAIC_PAIR;
+        else throw FatalError("gpuGAMG: unsupported agglomerator " + ag);
+        if ((int)d.lookupOrDefault("nPreSweeps", 0.0) != 0)
+            throw FatalError("gpuGAMG: nPreSweeps must be 0 (pre-smoothing is not built)");
+        if ((int)d.lookupOrDefault("mergeLevels", 1.0) != 1)
+            throw FatalError("gpuGAMG: mergeLevels must be 1");
     } else if (solverKind == MRG_SOLVER_SMOOTH) {
         // smoothSolver's own words: smoother and nSweeps
         const word sm = d.lookupWord("smoother", "GaussSeidel");
@@ -288,6 +312,22 @@ public:
               "mrg_coeffs_upload");
         const mrg_controls c = makeControls(controls_, solverKind_, precision_, matrix_.symmetric(), tolerance_,
                                             relTol_, minIter_, maxIter_);
+        if (c.solver == MRG_SOLVER_GAMG && c.gamg_agglomerator == MRG_AGGLOMERATOR_FACE_AREA_PAIR &&
+            !S.faceAreas.count(mesh)) {
+            // faceAreaPair weighs the pairing with the mesh's face area vectors
+            const fvMesh* fm = matrix_.hasMesh() ? dynamic_cast<const fvMesh*>(&matrix_.mesh()) : nullptr;
+            if (!fm) throw FatalError("gpuGAMG: agglomerator faceAreaPair needs the matrix's fvMesh");
+            const vectorField& Sf = fm->Sf().internalField();
+            if ((label)Sf.size() != nf) throw FatalError("gpuGAMG: Sf does not match the faces");
+            std::vector<double> sf(3 * (size_t)nf);
+            for (label f = 0; f < nf; ++f) {
+                sf[3 * (size_t)f] = Sf[f].x();
+                sf[3 * (size_t)f + 1] = Sf[f].y();
+                sf[3 * (size_t)f + 2] = Sf[f].z();
+            }
+            check(mrg_mesh_set_face_areas(mesh, sf.data()), "mrg_mesh_set_face_areas");
+            S.faceAreas.insert(mesh);
+        }
         mrg_perf perf;
         check(mrg_solve(mesh, source.data(), psi.data(), &c, &perf), "mrg_solve");
         lduMatrix::solverPerformance out;

@@ -172,6 +172,49 @@ private:
 typedef std::vector<labelList> labelListList;
 typedef std::vector<scalarField> scalarListList;
 
+// A 3-vector (foam's vector): x(), y(), z().
+class vector {
+public:
+    vector(scalar x = 0, scalar y = 0, scalar z = 0) : v_{x, y, z} {}
+    scalar x() const { return v_[0]; }
+    scalar y() const { return v_[1]; }
+    scalar z() const { return v_[2]; }
+
+private:
+    scalar v_[3];
+};
+typedef std::vector<vector> vectorField;
+
+// lduMesh: what an lduMatrix is built on (its addressing).  An fvMesh is
+// one, and carries the geometry; of it the adapter reads only the internal
+// faces' area vectors (Sf().internalField()), which GAMG's faceAreaPair
+// agglomeration weights the pairing with.
+class lduMesh {
+public:
+    virtual ~lduMesh() = default;
+    virtual const lduAddressing& lduAddr() const = 0;
+};
+
+class surfaceVectorField {
+public:
+    explicit surfaceVectorField(vectorField internal) : internal_(std::move(internal)) {}
+    const vectorField& internalField() const { return internal_; }
+
+private:
+    vectorField internal_;
+};
+
+class fvMesh : public lduMesh {
+public:
+    fvMesh(const lduAddressing& addr, vectorField Sf) : addr_(addr), Sf_(std::move(Sf)) {}
+    const lduAddressing& lduAddr() const override { return addr_; }
+    const surfaceVectorField& Sf() const { return Sf_; }
+
+private:
+    const lduAddressing& addr_;
+    surfaceVectorField Sf_;
+};
+
 // GGIInterpolation: the interpolator a regionCouplePolyPatch pair holds
 // (ggiInterfaceToInterfaceMapping.C:62-77 builds the same kind, with
 // rescaled weights).  For master face m, masterAddr()[m] lists the slave
@@ -273,7 +316,14 @@ typedef std::vector<scalarField> FieldField;  // per-interface coefficients
 class lduMatrix {
 public:
     explicit lduMatrix(const lduAddressing& a) : addr_(a) {}
+    explicit lduMatrix(const lduMesh& m) : addr_(m.lduAddr()), mesh_(&m) {}
     const lduAddressing& lduAddr() const { return addr_; }
+    const lduMesh& mesh() const
+    {
+        if (!mesh_) throw FatalError("lduMatrix: built on bare addressing, no mesh");
+        return *mesh_;
+    }
+    bool hasMesh() const { return mesh_ != nullptr; }
     scalarField& diag() { return diag_; }
     scalarField& upper() { return upper_; }
     scalarField& lower() { return lower_; }
@@ -352,6 +402,7 @@ public:
 
 private:
     const lduAddressing& addr_;
+    const lduMesh* mesh_ = nullptr;
     scalarField diag_, upper_, lower_;
 };
 

@@ -15,6 +15,8 @@
 //          (prints the controls read from that entry; no GPU)
 // system.bin: int32 R; per region: int32 n, nf, has_lower; int32 lower[nf],
 //             upper[nf]; f64 diag[n], upper_c[nf], (lower_c[nf]), b[n], x0[n];
+//             int32 nsf (0, or nf: the matrix is built on an fvMesh with
+//             these face area vectors), f64 sf[3 * nsf];
 //             int32 npatch (0 or 2); with 2 (a master patch A and its slave
 //             shadow B): int32 regionA, regionB, nA, nB; int32 cellsA[nA],
 //             cellsB[nB]; A's interpolator from B (masterAddr / masterWeights
@@ -46,6 +48,7 @@ static std::vector<T> readv(FILE* f, size_t n)
 
 struct Region {
     std::unique_ptr<lduAddressing> addr;
+    std::unique_ptr<fvMesh> mesh;
     std::unique_ptr<lduMatrix> A;
     scalarField b, x0;
 };
@@ -135,12 +138,24 @@ int main(int argc, char** argv)
         const int n = hdr[0], nf = hdr[1], hasLower = hdr[2];
         labelList lower = readv<int32_t>(f, nf), upper = readv<int32_t>(f, nf);
         g.addr.reset(new lduAddressing(n, lower, upper));
-        g.A.reset(new lduMatrix(*g.addr));
-        g.A->diag() = readv<double>(f, n);
-        g.A->upper() = readv<double>(f, nf);
-        if (hasLower) g.A->lower() = readv<double>(f, nf);
+        scalarField diag = readv<double>(f, n), up = readv<double>(f, nf), lo;
+        if (hasLower) lo = readv<double>(f, nf);
         g.b = readv<double>(f, n);
         g.x0 = readv<double>(f, n);
+        const int nsf = readv<int32_t>(f, 1)[0];
+        if (nsf != 0 && nsf != nf) return 2;
+        if (nsf) {
+            std::vector<double> sf = readv<double>(f, 3 * (size_t)nsf);
+            vectorField Sf;
+            for (int k = 0; k < nsf; ++k) Sf.emplace_back(sf[3 * k], sf[3 * k + 1], sf[3 * k + 2]);
+            g.mesh.reset(new fvMesh(*g.addr, std::move(Sf)));
+            g.A.reset(new lduMatrix(*g.mesh));
+        } else {
+            g.A.reset(new lduMatrix(*g.addr));
+        }
+        g.A->diag() = diag;
+        g.A->upper() = up;
+        if (hasLower) g.A->lower() = lo;
     }
     const int npatch = readv<int32_t>(f, 1)[0];
     std::unique_ptr<regionCouplePolyPatch> pa, pb;

@@ -17,15 +17,16 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmrgpu.so")
 MRG_OK, MRG_E_INVALID, MRG_E_OOM, MRG_E_BREAKDOWN, MRG_E_TIMEOUT, MRG_E_CUDA, MRG_E_BUSY = range(7)
 SOLVERS = {"PCG": 0, "PBiCG": 1, "BiCGStab": 2, "smoothSolver": 3, "GAMG": 4}
 SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "DILU": 2, "DICGaussSeidel": 3, "DILUGaussSeidel": 4}
-PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3, "block": 4}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 ORDERINGS = {"exact": 0, "colour": 1}
+AGGLOMERATORS = {"algebraicPair": 0, "faceAreaPair": 1}
 
 EXPORTED = [
     "mrg_last_error", "mrg_version", "mrg_controls_default", "mrg_ctx_create", "mrg_ctx_destroy",
     "mrg_ctx_set_watchdog",
     "mrg_ctx_mem_used", "mrg_host_alloc", "mrg_host_free", "mrg_mesh_upload", "mrg_mesh_destroy",
-    "mrg_mesh_levels", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
+    "mrg_mesh_levels", "mrg_mesh_set_face_areas", "mrg_mesh_set_blocks", "mrg_coeffs_upload", "mrg_coeffs_upload_device", "mrg_solve", "mrg_solve_device",
     "mrg_amul", "mrg_residual", "mrg_precondition", "mrg_factor_diag", "mrg_ggi_create", "mrg_ggi_destroy",
     "mrg_ggi_apply", "mrg_ggi_apply_device", "mrg_ggi_time", "mrg_ggi_build", "mrg_direct_map_build", "mrg_ggi_get", "mrg_dev_alloc", "mrg_dev_free", "mrg_dev_copy",
     "mrg_event_record", "mrg_event_elapsed", "mrg_kernel_launches", "mrg_time_kernel",
@@ -52,7 +53,9 @@ class Controls(C.Structure):
                 ("precision", C.c_int), ("ordering", C.c_int), ("inner_rel_tol", C.c_double),
                 ("inner_max_iter", C.c_int), ("max_outer", C.c_int), ("iters_per_launch", C.c_int),
                 ("smoother", C.c_int), ("n_sweeps", C.c_int), ("gamg_coarsest_cells", C.c_int),
-                ("gamg_post_sweeps", C.c_int), ("gamg_finest_sweeps", C.c_int)]
+                ("gamg_post_sweeps", C.c_int), ("gamg_finest_sweeps", C.c_int),
+                ("gamg_max_post_sweeps", C.c_int), ("gamg_post_sweeps_level_multiplier", C.c_int),
+                ("gamg_scale_correction", C.c_int), ("gamg_agglomerator", C.c_int)]
 
 
 class Perf(C.Structure):
@@ -128,6 +131,8 @@ def load(path: str = LIB_PATH):
     L.mrg_mesh_upload.argtypes = [vp, C.c_int, C.c_int, ip, ip, C.c_int, C.POINTER(IfaceDesc), C.POINTER(vp)]
     L.mrg_mesh_destroy.argtypes = [vp]
     L.mrg_mesh_levels.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.mrg_mesh_set_face_areas.argtypes = [vp, dp]
+    L.mrg_mesh_set_blocks.argtypes = [vp, C.c_int, C.c_int, C.c_int, ip, ip]
     L.mrg_coeffs_upload.argtypes = [vp, dp, dp, dp, dp, dp]
     L.mrg_coeffs_upload_device.argtypes = [vp, vp, vp, vp, vp, vp]
     L.mrg_solve.argtypes = [vp, dp, dp, C.POINTER(Controls), C.POINTER(Perf)]
@@ -204,7 +209,8 @@ def _i(a):
 def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", precond="DIC",
              precision="fp64", ordering="exact", inner_rel_tol=1e-5, inner_max_iter=0, max_outer=50,
              iters_per_launch=16, n_sweeps=1, smoother="GaussSeidel", n_coarsest_cells=10, n_post_sweeps=2,
-             n_finest_sweeps=2) -> Controls:
+             n_finest_sweeps=2, max_post_sweeps=4, post_sweeps_level_multiplier=1, scale_correction=True,
+             agglomerator="algebraicPair") -> Controls:
     c = Controls()
     load().mrg_controls_default(C.byref(c))
     c.tolerance, c.rel_tol, c.min_iter, c.max_iter = tol, rel_tol, min_iter, max_iter
@@ -214,6 +220,8 @@ def controls(tol=1e-6, rel_tol=0.0, min_iter=0, max_iter=1000, solver="PCG", pre
     c.iters_per_launch = iters_per_launch
     c.smoother, c.n_sweeps = SMOOTHERS[smoother], n_sweeps
     c.gamg_coarsest_cells, c.gamg_post_sweeps, c.gamg_finest_sweeps = n_coarsest_cells, n_post_sweeps, n_finest_sweeps
+    c.gamg_max_post_sweeps, c.gamg_post_sweeps_level_multiplier = max_post_sweeps, post_sweeps_level_multiplier
+    c.gamg_scale_correction, c.gamg_agglomerator = int(bool(scale_correction)), AGGLOMERATORS[agglomerator]
     return c
 
 
@@ -348,6 +356,20 @@ class Mesh:
         v = C.c_int()
         _check(load().mrg_mesh_levels(self.h, ORDERINGS[ordering], C.byref(v)))
         return v.value
+
+    def set_blocks(self, bs, n_cells, lower, upper):
+        """Declare this mesh the bs-expansion of the block mesh (n_cells,
+        lower, upper), for the block preconditioner (precond="block")."""
+        self._blo = np.ascontiguousarray(lower, dtype=np.int32)
+        self._bup = np.ascontiguousarray(upper, dtype=np.int32)
+        _check(load().mrg_mesh_set_blocks(self.h, int(bs), int(n_cells), len(self._blo), _i(self._blo),
+                                          _i(self._bup)))
+
+    def set_face_areas(self, sf):
+        """The internal faces' area vectors ([n_faces, 3]) for GAMG's
+        faceAreaPair agglomeration."""
+        self._sf = np.ascontiguousarray(sf, dtype=np.float64).reshape(self.nf, 3)
+        _check(load().mrg_mesh_set_face_areas(self.h, _d(self._sf)))
 
     def upload(self, diag, upper, lower=None, iface_bou=None, iface_int=None):
         self._c = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None

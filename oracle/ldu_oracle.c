@@ -897,6 +897,17 @@ double or_mirror_residual(const or_ldu* m, const double* b, const double* x, dou
     return s;
 }
 
+/* sum of a[c] * b[c] (fused) in the GPU's order for a row operation that
+ * walks the sliced ELL rows (GAMG's scaling dots). */
+double or_mirror_dot(const or_ldu* m, const double* a, const double* b)
+{
+    mr_order o;
+    mr_order_init(m, &o);
+    double s = mr_reduce(&o, 1, 0, a, b);
+    free(o.perm);
+    return s;
+}
+
 double or_mirror_norm_factor(const or_ldu* m, const double* b, const double* x)
 {
     int n = m->n;

@@ -62,6 +62,8 @@ def lib():
         L.or_mirror_residual.restype = C.c_double
         L.or_mirror_norm_factor.argtypes = [pldu, dp, dp]
         L.or_mirror_norm_factor.restype = C.c_double
+        L.or_mirror_dot.argtypes = [pldu, dp, dp]
+        L.or_mirror_dot.restype = C.c_double
         L.or_ggi_apply.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_int]
         L.gw_overlaps.argtypes = [C.c_int, ip, dp, C.c_int, ip, dp, C.c_double,
                                   C.c_long, ip, ip, dp]
@@ -215,6 +217,11 @@ class OracleMatrix:
         s = lib().or_mirror_residual(C.byref(self._s), _d(np.ascontiguousarray(b, np.float64)),
                                      _d(np.ascontiguousarray(x, np.float64)), _d(r))
         return r, s
+
+    def mirror_dot(self, a, b):
+        """sum a b (fused) in the GPU's reduction order (sliced rows)."""
+        return lib().or_mirror_dot(C.byref(self._s), _d(np.ascontiguousarray(a, np.float64)),
+                                   _d(np.ascontiguousarray(b, np.float64)))
 
     def mirror_norm_factor(self, b, x):
         return lib().or_mirror_norm_factor(C.byref(self._s), _d(np.ascontiguousarray(b, np.float64)),

@@ -74,3 +74,25 @@ def test_unordered_block_faces(mrg):
     perm = np.random.default_rng(1).permutation(len(c["lower"]))
     with pytest.raises(mrg.MrgError, match="upper-triangular"):
         mrg.block_system(c["n"], c["lower"][perm], c["upper"][perm], 3, c["D"], c["U"][perm], c["L"][perm])
+
+
+def test_block_preconditioner_oracle_exact_on_chain(bo):
+    """The restated block factorisation (oracle/block_oracle.py) is an exact
+    LU on a block tridiagonal matrix (a chain of cells: no fill-in to drop),
+    and for a symmetric block matrix M^-1 is symmetric."""
+    n, bs = 12, 4
+    rng = np.random.default_rng(3)
+    lower = np.arange(n - 1, dtype=np.int32)
+    upper = lower + 1
+    U = rng.uniform(-1, 1, (n - 1, bs, bs))
+    L = rng.uniform(-1, 1, (n - 1, bs, bs))
+    D = rng.uniform(-0.3, 0.3, (n, bs, bs)) + np.eye(bs) * 10.0
+    dD = bo.block_factor(n, lower, upper, D, U, L)
+    r = rng.standard_normal((n, bs))
+    w = bo.block_apply(n, lower, upper, D, U, L, dD, r)
+    assert np.abs(bo.block_amul(n, lower, upper, D, U, L, w) - r).max() < 1e-12
+    c = block_case(4, 3, 3, bs=3, seed=8, symmetric=True)
+    dD = bo.block_factor(c["n"], c["lower"], c["upper"], c["D"], c["U"], None)
+    E = np.eye(c["n"] * 3)
+    Minv = np.stack([bo.block_apply(c["n"], c["lower"], c["upper"], c["D"], c["U"], None, dD, e).ravel() for e in E])
+    assert np.allclose(Minv, Minv.T, rtol=0, atol=1e-12)

@@ -68,12 +68,16 @@ def patch_pair(s, n_a):
     return ca, cb, csr[0], csr[1], bou[:n_a], bou[n_a:]
 
 
-def _region(fh, n, lower, upper, diag, upper_c, lower_c, b, x0):
+def _region(fh, n, lower, upper, diag, upper_c, lower_c, b, x0, sf=None):
     np.array([n, len(lower), 0 if lower_c is None else 1], np.int32).tofile(fh)
     np.asarray(lower, np.int32).tofile(fh)
     np.asarray(upper, np.int32).tofile(fh)
     for a in (diag, upper_c) + (() if lower_c is None else (lower_c,)) + (b, x0):
         np.asarray(a, np.float64).tofile(fh)
+    # the fvMesh's face area vectors (none: the matrix has bare addressing)
+    np.array([0 if sf is None else len(lower)], np.int32).tofile(fh)
+    if sf is not None:
+        np.ascontiguousarray(sf, np.float64).tofile(fh)
 
 
 def _patches(fh, ra, rb, pair, off_a=0, off_b=0):
@@ -94,11 +98,12 @@ def n_iface_a(s):
     return int(s.meta.get("n_iface", s.meta.get("n_ifa", 0)))
 
 
-def write_system(path, s):
-    """One matrix (its interfaces a patch pair inside it)."""
+def write_system(path, s, sf=None):
+    """One matrix (its interfaces a patch pair inside it); sf: the face area
+    vectors of its fvMesh."""
     with open(path, "wb") as fh:
         np.array([1], np.int32).tofile(fh)
-        _region(fh, s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.b, s.x0)
+        _region(fh, s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.b, s.x0, sf)
         if s.iface is None:
             np.array([0], np.int32).tofile(fh)
         else:
@@ -123,11 +128,11 @@ def write_regions(path, s, n0):
         _patches(fh, 0, 1, pair, 0, n0)
 
 
-def run(mrg, tmp_path, s, solver, pc, tol, extra=()):
+def run(mrg, tmp_path, s, solver, pc, tol, extra=(), sf=None):
     from multiregionfoam_gb300 import _build
     exe = _build.build_adapter()
     sysf, outf = str(tmp_path / "sys.bin"), str(tmp_path / "x.bin")
-    write_system(sysf, s)
+    write_system(sysf, s, sf)
     r = subprocess.run([exe, sysf, solver, pc, repr(tol), outf, *extra], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     return np.fromfile(outf, np.float64), json.loads(r.stdout.strip().splitlines()[-1])
@@ -221,16 +226,35 @@ def test_smooth_solver_adapter(mrg, oracle_mod, tmp_path):
 
 
 def test_gamg_adapter(mrg, oracle_mod, tmp_path):
-    """gpuGAMG with the tutorials' words (smoother GaussSeidel,
-    nCellsInCoarsestLevel 10)."""
+    """gpuGAMG with the tutorials' words (smoother GaussSeidel, agglomerator
+    faceAreaPair on the fvMesh's Sf, nCellsInCoarsestLevel 10, mergeLevels
+    1, scaleCorrection true, nPreSweeps 0, nPostSweeps 0 / 2), and with
+    algebraicPair on a matrix without a mesh."""
     import gamg_oracle as G
-    s = cases.convdiff_system(12, 11, 10, seed=9)
-    x, perf = run(mrg, tmp_path, s, "gpuGAMG", "none", 1e-8, ("smoother=GaussSeidel", "nCellsInCoarsestLevel=10",
-                                                              "agglomerator=faceAreaPair", "mergeLevels=1"))
-    g = G.Gamg(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c)
-    xm, pm = g.solve(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.b, s.x0, tol=1e-8, max_iter=5000)
-    assert perf["solver"] == "gpuGAMG" and perf["converged"] == 1
-    assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+    s = cases.cht_system(12, 11, 6, 4, seed=9, form="global", k_range=(0.1, 50.0))
+    sf = cases.face_area_vectors(s)
+    g = G.Gamg(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, weights=G.face_area_weights(sf))
+    for post in (2, 0):
+        x, perf = run(mrg, tmp_path, s, "gpuGAMG", "none", 1e-8,
+                      ("smoother=GaussSeidel", "nCellsInCoarsestLevel=10", "agglomerator=faceAreaPair",
+                       "mergeLevels=1", "cacheAgglomeration=true", "scaleCorrection=true", "nPreSweeps=0",
+                       f"nPostSweeps={post}", "nFinestSweeps=2", "directSolveCoarsest=false"), sf=sf)
+        xm, pm = g.solve(s.n, s.lower, s.upper, s.diag, s.upper_c, s.lower_c, s.b, s.x0, tol=1e-8,
+                         max_iter=5000, n_post=post)
+        assert perf["solver"] == "gpuGAMG" and perf["converged"] == 1
+        assert perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+    t = cases.convdiff_system(12, 11, 10, seed=9)
+    x, perf = run(mrg, tmp_path, t, "gpuGAMG", "none", 1e-8, ("agglomerator=algebraicPair",))
+    g = G.Gamg(t.n, t.lower, t.upper, t.diag, t.upper_c, t.lower_c)
+    xm, pm = g.solve(t.n, t.lower, t.upper, t.diag, t.upper_c, t.lower_c, t.b, t.x0, tol=1e-8, max_iter=5000)
+    assert perf["converged"] == 1 and perf["n_iter"] == pm["n_iter"] and np.array_equal(x, xm)
+    # foam's default agglomerator is faceAreaPair: without a mesh it is an error
+    from multiregionfoam_gb300 import _build
+    exe = _build.build_adapter()
+    write_system(str(tmp_path / "t.bin"), t)
+    r = subprocess.run([exe, str(tmp_path / "t.bin"), "gpuGAMG", "none", "1e-8", str(tmp_path / "o.bin")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1 and "faceAreaPair" in r.stdout
 
 
 def test_unknown_solver_is_fatal(mrg, tmp_path):

@@ -470,14 +470,17 @@ def run_block(args, ctx, mrgpu):
     n_s, lo, up, d, uc, lc = mrgpu.block_system(c["n"], c["lower"], c["upper"], 4, c["D"], c["U"], c["L"])
     t_expand = time.perf_counter() - t0
     m = mrgpu.Mesh(ctx, n_s, lo, up)
+    m.set_blocks(4, c["n"], c["lower"], c["upper"])
     d_d, d_u, d_l = ctx.to_device(d), ctx.to_device(uc), ctx.to_device(lc)
     d_b, d_x0 = ctx.to_device(c["b"].ravel()), ctx.to_device(np.zeros(n_s))
     d_x = ctx.dev_alloc(8 * n_s)
     out = {"block_cells": c["n"], "block_size": 4, "scalar_cells": n_s, "scalar_faces": int(len(lo)),
-           "expand_ms": t_expand * 1e3, "solver": "BiCGStab+DILU", "tolerance": TOL}
+           "expand_ms": t_expand * 1e3, "solver": "BiCGStab+DILU (block_cholesky: BiCGStab + the block "
+                                                   "Cholesky preconditioner on the 4x4 blocks)", "tolerance": TOL}
     xs = {}
-    for name, prec, order in (("mixed", "mixed", "colour"), ("plain_fp64", "fp64", "exact")):
-        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="BiCGStab", precond="DILU", precision=prec,
+    for name, prec, order, pc in (("mixed", "mixed", "colour", "DILU"), ("plain_fp64", "fp64", "exact", "DILU"),
+                                  ("block_cholesky", "fp64", "exact", "block")):
+        ctl = mrgpu.controls(tol=TOL, max_iter=20000, solver="BiCGStab", precond=pc, precision=prec,
                              ordering=order, inner_rel_tol=args.inner_tol)
         ms, perf = [], None
         for rep in range(4):   # the first untimed: plans, views, graphs
@@ -493,6 +496,7 @@ def run_block(args, ctx, mrgpu):
         out[name] = {"solves_per_s": 1e3 / best, "ms_per_step": best, "iters": int(perf["n_iter"]),
                      "final_residual": perf["final_residual"], "converged": bool(perf["converged"])}
     out["speedup_mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    out["speedup_block_cholesky_vs_plain"] = out["block_cholesky"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
     for a in (d_d, d_u, d_l, d_b, d_x0, d_x):
         ctx.dev_free(a)
     m.close()
@@ -793,11 +797,12 @@ def run_gpu(args):
         jobs = [("c2", args.scale)]
         if c3 is not None:
             jobs.append(("c3", args.c3_scale))
-        jobs += [("c5", args.served_meshes, i, st) for (_, i, st) in x_c5 if _ == "mixed"]
+        c5_every = max(1, args.ref_every // 2)
+        jobs += [("c5", args.served_meshes, i, st) for (_, i, st) in x_c5 if _ == "mixed" and i % c5_every == 0]
         if block is not None:
             jobs.append(("block", args.block_n))
         if batched is not None:
-            jobs += [("c4", args.batched, i) for i in range(args.batched)]
+            jobs += [("c4", args.batched, i) for i in range(0, args.batched, args.ref_every)]
         t0 = time.perf_counter()
         refs = leg.references(jobs)
         leg.close()
@@ -820,13 +825,13 @@ def run_gpu(args):
             batched[f]["err_vs_fp64_oracle"] = err_stats(
                 [err(("c4", args.batched, i), x) for i, x in enumerate(x_c4[f])])
     if block is not None:
-        for f in ("mixed", "plain_fp64"):
+        for f in ("mixed", "plain_fp64", "block_cholesky"):
             block[f]["err_vs_fp64_oracle"] = err(("block", args.block_n), x_block[f])
     if served is not None:
         fam = served.pop("asym_of_mesh")
         served["err_vs_fp64_oracle"] = {
-            "sample": "one request per mesh (time step mesh % steps) of the last rate's runs; the FP64 oracle "
-                      f"converged to {REF_TOL_MANY:g}",
+            "sample": f"one request per {max(1, args.ref_every // 2)}-th mesh (time step mesh % steps) of the last "
+                      f"rate's runs; the FP64 oracle converged to {REF_TOL_MANY:g}",
             **{f"{f}_{kind}": err_stats([err(("c5", args.served_meshes, i, st), x) for (ff, i, st), x in x_c5.items()
                                          if ff == f and fam[i] == (kind == "asym")])
                for f in ("mixed", "plain_fp64") for kind in ("sym", "asym")}}
@@ -892,10 +897,13 @@ def main():
     ap.add_argument("--gamg-n", type=int, default=64, help="GAMG configuration: n^3 cells (0: skip)")
     ap.add_argument("--served-meshes", type=int, default=100, help="meshes of the served configuration (0: skip)")
     ap.add_argument("--served-steps", type=int, default=20)
-    ap.add_argument("--served-rates", default="50,100,200,500,1000,2000",
-                    help="Poisson arrival rates of the sweep, requests/s")
-    ap.add_argument("--served-plain-rates", default="",
-                    help="arrival rates of the plain FP64 server's sweep (default: --served-rates)")
+    ap.add_argument("--served-rates", default="200,2000",
+                    help="Poisson arrival rates of the mixed server's sweep, requests/s (the full C5 sweep: "
+                         "50,100,200,500,1000,2000)")
+    ap.add_argument("--served-plain-rates", default="2000",
+                    help="arrival rates of the plain FP64 server's sweep (empty: --served-rates)")
+    ap.add_argument("--ref-every", type=int, default=8,
+                    help="FP64 oracle errors for every n-th batched system and every (n/2)-th served mesh")
     ap.add_argument("--served-k", type=int, default=8, help="server: Krylov iterations per launch")
     ap.add_argument("--served-pbicg-inner", action="store_true",
                     help="also serve with FP32 PBiCG (not BiCGStab) for the asymmetric requests")

@@ -569,10 +569,16 @@ static bool part_sweeps()
 // The owner-computes launch shape of a batch's exact sweeps: one system
 // with a partitioned plan (not while the watchdog test hook withholds a
 // chunk), else parts = 0.
-void part_choice(const BatchHost& bh, int& parts, int& cells)
+void part_choice(const BatchHost& bh, int& parts, int& cells, bool gs)
 {
     const SysDev* S1 = bh.members.size() == 1 ? &bh.members[0]->sys : nullptr;
     parts = (S1 && S1->nparts > 0 && bh.ctx->unpublished1 == 0 && part_sweeps()) ? S1->nparts : 0;
+    // DIC / DILU sweeps (no division a row) gain only from few parts with
+    // enough rows per level each (measured on GB300: a 262k-cell CHT mesh in
+    // 64 parts 1.6x faster than ticketed; 3.1M cells in 152 parts, and a
+    // block expansion with 7 rows a part and level, 1.7x and 2.6x slower)
+    if (parts && !gs && (parts > kPartMaxTri || (long long)S1->n < (long long)kPartRowsPerLevel * S1->nlevels * parts))
+        parts = 0;
     cells = parts ? S1->part_cells : 0;
 }
 
@@ -651,7 +657,7 @@ static void record_iteration_gs(BatchHost& bh, const Controls& cfg, cudaStream_t
         if (gs) {
             if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
             int parts = 0, cells = 0;
-            part_choice(bh, parts, cells);
+            part_choice(bh, parts, cells, true);
             launch_gs_sweep(bh.d, grid_sweep(bh.ctx), st, parts, cells);
             launch_rows(OP_GS_COPY, 0, bh.d, nt, ns, 0, st);
         }
@@ -739,9 +745,10 @@ static BatchHost::Graph iteration_graph(BatchHost& bh, const Controls& cfg, int 
     {
         // the owner-computes launch shape is fixed at capture: it depends on
         // the member (a one-system batch), so it is part of the key
-        int parts = 0, cells = 0;
+        int parts = 0, cells = 0, gparts = 0, gcells = 0;
         part_choice(bh, parts, cells);
-        key += "/q" + std::to_string(parts) + "x" + std::to_string(cells);
+        part_choice(bh, gparts, gcells, true);
+        key += "/q" + std::to_string(parts) + "x" + std::to_string(cells) + "/g" + std::to_string(gparts);
     }
     auto it = bh.graphs.find(key);
     if (it != bh.graphs.end()) return it->second;
@@ -949,12 +956,13 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
                 launch_rows(OP_CORRECT, 0, bh.d, nt, ns, 0, st);
             }
             // members whose refinement stalled finish with FP64 Krylov
+            const Controls fb = fallback_controls(cfg);
             if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
-            launch_rows(OP_FALLBACK64, 0, bh.d, nt, ns, pb, st);
-            krylov_start(bh, cfg, 0);
+            launch_rows(OP_FALLBACK64, 0, bh.d, nt, ns, fb.solver == MRG_SOLVER_PBICG, st);
+            krylov_start(bh, fb, 0);
             poll(bh, h);
             if (h->n_active > 0) {
-                run_iterations(bh, cfg, 0, cfg.max_iter, h);
+                run_iterations(bh, fb, 0, fb.max_iter, h);
                 if (gen) launch_iface_gather(0, 1, bh.d, 64, st);
                 launch_rows(OP_FALLBACK64, 0, bh.d, nt, ns, 0, st);   // true residual of the result
             }
@@ -1026,11 +1034,19 @@ void batch_begin(BatchHost& bh, const Controls& cfg)
     MRG_CUDA(cudaGetLastError());
 }
 
+Controls fallback_controls(const Controls& cfg)
+{
+    Controls fb = cfg;
+    if (fb.solver == MRG_SOLVER_BICGSTAB) fb.solver = MRG_SOLVER_PBICG;
+    return fb;
+}
+
 void batch_fallback(BatchHost& bh, const Controls& cfg)
 {
+    const Controls fb = fallback_controls(cfg);
     if (any_general_iface(bh)) launch_iface_gather(0, 1, bh.d, 64, bh.ctx->st);
-    launch_rows(OP_FALLBACK64, 0, bh.d, bh.h.ntiles, bh.h.nsegs, cfg.solver == MRG_SOLVER_PBICG, bh.ctx->st);
-    krylov_start(bh, cfg, 0);
+    launch_rows(OP_FALLBACK64, 0, bh.d, bh.h.ntiles, bh.h.nsegs, fb.solver == MRG_SOLVER_PBICG, bh.ctx->st);
+    krylov_start(bh, fb, 0);
     MRG_CUDA(cudaGetLastError());
 }
 

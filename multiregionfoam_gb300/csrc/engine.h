@@ -197,6 +197,11 @@ void batch_begin(BatchHost& bh, const Controls& c);
 void batch_iterate(BatchHost& bh, const Controls& c, int prec = -1);
 // Mixed members whose refinement stalled (fallback requested): FP64 residual
 // of the best iterate and the start of an FP64 Krylov loop.
+// The FP64 continuation of mixed solves whose refinement stalled: the same
+// controls with PBiCG in place of BiCGStab (FP64 BiCGStab can break down on
+// convection-dominated systems where PBiCG -- foam's plain method for
+// asymmetric matrices -- converges).
+Controls fallback_controls(const Controls& cfg);
 void batch_fallback(BatchHost& bh, const Controls& c);
 void batch_outer(BatchHost& bh, const Controls& c);
 void batch_finish(BatchHost& bh);
@@ -221,7 +226,8 @@ void upload_coeffs(Mesh& m, const double* diag, const double* upper, const doubl
 PlanState& prepare(Mesh& m, const Controls& c);
 // Owner-computes exact sweeps of a batch: parts (0: the ticketed kernel) and
 // cells a part.
-void part_choice(const BatchHost& bh, int& parts, int& cells);
+// gs: for Gauss-Seidel sweeps (else DIC / DILU sweeps).
+void part_choice(const BatchHost& bh, int& parts, int& cells, bool gs = false);
 Perf solve_device(Mesh& m, const double* d_b, double* d_x, const Controls& c);
 
 void amul_device(Mesh& m, const double* d_x, double* d_y, int transpose);

@@ -592,7 +592,7 @@ Perf gamg_solve(Mesh& m, const double* d_b, double* d_x, const Controls& cfg)
     auto sweeps = [&](int l, int k) {
         BatchHost& bh = P[l]->single;
         int parts = 0, cells = 0;
-        part_choice(bh, parts, cells);
+        part_choice(bh, parts, cells, true);
         for (int s = 0; s < k; ++s) {
             launch_gs_sweep(bh.d, c->nsm * 4, st, parts, cells);
             launch_rows(OP_GS_COPY, 0, bh.d, P[l]->ntiles, bh.h.nsegs, 0, st);

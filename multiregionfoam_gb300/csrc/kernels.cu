@@ -184,6 +184,15 @@ __device__ __forceinline__ V wait_ready(const V* p, Ctl* ctl)
     }
 }
 
+// The value at p once published, given an earlier look v at it: the looks
+// at all of a row's dependencies are relaxed loads issued together, so their
+// round trips overlap; only a look that still saw the sentinel waits.
+template <typename V>
+__device__ __forceinline__ V ready(V v, const V* p, Ctl* ctl)
+{
+    return is_sent(v) ? wait_ready(p, ctl) : v;
+}
+
 // Coefficient value for a plan source code (see plan.h).
 __device__ __forceinline__ double src_val(const SysDev& S, int s, bool trans)
 {
@@ -2339,14 +2348,24 @@ __device__ __forceinline__ void factor_row(const SysDev& S, int c, int lane, Ctl
     const int F = S.nf;
     double D = S.diag[i];
     const int fe0 = S.f_sptr[c], fW = (S.f_sptr[c + 1] - fe0) >> 5;
-    for (int k = 0; k < fW; ++k) {
-        const int e = fe0 + k * 32 + lane;
-        const int col = S.f_col[e];
-        if (col < 0) break;
-        const int sc = S.f_src[e];
-        const double a = src_val(S, sc, false), at = src_val(S, swap_src(sc, F), false);
-        const double Dd = wait_ready(S.D + col, ctl);
-        D = __dsub_rn(D, __ddiv_rn(__dmul_rn(a, at), Dd));
+    for (int k0 = 0; k0 < fW; k0 += kMaxW) {
+        // a round of dependencies: indices, coefficients and looks at their
+        // D first, then the updates in order
+        int col[kMaxW];
+        double a[kMaxW], at[kMaxW], Dd[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) {
+            col[k] = k0 + k < fW ? S.f_col[fe0 + (k0 + k) * 32 + lane] : -1;
+            if (col[k] >= 0) {
+                const int sc = S.f_src[fe0 + (k0 + k) * 32 + lane];
+                a[k] = src_val(S, sc, false);
+                at[k] = src_val(S, swap_src(sc, F), false);
+                Dd[k] = ld_relaxed(S.D + col[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k)
+            if (col[k] >= 0) D = __dsub_rn(D, __ddiv_rn(__dmul_rn(a[k], at[k]), ready(Dd[k], S.D + col[k], ctl)));
     }
     st_relaxed(S.D + i, D);
     const double rd = __ddiv_rn(1.0, D);
@@ -2493,9 +2512,12 @@ __device__ __forceinline__ void sweep_round(const SweepPtrs<V>& P, int e0, int k
 #pragma unroll
     for (int k = 0; k < kMaxW; ++k) cf[k] = col[k] >= 0 ? __ldg(P.coef + e0 + (k0 + k) * 32 + lane) : V(0);
     if (syncfree) {
+        V d[kMaxW];
+#pragma unroll
+        for (int k = 0; k < kMaxW; ++k) d[k] = col[k] >= 0 ? ld_relaxed(dep + col[k]) : V(0);
 #pragma unroll
         for (int k = 0; k < kMaxW; ++k)
-            if (col[k] >= 0) acc = vfma(-cf[k], wait_ready(dep + col[k], ctl), acc);
+            if (col[k] >= 0) acc = vfma(-cf[k], ready(d[k], dep + col[k], ctl), acc);
     } else {
         V d[kMaxW];
 #pragma unroll
@@ -2988,13 +3010,18 @@ __device__ __forceinline__ double gs_row_acc(const SysDev& S, int i, Ctl* ctl, c
         for (int k = 0; k < kMaxW; ++k) {
             loc[k] = -1;
             if (own && sc[k] >= F) loc[k] = __ldg(S.perm + col[k]) - base;
-            v[k] = (sc[k] >= 0 && sc[k] < F) ? __ldca(x + col[k]) : 0.0;   // upper neighbours: old values
+            if (sc[k] >= 0 && sc[k] < F)
+                v[k] = __ldca(x + col[k]);   // upper neighbours: old values
+            else if (sc[k] >= F && (unsigned)loc[k] >= (unsigned)pc)
+                v[k] = ld_relaxed(y + col[k]);   // lower neighbours outside the part: a look
+            else
+                v[k] = 0.0;
         }
 #pragma unroll
         for (int k = 0; k < kMaxW; ++k) {
             if (sc[k] < 0) continue;
             if (sc[k] >= F)
-                v[k] = (unsigned)loc[k] < (unsigned)pc ? own[loc[k]] : wait_ready(y + col[k], ctl);
+                v[k] = (unsigned)loc[k] < (unsigned)pc ? own[loc[k]] : ready(v[k], y + col[k], ctl);
             acc = __fma_rn(-a[k], v[k], acc);
         }
     }
@@ -3281,7 +3308,11 @@ __device__ __forceinline__ void block_factor_cell(const BlockDev& K, int c, int 
 #pragma unroll
         for (int a = 0; a < BS; ++a)
 #pragma unroll
-            for (int b = 0; b < BS; ++b) Dl[a][b] = wait_ready(K.dD + (size_t)l * BB + a * BS + b, ctl);
+            for (int b = 0; b < BS; ++b) Dl[a][b] = ld_relaxed(K.dD + (size_t)l * BB + a * BS + b);
+#pragma unroll
+        for (int a = 0; a < BS; ++a)
+#pragma unroll
+            for (int b = 0; b < BS; ++b) Dl[a][b] = ready(Dl[a][b], K.dD + (size_t)l * BB + a * BS + b, ctl);
         bmat_mul<BS>(Dl, Uf, T);
         bmat_mul<BS>(Lf, T, P);
 #pragma unroll
@@ -3298,7 +3329,7 @@ __device__ __forceinline__ void block_factor_cell(const BlockDev& K, int c, int 
 }
 
 template <int BS>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_block_factor(const Batch* __restrict__ pB)
+__global__ void __launch_bounds__(kBlock, 1) k_block_factor(const Batch* __restrict__ pB)
 {
     pdl_enter();
     const Batch B = *pB;
@@ -3370,8 +3401,13 @@ __device__ __forceinline__ void block_sweep_cell(const BlockDev& K, int c, int l
         for (int a = 0; a < BS; ++a)
 #pragma unroll
             for (int b = 0; b < BS; ++b) Bf[a][b] = __ldg(blk + (size_t)f * BB + a * BS + b);
+        int vl[BS];
 #pragma unroll
-        for (int a = 0; a < BS; ++a) v[a] = wait_ready(dep + __ldg(K.vmap + (size_t)l * BS + a), ctl);
+        for (int a = 0; a < BS; ++a) vl[a] = __ldg(K.vmap + (size_t)l * BS + a);
+#pragma unroll
+        for (int a = 0; a < BS; ++a) v[a] = ld_relaxed(dep + vl[a]);
+#pragma unroll
+        for (int a = 0; a < BS; ++a) v[a] = ready(v[a], dep + vl[a], ctl);
         bmat_vec<BS>(Bf, v, t);
         bmat_vec<BS>(dD, t, u);
 #pragma unroll
@@ -3390,7 +3426,7 @@ __device__ __forceinline__ void block_sweep_cell(const BlockDev& K, int c, int l
 }
 
 template <int BS, bool FWD>
-__global__ void __launch_bounds__(kBlock, kMinCtas) k_block_sweep(const Batch* __restrict__ pB, int vs)
+__global__ void __launch_bounds__(kBlock, 1) k_block_sweep(const Batch* __restrict__ pB, int vs)
 {
     pdl_enter();
     const Batch B = *pB;

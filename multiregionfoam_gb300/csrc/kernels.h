@@ -75,6 +75,10 @@ void launch_gs_sweep(const Batch* dB, int grid, cudaStream_t st, int parts = 0, 
 constexpr int kPartMaxCells = 8192;
 constexpr int kPartTarget = 4096;
 constexpr int kPartTargetGs = 2048;
+// DIC / DILU sweeps take the owner-computes kernel only with at most
+// kPartMaxTri parts and at least kPartRowsPerLevel rows a part and level.
+constexpr int kPartMaxTri = 64;
+constexpr int kPartRowsPerLevel = 16;
 
 // Sentinel fill of a vector (sync-free readiness marker).
 void launch_fill_sentinel(void* p, long long n, int precision, cudaStream_t st);

@@ -241,7 +241,7 @@ void Server::loop()
         for (int f = 0; f < 2; ++f) {
             try {
                 if (!fam_[f].running.empty()) batch_iterate(fam_[f].main, fam_[f].cfg);
-                if (!fam_[f].fbrun.empty()) batch_iterate(fam_[f].fb, fam_[f].cfg, 0);
+                if (!fam_[f].fbrun.empty()) batch_iterate(fam_[f].fb, fallback_controls(fam_[f].cfg), 0);
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }

@@ -584,17 +584,28 @@ def run_served(args, ctx, mrgpu):
     out = {"requests": n_req, "meshes": len(specs), "steps_per_mesh": args.served_steps, "rates_per_s": rates,
            "iters_per_launch": args.served_k, "cells_mean": float(np.mean([m.n for m in meshes])),
            "asym_meshes": int(sum(asym)), "hbm_budget_gb": 150, "generate_s": t_gen}
-    forms = [("mixed", "mixed", "colour", "BiCGStab"), ("plain_fp64", "fp64", "exact", "PBiCG")]
+    # the fast form: mixed PCG + colour DIC for the symmetric requests; for
+    # the asymmetric (convection-diffusion) ones FP64 PBiCG + colour DILU,
+    # which on this mix converged in fewer seconds than any FP32-inner form
+    # (FP32 BiCG-type recurrences stall on the convection-dominated meshes
+    # and finish in the FP64 continuation); --served-mixed-asym keeps the
+    # mixed BiCGStab form for them
+    forms = [("mixed", "mixed", "colour", "PBiCG-fp64" if not args.served_mixed_asym else "BiCGStab"),
+             ("plain_fp64", "fp64", "exact", "PBiCG")]
     if args.served_pbicg_inner:
         forms.insert(1, ("mixed_pbicg_inner", "mixed", "colour", "PBiCG"))
-    out["forms"] = {f[0]: {"precision": f[1], "ordering": f[2], "sym_solver": "PCG+DIC", "asym_solver": f[3] + "+DILU"}
+    out["forms"] = {f[0]: {"precision": f[1], "ordering": f[2], "sym_solver": "PCG+DIC",
+                           "asym_solver": (f[3].replace("-fp64", "") + "+DILU FP64" if f[3].endswith("-fp64")
+                                           else f[3] + "+DILU")}
                     for f in forms}
 
     def server(prec, order, asym_solver):
-        kw = dict(tol=TOL, max_iter=20000, precision=prec, ordering=order, inner_rel_tol=args.inner_tol,
+        kw = dict(tol=TOL, max_iter=20000, ordering=order, inner_rel_tol=args.inner_tol,
                   iters_per_launch=args.served_k)
-        return mrgpu.Server(ctx, mrgpu.controls(solver="PCG", precond="DIC", **kw),
-                            mrgpu.controls(solver=asym_solver, precond="DILU", **kw), hbm_budget=150 * 2**30)
+        aprec = "fp64" if asym_solver.endswith("-fp64") else prec
+        return mrgpu.Server(ctx, mrgpu.controls(solver="PCG", precond="DIC", precision=prec, **kw),
+                            mrgpu.controls(solver=asym_solver.replace("-fp64", ""), precond="DILU", precision=aprec,
+                                           **kw), hbm_budget=150 * 2**30)
 
     order_req = [(i, k) for k in range(args.served_steps) for i in range(len(specs))]
     xbuf = [np.empty(m.n) for m in meshes]          # a mesh's steps run one after another
@@ -906,7 +917,9 @@ def main():
                     help="FP64 oracle errors for every n-th batched system and every (n/2)-th served mesh")
     ap.add_argument("--served-k", type=int, default=8, help="server: Krylov iterations per launch")
     ap.add_argument("--served-pbicg-inner", action="store_true",
-                    help="also serve with FP32 PBiCG (not BiCGStab) for the asymmetric requests")
+                    help="also serve with mixed FP32 PBiCG for the asymmetric requests")
+    ap.add_argument("--served-mixed-asym", action="store_true",
+                    help="serve the asymmetric requests with mixed FP32 BiCGStab (default: FP64 PBiCG + colour DILU)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -132,9 +132,10 @@ typedef struct {
                               (default 1e-5); each step aims at 0.1 x the
                               residual still to remove, never below this    */
     int inner_max_iter;    /* mixed: inner iterations per outer step; 0 =
-                              max_iter for PCG, 150 for PBiCG (an FP32 BiCG
-                              recurrence can drift and diverge; restarting
-                              it from the FP64 residual keeps it stable)     */
+                              max_iter for PCG, 150 for PBiCG, 300 for
+                              BiCGStab (an FP32 BiCG-type recurrence can
+                              drift and diverge; restarting it from the FP64
+                              residual keeps it stable)                      */
     int max_outer;         /* mixed: refinement steps (default 50)          */
     int iters_per_launch;  /* iterations per CUDA-graph launch (default 16) */
     int smoother;          /* MRG_SOLVER_SMOOTH: MRG_SMOOTHER_*             */

@@ -40,8 +40,8 @@ Beside the headline, the line carries the other configurations:
             convection-diffusion with DILU, 20 time steps each with 5%
             coefficient drift per step: 2000 requests) through the
             continuous-batching server under a 150 GB HBM budget, for each
-            arrival rate of the sweep (default 50, 100, 200, 500, 1000,
-            2000 /s): solves/s, p50/p99 ms, for the mixed form and the plain
+            arrival rate of the sweep (default 200 and 2000 /s; the plain
+            server at 2000 /s): solves/s, p50/p99 ms, for the mixed form and the plain
             FP64 method; the plain drop-in one request at a time beside
             (--served-meshes / --served-steps / --served-rates, 0 meshes
             skips)
@@ -586,11 +586,11 @@ def run_served(args, ctx, mrgpu):
            "asym_meshes": int(sum(asym)), "hbm_budget_gb": 150, "generate_s": t_gen}
     # the fast form: mixed PCG + colour DIC for the symmetric requests; for
     # the asymmetric (convection-diffusion) ones FP64 PBiCG + colour DILU,
-    # which on this mix converged in fewer seconds than any FP32-inner form
-    # (FP32 BiCG-type recurrences stall on the convection-dominated meshes
-    # and finish in the FP64 continuation); --served-mixed-asym keeps the
-    # mixed BiCGStab form for them
-    forms = [("mixed", "mixed", "colour", "PBiCG-fp64" if not args.served_mixed_asym else "BiCGStab"),
+    # which on this mix finished in less time than the mixed BiCGStab form:
+    # over the perturbed time steps a few FP32-inner solves stall and end in
+    # the FP64 continuation (one request of 2000 did not converge there);
+    # --served-mixed-asym serves them with mixed BiCGStab
+    forms = [("mixed", "mixed", "colour", "BiCGStab" if args.served_mixed_asym else "PBiCG-fp64"),
              ("plain_fp64", "fp64", "exact", "PBiCG")]
     if args.served_pbicg_inner:
         forms.insert(1, ("mixed_pbicg_inner", "mixed", "colour", "PBiCG"))

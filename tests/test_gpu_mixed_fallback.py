@@ -2,8 +2,8 @@
 
 When the FP64 outer loop ends without reaching the tolerance (FP32 BiCG
 drift, or the refinement-step limit), the solve restarts FP64 Krylov from
-the best refined iterate with the solve's own normFactor, and reports
-fallback = 1.  The refinement-step limit max_outer = 1 forces that path
+the best refined iterate with the solve's own normFactor (PBiCG for a
+BiCGStab solve), and reports fallback = 1.  The refinement-step limit max_outer = 1 forces that path
 here; the result must converge, its error against a tightly converged FP64
 solution must stay within 10x of the plain FP64 method's own at the same
 tolerance, and it must be bit-identical alone and inside the server's
@@ -17,14 +17,14 @@ from multiregionfoam_gb300 import cases
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case", ["cht", "convdiff"])
+@pytest.mark.parametrize("case", ["cht", "convdiff", "convdiff_bicgstab"])
 def test_stalled_refinement_finishes_in_fp64(mrg, ctx, case):
     if case == "cht":
         s = cases.cht_system(18, 14, 12, 6, seed=5, k_range=(0.1, 50.0))
         kw = dict(solver="PCG", precond="DIC")
     else:
         s = cases.convdiff_system(16, 14, 12, seed=6)
-        kw = dict(solver="PBiCG", precond="DILU")
+        kw = dict(solver="PBiCG" if case == "convdiff" else "BiCGStab", precond="DILU")
     m = mrg.Mesh(ctx, s.n, s.lower, s.upper)
     m.upload(s.diag, s.upper_c, s.lower_c)
     try:

@@ -19,10 +19,11 @@ constexpr int kMaxRed = 2;    // values reduced per tile
 // contiguous tile segments, segment j = tiles [j*T/G, (j+1)*T/G): the
 // summation order of every per-system reduction depends only on the system
 // itself -- not on the device, the launch grid or the other members of a
-// batch.  Segments of >= 4 tiles keep the per-segment tree and flush small
-// against the per-row work.
+// batch.  One tile a segment up to 608 tiles (622k cells) gives a system of
+// that size one CTA per tile, so its row kernels are not latency-bound on a
+// few CTAs; larger systems spread over 608 segments.
 constexpr int kRedSegs = 608;
-constexpr int kSegTiles = 4;
+constexpr int kSegTiles = 1;
 __host__ __device__ inline int red_segments(int tiles)
 {
     const int g = (tiles + kSegTiles - 1) / kSegTiles;

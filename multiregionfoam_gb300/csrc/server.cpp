@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 
 #include "../../include/mrgpu.h"
 
@@ -61,6 +63,8 @@ Server::Server(Ctx* ctx, const Controls& sym, const Controls* asym, size_t budge
     MRG_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
     MRG_CUDA(cudaEventCreateWithFlags(&side_done_, cudaEventDisableTiming));
     MRG_CUDA(cudaStreamSynchronize(ctx_->st));
+    const char* e = std::getenv("MRG_SERVER_PROFILE");
+    prof_.on = e && e[0] == '1';
     thread_ = std::thread([this] { loop(); });
 }
 
@@ -87,6 +91,12 @@ Server::~Server()
         cudaStreamDestroy(side_);
     }
     if (side_done_) cudaEventDestroy(side_done_);
+    if (prof_.on)
+        std::fprintf(stderr,
+                     "mrg server: %d passes, %d rebuilds; host ms: idle %.1f, iterate %.1f, admissions %.1f, "
+                     "harvest %.1f, rebuild %.1f\n",
+                     prof_.passes, prof_.rebuilds, prof_.idle, prof_.iterate, prof_.start, prof_.harvest,
+                     prof_.rebuild);
 }
 
 size_t Server::estimate(const Mesh& m) const
@@ -238,6 +248,12 @@ void Server::loop()
         }
         for (Request* r : rejected)
             complete(r, MRG_E_OOM, "the request's working set exceeds the server's HBM budget");
+        double tp = prof_.on ? now_ms() : 0.0;
+        if (prof_.on) {
+            ++prof_.passes;
+            if (prof_.t_sync > 0) prof_.idle += tp - prof_.t_sync;
+            prof_.t_sync = 0;
+        }
         for (int f = 0; f < 2; ++f) {
             try {
                 if (!fam_[f].running.empty()) batch_iterate(fam_[f].main, fam_[f].cfg);
@@ -245,6 +261,11 @@ void Server::loop()
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }
+        }
+        if (prof_.on) {
+            const double t = now_ms();
+            prof_.iterate += t - tp;
+            tp = t;
         }
         // admissions on the side stream, overlapping the iterations above
         bool any_admitted = false;
@@ -257,6 +278,11 @@ void Server::loop()
                 }
             if (any_admitted) cudaEventRecord(side_done_, side_);
         }
+        if (prof_.on) {
+            const double t = now_ms();
+            prof_.start += t - tp;
+            tp = t;
+        }
         for (int f = 0; f < 2; ++f) {
             try {
                 bool changed = false;
@@ -267,7 +293,20 @@ void Server::loop()
                     fam_[f].joining.clear();
                     changed = true;
                 }
-                if (changed) rebuild(f);
+                if (prof_.on) {
+                    const double t = now_ms();
+                    prof_.harvest += t - tp;
+                    tp = t;
+                }
+                if (changed) {
+                    rebuild(f);
+                    if (prof_.on) {
+                        const double t = now_ms();
+                        prof_.rebuild += t - tp;
+                        ++prof_.rebuilds;
+                        tp = t;
+                    }
+                }
             } catch (const Error& e) {
                 fail_family(f, e.code, e.what());
             }
@@ -341,6 +380,7 @@ bool Server::harvest(int f)
     if (!F.running.empty()) {
         std::vector<Scal> sc;
         batch_status(F.main, sc);
+        if (prof_.on && prof_.t_sync == 0) prof_.t_sync = now_ms();   // the main stream has drained
         for (size_t s = 0; s < F.running.size(); ++s) {
             if (sc[s].active) continue;
             if (mixed && sc[s].ostate)

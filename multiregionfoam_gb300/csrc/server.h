@@ -91,6 +91,14 @@ private:
     cudaStream_t side_ = nullptr;      // admissions: uploads, views, factor, initial residual
     cudaEvent_t side_done_ = nullptr;
     std::thread thread_;
+    // MRG_SERVER_PROFILE=1: host time by phase of the loop, printed to
+    // stderr when the server is destroyed (idle: from the first drained
+    // status of a pass to the next iteration launch)
+    struct Prof {
+        bool on = false;
+        int passes = 0, rebuilds = 0;
+        double idle = 0, iterate = 0, start = 0, harvest = 0, rebuild = 0, t_sync = 0;
+    } prof_;
 
     void loop();
     void start(int f, std::vector<Request*>& reqs);

@@ -47,7 +47,9 @@ def check_bs(mrg, ctx, O, s, pc, tol=1e-8, **kw):
     slack = 1 if pc in ("DIC", "DILU") else max(2, po["n_iter"] // 10)
     assert abs(pg["n_iter"] - po["n_iter"]) <= slack, (pg, po)
     if po["converged"]:
-        assert rel_err(xg, xo) <= 10 * tol
+        # two residual histories to the same tolerance: the solutions agree to
+        # the error that tolerance allows (wider without a factorisation)
+        assert rel_err(xg, xo) <= (10 if pc in ("DIC", "DILU") else 100) * tol
     return xg, pg
 
 

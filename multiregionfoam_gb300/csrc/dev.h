@@ -15,18 +15,21 @@ namespace mrg {
 
 constexpr int kBlock = 256;   // threads per CTA for row kernels
 constexpr int kMaxRed = 2;    // values reduced per tile
-// A system of T tiles is reduced in G = min(kRedSegs, ceil(T / kSegTiles))
-// contiguous tile segments, segment j = tiles [j*T/G, (j+1)*T/G): the
+// A system of T tiles is reduced in G contiguous tile segments, segment j =
+// tiles [j*T/G, (j+1)*T/G): G = ceil(T / 4) up to kSegSplit tiles, T above
+// (one tile a segment, so a lone system of that size runs its row kernels on
+// one CTA per tile instead of a quarter as many), at most kRedSegs.  The
 // summation order of every per-system reduction depends only on the system
 // itself -- not on the device, the launch grid or the other members of a
-// batch.  One tile a segment up to 608 tiles (622k cells) gives a system of
-// that size one CTA per tile, so its row kernels are not latency-bound on a
-// few CTAs; larger systems spread over 608 segments.
+// batch.  Small systems keep four-tile segments: a batch of hundreds of them
+// pays one segment flush per segment, and one-tile segments cost the 512-
+// system batch a quarter of its speed.
 constexpr int kRedSegs = 608;
-constexpr int kSegTiles = 1;
+constexpr int kSegTiles = 4;
+constexpr int kSegSplit = 256;
 __host__ __device__ inline int red_segments(int tiles)
 {
-    const int g = (tiles + kSegTiles - 1) / kSegTiles;
+    const int g = tiles > kSegSplit ? tiles : (tiles + kSegTiles - 1) / kSegTiles;
     return g < kRedSegs ? (g > 0 ? g : 1) : kRedSegs;
 }
 

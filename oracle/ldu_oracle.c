@@ -498,16 +498,17 @@ static int mr_row(int tile, int t, int k, int assign)
 }
 
 #define MR_GRID 608
-#define MR_SEG_TILES 1
+#define MR_SEG_TILES 4
+#define MR_SEG_SPLIT 256
 
 /* kind 0: acc = fma(a, b, acc); kind 1: acc += a  (a, b in cell order).
- * Segment g of G = min(608, tiles) owns tiles [g*T/G, (g+1)*T/G) and keeps
+ * Segment g of G = min(608, T > 256 ? T : ceil(T/4)) owns tiles [g*T/G, (g+1)*T/G) and keeps
  * accumulating across them; its tree sum lands in slot g.  Thread t then sums
  * slots t, t + 256, ... in order and one block tree combines the threads. */
 static double mr_reduce(const mr_order* o, int assign, int kind, const double* a, const double* b)
 {
     int ntiles = o->npad / MR_TILE;
-    int G = (ntiles + MR_SEG_TILES - 1) / MR_SEG_TILES;
+    int G = ntiles > MR_SEG_SPLIT ? ntiles : (ntiles + MR_SEG_TILES - 1) / MR_SEG_TILES;
     if (G > MR_GRID) G = MR_GRID;
     if (G < 1) G = 1;
     double* part = (double*)calloc((size_t)G, sizeof(double));

@@ -164,8 +164,9 @@ struct Batch {
     const int2* segs;      // [nsegs] (system, reduction segment), see kRedSegs
     const int2* items;     // level-sweep work: (system, chunk) grouped by level
     const int* item_off;   // [maxlevels + 1]
+    const int2* sf_items;  // sync-free sweep work of a batch of several systems: (system, chunk) by level
     Ctl* ctl;
-    int nsys, ntiles, nsegs, maxchunks, maxlevels, pad;
+    int nsys, ntiles, nsegs, maxchunks, maxlevels, n_sf;
 };
 
 enum { ERR_TIMEOUT = 1u, ERR_BREAKDOWN = 2u };

@@ -95,7 +95,7 @@ BatchHost::~BatchHost()
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     if (!ctx) return;
     for (void* p : {(void*)d, (void*)d_ctl, (void*)d_sys, (void*)d_tiles, (void*)d_segs, (void*)d_items,
-                    (void*)d_item_off, (void*)d_scal})
+                    (void*)d_item_off, (void*)d_scal, (void*)d_sf})
         ctx->release(p);
 }
 
@@ -137,11 +137,29 @@ void BatchHost::set(const std::vector<PlanState*>& systems)
         widest_level = std::max(widest_level, (int)items.size() - off[L]);
     }
     off[maxlevels] = (int)items.size();
+    // sync-free sweep work of several systems: every chunk of the sync-free
+    // members, level by level (a member's chunks in its own order), so a
+    // sweep's tickets visit only chunks that exist and every dependency's
+    // chunk comes earlier in the list (later for the backward sweep, which
+    // reads it from the end); one system claims its chunks directly
+    std::vector<int2> sf;
+    if (nsys > 1) {
+        int sl = 0;
+        for (const PlanState* P : systems)
+            if (P->sys.syncfree) sl = std::max(sl, P->sys.nlevels);
+        for (int L = 0; L < sl; ++L)
+            for (int s = 0; s < nsys; ++s) {
+                const PlanState* P = systems[s];
+                if (!P->sys.syncfree || L >= P->sys.nlevels) continue;
+                for (int c = P->host.lvl_chunk[L]; c < P->host.lvl_chunk[L + 1]; ++c) sf.push_back(make_int2(s, c));
+            }
+    }
     ensure(ctx, d_sys, cap_sys, (size_t)nsys);
     ensure(ctx, d_tiles, cap_tiles, tiles.size());
     ensure(ctx, d_segs, cap_segs, segs.size());
     ensure(ctx, d_items, cap_items, items.size());
     ensure(ctx, d_item_off, cap_off, off.size());
+    ensure(ctx, d_sf, cap_sf, sf.size());
     cudaStream_t st = ctx->st;
     if (nsys) MRG_CUDA(cudaMemcpyAsync(d_sys, sv.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, st));
     if (!tiles.empty())
@@ -151,6 +169,10 @@ void BatchHost::set(const std::vector<PlanState*>& systems)
     if (!items.empty())
         MRG_CUDA(cudaMemcpyAsync(d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, st));
     MRG_CUDA(cudaMemcpyAsync(d_item_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
+    if (!sf.empty())
+        MRG_CUDA(cudaMemcpyAsync(d_sf, sf.data(), sizeof(int2) * sf.size(), cudaMemcpyHostToDevice, st));
+    h.sf_items = d_sf;
+    h.n_sf = (int)sf.size();
     h.sys = d_sys;
     h.tiles = d_tiles;
     h.segs = d_segs;

@@ -92,8 +92,9 @@ struct BatchHost {
     int2* d_segs = nullptr;
     int2* d_items = nullptr;
     int* d_item_off = nullptr;
+    int2* d_sf = nullptr;      // sync-free sweep work list (several systems)
     Scal* d_scal = nullptr;    // gathered member states (serving)
-    size_t cap_sys = 0, cap_tiles = 0, cap_segs = 0, cap_items = 0, cap_off = 0, cap_scal = 0;
+    size_t cap_sys = 0, cap_tiles = 0, cap_segs = 0, cap_items = 0, cap_off = 0, cap_scal = 0, cap_sf = 0;
     int widest_level = 1;      // items of the widest sweep level (grid sizing)
     std::vector<PlanState*> members;
     struct Graph {

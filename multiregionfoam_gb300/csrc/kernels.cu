@@ -1440,6 +1440,28 @@ __device__ __forceinline__ int first_system(const Batch& B)
     return RED ? B.segs[g].x : B.tiles[g].x;
 }
 
+// Tiles [t0, t1) of one reduction segment of a system, accumulated in acc
+// (element-wise ops: two tiles' loads in flight, the same order).
+template <typename V, RowOp OP, bool PB>
+__device__ __forceinline__ void segment_tiles(const Batch& B, const SysDev& sS, int t0, int t1,
+                                              double (&acc)[kMaxRed])
+{
+    if constexpr (OpTraits<OP>::kElem) {
+        int t = t0;
+        for (; t + 1 < t1; t += 2) {
+            if constexpr (!PB && kPairOp<V, OP>) {
+                tile_pair<V, OP>(sS, t * kTileRows, (t + 1) * kTileRows, acc);
+            } else {
+                tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+                tile_body<V, OP, PB>(B, sS, (t + 1) * kTileRows, acc);
+            }
+        }
+        if (t < t1) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+    } else {
+        for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
+    }
+}
+
 // One row operation over the whole batch by this CTA: grid-stride over the
 // tile table (non-reducing ops) or the segment table (reducing ops).  `cur`
 // names the system whose descriptor sS holds, so a persistent kernel that
@@ -1518,20 +1540,7 @@ __device__ __forceinline__ void rows_phase(const Batch& B, SysDev& sS, double* s
             }
             const int t0 = (int)(((unsigned)sg.y * T) / G), t1 = (int)(((unsigned)(sg.y + 1) * T) / G);
             double acc[kMaxRed] = {0.0, 0.0};
-            if constexpr (OpTraits<OP>::kElem) {
-                int t = t0;
-                for (; t + 1 < t1; t += 2) {   // same order, two tiles' loads in flight
-                    if constexpr (!PB && kPairOp<V, OP>) {
-                        tile_pair<V, OP>(sS, t * kTileRows, (t + 1) * kTileRows, acc);
-                    } else {
-                        tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
-                        tile_body<V, OP, PB>(B, sS, (t + 1) * kTileRows, acc);
-                    }
-                }
-                if (t < t1) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
-            } else {
-                for (int t = t0; t < t1; ++t) tile_body<V, OP, PB>(B, sS, t * kTileRows, acc);
-            }
+            segment_tiles<V, OP, PB>(B, sS, t0, t1, acc);
             flush_segment<OP>(B, sS, sg.y, t1 - t0, acc, sh, s_last);
         }
     }
@@ -2687,7 +2696,10 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
     const int nsys = B.nsys;
     Ctl* ctl = B.ctl;
     const int lane = threadIdx.x & 31;
-    const unsigned total = (unsigned)nsys * (unsigned)B.maxchunks;
+    // several systems: the batch's list of their chunks by level (the
+    // backward sweep reads it from the end); one system: its chunks in order
+    const bool list = B.n_sf > 0;
+    const unsigned total = list ? (unsigned)B.n_sf : (unsigned)nsys * (unsigned)B.maxchunks;
     const int slot = FWD ? 2 : 4;
     const int unpublished = FWD ? ctl->unpublished1 - 1 : -1;   // watchdog test hook
     for (;;) {
@@ -2695,12 +2707,22 @@ __device__ __forceinline__ void sweep_sf_phase(const Batch& B, int trans)
         if (lane == 0) t = atomicAdd(&ctl->ticket[slot], 1u);
         t = __shfl_sync(kFull, t, 0);
         if (t >= total) break;
-        const int s = (int)(t % (unsigned)nsys), c = (int)(t / (unsigned)nsys);
+        int s, c;
+        if (list) {
+            const int2 it = B.sf_items[FWD ? t : total - 1u - t];
+            s = it.x;
+            c = it.y;
+        } else {
+            s = (int)(t % (unsigned)nsys);
+            c = (int)(t / (unsigned)nsys);
+        }
         const SysDev& S = Ss[s];
         const int nch = S.nchunks;
-        if (c >= nch || !S.sc->active || !S.syncfree || !scalar_tri(S.pc) || c == unpublished) continue;
+        if (c >= nch || !S.sc->active || !S.syncfree || !scalar_tri(S.pc)) continue;
+        const int chunk = list || FWD ? c : nch - 1 - c;
+        if (chunk == unpublished) continue;
         const SweepPtrs<V> P = sweep_ptrs<V, FWD>(S, trans);
-        sweep_chunk<V, FWD>(P, FWD ? c : nch - 1 - c, true, ctl, 0, false, false);
+        sweep_chunk<V, FWD>(P, chunk, true, ctl, 0, false, false);
     }
     if (lane == 0) {
         const unsigned nw = gridDim.x * (blockDim.x / 32);

@@ -6,8 +6,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstddef>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 
@@ -844,16 +846,49 @@ static void launch_recount_host(BatchHost& bh);
 // rest to its compacted sub-batch (recursively), so the loop's tail no
 // longer walks the finished members' tiles; afterwards the batch's counters
 // are recomputed from its members' states.
+// MRG_BATCH_PROFILE=1: a batched solve prints, when it ends, its graph
+// launches, compactions and the host time spent on compaction (member
+// states, the sub-batch's tables) and on iteration graphs (capture or
+// lookup) -- time the stream waits on the host.
+namespace {
+struct BatchProf {
+    int on = -1;
+    long launches = 0, compactions = 0;
+    double compact_ms = 0, graph_ms = 0;
+};
+BatchProf g_bprof;
+bool bprof_on()
+{
+    if (g_bprof.on < 0) {
+        const char* e = std::getenv("MRG_BATCH_PROFILE");
+        g_bprof.on = e && e[0] == '1';
+    }
+    return g_bprof.on == 1;
+}
+double host_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
 static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long cap_iters, Ctl* h)
 {
     const int k = iters_per_launch(bh, cfg);
+    const bool prof = bprof_on();
+    double t0 = prof ? host_ms() : 0.0;
     BatchHost::Graph gr = iteration_graph(bh, cfg, prec, k);
+    if (prof) g_bprof.graph_ms += host_ms() - t0;
     poll(bh, h);
     long launches = 0;
     const long cap = cap_iters / k + 2;
     const int nmem = (int)bh.members.size();
     while (h->n_active > 0 && launches <= cap) {
         if (nmem >= 8 && 2 * (long)h->n_active <= nmem) {
+            if (prof) {
+                t0 = host_ms();
+                ++g_bprof.compactions;
+            }
             std::vector<Scal> sc;
             batch_status(bh, sc);
             std::vector<PlanState*> act;
@@ -867,6 +902,7 @@ static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long ca
             sub.tune = bh.tune;
             sub.set(act);
             launch_recount_host(sub);
+            if (prof) g_bprof.compact_ms += host_ms() - t0;
             run_iterations(sub, cfg, prec, (cap - launches) * k, h);
             launch_recount_host(bh);
             poll(bh, h);
@@ -874,6 +910,7 @@ static void run_iterations(BatchHost& bh, const Controls& cfg, int prec, long ca
         }
         launch_iterations(bh, cfg, prec, gr);
         ++launches;
+        if (prof) ++g_bprof.launches;
         poll(bh, h);
     }
 }
@@ -998,6 +1035,13 @@ std::vector<Perf> solve_batch(BatchHost& bh, const Controls& cfg)
         MRG_CUDA(cudaEventSynchronize(e1));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
+        if (bprof_on() && bh.members.size() > 1) {
+            std::fprintf(stderr, "mrg batch: %zu systems, %.1f ms; %ld graph launches, %ld compactions; host ms: "
+                                 "compaction %.1f, graphs %.1f\n",
+                         bh.members.size(), ms, g_bprof.launches, g_bprof.compactions, g_bprof.compact_ms,
+                         g_bprof.graph_ms);
+            g_bprof = BatchProf{1};
+        }
         std::vector<Scal> sc(bh.members.size());
         for (size_t s = 0; s < bh.members.size(); ++s)
             MRG_CUDA(cudaMemcpyAsync(&sc[s], bh.members[s]->sys.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));

@@ -83,6 +83,19 @@ static T* upload_padded(Ctx* c, const std::vector<T>& v, size_t extra)
 
 // One wave of 256-thread CTAs at the 4 per SM the kernels are compiled for.
 static int grid_sweep(const Ctx* c) { return c->nsm * 4; }
+// CTAs per SM of the sync-free exact sweeps (MRG_SF_CTAS, 1..4, default 3):
+// every warp beyond the level front polls its dependencies in L2, and three
+// CTAs an SM measured fastest (the 737k-cell PBiCG solve 200 -> 191 ms; the
+// 3.1M-cell PCG solve within 1 %)
+static int grid_sf(const Ctx* c)
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("MRG_SF_CTAS");
+        v = e ? std::max(1, std::min(4, std::atoi(e))) : 3;
+    }
+    return c->nsm * v;
+}
 
 // ------------------------------------------------------------------ BatchHost
 void BatchHost::init(Ctx* c)
@@ -622,8 +635,8 @@ static void record_precondition(BatchHost& bh, const Controls& cfg, int prec, in
         // (not while the watchdog test hook withholds a chunk)
         int parts = 0, cells = 0;
         part_choice(bh, parts, cells);
-        launch_sweep(prec, 1, trans, 1, 0, bh.d, grid_sweep(c), st, 0, parts, cells);
-        launch_sweep(prec, 0, trans, 1, 0, bh.d, grid_sweep(c), st, 0, parts, cells);
+        launch_sweep(prec, 1, trans, 1, 0, bh.d, grid_sf(c), st, 0, parts, cells);
+        launch_sweep(prec, 0, trans, 1, 0, bh.d, grid_sf(c), st, 0, parts, cells);
     } else {
         // forward levels 1..nl-1, backward levels nl-2..0 (level 0 alone if
         // nl == 1); one chunk per warp of the widest level

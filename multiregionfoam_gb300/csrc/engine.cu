@@ -869,7 +869,7 @@ struct BatchProf {
     long launches = 0, compactions = 0;
     double compact_ms = 0, graph_ms = 0;
 };
-BatchProf g_bprof;
+thread_local BatchProf g_bprof;   // per host thread: solves on several threads keep their own counts
 bool bprof_on()
 {
     if (g_bprof.on < 0) {

@@ -13,6 +13,8 @@
   MRG_PART_SWEEPS  exact-order sweeps of one system by the owner-computes
                    kernel, one CTA a part of the cells (default), or by the
                    ticketed sync-free kernel (=0)
+  MRG_SF_CTAS      CTAs per SM of the ticketed sync-free sweeps (default 3;
+                   =1 here)
 
 Solves with every variant give bit-identical solutions and iteration counts.
 The switches are read once per process, so each variant runs in a child
@@ -104,7 +106,8 @@ def default_run(tmp_path_factory):
 
 @pytest.mark.parametrize("switch,value", [("MRG_SWEEP_PAIRS", "0"), ("MRG_ITERATION", "persistent"),
                                           ("MRG_SPMV", "warp"), ("MRG_SPMV", "stream1"),
-                                          ("MRG_SPMV", "stream2"), ("MRG_PART_SWEEPS", "0")])
+                                          ("MRG_SPMV", "stream2"), ("MRG_PART_SWEEPS", "0"),
+                                          ("MRG_SF_CTAS", "1")])
 def test_variant_bit_identical(tmp_path, default_run, switch, value):
     s1, p1 = default_run
     s0, p0 = _run(tmp_path, switch, **{switch: value})
